@@ -1,0 +1,198 @@
+/*
+ * tqec_gb300.h -- C ABI of the GB300 tensor-network decoder for TensorQEC.jl.
+ *
+ * This library replaces the hot path of TensorQEC's TNMMAP decoder: the
+ * contraction `ct.code(ct.tensors...)` of the syndrome-conditioned factor
+ * graph followed by `findmax` (src/decoding/tndecoder.jl:160-165 and
+ * :248-253 in the TensorQEC.jl project).  The caller hands over the same
+ * network the reference builds in `compile` (tndecoder.jl:97-146,
+ * :186-219) together with a contraction tree (the reference's OMEinsum
+ * `optimize_code` result, tndecoder.jl:140-144), and then decodes whole
+ * batches of syndromes on one GPU.
+ *
+ * Conventions
+ *  - Every entry point returns an int status: 0 (TQEC_OK) or a negative
+ *    TQEC_ERR_* code; `tqec_last_error` gives the message of the calling
+ *    thread's last failure.  No C++ exception crosses this boundary.
+ *  - Tensor data are float64 in Julia (column-major) order: for a tensor with
+ *    labels (l_0, ..., l_{r-1}) the element with index bits (x_0, ..., x_{r-1})
+ *    sits at offset sum_j x_j * 2^j.  All labels have dimension 2, as in the
+ *    reference (`uniformsize(code, 2)`).
+ *  - Syndromes are bit-packed rows of ceil(n_syndrome/8) bytes, bit j of a
+ *    row at byte j/8, bit j%8 (least significant first).  Bit j drives the
+ *    j-th syndrome leaf, i.e. the order of `update_syndrome!`
+ *    (tndecoder.jl:148-158: all X-check bits, then all Z-check bits).
+ *  - Pointers passed to the decode calls may be host or device memory; the
+ *    library detects which.  With stream == NULL a call is synchronous.
+ *  - Calls on one program are serialised by an internal mutex, like the
+ *    reference's compiled decoder, which mutates its tensors per call
+ *    (tndecoder.jl:148-158).  Distinct programs are independent.
+ */
+#ifndef TQEC_GB300_H
+#define TQEC_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define TQEC_OK 0
+#define TQEC_ERR_INVALID (-1)     /* bad argument, shape or tree */
+#define TQEC_ERR_CUDA (-2)        /* CUDA runtime failure */
+#define TQEC_ERR_OOM (-3)         /* device allocation failed */
+#define TQEC_ERR_UNSUPPORTED (-4) /* network outside what the kernels support */
+#define TQEC_ERR_TIMEOUT (-5)     /* a bounded device wait gave up */
+#define TQEC_ERR_IO (-6)          /* file could not be read or written */
+
+/* Arithmetic of a contraction. */
+#define TQEC_F64 0 /* float64 throughout (the reference's arithmetic) */
+#define TQEC_F32 1 /* float32 with per-tensor power-of-two renormalisation */
+
+/* Option flags. */
+#define TQEC_FLAG_PLAIN 1u   /* decode one syndrome per kernel launch (drop-in form) */
+#define TQEC_FLAG_NORECHECK 2u /* TQEC_F32: skip the float64 recheck of low margins */
+
+/* The factor graph, as built by compile(::TNMMAP, ...) (tndecoder.jl:97-146
+ * for CSS codes, :186-219 for detector error models). */
+typedef struct {
+  int32_t n_tensors;
+  const int32_t* ix_offsets;   /* n_tensors + 1 offsets into ix_labels */
+  const int32_t* ix_labels;    /* positive variable labels (the reference's ixs) */
+  const int64_t* data_offsets; /* n_tensors + 1 offsets into data */
+  const double* data;          /* tensor entries, Julia order (see above) */
+  int32_t n_out;
+  const int32_t* out_labels;   /* the reference's iy */
+  int32_t n_syndrome;
+  const int32_t* syndrome_tensors; /* 0-based tensor positions of the one-hot
+                                      syndrome leaves, in syndrome-bit order */
+} tqec_network;
+
+/* A binary contraction tree: step s merges nodes steps[2s] and steps[2s+1];
+ * node ids < n_tensors are the network's tensors, node n_tensors + s is the
+ * result of step s.  The last step is the root and every node is used once
+ * (the flattened form of OMEinsum's NestedEinsum). */
+typedef struct {
+  int32_t n_steps;
+  const int32_t* steps;
+} tqec_tree;
+
+typedef struct {
+  int32_t precision;      /* TQEC_F64 or TQEC_F32 */
+  uint32_t flags;         /* TQEC_FLAG_* */
+  int32_t device;         /* CUDA device ordinal */
+  int32_t group;          /* syndromes per thread block (power of two); 0 = auto */
+  int32_t threads;        /* threads per block (multiple of 32); 0 = auto */
+  double margin;          /* TQEC_F32: recheck when the log-probability margin
+                             of the top class is below this; < 0 = the
+                             rounding-error bound the planner derives */
+} tqec_options;
+
+typedef struct {
+  int32_t n_syndrome;        /* syndrome bits per row */
+  int32_t syndrome_bytes;    /* bytes per packed row */
+  int32_t n_classes;         /* 2^n_out entries of the marginal */
+  int32_t n_steps;           /* runtime steps left after constant folding */
+  int32_t n_tree_steps;      /* steps of the tree as given */
+  int32_t width;             /* log2 of the largest runtime intermediate */
+  int64_t arena_elems;       /* per-syndrome working set, elements */
+  double flops_per_syndrome; /* 2 x multiply-adds of the runtime steps */
+  double flops_tree;         /* 2 x multiply-adds of the whole tree as given */
+  double err_bound_f32;      /* relative error bound of a TQEC_F32 marginal */
+  double err_bound_f64;      /* relative error bound of a TQEC_F64 marginal */
+  int32_t group_f32, threads_f32, smem_f32; /* launch shape chosen for F32 */
+  int32_t group_f64, threads_f64, smem_f64; /* launch shape chosen for F64 */
+} tqec_program_info_t;
+
+typedef struct tqec_program tqec_program;
+
+/* compile(::TNMMAP, problem) -> CompiledTNMMAP (tndecoder.jl:97-146,
+ * :186-219).  Host data are copied; the program owns its device memory. */
+int tqec_program_create(const tqec_network* net, const tqec_tree* tree,
+                        const tqec_options* opts, tqec_program** out);
+
+int tqec_program_destroy(tqec_program* prog);
+
+int tqec_program_info(const tqec_program* prog, tqec_program_info_t* info);
+
+/* decode(ct, syndrome) over a batch (tndecoder.jl:160-165, :248-253):
+ * contracts every syndrome, writes the argmax class (findmax's first maximum
+ * in Julia linear order), the natural-log marginal of every class
+ * (n x n_classes, Julia linear order of `mar`) and a per-syndrome relative
+ * error bound.  logp_out and err_bound_out may be NULL.  With TQEC_F32 the
+ * syndromes whose class margin is below the bound are contracted again in
+ * float64 before the call returns. */
+int tqec_decode_batch(tqec_program* prog, const uint8_t* syndromes, int64_t n,
+                      int32_t* class_out, double* logp_out,
+                      float* err_bound_out, void* stream);
+
+/* The contraction alone in a chosen precision, without argmax or recheck:
+ * writes n x n_classes natural-log marginals (the reference's
+ * `ct.code(ct.tensors...)`, tndecoder.jl:162, in log form). */
+int tqec_contract_batch(tqec_program* prog, const uint8_t* syndromes,
+                        int64_t n, int32_t precision, double* logp_out,
+                        void* stream);
+
+/* Count of syndromes the last TQEC_F32 decode call sent to the float64
+ * recheck (a measure of how often the rounding bound was not enough). */
+int tqec_last_recheck_count(const tqec_program* prog, int64_t* count);
+
+/* Tries the launch shapes that fit and keeps the fastest for each
+ * precision, timing n_probe synthetic syndromes. */
+int tqec_program_autotune(tqec_program* prog, int64_t n_probe);
+
+/* The compiled program without a device, for inspection (the counterpart of
+ * OMEinsum.contraction_complexity(ct), tndecoder.jl:273-279).  `steps` holds
+ * n_steps records of 64 bytes: int32 a_kind, b_kind, a_ref, b_ref, a_prod,
+ * b_prod; int8 a_sel[4], b_sel[4]; int32 lh, lfa, lfb, lk, out_off,
+ * perm_off, pad, pad.  Release the view with tqec_plan_release. */
+typedef struct {
+  int32_t n_steps;
+  const void* steps;
+  int64_t n_perm;
+  const int32_t* perm;
+  int64_t n_consts;
+  const double* consts;
+  int64_t arena_elems;
+  int32_t width;
+  int32_t n_classes;
+  int32_t n_syndrome;
+  double flops_per_syndrome;
+  double flops_tree;
+  double err_terms;
+} tqec_plan_view;
+
+int tqec_plan_inspect(const tqec_network* net, const tqec_tree* tree,
+                      tqec_plan_view* view, void** handle);
+int tqec_plan_release(void* handle);
+
+/* Contraction-order search, in place of OMEinsum's
+ * optimize_code(code, uniformsize(code, 2), TreeSA()) (tndecoder.jl:140-144,
+ * :213-217): randomised greedy passes refined by simulated annealing over
+ * tree rotations.  Only the network's labels and outputs are read.  Writes
+ * 2 * (n_tensors - 1) node ids in the tqec_tree convention, log2 of the
+ * tree's multiply-adds and the width of its widest intermediate. */
+typedef struct {
+  int32_t trials;        /* randomised greedy passes (default 32) */
+  int32_t sweeps;        /* annealing sweeps (default 60; 0 = none) */
+  int32_t target_width;  /* widths above this are penalised (0 = none) */
+  double width_penalty;  /* energy per label above target_width (default 1) */
+  uint64_t seed;         /* random seed (0 = 1) */
+} tqec_order_options;
+
+int tqec_optimize_order(const tqec_network* net, const tqec_order_options* opts,
+                        int32_t* steps_out, double* log2_macs_out,
+                        int32_t* width_out);
+
+/* Message of the calling thread's last failure (always NUL-terminated). */
+int tqec_last_error(char* buf, size_t len);
+
+/* Library version string, e.g. "tqec-gb300 0.1.0 sm_103a". */
+const char* tqec_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* TQEC_GB300_H */

@@ -1,0 +1,551 @@
+// abi.cu -- the C ABI (include/tqec_gb300.h): program lifetime and decode
+// orchestration.  The Julia side binds these with ccall in place of
+// `decode(ct::CompiledTNMMAP, syndrome)` (src/decoding/tndecoder.jl:160-165)
+// and `decode(ct::CompiledDEMTNMMAP, syndrome)` (:248-253).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/tqec_gb300.h"
+#include "contract.cuh"
+#include "plan.h"
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const std::string& msg) {
+  g_last_error = msg;
+  return code;
+}
+
+#define TQ_CUDA(call)                                                                     \
+  do {                                                                                    \
+    cudaError_t e__ = (call);                                                             \
+    if (e__ != cudaSuccess) {                                                             \
+      return fail(e__ == cudaErrorMemoryAllocation ? TQEC_ERR_OOM : TQEC_ERR_CUDA,        \
+                  std::string(#call) + ": " + cudaGetErrorString(e__));                   \
+    }                                                                                     \
+  } while (0)
+
+struct Shape {
+  int G = 1;
+  int threads = 256;
+  bool smem_arena = true;
+  size_t smem = 0;
+  int grid_cap = 1;  // blocks resident on the whole device
+};
+
+struct DevBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+  cudaError_t ensure(size_t want) {
+    if (want <= bytes) return cudaSuccess;
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+    cudaError_t e = cudaMalloc(&p, want);
+    if (e == cudaSuccess) bytes = want;
+    return e;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+  }
+};
+
+}  // namespace
+
+struct tqec_program {
+  tqec::Plan plan;
+  int device = 0;
+  int sm_count = 1;
+  int precision = TQEC_F32;
+  uint32_t flags = 0;
+  double margin = -1.0;
+  cudaStream_t stream = nullptr;
+  tqec::StepDesc* d_steps = nullptr;
+  int32_t* d_perm = nullptr;
+  double* d_c64 = nullptr;
+  float* d_c32 = nullptr;
+  Shape shape[2];  // indexed by precision
+  DevBuf arena[2];
+  DevBuf syn, cls, logp, err, list, count;
+  int32_t* h_count = nullptr;  // pinned
+  int64_t last_recheck = 0;
+  std::mutex mu;
+};
+
+namespace {
+
+bool is_device_ptr(const void* p) {
+  if (!p) return false;
+  cudaPointerAttributes at;
+  if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged;
+}
+
+double err_bound(const tqec_program* p, int precision) {
+  const double u = precision == TQEC_F32 ? std::ldexp(1.0, -24) : std::ldexp(1.0, -53);
+  const double b = u * p->plan.err_terms * 1.01;
+  return b / (1.0 - std::min(b, 0.5));
+}
+
+int syn_words(const tqec_program* p) { return std::max(1, (p->plan.n_syndrome + 31) / 32); }
+
+// Picks (G, threads) for one precision: the largest group whose arena fits
+// about half of the shared memory (two blocks per SM), else a global arena.
+int choose_shape(tqec_program* p, int precision, int G_req, int threads_req, Shape* out) {
+  const size_t limit = tqec::contract_smem_limit(p->device);
+  const size_t esz = precision == TQEC_F32 ? 4 : 8;
+  const int64_t arena = p->plan.arena_elems;
+  const int nsteps = (int)p->plan.steps.size();
+  const int sw = syn_words(p);
+  Shape s;
+  s.threads = threads_req > 0 ? threads_req : 256;
+  if (G_req > 0) {
+    s.G = G_req;
+    s.smem_arena = tqec::contract_smem_bytes(precision, nsteps, sw, s.G, arena, true) <= limit;
+  } else {
+    const size_t target = limit / 2 - 1024;
+    int G = 1;
+    while (G < 256 && tqec::contract_smem_bytes(precision, nsteps, sw, G * 2, arena, true) <= target &&
+           (int64_t(G) * 2 << p->plan.width) <= 16 * 4096)
+      G *= 2;
+    s.G = G;
+    s.smem_arena = tqec::contract_smem_bytes(precision, nsteps, sw, G, arena, true) <= limit;
+    if (!s.smem_arena) s.threads = threads_req > 0 ? threads_req : 512;
+    (void)esz;
+  }
+  s.smem = tqec::contract_smem_bytes(precision, nsteps, sw, s.G, arena, s.smem_arena);
+  if (s.smem > limit) return fail(TQEC_ERR_UNSUPPORTED, "program does not fit shared memory even with a global arena");
+  int occ = tqec::contract_occupancy(precision, s.threads, s.smem);
+  if (occ < 1) return fail(TQEC_ERR_UNSUPPORTED, "launch shape cannot be resident on this device");
+  s.grid_cap = occ * p->sm_count;
+  *out = s;
+  return TQEC_OK;
+}
+
+int ensure_arena(tqec_program* p, int precision, int grid) {
+  const Shape& s = p->shape[precision];
+  if (s.smem_arena) return TQEC_OK;
+  const size_t esz = precision == TQEC_F32 ? 4 : 8;
+  const size_t want = size_t(grid) * s.G * size_t(p->plan.arena_elems) * esz;
+  TQ_CUDA(p->arena[precision].ensure(want));
+  return TQEC_OK;
+}
+
+tqec::KArgs base_args(tqec_program* p, int precision) {
+  tqec::KArgs a;
+  std::memset(&a, 0, sizeof(a));
+  a.steps = p->d_steps;
+  a.n_steps = (int32_t)p->plan.steps.size();
+  a.perm = p->d_perm;
+  a.consts = precision == TQEC_F32 ? (const void*)p->d_c32 : (const void*)p->d_c64;
+  a.syn_bytes = p->plan.syndrome_bytes;
+  a.syn_words = syn_words(p);
+  const Shape& s = p->shape[precision];
+  a.G = s.G;
+  a.lg = 0;
+  while ((1 << a.lg) < s.G) a.lg++;
+  a.arena_elems = p->plan.arena_elems;
+  a.arena_global = s.smem_arena ? nullptr : p->arena[precision].p;
+  a.n_classes = p->plan.n_classes;
+  a.err_bound = (float)err_bound(p, precision);
+  a.recheck_margin = -1.0;
+  return a;
+}
+
+int launch_rows(tqec_program* p, int precision, tqec::KArgs a, int64_t n_rows_max, cudaStream_t st) {
+  const Shape& s = p->shape[precision];
+  int64_t want = (n_rows_max + s.G - 1) / s.G;
+  int grid = (int)std::max<int64_t>(1, std::min<int64_t>(want, s.grid_cap));
+  int rc = ensure_arena(p, precision, grid);
+  if (rc) return rc;
+  a.arena_global = s.smem_arena ? nullptr : p->arena[precision].p;
+  TQ_CUDA(tqec::contract_launch(precision, a, grid, s.threads, s.smem, st));
+  return TQEC_OK;
+}
+
+// Runs the plain form: one launch (one block, one syndrome) per row.
+int launch_plain(tqec_program* p, int precision, tqec::KArgs a, int64_t n, cudaStream_t st) {
+  Shape s = p->shape[precision];
+  const size_t limit = tqec::contract_smem_limit(p->device);
+  const int nsteps = (int)p->plan.steps.size();
+  Shape one;
+  one.G = 1;
+  one.threads = s.threads;
+  one.smem_arena = tqec::contract_smem_bytes(precision, nsteps, syn_words(p), 1, p->plan.arena_elems, true) <= limit;
+  one.smem = tqec::contract_smem_bytes(precision, nsteps, syn_words(p), 1, p->plan.arena_elems, one.smem_arena);
+  a.G = 1;
+  a.lg = 0;
+  if (!one.smem_arena) {
+    const size_t esz = precision == TQEC_F32 ? 4 : 8;
+    TQ_CUDA(p->arena[precision].ensure(size_t(p->plan.arena_elems) * esz));
+    a.arena_global = p->arena[precision].p;
+  } else {
+    a.arena_global = nullptr;
+  }
+  a.n = 1;
+  for (int64_t i = 0; i < n; ++i) {
+    a.row_offset = i;
+    TQ_CUDA(tqec::contract_launch(precision, a, 1, one.threads, one.smem, st));
+  }
+  return TQEC_OK;
+}
+
+struct Staged {
+  const uint8_t* d_syn;
+  int32_t* d_cls;
+  double* d_logp;
+  float* d_err;
+  bool host_cls, host_logp, host_err;
+};
+
+int stage_inputs(tqec_program* p, const uint8_t* syn, int64_t n, int32_t* cls, double* logp, float* err,
+                 cudaStream_t st, Staged* s) {
+  const size_t sb = size_t(p->plan.syndrome_bytes) * size_t(n);
+  if (sb > 0 && is_device_ptr(syn)) {
+    s->d_syn = syn;
+  } else {
+    TQ_CUDA(p->syn.ensure(std::max<size_t>(sb, 16)));
+    if (sb) TQ_CUDA(cudaMemcpyAsync(p->syn.p, syn, sb, cudaMemcpyHostToDevice, st));
+    s->d_syn = (const uint8_t*)p->syn.p;
+  }
+  s->host_cls = cls && !is_device_ptr(cls);
+  s->host_logp = logp && !is_device_ptr(logp);
+  s->host_err = err && !is_device_ptr(err);
+  if (s->host_cls) {
+    TQ_CUDA(p->cls.ensure(sizeof(int32_t) * std::max<int64_t>(n, 1)));
+    s->d_cls = (int32_t*)p->cls.p;
+  } else {
+    s->d_cls = cls;
+  }
+  if (s->host_logp) {
+    TQ_CUDA(p->logp.ensure(sizeof(double) * std::max<int64_t>(n, 1) * p->plan.n_classes));
+    s->d_logp = (double*)p->logp.p;
+  } else {
+    s->d_logp = logp;
+  }
+  if (s->host_err) {
+    TQ_CUDA(p->err.ensure(sizeof(float) * std::max<int64_t>(n, 1)));
+    s->d_err = (float*)p->err.p;
+  } else {
+    s->d_err = err;
+  }
+  return TQEC_OK;
+}
+
+int unstage_outputs(tqec_program* p, int64_t n, int32_t* cls, double* logp, float* err, cudaStream_t st,
+                    const Staged& s) {
+  if (s.host_cls && n) TQ_CUDA(cudaMemcpyAsync(cls, s.d_cls, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, st));
+  if (s.host_logp && n)
+    TQ_CUDA(cudaMemcpyAsync(logp, s.d_logp, sizeof(double) * n * p->plan.n_classes, cudaMemcpyDeviceToHost, st));
+  if (s.host_err && n) TQ_CUDA(cudaMemcpyAsync(err, s.d_err, sizeof(float) * n, cudaMemcpyDeviceToHost, st));
+  return TQEC_OK;
+}
+
+int decode_locked(tqec_program* p, const uint8_t* syn, int64_t n, int32_t* cls, double* logp, float* err,
+                  int precision, bool recheck, bool plain, cudaStream_t st) {
+  Staged s;
+  int rc = stage_inputs(p, syn, n, cls, logp, err, st, &s);
+  if (rc) return rc;
+  if (n > 0) {
+    tqec::KArgs a = base_args(p, precision);
+    a.syn = s.d_syn;
+    a.n = n;
+    a.class_out = s.d_cls;
+    a.logp_out = s.d_logp;
+    a.err_out = s.d_err;
+    if (recheck && precision == TQEC_F32) {
+      if (n > INT32_MAX) return fail(TQEC_ERR_INVALID, "batch above 2^31 rows");
+      TQ_CUDA(p->list.ensure(sizeof(int32_t) * n));
+      TQ_CUDA(p->count.ensure(sizeof(int32_t)));
+      TQ_CUDA(cudaMemsetAsync(p->count.p, 0, sizeof(int32_t), st));
+      a.recheck_margin = p->margin >= 0.0 ? p->margin : 2.0 * err_bound(p, TQEC_F32);
+      a.recheck_list = (int32_t*)p->list.p;
+      a.recheck_count = (int32_t*)p->count.p;
+      // the float64 pass needs class/err outputs even if the caller did not ask
+      if (!a.class_out) {
+        TQ_CUDA(p->cls.ensure(sizeof(int32_t) * n));
+        a.class_out = (int32_t*)p->cls.p;
+      }
+    }
+    rc = plain ? launch_plain(p, precision, a, n, st) : launch_rows(p, precision, a, n, st);
+    if (rc) return rc;
+    if (recheck && precision == TQEC_F32) {
+      tqec::KArgs b = base_args(p, TQEC_F64);
+      b.syn = s.d_syn;
+      b.list = (const int32_t*)p->list.p;
+      b.list_count = (const int32_t*)p->count.p;
+      b.class_out = a.class_out;
+      b.logp_out = s.d_logp;
+      b.err_out = s.d_err;
+      rc = launch_rows(p, TQEC_F64, b, n, st);
+      if (rc) return rc;
+      TQ_CUDA(cudaMemcpyAsync(p->h_count, p->count.p, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+    }
+  }
+  rc = unstage_outputs(p, n, cls, logp, err, st, s);
+  if (rc) return rc;
+  return TQEC_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* tqec_version(void) { return "tqec-gb300 0.1.0 sm_103a"; }
+
+int tqec_last_error(char* buf, size_t len) {
+  if (!buf || len == 0) return TQEC_ERR_INVALID;
+  size_t n = std::min(len - 1, g_last_error.size());
+  std::memcpy(buf, g_last_error.data(), n);
+  buf[n] = '\0';
+  return TQEC_OK;
+}
+
+int tqec_program_create(const tqec_network* net, const tqec_tree* tree, const tqec_options* opts,
+                        tqec_program** out) {
+  if (!net || !tree || !out) return fail(TQEC_ERR_INVALID, "NULL argument");
+  *out = nullptr;
+  tqec_options o;
+  std::memset(&o, 0, sizeof(o));
+  o.precision = TQEC_F32;
+  o.margin = -1.0;
+  if (opts) o = *opts;
+  if (o.precision != TQEC_F32 && o.precision != TQEC_F64) return fail(TQEC_ERR_INVALID, "unknown precision");
+  if (o.group < 0 || (o.group & (o.group - 1)) || o.group > 1024) return fail(TQEC_ERR_INVALID, "group must be 0 or a power of two <= 1024");
+  if (o.threads < 0 || (o.threads % 32) || o.threads > 512) return fail(TQEC_ERR_INVALID, "threads must be 0 or a multiple of 32 up to 512");
+  tqec::NetworkView v{net->n_tensors, net->ix_offsets, net->ix_labels, net->data_offsets, net->data,
+                      net->n_out, net->out_labels, net->n_syndrome, net->syndrome_tensors};
+  tqec::PlanLimits lim;
+  auto* p = new tqec_program();
+  bool unsupported = false;
+  std::string err = tqec::build_plan(v, tree->n_steps, tree->steps, lim, &p->plan, &unsupported);
+  if (!err.empty()) {
+    delete p;
+    return fail(unsupported ? TQEC_ERR_UNSUPPORTED : TQEC_ERR_INVALID, err);
+  }
+  p->device = o.device;
+  p->precision = o.precision;
+  p->flags = o.flags;
+  p->margin = o.margin;
+  auto bail = [&](int code, const std::string& m) {
+    tqec_program_destroy(p);
+    return fail(code, m);
+  };
+  cudaError_t e = cudaSetDevice(o.device);
+  if (e != cudaSuccess) return bail(TQEC_ERR_CUDA, std::string("cudaSetDevice: ") + cudaGetErrorString(e));
+  cudaDeviceGetAttribute(&p->sm_count, cudaDevAttrMultiProcessorCount, o.device);
+  if ((e = cudaStreamCreateWithFlags(&p->stream, cudaStreamNonBlocking)) != cudaSuccess)
+    return bail(TQEC_ERR_CUDA, cudaGetErrorString(e));
+  const tqec::Plan& P = p->plan;
+  size_t nst = P.steps.size();
+  if ((e = cudaMalloc(&p->d_steps, nst * sizeof(tqec::StepDesc))) != cudaSuccess) return bail(TQEC_ERR_OOM, "steps");
+  cudaMemcpy(p->d_steps, P.steps.data(), nst * sizeof(tqec::StepDesc), cudaMemcpyHostToDevice);
+  size_t np = std::max<size_t>(P.perm.size(), 1);
+  if ((e = cudaMalloc(&p->d_perm, np * sizeof(int32_t))) != cudaSuccess) return bail(TQEC_ERR_OOM, "perm");
+  if (!P.perm.empty()) cudaMemcpy(p->d_perm, P.perm.data(), P.perm.size() * sizeof(int32_t), cudaMemcpyHostToDevice);
+  size_t nc = std::max<size_t>(P.consts.size(), 4);
+  if ((e = cudaMalloc(&p->d_c64, nc * sizeof(double))) != cudaSuccess) return bail(TQEC_ERR_OOM, "consts");
+  if ((e = cudaMalloc(&p->d_c32, nc * sizeof(float))) != cudaSuccess) return bail(TQEC_ERR_OOM, "consts");
+  if (!P.consts.empty()) {
+    std::vector<float> c32(P.consts.begin(), P.consts.end());
+    cudaMemcpy(p->d_c64, P.consts.data(), P.consts.size() * sizeof(double), cudaMemcpyHostToDevice);
+    cudaMemcpy(p->d_c32, c32.data(), c32.size() * sizeof(float), cudaMemcpyHostToDevice);
+  }
+  if ((e = cudaMallocHost(&p->h_count, sizeof(int32_t))) != cudaSuccess) return bail(TQEC_ERR_OOM, "pinned count");
+  *p->h_count = 0;
+  if ((e = cudaGetLastError()) != cudaSuccess) return bail(TQEC_ERR_CUDA, cudaGetErrorString(e));
+  int rc;
+  if ((rc = choose_shape(p, TQEC_F32, o.group, o.threads, &p->shape[TQEC_F32])) != TQEC_OK) {
+    std::string m = g_last_error;
+    return bail(rc, m);
+  }
+  if ((rc = choose_shape(p, TQEC_F64, o.group, o.threads, &p->shape[TQEC_F64])) != TQEC_OK) {
+    std::string m = g_last_error;
+    return bail(rc, m);
+  }
+  *out = p;
+  return TQEC_OK;
+}
+
+int tqec_program_destroy(tqec_program* p) {
+  if (!p) return TQEC_OK;
+  cudaSetDevice(p->device);
+  if (p->stream) cudaStreamSynchronize(p->stream);
+  cudaFree(p->d_steps);
+  cudaFree(p->d_perm);
+  cudaFree(p->d_c64);
+  cudaFree(p->d_c32);
+  if (p->h_count) cudaFreeHost(p->h_count);
+  for (auto* b : {&p->arena[0], &p->arena[1], &p->syn, &p->cls, &p->logp, &p->err, &p->list, &p->count}) b->release();
+  if (p->stream) cudaStreamDestroy(p->stream);
+  delete p;
+  return TQEC_OK;
+}
+
+int tqec_program_info(const tqec_program* p, tqec_program_info_t* info) {
+  if (!p || !info) return fail(TQEC_ERR_INVALID, "NULL argument");
+  std::memset(info, 0, sizeof(*info));
+  const tqec::Plan& P = p->plan;
+  info->n_syndrome = P.n_syndrome;
+  info->syndrome_bytes = P.syndrome_bytes;
+  info->n_classes = P.n_classes;
+  info->n_steps = (int32_t)P.steps.size();
+  info->n_tree_steps = P.n_tree_steps;
+  info->width = P.width;
+  info->arena_elems = P.arena_elems;
+  info->flops_per_syndrome = 2.0 * P.macs_runtime;
+  info->flops_tree = 2.0 * P.macs_tree;
+  info->err_bound_f32 = err_bound(p, TQEC_F32);
+  info->err_bound_f64 = err_bound(p, TQEC_F64);
+  info->group_f32 = p->shape[TQEC_F32].G;
+  info->threads_f32 = p->shape[TQEC_F32].threads;
+  info->smem_f32 = (int32_t)p->shape[TQEC_F32].smem;
+  info->group_f64 = p->shape[TQEC_F64].G;
+  info->threads_f64 = p->shape[TQEC_F64].threads;
+  info->smem_f64 = (int32_t)p->shape[TQEC_F64].smem;
+  return TQEC_OK;
+}
+
+int tqec_decode_batch(tqec_program* p, const uint8_t* syndromes, int64_t n, int32_t* class_out, double* logp_out,
+                      float* err_bound_out, void* stream) {
+  if (!p || n < 0 || (n > 0 && !syndromes)) return fail(TQEC_ERR_INVALID, "bad argument");
+  std::lock_guard<std::mutex> lk(p->mu);
+  TQ_CUDA(cudaSetDevice(p->device));
+  cudaStream_t st = stream ? (cudaStream_t)stream : p->stream;
+  const bool plain = (p->flags & TQEC_FLAG_PLAIN) != 0;
+  const bool recheck = p->precision == TQEC_F32 && !(p->flags & TQEC_FLAG_NORECHECK);
+  int rc = decode_locked(p, syndromes, n, class_out, logp_out, err_bound_out, p->precision, recheck, plain, st);
+  if (rc) return rc;
+  if (!stream || (class_out && !is_device_ptr(class_out)) || (logp_out && !is_device_ptr(logp_out)) ||
+      (err_bound_out && !is_device_ptr(err_bound_out))) {
+    TQ_CUDA(cudaStreamSynchronize(st));
+    p->last_recheck = recheck ? *p->h_count : 0;
+  }
+  return TQEC_OK;
+}
+
+int tqec_contract_batch(tqec_program* p, const uint8_t* syndromes, int64_t n, int32_t precision, double* logp_out,
+                        void* stream) {
+  if (!p || n < 0 || (n > 0 && (!syndromes || !logp_out))) return fail(TQEC_ERR_INVALID, "bad argument");
+  if (precision != TQEC_F32 && precision != TQEC_F64) return fail(TQEC_ERR_INVALID, "unknown precision");
+  std::lock_guard<std::mutex> lk(p->mu);
+  TQ_CUDA(cudaSetDevice(p->device));
+  cudaStream_t st = stream ? (cudaStream_t)stream : p->stream;
+  const bool plain = (p->flags & TQEC_FLAG_PLAIN) != 0;
+  int rc = decode_locked(p, syndromes, n, nullptr, logp_out, nullptr, precision, false, plain, st);
+  if (rc) return rc;
+  if (!stream || !is_device_ptr(logp_out)) TQ_CUDA(cudaStreamSynchronize(st));
+  return TQEC_OK;
+}
+
+int tqec_last_recheck_count(const tqec_program* p, int64_t* count) {
+  if (!p || !count) return fail(TQEC_ERR_INVALID, "NULL argument");
+  *count = p->last_recheck;
+  return TQEC_OK;
+}
+
+int tqec_program_autotune(tqec_program* p, int64_t n_probe) {
+  if (!p || n_probe <= 0) return fail(TQEC_ERR_INVALID, "bad argument");
+  std::lock_guard<std::mutex> lk(p->mu);
+  TQ_CUDA(cudaSetDevice(p->device));
+  const int64_t n = n_probe;
+  std::vector<uint8_t> h((size_t)n * p->plan.syndrome_bytes);
+  uint64_t x = 0x9E3779B97F4A7C15ull;
+  for (auto& b : h) {
+    x ^= x << 13; x ^= x >> 7; x ^= x << 17;
+    b = uint8_t(x & 0x11);  // sparse bits, like low-noise syndromes
+  }
+  TQ_CUDA(p->syn.ensure(std::max<size_t>(h.size(), 16)));
+  TQ_CUDA(cudaMemcpy(p->syn.p, h.data(), h.size(), cudaMemcpyHostToDevice));
+  TQ_CUDA(p->logp.ensure(sizeof(double) * n * p->plan.n_classes));
+  cudaEvent_t e0, e1;
+  TQ_CUDA(cudaEventCreate(&e0));
+  TQ_CUDA(cudaEventCreate(&e1));
+  for (int prec : {TQEC_F32, TQEC_F64}) {
+    Shape best = p->shape[prec];
+    float best_ms = 1e30f;
+    for (int G : {1, 2, 4, 8, 16, 32, 64, 128}) {
+      for (int th : {128, 256, 512}) {
+        Shape s;
+        if (choose_shape(p, prec, G, th, &s) != TQEC_OK) continue;
+        p->shape[prec] = s;
+        tqec::KArgs a = base_args(p, prec);
+        a.syn = (const uint8_t*)p->syn.p;
+        a.n = n;
+        a.logp_out = (double*)p->logp.p;
+        if (launch_rows(p, prec, a, n, p->stream) != TQEC_OK) continue;  // warm-up
+        cudaEventRecord(e0, p->stream);
+        launch_rows(p, prec, a, n, p->stream);
+        cudaEventRecord(e1, p->stream);
+        if (cudaEventSynchronize(e1) != cudaSuccess) {
+          cudaEventDestroy(e0);
+          cudaEventDestroy(e1);
+          return fail(TQEC_ERR_CUDA, "autotune launch failed");
+        }
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (ms < best_ms) {
+          best_ms = ms;
+          best = s;
+        }
+      }
+    }
+    p->shape[prec] = best;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  g_last_error.clear();
+  return TQEC_OK;
+}
+
+int tqec_plan_inspect(const tqec_network* net, const tqec_tree* tree, tqec_plan_view* view, void** handle) {
+  if (!net || !tree || !view || !handle) return fail(TQEC_ERR_INVALID, "NULL argument");
+  *handle = nullptr;
+  tqec::NetworkView v{net->n_tensors, net->ix_offsets, net->ix_labels, net->data_offsets, net->data,
+                      net->n_out, net->out_labels, net->n_syndrome, net->syndrome_tensors};
+  auto* P = new tqec::Plan();
+  bool unsupported = false;
+  std::string err = tqec::build_plan(v, tree->n_steps, tree->steps, tqec::PlanLimits(), P, &unsupported);
+  if (!err.empty()) {
+    delete P;
+    return fail(unsupported ? TQEC_ERR_UNSUPPORTED : TQEC_ERR_INVALID, err);
+  }
+  std::memset(view, 0, sizeof(*view));
+  view->n_steps = (int32_t)P->steps.size();
+  view->steps = P->steps.data();
+  view->n_perm = (int64_t)P->perm.size();
+  view->perm = P->perm.data();
+  view->n_consts = (int64_t)P->consts.size();
+  view->consts = P->consts.data();
+  view->arena_elems = P->arena_elems;
+  view->width = P->width;
+  view->n_classes = P->n_classes;
+  view->n_syndrome = P->n_syndrome;
+  view->flops_per_syndrome = 2.0 * P->macs_runtime;
+  view->flops_tree = 2.0 * P->macs_tree;
+  view->err_terms = P->err_terms;
+  *handle = P;
+  return TQEC_OK;
+}
+
+int tqec_plan_release(void* handle) {
+  delete static_cast<tqec::Plan*>(handle);
+  return TQEC_OK;
+}
+
+}  // extern "C"

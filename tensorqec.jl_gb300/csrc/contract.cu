@@ -1,0 +1,291 @@
+// contract.cu -- batched contraction of a syndrome-conditioned factor graph.
+//
+// This evaluates, for many syndromes at once, what TensorQEC evaluates one
+// syndrome at a time with `ct.code(ct.tensors...)` followed by `findmax`
+// (src/decoding/tndecoder.jl:160-165, :248-253).  A thread block owns G
+// syndromes and walks the program (plan.h) step by step; each syndrome's
+// intermediates live in its arena (shared memory when it fits, otherwise a
+// per-block slice of global memory that stays resident in L2).  All threads
+// of the block share every step: work items are (syndrome, output element)
+// pairs, so small steps are filled with many syndromes and large steps with
+// many elements of one syndrome.
+//
+// float32 arithmetic keeps every intermediate normalised: a step records the
+// maximum of its output per syndrome, and the consumer scales the operand by
+// the power of two that brings that maximum to [1, 2).  Scaling by powers of
+// two is exact, so the only rounding is that of the products and sums.  The
+// exponents are summed into the final log-probability.
+#include <cstdio>
+
+#include "contract.cuh"
+
+namespace tqec {
+namespace {
+
+__device__ __forceinline__ int syn_bit(const uint32_t* syn, int j) {
+  return (syn[j >> 5] >> (j & 31)) & 1;
+}
+
+template <typename T>
+__device__ __forceinline__ T parity_val(int idx, int s) {
+  return ((__popc(idx) ^ s) & 1) ? T(0) : T(1);
+}
+
+// Power-of-two normaliser of a tensor whose maximum has float bits `m`:
+// returns 2^-E with E = floor(log2(max)); writes E.
+__device__ __forceinline__ float norm_factor(uint32_t m, int* e) {
+  if (m == 0u) {
+    *e = 0;
+    return 1.0f;
+  }
+  int be = int((m >> 23) & 0xffu);
+  be = be < 1 ? 1 : (be > 253 ? 253 : be);
+  *e = be - 127;
+  return __uint_as_float(uint32_t(254 - be) << 23);
+}
+
+template <typename T>
+__device__ __forceinline__ const T* operand_ptr(int kind, int32_t ref, const int8_t* sel, int obits,
+                                                T* arena_g, const T* consts, const uint32_t* syn) {
+  if (kind == OP_ARENA) return arena_g + ref;
+  int v = 0;
+#pragma unroll
+  for (int i = 0; i < kMaxSel; ++i)
+    if (sel[i] >= 0) v |= syn_bit(syn, sel[i]) << i;
+  return consts + ref + (int64_t(v) << obits);
+}
+
+__device__ __forceinline__ int perm_addr(const int32_t* __restrict__ perm, int e, int lw) {
+  int addr = 0;
+  int tab = 0;
+  for (int sh = 0; sh < lw; sh += 8) {
+    const int cb = lw - sh < 8 ? lw - sh : 8;
+    addr |= __ldg(perm + tab + ((e >> sh) & ((1 << cb) - 1)));
+    tab += 1 << cb;
+  }
+  return addr;
+}
+
+template <typename T, bool NORM, bool APAR, bool BPAR>
+__device__ void run_step(const KArgs& a, const StepDesc& d, int st, const uint32_t* s_syn,
+                         uint32_t* s_max, T* arena, const T* consts) {
+  const int lw = d.lh + d.lfa + d.lfb;
+  const int total = 1 << (lw + a.lg);
+  const int total_r = (total + 31) & ~31;
+  const int mfb = (1 << d.lfb) - 1;
+  const int mfa = (1 << d.lfa) - 1;
+  const int mw = (1 << lw) - 1;
+  const int K = 1 << d.lk;
+  const int abits = d.lh + d.lfa + d.lk;
+  const int bbits = d.lh + d.lk + d.lfb;
+  for (int i = threadIdx.x; i < total_r; i += blockDim.x) {
+    const bool valid = i < total;
+    const int g = valid ? (i >> lw) : 0;
+    const int e = i & mw;
+    T acc = T(0);
+    if (valid) {
+      const uint32_t* syn = s_syn + g * a.syn_words;
+      T* arena_g = arena + int64_t(g) * a.arena_elems;
+      const int fb = e & mfb;
+      const int fa = (e >> d.lfb) & mfa;
+      const int h = e >> (d.lfb + d.lfa);
+      const int abase = ((h << d.lfa) | fa) << d.lk;
+      const int bbase = (h << (d.lk + d.lfb)) | fb;
+      const T* ap = nullptr;
+      const T* bp = nullptr;
+      int as = 0, bs = 0;
+      if (APAR) as = syn_bit(syn, d.a_ref);
+      else ap = operand_ptr<T>(d.a_kind, d.a_ref, d.a_sel, abits, arena_g, consts, syn);
+      if (BPAR) bs = syn_bit(syn, d.b_ref);
+      else bp = operand_ptr<T>(d.b_kind, d.b_ref, d.b_sel, bbits, arena_g, consts, syn);
+      T fa_s = T(1), fb_s = T(1);
+      if (NORM) {
+        int ee;
+        if (!APAR && d.a_kind == OP_ARENA) fa_s = T(norm_factor(s_max[g * a.n_steps + d.a_prod], &ee));
+        if (!BPAR && d.b_kind == OP_ARENA) fb_s = T(norm_factor(s_max[g * a.n_steps + d.b_prod], &ee));
+      }
+      if (APAR && BPAR) {
+        for (int k = 0; k < K; ++k)
+          acc += parity_val<T>(abase + k, as) * parity_val<T>(bbase + (k << d.lfb), bs);
+      } else if (APAR) {
+        for (int k = 0; k < K; ++k)
+          if (parity_val<T>(abase + k, as) != T(0)) acc += bp[bbase + (k << d.lfb)];
+      } else if (BPAR) {
+        for (int k = 0; k < K; ++k)
+          if (parity_val<T>(bbase + (k << d.lfb), bs) != T(0)) acc += ap[abase + k];
+        if (NORM) acc *= fa_s;
+      } else {
+        int k = 0;
+        for (; k + 4 <= K; k += 4) {
+          T a0 = ap[abase + k], a1 = ap[abase + k + 1], a2 = ap[abase + k + 2], a3 = ap[abase + k + 3];
+          if (NORM) { a0 *= fa_s; a1 *= fa_s; a2 *= fa_s; a3 *= fa_s; }
+          acc = fma(a0, bp[bbase + (k << d.lfb)], acc);
+          acc = fma(a1, bp[bbase + ((k + 1) << d.lfb)], acc);
+          acc = fma(a2, bp[bbase + ((k + 2) << d.lfb)], acc);
+          acc = fma(a3, bp[bbase + ((k + 3) << d.lfb)], acc);
+        }
+        for (; k < K; ++k) {
+          T a0 = ap[abase + k];
+          if (NORM) a0 *= fa_s;
+          acc = fma(a0, bp[bbase + (k << d.lfb)], acc);
+        }
+      }
+      if (NORM && !BPAR) acc *= fb_s;
+      const int addr = d.perm_off < 0 ? e : perm_addr(a.perm + d.perm_off, e, lw);
+      arena_g[d.out_off + addr] = acc;
+    }
+    if (NORM) {
+      uint32_t bits = __float_as_uint(float(acc));
+      const int seg = lw >= 5 ? 32 : (1 << lw);
+      for (int o = 1; o < seg; o <<= 1) {
+        uint32_t other = __shfl_xor_sync(0xffffffffu, bits, o);
+        bits = other > bits ? other : bits;
+      }
+      if (valid && (threadIdx.x & (seg - 1)) == 0) atomicMax(&s_max[g * a.n_steps + st], bits);
+    }
+  }
+}
+
+template <typename T, bool NORM>
+__global__ void __launch_bounds__(512) tn_contract_kernel(KArgs a) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  StepDesc* s_steps = reinterpret_cast<StepDesc*>(smem);
+  size_t off = size_t(a.n_steps) * sizeof(StepDesc);
+  uint32_t* s_syn = reinterpret_cast<uint32_t*>(smem + off);
+  off += size_t(a.G) * a.syn_words * 4;
+  uint32_t* s_max = reinterpret_cast<uint32_t*>(smem + off);
+  if (NORM) off += size_t(a.G) * a.n_steps * 4;
+  off = (off + 15) & ~size_t(15);
+  T* arena = a.arena_global
+                 ? reinterpret_cast<T*>(a.arena_global) + int64_t(blockIdx.x) * a.G * a.arena_elems
+                 : reinterpret_cast<T*>(smem + off);
+  const T* consts = reinterpret_cast<const T*>(a.consts);
+  {
+    const int4* src = reinterpret_cast<const int4*>(a.steps);
+    int4* dst = reinterpret_cast<int4*>(s_steps);
+    for (int i = threadIdx.x; i < a.n_steps * int(sizeof(StepDesc) / 16); i += blockDim.x) dst[i] = src[i];
+  }
+  const int64_t nrows = a.list ? int64_t(*a.list_count) : a.n;
+  for (int64_t base = int64_t(blockIdx.x) * a.G; base < nrows; base += int64_t(gridDim.x) * a.G) {
+    for (int i = threadIdx.x; i < a.G * a.syn_words; i += blockDim.x) {
+      const int g = i / a.syn_words, w = i - g * a.syn_words;
+      const int64_t r = base + g;
+      uint32_t word = 0;
+      if (r < nrows) {
+        const int64_t row = a.list ? int64_t(a.list[r]) : r + a.row_offset;
+        const uint8_t* p = a.syn + row * a.syn_bytes;
+        for (int b = 0; b < 4; ++b) {
+          const int byte = 4 * w + b;
+          if (byte < a.syn_bytes) word |= uint32_t(p[byte]) << (8 * b);
+        }
+      }
+      s_syn[i] = word;
+    }
+    if (NORM)
+      for (int i = threadIdx.x; i < a.G * a.n_steps; i += blockDim.x) s_max[i] = 0u;
+    __syncthreads();
+    for (int st = 0; st < a.n_steps; ++st) {
+      const StepDesc& d = s_steps[st];
+      const bool ap = d.a_kind == OP_PARITY, bp = d.b_kind == OP_PARITY;
+      if (ap && bp) run_step<T, NORM, true, true>(a, d, st, s_syn, s_max, arena, consts);
+      else if (ap) run_step<T, NORM, true, false>(a, d, st, s_syn, s_max, arena, consts);
+      else if (bp) run_step<T, NORM, false, true>(a, d, st, s_syn, s_max, arena, consts);
+      else run_step<T, NORM, false, false>(a, d, st, s_syn, s_max, arena, consts);
+      __syncthreads();
+    }
+    // epilogue: log-marginals, first argmax (Julia findmax order), recheck flag
+    const StepDesc& root = s_steps[a.n_steps - 1];
+    for (int g = threadIdx.x; g < a.G; g += blockDim.x) {
+      const int64_t r = base + g;
+      if (r >= nrows) continue;
+      const int64_t row = a.list ? int64_t(a.list[r]) : r + a.row_offset;
+      const T* rv = arena + int64_t(g) * a.arena_elems + root.out_off;
+      double lsc = 0.0;
+      if (NORM) {
+        for (int st = 0; st < a.n_steps - 1; ++st) {
+          int ee;
+          norm_factor(s_max[g * a.n_steps + st], &ee);
+          lsc += double(ee);
+        }
+        lsc *= 0.69314718055994530942;
+      }
+      double best = -INFINITY, second = -INFINITY;
+      int bc = 0;
+      for (int c = 0; c < a.n_classes; ++c) {
+        const double v = double(rv[c]);
+        const double lp = v > 0.0 ? log(v) + lsc : -INFINITY;
+        if (a.logp_out) a.logp_out[row * a.n_classes + c] = lp;
+        if (lp > best) {
+          second = best;
+          best = lp;
+          bc = c;
+        } else if (lp > second) {
+          second = lp;
+        }
+      }
+      if (a.class_out) a.class_out[row] = bc;
+      if (a.err_out) a.err_out[row] = a.err_bound;
+      if (a.recheck_margin >= 0.0) {
+        const double margin = best - second;
+        if (!(margin >= a.recheck_margin) || best == -INFINITY) {
+          const int slot = atomicAdd(a.recheck_count, 1);
+          a.recheck_list[slot] = int32_t(row);
+        }
+      }
+    }
+    __syncthreads();
+  }
+}
+
+}  // namespace
+
+size_t contract_smem_bytes(int precision, int32_t n_steps, int32_t syn_words, int G,
+                           int64_t arena_elems, bool arena_in_smem) {
+  const bool norm = precision == 1;
+  size_t off = size_t(n_steps) * sizeof(StepDesc) + size_t(G) * syn_words * 4;
+  if (norm) off += size_t(G) * n_steps * 4;
+  off = (off + 15) & ~size_t(15);
+  if (arena_in_smem) off += size_t(G) * size_t(arena_elems) * (precision == 1 ? 4 : 8);
+  return off;
+}
+
+size_t contract_smem_limit(int device) {
+  int v = 0;
+  if (cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, device) != cudaSuccess) return 48 * 1024;
+  return size_t(v);
+}
+
+int contract_occupancy(int precision, int threads, size_t smem) {
+  int blocks = 0;
+  cudaError_t e;
+  if (precision == 1) {
+    cudaFuncSetAttribute(tn_contract_kernel<float, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, tn_contract_kernel<float, true>, threads, smem);
+  } else {
+    cudaFuncSetAttribute(tn_contract_kernel<double, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, tn_contract_kernel<double, false>, threads, smem);
+  }
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  return blocks;
+}
+
+cudaError_t contract_launch(int precision, const KArgs& a, int grid, int threads, size_t smem,
+                            cudaStream_t stream) {
+  if (precision == 1) {
+    cudaError_t e = cudaFuncSetAttribute(tn_contract_kernel<float, true>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+    if (e != cudaSuccess) return e;
+    tn_contract_kernel<float, true><<<grid, threads, smem, stream>>>(a);
+  } else {
+    cudaError_t e = cudaFuncSetAttribute(tn_contract_kernel<double, false>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+    if (e != cudaSuccess) return e;
+    tn_contract_kernel<double, false><<<grid, threads, smem, stream>>>(a);
+  }
+  return cudaGetLastError();
+}
+
+}  // namespace tqec

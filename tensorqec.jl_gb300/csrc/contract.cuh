@@ -1,0 +1,53 @@
+// contract.cuh -- launch interface of the batched tensor-network contraction.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "plan.h"
+
+namespace tqec {
+
+// Everything one launch of the contraction kernel needs.  Rows are syndromes;
+// with `list` set, the kernel decodes rows list[0..*list_count) instead of
+// rows row_offset .. row_offset + n.
+struct KArgs {
+  const StepDesc* steps;
+  int32_t n_steps;
+  const int32_t* perm;
+  const void* consts;  // float or double, matching the kernel
+  const uint8_t* syn;
+  int32_t syn_bytes;
+  int32_t syn_words;  // 32-bit words per syndrome in shared memory (>= 1)
+  int64_t n;
+  int64_t row_offset;
+  const int32_t* list;
+  const int32_t* list_count;
+  int32_t G, lg;  // syndromes per block and log2(G)
+  int64_t arena_elems;
+  void* arena_global;  // NULL: arena in shared memory
+  int32_t n_classes;
+  int32_t* class_out;
+  double* logp_out;
+  float* err_out;
+  float err_bound;
+  double recheck_margin;  // < 0: never flag
+  int32_t* recheck_list;
+  int32_t* recheck_count;
+};
+
+// Shared memory a launch needs (bytes).
+size_t contract_smem_bytes(int precision, int32_t n_steps, int32_t syn_words, int G,
+                           int64_t arena_elems, bool arena_in_smem);
+
+// Largest dynamic shared memory a block may use on this device.
+size_t contract_smem_limit(int device);
+
+// Resident blocks per SM for a launch shape (0 if it cannot launch).
+int contract_occupancy(int precision, int threads, size_t smem);
+
+cudaError_t contract_launch(int precision, const KArgs& a, int grid, int threads, size_t smem,
+                            cudaStream_t stream);
+
+}  // namespace tqec

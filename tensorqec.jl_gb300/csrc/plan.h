@@ -1,0 +1,85 @@
+// plan.h -- the contraction program a network + tree compiles into.
+//
+// A program is a list of runtime steps over one syndrome's "arena" (its
+// working set).  Every step is a batched product with binary dimensions
+//     C[h, fa, fb] = sum_k A[h, fa, k] * B[h, k, fb]
+// where h are labels shared by both operands and still needed later, k are
+// labels shared and summed here, fa / fb are labels of only one operand.
+// Operand layouts are chosen top-down so that every operand is stored in
+// exactly the order its consumer reads ([h][fa][k] for A, [h][k][fb] for B);
+// a step writes its output through a bit-permutation table into the layout
+// its own consumer wants.  Leaves that do not depend on the syndrome are
+// folded on the host; leaves that depend on a few syndrome bits are kept as
+// small lookup tables ("select" operands) or, for parity checks, evaluated
+// from the index bits.
+#pragma once
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+namespace tqec {
+
+enum OperandKind : int32_t {
+  OP_ARENA = 0,   // a runtime intermediate in the syndrome's arena
+  OP_CONST = 1,   // constant data, optionally one of 2^m variants chosen by
+                  // m syndrome bits (sel[])
+  OP_PARITY = 2,  // 1 where popcount(index) has the parity of syndrome bit ref
+};
+
+constexpr int kMaxSel = 4;
+
+struct StepDesc {
+  int32_t a_kind, b_kind;
+  int32_t a_ref, b_ref;      // arena offset | const offset | syndrome bit
+  int32_t a_prod, b_prod;    // runtime step producing an arena operand, else -1
+  int8_t a_sel[kMaxSel];     // syndrome bits choosing the const variant (-1: unused)
+  int8_t b_sel[kMaxSel];
+  int32_t lh, lfa, lfb, lk;  // log2 sizes of the index groups
+  int32_t out_off;           // arena offset of the output
+  int32_t perm_off;          // output permutation tables, -1 = identity
+  int32_t pad0, pad1;
+};
+static_assert(sizeof(StepDesc) == 64, "StepDesc is 64 bytes");
+
+struct Plan {
+  int32_t n_syndrome = 0;
+  int32_t syndrome_bytes = 0;
+  int32_t n_out = 0;
+  int32_t n_classes = 1;
+  int32_t n_tree_steps = 0;
+  int32_t width = 0;               // log2 of the widest runtime intermediate
+  int64_t arena_elems = 0;         // per syndrome
+  int32_t root_step = -1;          // the last runtime step
+  double macs_runtime = 0.0;       // multiply-adds per syndrome, runtime steps
+  double macs_tree = 0.0;          // multiply-adds of the tree as given
+  double err_terms = 0.0;          // sum over runtime steps of (K + 1) plus leaves
+  std::vector<StepDesc> steps;
+  std::vector<int32_t> perm;       // concatenated permutation tables
+  std::vector<double> consts;      // constant operand data (all variants)
+};
+
+struct NetworkView {
+  int32_t n_tensors;
+  const int32_t* ix_offsets;
+  const int32_t* ix_labels;
+  const int64_t* data_offsets;
+  const double* data;
+  int32_t n_out;
+  const int32_t* out_labels;
+  int32_t n_syndrome;
+  const int32_t* syndrome_tensors;
+};
+
+struct PlanLimits {
+  int max_sel_bits = 2;       // fold syndrome-dependent leaves up to this many bits
+  int max_sel_rank = 8;       // ... and up to this many labels
+  int max_width = 30;         // refuse intermediates wider than 2^max_width
+};
+
+// Builds the program; returns "" on success or an error message.
+// *unsupported is set when the network is valid but outside the kernels' scope.
+std::string build_plan(const NetworkView& net, int32_t n_steps, const int32_t* steps,
+                       const PlanLimits& lim, Plan* out, bool* unsupported);
+
+}  // namespace tqec

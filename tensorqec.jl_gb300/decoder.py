@@ -1,0 +1,293 @@
+"""The decoder API: TNMMAP / compile / decode, as in TensorQEC
+(src/decoding/interfaces.jl:58-105, src/decoding/tndecoder.jl:59-271).
+
+``compile`` builds the reference's factor graph on the host, finds a
+contraction order (the role of OMEinsum's ``optimize_code``) and hands both to
+the native library, which plans and owns the GPU program.  ``decode`` then
+contracts on the GPU; batched calls (``decode_batch``, ``class_logprobs``)
+push thousands of syndromes through one launch.
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import gf2, native
+from .codes import CSSTannerGraph, SimpleTannerGraph
+from .dem import DetectorErrorModel, dem2tanner, logical_map
+from .error_model import (CSSErrorPattern, CSSSyndrome, DecodingResult, IndependentDepolarizingError,
+                          SimpleSyndrome, iid_error, pack_syndromes)
+from .network import FactorGraph, tnmmap_css_graph, tnmmap_dem_graph
+
+
+# ---------------------------------------------------------------------------
+# contraction-order optimisers (stand-ins for OMEinsum's CodeOptimizer)
+# ---------------------------------------------------------------------------
+
+
+@dataclass
+class TreeSA:
+    """Randomised greedy passes refined by simulated annealing over tree
+    rotations (our own search; OMEinsum's TreeSA plays this role in the
+    reference, tndecoder.jl:78)."""
+    trials: int = 16
+    sweeps: int = 1000
+    target_width: int = 0
+    width_penalty: float = 1.0
+    seed: int = 1
+
+
+@dataclass
+class GreedyMethod:
+    trials: int = 1
+    seed: int = 1
+
+
+@dataclass
+class NoOptimizer:
+    """tndecoder.jl:64: contract the tensors left to right."""
+
+
+def optimize_code(graph: FactorGraph, optimizer) -> np.ndarray:
+    """Returns the tree as an (n_tensors - 1, 2) array of node ids."""
+    n = graph.n_tensors
+    if isinstance(optimizer, NoOptimizer) or n == 1:
+        steps = np.zeros((max(n - 1, 0), 2), dtype=np.int32)
+        acc = 0
+        for i in range(1, n):
+            steps[i - 1] = (acc, i)
+            acc = n + i - 1
+        return steps
+    if isinstance(optimizer, GreedyMethod):
+        steps, _, _ = native.optimize_order(graph, trials=optimizer.trials, sweeps=0, seed=optimizer.seed)
+        return steps
+    if isinstance(optimizer, TreeSA):
+        steps, _, _ = native.optimize_order(graph, trials=optimizer.trials, sweeps=optimizer.sweeps,
+                                            target_width=optimizer.target_width,
+                                            width_penalty=optimizer.width_penalty, seed=optimizer.seed)
+        return steps
+    raise TypeError(f"unknown optimizer {optimizer!r}")
+
+
+# ---------------------------------------------------------------------------
+# decoders
+# ---------------------------------------------------------------------------
+
+
+@dataclass
+class TNMMAP:
+    """Marginal-MAP decoder over logical classes (tndecoder.jl:77-80).
+
+    ``precision``: "f64" contracts in float64 (the reference's arithmetic);
+    "f32" contracts in float32 with power-of-two renormalisation and
+    re-contracts in float64 every syndrome whose class margin is below the
+    rounding-error bound.  ``plain`` launches one syndrome at a time (the
+    drop-in form of the reference's per-syndrome ``decode``)."""
+    optimizer: object = field(default_factory=TreeSA)
+    factorize: bool = True
+    precision: str = "f32"
+    plain: bool = False
+    margin: float = -1.0
+    device: int = 0
+    group: int = 0
+    threads: int = 0
+
+    def _native_precision(self):
+        return {"f64": native.TQEC_F64, "f32": native.TQEC_F32}[self.precision]
+
+    def _flags(self):
+        return native.TQEC_FLAG_PLAIN if self.plain else 0
+
+
+class CompiledTNMMAP:
+    """CompiledTNMMAP (tndecoder.jl:85-92) with its GPU program."""
+
+    def __init__(self, decoder: TNMMAP, tanner: CSSTannerGraph, em: IndependentDepolarizingError):
+        self.decoder = decoder
+        self.tanner = tanner
+        self.em = em
+        self.lx, self.lz = gf2.logical_operator(tanner)
+        self.graph = tnmmap_css_graph(tanner, em, self.lx, self.lz)
+        self.steps = optimize_code(self.graph, decoder.optimizer)
+        self.program = native.Program(self.graph, self.steps, decoder._native_precision(), decoder._flags(),
+                                      decoder.device, decoder.group, decoder.threads, decoder.margin)
+        self._px = gf2.solve_particular(tanner.stgz.H)   # ex from sz
+        self._pz = gf2.solve_particular(tanner.stgx.H)   # ez from sx
+        self.k = self.lx.shape[0]
+
+    @property
+    def n_syndrome(self):
+        return self.tanner.ns
+
+    @property
+    def n_classes(self):
+        return self.program.n_classes
+
+    def _bits(self, syndromes):
+        if isinstance(syndromes, CSSSyndrome):
+            return syndromes.bits()[None, :]
+        if isinstance(syndromes, (list, tuple)) and syndromes and isinstance(syndromes[0], CSSSyndrome):
+            return np.stack([s.bits() for s in syndromes])
+        if isinstance(syndromes, CSSSyndrome.__mro__[0]):
+            return syndromes.bits()[None, :]
+        b = np.asarray(syndromes, dtype=np.uint8)
+        return np.atleast_2d(b) & 1
+
+    def decode_batch(self, syndromes, return_logp=False):
+        """Argmax classes (Julia linear index of ``mar``) for a batch of
+        syndrome rows ([sx..., sz...] bits)."""
+        packed = pack_syndromes(self._bits(syndromes))
+        n = packed.shape[0]
+        logp = np.empty((n, self.n_classes), dtype=np.float64) if return_logp else None
+        cls = self.program.decode_packed(packed, logp=logp)
+        return (cls, logp) if return_logp else cls
+
+    def class_logprobs(self, syndromes, precision=None):
+        """Natural log of the unnormalised marginal ``mar`` for each syndrome
+        (Julia linear order), contracted in the given precision."""
+        packed = pack_syndromes(self._bits(syndromes))
+        prec = self.decoder._native_precision() if precision is None else \
+            {"f64": native.TQEC_F64, "f32": native.TQEC_F32}[precision]
+        return self.program.contract_packed(packed, prec)
+
+    def error_pattern(self, cls: int, syndrome: CSSSyndrome):
+        """error_pattern(pos, ct, syndrome), tndecoder.jl:167-174, with a
+        GF(2) particular solution in place of the integer program
+        (ipdecoder.jl:150-169).  Returns None for a syndrome no error
+        produces."""
+        ex = self._px(np.asarray(syndrome.sz))
+        ez = self._pz(np.asarray(syndrome.sx))
+        if ex is None or ez is None:
+            return None
+        k = self.k
+        for i in range(k):
+            a_i = (cls >> i) & 1
+            b_i = (cls >> (k + i)) & 1
+            if int(self.lz[i].astype(np.int64) @ ex) % 2 != b_i:
+                ex = ex ^ self.lx[i]
+            if int(self.lx[i].astype(np.int64) @ ez) % 2 != a_i:
+                ez = ez ^ self.lz[i]
+        return CSSErrorPattern(ex, ez)
+
+    def decode(self, syndrome: CSSSyndrome) -> DecodingResult:
+        """decode(ct, syndrome), tndecoder.jl:160-165."""
+        cls = int(self.decode_batch(syndrome)[0])
+        ep = self.error_pattern(cls, syndrome)
+        return DecodingResult(ep is not None, ep)
+
+    def close(self):
+        self.program.close()
+
+
+class CompiledDEMTNMMAP:
+    """CompiledDEMTNMMAP (tndecoder.jl:176-182) with its GPU program."""
+
+    def __init__(self, decoder: TNMMAP, dem: DetectorErrorModel):
+        self.decoder = decoder
+        self.dem = dem
+        self.tanner = dem2tanner(dem)
+        self.l2q = logical_map(dem)
+        self.graph = tnmmap_dem_graph(self.tanner, self.l2q, dem.error_rates, len(dem.logical_list),
+                                      decoder.factorize)
+        self.steps = optimize_code(self.graph, decoder.optimizer)
+        self.program = native.Program(self.graph, self.steps, decoder._native_precision(), decoder._flags(),
+                                      decoder.device, decoder.group, decoder.threads, decoder.margin)
+        self._part = gf2.solve_particular(self.tanner.H)
+        self._logical_fix = self._logical_corrections()
+
+    def _logical_corrections(self):
+        """For each logical i, a set of mechanisms that flips no detector and
+        only logical i (None if the model has none)."""
+        nq = self.tanner.nq
+        L = np.zeros((len(self.l2q), nq), dtype=np.uint8)
+        for i, l in enumerate(self.l2q):
+            L[i, np.array(l, dtype=np.int64) - 1] = 1
+        A = np.vstack([self.tanner.H, L]) if L.size else self.tanner.H
+        solve = gf2.solve_particular(A)
+        out = []
+        for i in range(L.shape[0]):
+            rhs = np.zeros(A.shape[0], dtype=np.uint8)
+            rhs[self.tanner.ns + i] = 1
+            out.append(solve(rhs))
+        return out
+
+    @property
+    def n_syndrome(self):
+        return self.tanner.ns
+
+    @property
+    def n_classes(self):
+        return self.program.n_classes
+
+    def decode_batch(self, syndromes, return_logp=False):
+        bits = np.atleast_2d(np.asarray(syndromes, dtype=np.uint8)) & 1
+        packed = pack_syndromes(bits)
+        n = packed.shape[0]
+        logp = np.empty((n, self.n_classes), dtype=np.float64) if return_logp else None
+        cls = self.program.decode_packed(packed, logp=logp)
+        return (cls, logp) if return_logp else cls
+
+    def class_logprobs(self, syndromes, precision=None):
+        packed = pack_syndromes(np.atleast_2d(np.asarray(syndromes, dtype=np.uint8)) & 1)
+        prec = self.decoder._native_precision() if precision is None else \
+            {"f64": native.TQEC_F64, "f32": native.TQEC_F32}[precision]
+        return self.program.contract_packed(packed, prec)
+
+    def error_pattern(self, cls: int, syndrome: SimpleSyndrome):
+        """error_pattern(pos, ct, syndrome), tndecoder.jl:255-271: a
+        syndrome-consistent error whose logical flips equal the decoded
+        class.  Where the reference flips every mechanism of a logical, this
+        applies a detector-neutral correction of that logical instead, so the
+        pattern keeps reproducing the syndrome."""
+        ep = self._part(np.asarray(syndrome.s))
+        if ep is None:
+            return None
+        for i, l in enumerate(self.l2q):
+            idx = np.array(l, dtype=np.int64) - 1
+            par = int(ep[idx].sum()) % 2
+            want = (cls >> i) & 1
+            if par != want:
+                fix = self._logical_fix[i]
+                if fix is None:
+                    ep[idx] ^= 1
+                else:
+                    ep = ep ^ fix
+        return ep
+
+    def decode(self, syndrome: SimpleSyndrome) -> DecodingResult:
+        cls = int(self.decode_batch(np.asarray(syndrome.s)[None, :])[0])
+        ep = self.error_pattern(cls, syndrome)
+        return DecodingResult(ep is not None, ep)
+
+    def close(self):
+        self.program.close()
+
+
+def compile(decoder, problem, em=None):
+    """compile(decoder, tanner[, em]) / compile(decoder, dem)
+    (interfaces.jl:74-79, tndecoder.jl:97, :186).  Without ``em`` a CSS code
+    gets the reference's default ``iid_error(0.05, tanner)``."""
+    if not isinstance(decoder, TNMMAP):
+        raise TypeError("compile supports TNMMAP")
+    if isinstance(problem, DetectorErrorModel):
+        return CompiledDEMTNMMAP(decoder, problem)
+    if isinstance(problem, CSSTannerGraph):
+        if em is None:
+            em = iid_error(0.05, problem)
+        return CompiledTNMMAP(decoder, problem, em)
+    raise TypeError(f"cannot compile for {type(problem).__name__}")
+
+
+def decode(ct_or_decoder, *args):
+    """decode(ct, syndrome) or decode(decoder, tanner, syndrome[, em])
+    (interfaces.jl:96-105)."""
+    if isinstance(ct_or_decoder, (CompiledTNMMAP, CompiledDEMTNMMAP)):
+        return ct_or_decoder.decode(*args)
+    decoder, tanner, syndrome = ct_or_decoder, args[0], args[1]
+    em = args[2] if len(args) > 2 else None
+    ct = compile(decoder, tanner, em)
+    try:
+        return ct.decode(syndrome)
+    finally:
+        ct.close()

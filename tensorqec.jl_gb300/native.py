@@ -1,0 +1,246 @@
+"""ctypes binding of ``libtqec_gb300.so`` (declared in include/tqec_gb300.h).
+
+The library is the product: when it is missing the package raises instead
+of falling back to any other implementation.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libtqec_gb300.so")
+
+TQEC_OK = 0
+TQEC_F64 = 0
+TQEC_F32 = 1
+TQEC_FLAG_PLAIN = 1
+TQEC_FLAG_NORECHECK = 2
+
+ERRORS = {-1: "invalid argument", -2: "CUDA error", -3: "out of device memory",
+          -4: "unsupported network", -5: "timeout", -6: "I/O error"}
+
+
+class TqecError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"{ERRORS.get(code, code)}: {msg}")
+        self.code = code
+
+
+class Network(C.Structure):
+    _fields_ = [("n_tensors", C.c_int32), ("ix_offsets", C.c_void_p), ("ix_labels", C.c_void_p),
+                ("data_offsets", C.c_void_p), ("data", C.c_void_p), ("n_out", C.c_int32),
+                ("out_labels", C.c_void_p), ("n_syndrome", C.c_int32), ("syndrome_tensors", C.c_void_p)]
+
+
+class Tree(C.Structure):
+    _fields_ = [("n_steps", C.c_int32), ("steps", C.c_void_p)]
+
+
+class Options(C.Structure):
+    _fields_ = [("precision", C.c_int32), ("flags", C.c_uint32), ("device", C.c_int32),
+                ("group", C.c_int32), ("threads", C.c_int32), ("margin", C.c_double)]
+
+
+class ProgramInfo(C.Structure):
+    _fields_ = [("n_syndrome", C.c_int32), ("syndrome_bytes", C.c_int32), ("n_classes", C.c_int32),
+                ("n_steps", C.c_int32), ("n_tree_steps", C.c_int32), ("width", C.c_int32),
+                ("arena_elems", C.c_int64), ("flops_per_syndrome", C.c_double), ("flops_tree", C.c_double),
+                ("err_bound_f32", C.c_double), ("err_bound_f64", C.c_double),
+                ("group_f32", C.c_int32), ("threads_f32", C.c_int32), ("smem_f32", C.c_int32),
+                ("group_f64", C.c_int32), ("threads_f64", C.c_int32), ("smem_f64", C.c_int32)]
+
+
+class PlanView(C.Structure):
+    _fields_ = [("n_steps", C.c_int32), ("steps", C.c_void_p), ("n_perm", C.c_int64),
+                ("perm", C.c_void_p), ("n_consts", C.c_int64), ("consts", C.c_void_p),
+                ("arena_elems", C.c_int64), ("width", C.c_int32), ("n_classes", C.c_int32),
+                ("n_syndrome", C.c_int32), ("flops_per_syndrome", C.c_double), ("flops_tree", C.c_double),
+                ("err_terms", C.c_double)]
+
+
+class OrderOptions(C.Structure):
+    _fields_ = [("trials", C.c_int32), ("sweeps", C.c_int32), ("target_width", C.c_int32),
+                ("width_penalty", C.c_double), ("seed", C.c_uint64)]
+
+
+STEP_DTYPE = np.dtype([("a_kind", "<i4"), ("b_kind", "<i4"), ("a_ref", "<i4"), ("b_ref", "<i4"),
+                       ("a_prod", "<i4"), ("b_prod", "<i4"), ("a_sel", "i1", (4,)), ("b_sel", "i1", (4,)),
+                       ("lh", "<i4"), ("lfa", "<i4"), ("lfb", "<i4"), ("lk", "<i4"),
+                       ("out_off", "<i4"), ("perm_off", "<i4"), ("pad0", "<i4"), ("pad1", "<i4")])
+assert STEP_DTYPE.itemsize == 64
+
+_lib = None
+
+
+def lib():
+    """Loads the native library (built by build_native.build())."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise ImportError(f"{LIB_PATH} is missing: build it with build_native.build() "
+                          "(the decoder has no non-native implementation)")
+    L = C.CDLL(LIB_PATH)
+    vp, i32, i64 = C.c_void_p, C.c_int32, C.c_int64
+    sig = {
+        "tqec_program_create": [vp, vp, vp, vp],
+        "tqec_program_destroy": [vp],
+        "tqec_program_info": [vp, vp],
+        "tqec_decode_batch": [vp, vp, i64, vp, vp, vp, vp],
+        "tqec_contract_batch": [vp, vp, i64, i32, vp, vp],
+        "tqec_last_recheck_count": [vp, vp],
+        "tqec_program_autotune": [vp, i64],
+        "tqec_plan_inspect": [vp, vp, vp, vp],
+        "tqec_plan_release": [vp],
+        "tqec_optimize_order": [vp, vp, vp, vp, vp],
+        "tqec_last_error": [vp, C.c_size_t],
+    }
+    for name, args in sig.items():
+        f = getattr(L, name)
+        f.argtypes = args
+        f.restype = C.c_int
+    L.tqec_version.restype = C.c_char_p
+    L.tqec_version.argtypes = []
+    _lib = L
+    return L
+
+
+def last_error() -> str:
+    buf = C.create_string_buffer(1024)
+    lib().tqec_last_error(buf, 1024)
+    return buf.value.decode(errors="replace")
+
+
+def check(code):
+    if code != TQEC_OK:
+        raise TqecError(code, last_error())
+    return code
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+class NetworkArrays:
+    """Keeps the flattened network arrays alive while the struct is used."""
+
+    def __init__(self, graph):
+        (self.ix_off, self.labels, self.d_off, self.data, self.iy,
+         self.synd) = graph.flat()
+        self.struct = Network(len(graph.ixs), _ptr(self.ix_off), _ptr(self.labels), _ptr(self.d_off),
+                              _ptr(self.data), len(self.iy), _ptr(self.iy), len(self.synd), _ptr(self.synd))
+
+
+def optimize_order(graph, trials=32, sweeps=60, target_width=0, width_penalty=1.0, seed=1):
+    """Contraction order for a FactorGraph: an (n_tensors - 1, 2) int32 array
+    of node ids (tqec_tree convention), log2 of its multiply-adds and its
+    width."""
+    na = NetworkArrays(graph)
+    steps = np.zeros((max(graph.n_tensors - 1, 0), 2), dtype=np.int32)
+    lm = C.c_double(0)
+    w = C.c_int32(0)
+    o = OrderOptions(trials, sweeps, target_width, width_penalty, seed)
+    check(lib().tqec_optimize_order(C.byref(na.struct), C.byref(o), _ptr(steps), C.byref(lm), C.byref(w)))
+    return steps, lm.value, w.value
+
+
+def inspect_plan(graph, steps):
+    """The compiled program as numpy arrays (no GPU needed)."""
+    na = NetworkArrays(graph)
+    steps = np.ascontiguousarray(steps, dtype=np.int32)
+    tree = Tree(steps.shape[0], _ptr(steps))
+    view = PlanView()
+    h = C.c_void_p()
+    check(lib().tqec_plan_inspect(C.byref(na.struct), C.byref(tree), C.byref(view), C.byref(h)))
+    try:
+        st = np.frombuffer(C.string_at(view.steps, 64 * view.n_steps), dtype=STEP_DTYPE).copy()
+        perm = (np.frombuffer(C.string_at(view.perm, 4 * view.n_perm), dtype=np.int32).copy()
+                if view.n_perm else np.zeros(0, np.int32))
+        consts = (np.frombuffer(C.string_at(view.consts, 8 * view.n_consts), dtype=np.float64).copy()
+                  if view.n_consts else np.zeros(0))
+        return {"steps": st, "perm": perm, "consts": consts, "arena_elems": view.arena_elems,
+                "width": view.width, "n_classes": view.n_classes, "n_syndrome": view.n_syndrome,
+                "flops_per_syndrome": view.flops_per_syndrome, "flops_tree": view.flops_tree,
+                "err_terms": view.err_terms}
+    finally:
+        lib().tqec_plan_release(h)
+
+
+class Program:
+    """Owner of a ``tqec_program`` (a compiled network on one GPU)."""
+
+    def __init__(self, graph, steps, precision=TQEC_F32, flags=0, device=0, group=0, threads=0, margin=-1.0):
+        L = lib()
+        na = NetworkArrays(graph)
+        steps = np.ascontiguousarray(steps, dtype=np.int32)
+        tree = Tree(steps.shape[0], _ptr(steps))
+        opts = Options(precision, flags, device, group, threads, margin)
+        h = C.c_void_p()
+        check(L.tqec_program_create(C.byref(na.struct), C.byref(tree), C.byref(opts), C.byref(h)))
+        self._h = h
+        self.precision = precision
+        self.flags = flags
+        info = ProgramInfo()
+        check(L.tqec_program_info(self._h, C.byref(info)))
+        self.info = {f: getattr(info, f) for f, _ in ProgramInfo._fields_}
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().tqec_program_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def n_classes(self):
+        return self.info["n_classes"]
+
+    @property
+    def syndrome_bytes(self):
+        return self.info["syndrome_bytes"]
+
+    def decode_packed(self, packed, classes=None, logp=None, err=None, stream=None):
+        """Host numpy arrays in and out (copies inside the call)."""
+        packed = np.ascontiguousarray(packed, dtype=np.uint8)
+        n = packed.shape[0]
+        if classes is None:
+            classes = np.empty(n, dtype=np.int32)
+        check(lib().tqec_decode_batch(self._h, _ptr(packed), n, _ptr(classes), _ptr(logp), _ptr(err), stream))
+        return classes
+
+    def decode_ptrs(self, syn_ptr, n, cls_ptr, logp_ptr=None, err_ptr=None, stream=None):
+        """Raw (device or host) pointers, e.g. from torch tensors."""
+        check(lib().tqec_decode_batch(self._h, C.c_void_p(syn_ptr), n, C.c_void_p(cls_ptr),
+                                      C.c_void_p(logp_ptr) if logp_ptr else None,
+                                      C.c_void_p(err_ptr) if err_ptr else None,
+                                      C.c_void_p(stream) if stream else None))
+
+    def contract_packed(self, packed, precision, logp=None):
+        packed = np.ascontiguousarray(packed, dtype=np.uint8)
+        n = packed.shape[0]
+        if logp is None:
+            logp = np.empty((n, self.n_classes), dtype=np.float64)
+        check(lib().tqec_contract_batch(self._h, _ptr(packed), n, precision, _ptr(logp), None))
+        return logp
+
+    def contract_ptrs(self, syn_ptr, n, precision, logp_ptr, stream=None):
+        check(lib().tqec_contract_batch(self._h, C.c_void_p(syn_ptr), n, precision, C.c_void_p(logp_ptr),
+                                        C.c_void_p(stream) if stream else None))
+
+    def last_recheck_count(self):
+        c = C.c_int64(0)
+        check(lib().tqec_last_recheck_count(self._h, C.byref(c)))
+        return c.value
+
+    def autotune(self, n_probe=4096):
+        check(lib().tqec_program_autotune(self._h, n_probe))
+        info = ProgramInfo()
+        check(lib().tqec_program_info(self._h, C.byref(info)))
+        self.info = {f: getattr(info, f) for f, _ in ProgramInfo._fields_}

@@ -1,0 +1,129 @@
+"""Factor graphs of the TNMMAP decoder (TensorQEC's src/decoding/tndecoder.jl).
+
+A ``FactorGraph`` holds the reference's ``ixs`` (labels per tensor),
+``tensors`` (float64, flattened in Julia column-major order: the entry with
+index bits (x_0, ..., x_{r-1}) sits at offset sum_j x_j 2^j), the output
+labels ``iy`` and the positions of the one-hot syndrome leaves.
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass
+
+import numpy as np
+
+
+def parity_tensor(rank: int) -> np.ndarray:
+    """parity_check_matrix(rank - 1) (tndecoder.jl:42-44) flattened:
+    1 where the sum of the indices is even."""
+    idx = np.arange(1 << rank, dtype=np.int64)
+    pc = np.zeros_like(idx)
+    for b in range(rank):
+        pc += (idx >> b) & 1
+    return (1 - (pc & 1)).astype(np.float64)
+
+
+def parity_check_matrix(q: int) -> np.ndarray:
+    """The reference's ``parity_check_matrix(q)`` as a (2,)*(q+1) array
+    indexed [x_1, ..., x_{q+1}] (tndecoder.jl:42-44)."""
+    return parity_tensor(q + 1).reshape((2,) * (q + 1), order="F")
+
+
+@dataclass
+class FactorGraph:
+    ixs: list
+    tensors: list
+    iy: list
+    syndrome_positions: list
+
+    @property
+    def n_tensors(self):
+        return len(self.ixs)
+
+    def flat(self):
+        """The arrays of the native ``tqec_network`` struct."""
+        ix_off = np.zeros(len(self.ixs) + 1, dtype=np.int32)
+        ix_off[1:] = np.cumsum([len(ix) for ix in self.ixs])
+        labels = np.array([v for ix in self.ixs for v in ix], dtype=np.int32)
+        d_off = np.zeros(len(self.tensors) + 1, dtype=np.int64)
+        d_off[1:] = np.cumsum([t.size for t in self.tensors])
+        data = np.concatenate([np.asarray(t, dtype=np.float64).ravel() for t in self.tensors])
+        return (ix_off, labels, d_off, data, np.asarray(self.iy, dtype=np.int32),
+                np.asarray(self.syndrome_positions, dtype=np.int32))
+
+
+def tnmmap_css_graph(tanner, em, lx, lz) -> FactorGraph:
+    """compile(::TNMMAP, ::IndependentDepolarizingDecodingProblem),
+    tndecoder.jl:97-139.  Labels: xerr 1..nq, zerr nq+1..2nq, X-check
+    syndromes, Z-check syndromes, logical-x outputs, logical-z outputs."""
+    nq = tanner.nq
+    ns = tanner.ns
+    nsx = tanner.stgx.ns
+    k = lx.shape[0]
+    ixs, tensors = [], []
+    for i, c in enumerate(tanner.stgx.s2q, 1):
+        ixs.append([q + nq for q in c] + [i + 2 * nq])
+        tensors.append(parity_tensor(len(c) + 1))
+    for i, c in enumerate(tanner.stgz.s2q, 1):
+        ixs.append(list(c) + [i + 2 * nq + nsx])
+        tensors.append(parity_tensor(len(c) + 1))
+    for i in range(nq):
+        px, py, pz = float(em.px[i]), float(em.py[i]), float(em.pz[i])
+        ixs.append([i + 1, i + 1 + nq])
+        # [1-px-py-pz pz; px py] in column-major order
+        tensors.append(np.array([1 - px - py - pz, px, pz, py], dtype=np.float64))
+    for i in range(lz.shape[0]):
+        sup = [int(q) + 1 for q in np.flatnonzero(lz[i])]
+        ixs.append(sup + [i + 1 + 2 * nq + ns + lz.shape[0]])
+        tensors.append(parity_tensor(len(sup) + 1))
+    for i in range(k):
+        sup = [int(q) + 1 + nq for q in np.flatnonzero(lx[i])]
+        ixs.append(sup + [i + 1 + 2 * nq + ns])
+        tensors.append(parity_tensor(len(sup) + 1))
+    synd = []
+    for v in range(2 * nq + 1, 2 * nq + ns + 1):
+        synd.append(len(ixs))
+        ixs.append([v])
+        tensors.append(np.array([1.0, 0.0]))
+    iy = list(range(2 * nq + ns + 1, 2 * nq + ns + 2 * k + 1))
+    return FactorGraph(ixs, tensors, iy, synd)
+
+
+def push_check_node(ixs, tensors, c, node, nvars, factorize):
+    """tndecoder.jl:221-238: a parity check over bits c and label `node`,
+    optionally as a chain of rank-3 parity tensors over new labels."""
+    L = len(c)
+    if not factorize or L == 2:
+        ixs.append(list(c) + [node])
+        tensors.append(parity_tensor(L + 1))
+        return nvars
+    ixs.append([c[0], c[1], nvars + 1])
+    tensors.append(parity_tensor(3))
+    for j in range(3, L):
+        ixs.append([nvars + j - 1, c[j - 1], nvars + j - 2])
+        tensors.append(parity_tensor(3))
+    ixs.append([node, c[L - 1], nvars + L - 2])
+    tensors.append(parity_tensor(3))
+    return nvars + L - 2
+
+
+def tnmmap_dem_graph(tanner, l2q, error_rates, n_logicals, factorize=True) -> FactorGraph:
+    """compile(::TNMMAP, ::DetectorErrorModel), tndecoder.jl:186-212.
+    Labels: errors 1..nq, detectors nq+1..nq+ns, logicals, then chain
+    auxiliaries."""
+    nq, ns = tanner.nq, tanner.ns
+    nvars = nq + ns + n_logicals
+    iy = list(range(nq + ns + 1, nvars + 1))
+    ixs, tensors = [], []
+    for i, c in enumerate(tanner.s2q, 1):
+        nvars = push_check_node(ixs, tensors, c, i + nq, nvars, factorize)
+    for i, c in enumerate(l2q, 1):
+        nvars = push_check_node(ixs, tensors, c, i + nq + ns, nvars, factorize)
+    for i, p in enumerate(error_rates, 1):
+        ixs.append([i])
+        tensors.append(np.array([1 - p, p], dtype=np.float64))
+    synd = []
+    for v in range(nq + 1, nq + ns + 1):
+        synd.append(len(ixs))
+        ixs.append([v])
+        tensors.append(np.array([1.0, 0.0]))
+    return FactorGraph(ixs, tensors, iy, synd)

@@ -1,0 +1,191 @@
+"""GPU parity: the CUDA contraction against the oracle.
+
+Tolerances: float64 marginals within 1e-10 relative to the row maximum;
+float32 marginals within the program's stated rounding bound; decisions
+equal to the oracle's argmax except where the oracle's top two classes are
+within 1e-9 relative of each other (a tie that summation order decides).
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from conftest import gpu_available
+
+pytestmark = [pytest.mark.gpu, pytest.mark.skipif(not gpu_available(), reason="needs a CUDA GPU")]
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+TIE = 1e-9
+
+
+def assert_decisions(cls, want_mar):
+    want_mar = np.asarray(want_mar)
+    best = want_mar.argmax(axis=1)
+    srt = np.sort(want_mar, axis=1)
+    top, second = srt[:, -1], srt[:, -2]
+    tie = (top - second) <= TIE * np.maximum(top, 1e-300)
+    bad = (cls != best) & ~tie
+    assert not bad.any(), f"{bad.sum()} decision mismatches outside ties, rows {np.flatnonzero(bad)[:10]}"
+    # when the classes differ on a tie, the chosen class must be one of the tied maxima
+    ok = want_mar[np.arange(len(cls)), cls] >= top * (1 - 1e-9)
+    assert ok.all()
+
+
+def assert_marginals(logp, want_mar, rtol):
+    want_mar = np.asarray(want_mar)
+    got = np.exp(logp)
+    scale = want_mar.max(axis=1, keepdims=True)
+    err = np.abs(got - want_mar) / np.maximum(scale, 1e-300)
+    assert err.max() <= rtol, f"max relative error {err.max():.3e} > {rtol:.1e}"
+
+
+def css_case(pkg, oracle, kind, d, p, n, seed):
+    code = {"surface": lambda: pkg.SurfaceCode(d, d), "toric": lambda: pkg.ToricCode(d, d),
+            "488": lambda: pkg.Color488(d), "666": lambda: pkg.Color666(d)}[kind]()
+    t = pkg.tanner_graph(code)
+    em = pkg.depolarizing(p, t.nq)
+    rng = np.random.default_rng(seed)
+    ep = pkg.random_error_pattern(em, rng, nsamples=n)
+    syn = pkg.syndrome_extraction(ep, t)
+    bits = np.concatenate([syn.sx, syn.sz], axis=1)
+    if kind == "surface":
+        st, nq = oracle.surface_code_stabilizers(d, d)
+    elif kind == "toric":
+        st, nq = oracle.toric_code_stabilizers(d, d)
+    else:
+        st, nq = oracle.color_code_stabilizers(kind, d)
+    dec = oracle.OracleDecoder(oracle.css_tanner(st, nq), em.px, em.py, em.pz)
+    return t, em, bits, dec
+
+
+@pytest.fixture(scope="module")
+def d3(pkg, oracle):
+    t = pkg.tanner_graph(pkg.SurfaceCode(3, 3))
+    em = pkg.depolarizing(0.05, t.nq)
+    st, nq = oracle.surface_code_stabilizers(3, 3)
+    ot = oracle.css_tanner(st, nq)
+    lx, lz = oracle.logical_operator(ot)
+    brute = oracle.brute_force_marginals(ot, em.px, em.py, em.pz, lx, lz)
+    bits = ((np.arange(256)[:, None] >> np.arange(8)[None, :]) & 1).astype(np.uint8)
+    return t, em, bits, brute
+
+
+@pytest.mark.parametrize("precision,plain", [("f64", True), ("f64", False), ("f32", False)])
+def test_d3_every_syndrome_vs_enumeration(pkg, d3, precision, plain):
+    t, em, bits, brute = d3
+    ct = pkg.compile(pkg.TNMMAP(precision=precision, plain=plain), t, em)
+    cls, logp = ct.decode_batch(bits, return_logp=True)
+    assert_decisions(cls, brute)
+    if precision == "f64":
+        assert_marginals(logp, brute, 1e-10)
+    else:
+        lp64 = ct.class_logprobs(bits, precision="f64")
+        lp32 = ct.class_logprobs(bits, precision="f32")
+        assert_marginals(lp64, brute, 1e-10)
+        bound = ct.program.info["err_bound_f32"]
+        assert_marginals(lp32, brute, 2 * bound)
+    ct.close()
+
+
+def test_zero_syndrome_kat_on_gpu(pkg):
+    """test/decoding/tndecoder.jl:101-110 on the device."""
+    t = pkg.tanner_graph(pkg.SurfaceCode(3, 3))
+    ct = pkg.compile(pkg.TNMMAP(precision="f64", plain=True), t, pkg.iid_error(0.1, 0.0, 0.0, 9))
+    lp = ct.class_logprobs(np.zeros((1, 8), dtype=np.uint8))
+    np.testing.assert_allclose(np.exp(lp[0]), [0.3972875040000002, 0.0, 0.004284496000000001, 0.0],
+                               atol=1e-10)
+    ct.close()
+
+
+def test_decision_kat_x1_on_gpu(pkg):
+    """tndecoder.jl:60-73: X1 with px=0.1 decodes with no logical error and
+    the rebuilt pattern reproduces the syndrome."""
+    t = pkg.tanner_graph(pkg.SurfaceCode(3, 3))
+    em = pkg.iid_error(0.1, 0.0, 0.0, 9)
+    ct = pkg.compile(pkg.TNMMAP(precision="f64"), t, em)
+    ex = np.array([1, 0, 0, 0, 0, 0, 0, 0, 0], dtype=np.uint8)
+    truth = pkg.CSSErrorPattern(ex, np.zeros(9, np.uint8))
+    syn = pkg.syndrome_extraction(truth, t)
+    res = pkg.decode(ct, syn)
+    assert res.success_tag
+    assert not pkg.check_logical_error(res.error_pattern, truth, ct.lx, ct.lz)
+    assert pkg.syndrome_extraction(res.error_pattern, t) == syn
+    ct.close()
+
+
+@pytest.mark.parametrize("kind,d,p,n", [("surface", 5, 0.08, 400), ("surface", 7, 0.05, 48),
+                                        ("toric", 3, 0.05, 128), ("488", 5, 0.05, 128),
+                                        ("666", 5, 0.08, 128)])
+def test_css_codes_vs_oracle(pkg, oracle, kind, d, p, n):
+    t, em, bits, dec = css_case(pkg, oracle, kind, d, p, n, seed=100 + d)
+    want = dec.marginals(bits)
+    for precision in ("f64", "f32"):
+        ct = pkg.compile(pkg.TNMMAP(precision=precision), t, em)
+        cls, logp = ct.decode_batch(bits, return_logp=True)
+        assert_decisions(cls, want)
+        lp = ct.class_logprobs(bits)
+        tol = 1e-10 if precision == "f64" else 2 * ct.program.info["err_bound_f32"]
+        assert_marginals(lp, want, tol)
+        ct.close()
+
+
+def test_dem_every_syndrome_vs_oracle(pkg, oracle):
+    text = json.load(open(os.path.join(ROOT, "tests", "golden", "reference_kat.json")))["dem_small"]["text"]
+    dem = pkg.parse_dem_string(text)
+    bits = ((np.arange(64)[:, None] >> np.arange(6)[None, :]) & 1).astype(np.uint8)
+    want = oracle.OracleDEMDecoder(oracle.parse_dem_string(text)).marginals(bits)
+    for precision in ("f64", "f32"):
+        ct = pkg.compile(pkg.TNMMAP(precision=precision, factorize=True), dem)
+        cls, logp = ct.decode_batch(bits, return_logp=True)
+        assert_decisions(cls, want)
+        tol = 1e-10 if precision == "f64" else 2 * ct.program.info["err_bound_f32"]
+        assert_marginals(ct.class_logprobs(bits), want, tol)
+        for r in range(0, 64, 7):
+            res = ct.decode(pkg.SimpleSyndrome(bits[r]))
+            if res.success_tag:
+                s = pkg.syndrome_extraction(res.error_pattern, ct.tanner).s
+                assert np.array_equal(s, bits[r])
+        ct.close()
+
+
+def test_f32_recheck_decisions_equal_f64_at_scale(pkg):
+    """65,536 d=5 syndromes: float32 + recheck decides exactly like float64
+    wherever float64's margin exceeds the float64 bound."""
+    t = pkg.tanner_graph(pkg.SurfaceCode(5, 5))
+    em = pkg.depolarizing(0.11, t.nq)
+    rng = np.random.default_rng(5)
+    ep = pkg.random_error_pattern(em, rng, nsamples=65536)
+    syn = pkg.syndrome_extraction(ep, t)
+    bits = np.concatenate([syn.sx, syn.sz], axis=1)
+    ct = pkg.compile(pkg.TNMMAP(precision="f32"), t, em)
+    cls32 = ct.decode_batch(bits)
+    lp64 = ct.class_logprobs(bits, precision="f64")
+    cls64 = np.argmax(lp64, axis=1)
+    srt = np.sort(lp64, axis=1)
+    tie = (srt[:, -1] - srt[:, -2]) <= 1e-9
+    assert not ((cls32 != cls64) & ~tie).any()
+    n_re = ct.program.last_recheck_count()
+    assert 0 <= n_re < 65536 // 10
+    ct.close()
+
+
+def test_empty_batch_and_device_pointers(pkg):
+    torch = pytest.importorskip("torch")
+    t = pkg.tanner_graph(pkg.SurfaceCode(5, 5))
+    em = pkg.depolarizing(0.05, t.nq)
+    ct = pkg.compile(pkg.TNMMAP(precision="f32"), t, em)
+    assert ct.decode_batch(np.zeros((0, t.ns), np.uint8)).shape == (0,)
+    rng = np.random.default_rng(9)
+    ep = pkg.random_error_pattern(em, rng, nsamples=1000)
+    syn = pkg.syndrome_extraction(ep, t)
+    bits = np.concatenate([syn.sx, syn.sz], axis=1)
+    want = ct.decode_batch(bits)
+    d_syn = torch.from_numpy(pkg.pack_syndromes(bits)).cuda()
+    d_cls = torch.empty(1000, dtype=torch.int32, device="cuda")
+    d_lp = torch.empty((1000, 4), dtype=torch.float64, device="cuda")
+    stream = torch.cuda.current_stream().cuda_stream
+    ct.program.decode_ptrs(d_syn.data_ptr(), 1000, d_cls.data_ptr(), d_lp.data_ptr(), None, stream)
+    torch.cuda.synchronize()
+    assert np.array_equal(d_cls.cpu().numpy(), want)
+    ct.close()
