@@ -185,6 +185,47 @@ int tqec_optimize_order(const tqec_network* net, const tqec_order_options* opts,
                         int32_t* steps_out, double* log2_macs_out,
                         int32_t* width_out);
 
+/* ---- learned surrogate (no counterpart in the reference) -----------------
+ * A ReLU MLP over the syndrome bits proposes the logical class with a
+ * softmax confidence; tqec_gated_decode sends the rows below a confidence
+ * threshold to the exact contraction of a program.  Parameters are float32
+ * masters (bf16 copies feed the GEMMs, which accumulate in float32); layer l
+ * stores W[dout][din] row-major then b[dout], padded to 8 floats, where din
+ * of layer 0 is n_in rounded up to 64 (extra columns are zero). */
+typedef struct {
+  int32_t n_in;      /* syndrome bits */
+  int32_t hidden;    /* units per hidden layer (multiple of 32) */
+  int32_t n_layers;  /* linear layers (>= 2) */
+  int32_t n_out;     /* classes */
+  uint64_t seed;     /* initialisation seed */
+  int32_t device;
+} tqec_mlp_config;
+
+typedef struct tqec_mlp tqec_mlp;
+
+int tqec_mlp_create(const tqec_mlp_config* cfg, tqec_mlp** out);
+int tqec_mlp_destroy(tqec_mlp* mlp);
+int tqec_mlp_param_count(const tqec_mlp* mlp, int64_t* n);
+int tqec_mlp_get_params(tqec_mlp* mlp, float* out, int64_t n);
+int tqec_mlp_set_params(tqec_mlp* mlp, const float* in, int64_t n);
+/* Gradients of the mean soft-target cross-entropy (targets: n x n_out
+ * class probabilities) without updating the parameters. */
+int tqec_mlp_gradients(tqec_mlp* mlp, const uint8_t* syndromes, const float* targets, int64_t n,
+                       float* grads_out, float* loss_out);
+/* One Adam step (beta 0.9/0.999, eps 1e-8) on a batch; loss_out may be NULL. */
+int tqec_mlp_train_step(tqec_mlp* mlp, const uint8_t* syndromes, const float* targets, int64_t n,
+                        float lr, float* loss_out, void* stream);
+/* Argmax class and its softmax probability for each row. */
+int tqec_mlp_infer(tqec_mlp* mlp, const uint8_t* syndromes, int64_t n, int32_t* class_out,
+                   float* conf_out, void* stream);
+/* Surrogate first; rows with confidence < threshold are decoded by `prog`
+ * (tqec_decode_batch).  Writes the number of such rows. */
+int tqec_gated_decode(tqec_mlp* mlp, tqec_program* prog, float threshold, const uint8_t* syndromes,
+                      int64_t n, int32_t* class_out, int64_t* n_fallback_out, void* stream);
+/* Checkpoint: one JSON header line, then the float32 parameters. */
+int tqec_mlp_save(tqec_mlp* mlp, const char* path);
+int tqec_mlp_load(tqec_mlp* mlp, const char* path);
+
 /* Message of the calling thread's last failure (always NUL-terminated). */
 int tqec_last_error(char* buf, size_t len);
 

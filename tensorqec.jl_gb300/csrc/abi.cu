@@ -17,9 +17,16 @@
 #include "contract.cuh"
 #include "plan.h"
 
+namespace tqec {
+std::string& last_error_ref() {
+  thread_local std::string msg;
+  return msg;
+}
+}  // namespace tqec
+
 namespace {
 
-thread_local std::string g_last_error;
+#define g_last_error (tqec::last_error_ref())
 
 int fail(int code, const std::string& msg) {
   g_last_error = msg;
@@ -125,7 +132,9 @@ int choose_shape(tqec_program* p, int precision, int G_req, int threads_req, Sha
       G *= 2;
     s.G = G;
     s.smem_arena = tqec::contract_smem_bytes(precision, nsteps, sw, G, arena, true) <= limit;
-    if (!s.smem_arena) s.threads = threads_req > 0 ? threads_req : 512;
+    // one syndrome per block with a wide arena: use more threads per block
+    if (G == 1 && (!s.smem_arena || tqec::contract_smem_bytes(precision, nsteps, sw, 1, arena, true) > target))
+      s.threads = threads_req > 0 ? threads_req : 512;
     (void)esz;
   }
   s.smem = tqec::contract_smem_bytes(precision, nsteps, sw, s.G, arena, s.smem_arena);
@@ -483,6 +492,10 @@ int tqec_program_autotune(tqec_program* p, int64_t n_probe) {
       for (int th : {128, 256, 512}) {
         Shape s;
         if (choose_shape(p, prec, G, th, &s) != TQEC_OK) continue;
+        // a global arena bigger than 4 GB is not worth probing on a shared GPU
+        const size_t esz = prec == TQEC_F32 ? 4 : 8;
+        if (!s.smem_arena && (G > 8 || size_t(s.grid_cap) * G * size_t(p->plan.arena_elems) * esz > (size_t(4) << 30)))
+          continue;
         p->shape[prec] = s;
         tqec::KArgs a = base_args(p, prec);
         a.syn = (const uint8_t*)p->syn.p;

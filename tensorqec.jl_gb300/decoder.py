@@ -36,6 +36,7 @@ class TreeSA:
     target_width: int = 0
     width_penalty: float = 1.0
     seed: int = 1
+    restarts: int = 4
 
 
 @dataclass
@@ -63,11 +64,44 @@ def optimize_code(graph: FactorGraph, optimizer) -> np.ndarray:
         steps, _, _ = native.optimize_order(graph, trials=optimizer.trials, sweeps=0, seed=optimizer.seed)
         return steps
     if isinstance(optimizer, TreeSA):
-        steps, _, _ = native.optimize_order(graph, trials=optimizer.trials, sweeps=optimizer.sweeps,
-                                            target_width=optimizer.target_width,
-                                            width_penalty=optimizer.width_penalty, seed=optimizer.seed)
-        return steps
+        if optimizer.target_width or optimizer.restarts <= 1:
+            steps, _, _ = native.optimize_order(graph, trials=optimizer.trials, sweeps=optimizer.sweeps,
+                                                target_width=optimizer.target_width,
+                                                width_penalty=optimizer.width_penalty, seed=optimizer.seed)
+            return steps
+        return _search_fitting(graph, optimizer)
     raise TypeError(f"unknown optimizer {optimizer!r}")
+
+
+# per-syndrome working set that still lets a thread block keep it in shared
+# memory (float32), with room for the step records
+_SMEM_ARENA_BYTES = 200 * 1024
+
+
+def _estimated_cost(plan):
+    """Relative runtime estimate of a compiled program: runtime flops, tripled
+    when the float32 working set spills out of shared memory."""
+    fits = plan["arena_elems"] * 4 <= _SMEM_ARENA_BYTES
+    return plan["flops_per_syndrome"] * (1.0 if fits else 3.0)
+
+
+def _search_fitting(graph, opt):
+    """Several annealing restarts (and narrower width targets) scored by the
+    planner's own flops and working-set size; the cheapest tree wins."""
+    best = None
+    widths = [0]
+    for r in range(opt.restarts):
+        for tw in widths:
+            steps, _, w = native.optimize_order(graph, trials=opt.trials, sweeps=opt.sweeps, target_width=tw,
+                                                width_penalty=2.0 if tw else opt.width_penalty,
+                                                seed=opt.seed + r)
+            plan = native.inspect_plan(graph, steps)
+            cost = _estimated_cost(plan)
+            if best is None or cost < best[0]:
+                best = (cost, steps, plan)
+        if best[2]["arena_elems"] * 4 > _SMEM_ARENA_BYTES and len(widths) == 1:
+            widths.append(best[2]["width"] - 1)
+    return best[1]
 
 
 # ---------------------------------------------------------------------------

@@ -1,0 +1,223 @@
+"""The learned surrogate with exact fallback.
+
+A ReLU MLP (float32 master weights, bf16 GEMM operands, float32
+accumulation; trained by the native library's own kernels) maps syndrome
+bits to the logical class.  Its labels are the exact contraction's class
+probabilities.  At decode time the rows whose softmax confidence is below a
+calibrated threshold go to the exact contraction, which is therefore also
+the judge of the surrogate's decisions.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import time
+
+import numpy as np
+
+from . import native
+from .error_model import pack_syndromes, random_error_pattern, syndrome_extraction
+
+
+class MLPConfig(C.Structure):
+    _fields_ = [("n_in", C.c_int32), ("hidden", C.c_int32), ("n_layers", C.c_int32), ("n_out", C.c_int32),
+                ("seed", C.c_uint64), ("device", C.c_int32)]
+
+
+def _lib():
+    L = native.lib()
+    if not getattr(L, "_tqec_mlp_bound", False):
+        vp, i64 = C.c_void_p, C.c_int64
+        sig = {"tqec_mlp_create": [vp, vp], "tqec_mlp_destroy": [vp], "tqec_mlp_param_count": [vp, vp],
+               "tqec_mlp_get_params": [vp, vp, i64], "tqec_mlp_set_params": [vp, vp, i64],
+               "tqec_mlp_gradients": [vp, vp, vp, i64, vp, vp],
+               "tqec_mlp_train_step": [vp, vp, vp, i64, C.c_float, vp, vp],
+               "tqec_mlp_infer": [vp, vp, i64, vp, vp, vp],
+               "tqec_gated_decode": [vp, vp, C.c_float, vp, i64, vp, vp, vp],
+               "tqec_mlp_save": [vp, C.c_char_p], "tqec_mlp_load": [vp, C.c_char_p]}
+        for name, args in sig.items():
+            f = getattr(L, name)
+            f.argtypes = args
+            f.restype = C.c_int
+        L._tqec_mlp_bound = True
+    return L
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+class Surrogate:
+    """Owner of a native ``tqec_mlp``."""
+
+    def __init__(self, n_in, n_out, hidden=512, n_layers=4, seed=1, device=0):
+        self.cfg = dict(n_in=n_in, n_out=n_out, hidden=hidden, n_layers=n_layers)
+        h = C.c_void_p()
+        native.check(_lib().tqec_mlp_create(C.byref(MLPConfig(n_in, hidden, n_layers, n_out, seed, device)),
+                                            C.byref(h)))
+        self._h = h
+        n = C.c_int64()
+        native.check(_lib().tqec_mlp_param_count(self._h, C.byref(n)))
+        self.n_params = n.value
+        self.threshold = None
+
+    def close(self):
+        if getattr(self, "_h", None):
+            _lib().tqec_mlp_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def handle(self):
+        return self._h
+
+    def params(self):
+        out = np.empty(self.n_params, dtype=np.float32)
+        native.check(_lib().tqec_mlp_get_params(self._h, _p(out), self.n_params))
+        return out
+
+    def set_params(self, p):
+        p = np.ascontiguousarray(p, dtype=np.float32)
+        native.check(_lib().tqec_mlp_set_params(self._h, _p(p), p.size))
+
+    def gradients(self, packed, targets):
+        packed = np.ascontiguousarray(packed, dtype=np.uint8)
+        targets = np.ascontiguousarray(targets, dtype=np.float32)
+        g = np.empty(self.n_params, dtype=np.float32)
+        loss = C.c_float()
+        native.check(_lib().tqec_mlp_gradients(self._h, _p(packed), _p(targets), packed.shape[0], _p(g),
+                                                C.byref(loss)))
+        return g, loss.value
+
+    def train_step(self, packed, targets, lr):
+        packed = np.ascontiguousarray(packed, dtype=np.uint8)
+        targets = np.ascontiguousarray(targets, dtype=np.float32)
+        loss = C.c_float()
+        native.check(_lib().tqec_mlp_train_step(self._h, _p(packed), _p(targets), packed.shape[0], lr,
+                                                C.byref(loss), None))
+        return loss.value
+
+    def infer(self, packed):
+        packed = np.ascontiguousarray(packed, dtype=np.uint8)
+        n = packed.shape[0]
+        cls = np.empty(n, dtype=np.int32)
+        conf = np.empty(n, dtype=np.float32)
+        native.check(_lib().tqec_mlp_infer(self._h, _p(packed), n, _p(cls), _p(conf), None))
+        return cls, conf
+
+    def save(self, path):
+        native.check(_lib().tqec_mlp_save(self._h, path.encode()))
+
+    def load(self, path):
+        native.check(_lib().tqec_mlp_load(self._h, path.encode()))
+
+
+def soft_labels(logp):
+    """Class probabilities from log-marginals (rows normalised)."""
+    m = np.max(logp, axis=1, keepdims=True)
+    m = np.where(np.isfinite(m), m, 0.0)
+    p = np.exp(logp - m)
+    s = p.sum(axis=1, keepdims=True)
+    return (p / np.where(s > 0, s, 1.0)).astype(np.float32)
+
+
+def sample_bits(ct, n, rng):
+    ep = random_error_pattern(ct.em, rng, nsamples=n)
+    s = syndrome_extraction(ep, ct.tanner)
+    return np.concatenate([s.sx, s.sz], axis=1)
+
+
+def train_surrogate(ct, n_train=1 << 22, batch=8192, epochs=2, lr=2e-3, hidden=512, n_layers=4, seed=1,
+                    rng=None, log=None):
+    """Trains a surrogate for a compiled CSS decoder on n_train sampled
+    syndromes labelled by the exact contraction (float32 with its rounding
+    bound).  Returns (surrogate, stats)."""
+    rng = np.random.default_rng(seed) if rng is None else rng
+    t0 = time.time()
+    bits = sample_bits(ct, n_train, rng)
+    packed = pack_syndromes(bits)
+    logp = np.empty((n_train, ct.n_classes), dtype=np.float64)
+    chunk = 1 << 18
+    for i in range(0, n_train, chunk):
+        logp[i:i + chunk] = ct.program.contract_packed(packed[i:i + chunk], native.TQEC_F32)
+    targets = soft_labels(logp)
+    t_label = time.time() - t0
+    sur = Surrogate(ct.n_syndrome, ct.n_classes, hidden, n_layers, seed, ct.decoder.device)
+    steps = epochs * (n_train // batch)
+    losses = []
+    t1 = time.time()
+    for s in range(steps):
+        if s % (n_train // batch) == 0:
+            perm = rng.permutation(n_train)
+        j = s % (n_train // batch)
+        idx = perm[j * batch:(j + 1) * batch]
+        cur_lr = lr * 0.5 * (1 + np.cos(np.pi * s / steps))
+        losses.append(sur.train_step(packed[idx], targets[idx], cur_lr))
+        if log and s % 200 == 0:
+            log(f"step {s}/{steps} loss {losses[-1]:.5f}")
+    stats = {"label_seconds": t_label, "train_seconds": time.time() - t1, "steps": steps, "batch": batch,
+             "n_train": n_train, "final_loss": float(np.mean(losses[-50:])) if losses else None}
+    return sur, stats
+
+
+def calibrate(sur, ct, n_val=1 << 20, target_mismatch=1e-4, rng=None, seed=2):
+    """Smallest confidence threshold whose accepted rows disagree with the
+    exact decoder on at most target_mismatch of all rows (measured on n_val
+    fresh syndromes).  Returns (threshold, stats)."""
+    rng = np.random.default_rng(seed) if rng is None else rng
+    bits = sample_bits(ct, n_val, rng)
+    packed = pack_syndromes(bits)
+    exact = ct.program.decode_packed(packed)
+    cls, conf = sur.infer(packed)
+    wrong = cls != exact
+    order = np.argsort(-conf, kind="stable")
+    cum_wrong = np.cumsum(wrong[order])
+    allowed = target_mismatch * n_val
+    ok = np.flatnonzero(cum_wrong <= allowed)
+    k = int(ok[-1]) + 1 if ok.size else 0   # accept the k most confident rows
+    thr = float(conf[order[k - 1]]) if k > 0 else 2.0
+    # ties at the threshold: accept only rows strictly above when needed
+    acc = conf >= thr
+    if (wrong & acc).sum() > allowed:
+        thr = float(np.nextafter(np.float32(thr), np.float32(2.0)))
+        acc = conf >= thr
+    stats = {"threshold": thr, "accept_fraction": float(acc.mean()),
+             "mismatch_accepted": float((wrong & acc).mean()), "raw_accuracy_vs_exact": float((~wrong).mean()),
+             "n_val": n_val}
+    sur.threshold = thr
+    return thr, stats
+
+
+class GatedDecoder:
+    """Surrogate first, exact contraction for rows below the threshold."""
+
+    def __init__(self, ct, sur, threshold=None):
+        self.ct = ct
+        self.sur = sur
+        self.threshold = sur.threshold if threshold is None else threshold
+
+    def decode_packed(self, packed, classes=None):
+        packed = np.ascontiguousarray(packed, dtype=np.uint8)
+        n = packed.shape[0]
+        if classes is None:
+            classes = np.empty(n, dtype=np.int32)
+        nf = C.c_int64()
+        native.check(_lib().tqec_gated_decode(self.sur.handle, self.ct.program._h, self.threshold, _p(packed), n,
+                                              _p(classes), C.byref(nf), None))
+        self.last_fallback = nf.value
+        return classes
+
+    def decode_ptrs(self, syn_ptr, n, cls_ptr, stream=None):
+        nf = C.c_int64()
+        native.check(_lib().tqec_gated_decode(self.sur.handle, self.ct.program._h, self.threshold,
+                                              C.c_void_p(syn_ptr), n, C.c_void_p(cls_ptr), C.byref(nf),
+                                              C.c_void_p(stream) if stream else None))
+        self.last_fallback = nf.value
+        return nf.value
+
+    def decode_batch(self, bits):
+        return self.decode_packed(pack_syndromes(bits))

@@ -1,0 +1,103 @@
+"""GPU tests of the learned surrogate: gradients against the float64 CPU
+checker, training that reduces the loss, checkpoint round trip, and the
+gated decoder's decisions against the exact contraction.
+
+Gradient tolerance: relative L2 error 2e-3 against the checker with bf16
+rounding at the kernels' rounding points (float32 accumulation order is the
+only other difference), and 5e-2 against the exact float64 network.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import gpu_available
+
+pytestmark = [pytest.mark.gpu, pytest.mark.skipif(not gpu_available(), reason="needs a CUDA GPU")]
+
+
+def rel_l2(a, b):
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-30))
+
+
+@pytest.mark.parametrize("n_in,hidden,layers,n_out,rows", [(8, 32, 3, 4, 64), (48, 64, 4, 4, 300),
+                                                            (70, 96, 4, 16, 130)])
+def test_gradients_match_cpu_float64(pkg, n_in, hidden, layers, n_out, rows):
+    from oracle import mlp_oracle
+
+    from tensorqec_gb300.surrogate import Surrogate
+
+    rng = np.random.default_rng(n_in)
+    sur = Surrogate(n_in, n_out, hidden, layers, seed=3)
+    bits = (rng.random((rows, n_in)) < 0.3).astype(np.uint8)
+    packed = pkg.pack_syndromes(bits)
+    t = rng.random((rows, n_out)).astype(np.float32)
+    t /= t.sum(axis=1, keepdims=True)
+    p = sur.params()
+    g, loss = sur.gradients(packed, t)
+    l64, g64 = mlp_oracle.forward_backward(p, packed, t, n_in, hidden, layers, n_out, bf16=True)
+    _, gx = mlp_oracle.forward_backward(p, packed, t, n_in, hidden, layers, n_out, bf16=False)
+    assert abs(loss - l64) < 1e-3 * max(1.0, abs(l64))
+    assert rel_l2(g, g64) < 2e-3, rel_l2(g, g64)
+    assert rel_l2(g, gx) < 5e-2
+    sur.close()
+
+
+def test_training_reduces_loss_and_checkpoint_roundtrip(pkg, tmp_path):
+    from tensorqec_gb300.surrogate import Surrogate, soft_labels
+
+    t = pkg.tanner_graph(pkg.SurfaceCode(5, 5))
+    em = pkg.depolarizing(0.05, t.nq)
+    ct = pkg.compile(pkg.TNMMAP(precision="f32"), t, em)
+    rng = np.random.default_rng(4)
+    ep = pkg.random_error_pattern(em, rng, nsamples=1 << 16)
+    syn = pkg.syndrome_extraction(ep, t)
+    bits = np.concatenate([syn.sx, syn.sz], axis=1)
+    packed = pkg.pack_syndromes(bits)
+    tgt = soft_labels(ct.class_logprobs(bits))
+    sur = Surrogate(t.ns, 4, 128, 4, seed=5)
+    first = sur.train_step(packed[:4096], tgt[:4096], 2e-3)
+    for s in range(1, 120):
+        j = (s * 4096) % (len(packed) - 4096)
+        last = sur.train_step(packed[j:j + 4096], tgt[j:j + 4096], 2e-3)
+    assert last < 0.6 * first
+    cls, conf = sur.infer(packed)
+    exact = ct.decode_batch(bits)
+    assert (cls == exact).mean() > 0.9
+    path = os.path.join(tmp_path, "sur.bin")
+    sur.save(path)
+    sur2 = Surrogate(t.ns, 4, 128, 4, seed=99)
+    sur2.load(path)
+    np.testing.assert_array_equal(sur2.params(), sur.params())
+    cls2, conf2 = sur2.infer(packed)
+    np.testing.assert_array_equal(cls2, cls)
+    sur.close()
+    sur2.close()
+    ct.close()
+
+
+def test_gated_decoder_matches_exact_where_it_answers(pkg):
+    from tensorqec_gb300.surrogate import GatedDecoder, calibrate, train_surrogate
+
+    t = pkg.tanner_graph(pkg.SurfaceCode(5, 5))
+    em = pkg.depolarizing(0.05, t.nq)
+    ct = pkg.compile(pkg.TNMMAP(precision="f32"), t, em)
+    sur, stats = train_surrogate(ct, n_train=1 << 17, batch=4096, epochs=2, hidden=128, n_layers=4, seed=6)
+    thr, cst = calibrate(sur, ct, n_val=1 << 16, target_mismatch=1e-3, seed=7)
+    assert 0.0 < cst["accept_fraction"] <= 1.0
+    gd = GatedDecoder(ct, sur, thr)
+    rng = np.random.default_rng(8)
+    ep = pkg.random_error_pattern(em, rng, nsamples=1 << 16)
+    syn = pkg.syndrome_extraction(ep, t)
+    bits = np.concatenate([syn.sx, syn.sz], axis=1)
+    got = gd.decode_batch(bits)
+    exact = ct.decode_batch(bits)
+    cls, conf = sur.infer(pkg.pack_syndromes(bits))
+    # rows the gate sent to the exact path are exact; answered rows are the surrogate's
+    fb = conf < thr
+    assert gd.last_fallback == int(fb.sum())
+    np.testing.assert_array_equal(got[fb], exact[fb])
+    np.testing.assert_array_equal(got[~fb], cls[~fb])
+    assert (got != exact).mean() < 5e-3
+    sur.close()
+    ct.close()
