@@ -44,6 +44,10 @@ def parse():
     ap.add_argument("--profile", action="store_true",
                     help="one float32 contraction launch of --batch syndromes (for ncu), no timing")
     ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--no-surrogate", action="store_true", help="time the batched exact decoder alone")
+    ap.add_argument("--train-n", type=int, default=1 << 22, help="surrogate training syndromes")
+    ap.add_argument("--calib-n", type=int, default=1 << 20, help="surrogate calibration syndromes")
+    ap.add_argument("--eval-n", type=int, default=1 << 20, help="fresh syndromes for the evaluation")
     return ap.parse_args()
 
 
@@ -193,6 +197,40 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def wilson(k, n, z=1.96):
+    """95% Wilson interval of a binomial rate."""
+    if n == 0:
+        return (0.0, 1.0)
+    p = k / n
+    den = 1 + z * z / n
+    c = (p + z * z / (2 * n)) / den
+    h = z * np.sqrt(p * (1 - p) / n + z * z / (4 * n * n)) / den
+    return (max(0.0, c - h), min(1.0, c + h))
+
+
+def surrogate_eval(pkg, ct, gd, n, seed):
+    """Config-5 style evaluation on n fresh syndromes: fallback fraction,
+    decision mismatch against the exact decoder, logical error rates."""
+    rng = np.random.default_rng(seed)
+    ep = pkg.random_error_pattern(ct.em, rng, nsamples=n)
+    s = pkg.syndrome_extraction(ep, ct.tanner)
+    bits = np.concatenate([s.sx, s.sz], axis=1)
+    packed = pkg.pack_syndromes(bits)
+    exact = ct.program.decode_packed(packed)
+    gated = gd.decode_packed(packed)
+    fb = gd.last_fallback
+    # class of the true error: a = lx.ez, b = lz.ex (Julia linear index of mar)
+    a = (ep.zerror.astype(np.int64) @ ct.lx.T.astype(np.int64)) % 2
+    b = (ep.xerror.astype(np.int64) @ ct.lz.T.astype(np.int64)) % 2
+    k = ct.lx.shape[0]
+    truth = (a * (1 << np.arange(k))).sum(1) + (b * (1 << (k + np.arange(k)))).sum(1)
+    le_exact = int((exact != truth).sum())
+    le_gated = int((gated != truth).sum())
+    return {"n": n, "fallback_fraction": fb / n, "decision_mismatch_vs_exact": float((gated != exact).mean()),
+            "ler_exact": le_exact / n, "ler_exact_ci95": wilson(le_exact, n),
+            "ler_gated": le_gated / n, "ler_gated_ci95": wilson(le_gated, n)}
+
+
 def run_ours(args):
     import torch
 
@@ -208,6 +246,8 @@ def run_ours(args):
 
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     pkg = G.load_package()
+    from tensorqec_gb300.surrogate import GatedDecoder, calibrate, train_surrogate
+
     W, K, B = args.warmup, args.steps, args.batch
     t, em, bits = workload(pkg, rank, W + K, B)
     ct = pkg.compile(pkg.TNMMAP(precision="f32", device=local), t, em)
@@ -216,6 +256,24 @@ def run_ours(args):
     info = ct.program.info
     stream = torch.cuda.current_stream()
     sptr = stream.cuda_stream
+
+    # ---- the learned surrogate: trained on exact-contraction labels --------
+    gd = None
+    sur_stats = None
+    if not args.no_surrogate:
+        t0 = time.time()
+        sur, tstats = train_surrogate(ct, n_train=args.train_n, batch=8192, epochs=2, lr=2e-3, hidden=512,
+                                      n_layers=4, seed=SEED + 17 + rank)
+        thr, cstats = calibrate(sur, ct, n_val=args.calib_n, target_mismatch=1e-4, seed=SEED + 29 + rank)
+        gd = GatedDecoder(ct, sur, thr)
+        sur_stats = {"train": tstats, "calibration": cstats, "setup_seconds": time.time() - t0}
+
+    def decode(syn_ptr, cls_ptr):
+        if gd is not None:
+            gd.decode_ptrs(syn_ptr, B, cls_ptr, sptr)
+        else:
+            ct.program.decode_ptrs(syn_ptr, B, cls_ptr, None, None, sptr)
+
     packed = [pkg.pack_syndromes(b) for b in bits]
     d_syn = [torch.from_numpy(p).cuda() for p in packed]
     d_cls = torch.empty(B, dtype=torch.int32, device="cuda")
@@ -224,9 +282,22 @@ def run_ours(args):
     def flush_l2():
         flush.fill_(1.0)
 
+    def timed(fn, idx):
+        out = []
+        for i in idx:
+            flush_l2()
+            torch.cuda.synchronize()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            fn(i)
+            b.record(stream)
+            torch.cuda.synchronize()
+            out.append(a.elapsed_time(b))
+        return out
+
     # warm-up (also the first-call allocations inside the library)
     for i in range(W):
-        ct.program.decode_ptrs(d_syn[i].data_ptr(), B, d_cls.data_ptr(), None, None, sptr)
+        decode(d_syn[i].data_ptr(), d_cls.data_ptr())
     torch.cuda.synchronize()
 
     # ---- value: device-resident decode ------------------------------------
@@ -235,52 +306,52 @@ def run_ours(args):
     if dist:
         dist.barrier()
     torch.cuda.synchronize()
-    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(K)]
-    rechecks = 0
-    for i in range(K):
-        flush_l2()
-        ev[i][0].record(stream)
-        ct.program.decode_ptrs(d_syn[W + i].data_ptr(), B, d_cls.data_ptr(), None, None, sptr)
-        ev[i][1].record(stream)
-    torch.cuda.synchronize()
+    ms = timed(lambda i: decode(d_syn[W + i].data_ptr(), d_cls.data_ptr()), range(K))
     if dist:
         dist.barrier()
     clk = clocks.stop()
-    ms = [a.elapsed_time(b) for a, b in ev]
     step_ms = sum(ms) / K
+    fallback = gd.last_fallback if gd is not None else B
+
+    # ---- the batched exact decoder alone (float32 + float64 recheck) -------
+    tn_ms = timed(lambda i: ct.program.decode_ptrs(d_syn[W + i].data_ptr(), B, d_cls.data_ptr(), None, None, sptr),
+                  range(min(K, 5)))
+    tn_rate = B / (statistics.median(tn_ms) / 1e3)
     rechecks = ct.program.last_recheck_count()
 
     # ---- roofline: the float32 contraction kernel alone --------------------
     d_lp = torch.empty((B, info["n_classes"]), dtype=torch.float64, device="cuda")
-    kms = []
-    for i in range(min(K, 5)):
-        flush_l2()
-        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        a.record(stream)
-        ct.program.contract_ptrs(d_syn[W + i].data_ptr(), B, pkg.native.TQEC_F32, d_lp.data_ptr(), sptr)
-        b.record(stream)
-        torch.cuda.synchronize()
-        kms.append(a.elapsed_time(b))
+    kms = timed(lambda i: ct.program.contract_ptrs(d_syn[W + i].data_ptr(), B, pkg.native.TQEC_F32,
+                                                   d_lp.data_ptr(), sptr), range(min(K, 5)))
     kernel_ms = statistics.median(kms)
     flops = info["flops_per_syndrome"]
     achieved_tflops = flops * B / (kernel_ms / 1e3) / 1e12
     bf16_peak, hbm_peak, peak_kind = peaks()
 
+    # the surrogate's forward pass alone (tensor-core GEMMs)
+    mlp_part = None
+    if gd is not None:
+        import ctypes as C
+
+        from tensorqec_gb300 import surrogate as S
+
+        L = S._lib()
+        d_cls2 = torch.empty(B, dtype=torch.int32, device="cuda")
+        mms = timed(lambda i: L.tqec_mlp_infer(gd.sur.handle, C.c_void_p(d_syn[W + i].data_ptr()), B,
+                                               C.c_void_p(d_cls2.data_ptr()), None, C.c_void_p(sptr)),
+                    range(min(K, 5)))
+        mlp_ms = statistics.median(mms)
+        mlp_flops = 2.0 * (64 * 512 + 2 * 512 * 512 + 512 * 4)
+        mlp_part = {"forward_ms": mlp_ms, "achieved_tflops": mlp_flops * B / (mlp_ms / 1e3) / 1e12,
+                    "peak_tflops": bf16_peak, "frac": mlp_flops * B / (mlp_ms / 1e3) / 1e12 / bf16_peak,
+                    "flops_per_syndrome": mlp_flops}
+
     # ---- e2e: pinned host in, pinned host out, through the C ABI -----------
     h_syn = [torch.from_numpy(p).pin_memory() for p in packed]
     h_cls = torch.empty(B, dtype=torch.int32).pin_memory()
-    ct.program.decode_ptrs(h_syn[0].data_ptr(), B, h_cls.data_ptr(), None, None, sptr)
+    decode(h_syn[0].data_ptr(), h_cls.data_ptr())
     torch.cuda.synchronize()
-    e2e_ms = []
-    for i in range(K):
-        flush_l2()
-        torch.cuda.synchronize()
-        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        a.record(stream)
-        ct.program.decode_ptrs(h_syn[W + i].data_ptr(), B, h_cls.data_ptr(), None, None, sptr)
-        b.record(stream)
-        torch.cuda.synchronize()
-        e2e_ms.append(a.elapsed_time(b))
+    e2e_ms = timed(lambda i: decode(h_syn[W + i].data_ptr(), h_cls.data_ptr()), range(K))
     e2e_step = sum(e2e_ms) / K
 
     # ---- plain float64 form: one launch per syndrome (drop-in baseline) ----
@@ -288,12 +359,9 @@ def run_ours(args):
     m = 128
     plain.program.decode_ptrs(d_syn[0].data_ptr(), 8, d_cls.data_ptr(), None, None, sptr)
     torch.cuda.synchronize()
-    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    a.record(stream)
-    plain.program.decode_ptrs(d_syn[0].data_ptr(), m, d_cls.data_ptr(), None, None, sptr)
-    b.record(stream)
-    torch.cuda.synchronize()
-    plain_rate = m / (a.elapsed_time(b) / 1e3)
+    pms = timed(lambda i: plain.program.decode_ptrs(d_syn[0].data_ptr(), m, d_cls.data_ptr(), None, None, sptr),
+                range(1))
+    plain_rate = m / (pms[0] / 1e3)
     plain.close()
 
     # max over ranks
@@ -304,16 +372,21 @@ def run_ours(args):
     value = world * B / (step_ms / 1e3)
     e2e_value = world * B / (e2e_step / 1e3)
 
-    line = None
     if rank == 0:
         cpu, cpu_cls = cpu_baseline(pkg, ct, bits[W], args.cpu_sample)
-        gpu_cls = ct.decode_batch(bits[W][:args.cpu_sample])
+        sub = pkg.pack_syndromes(bits[W][:args.cpu_sample])
+        gpu_cls = gd.decode_packed(sub) if gd is not None else ct.program.decode_packed(sub)
         mismatch = float(np.mean(gpu_cls != cpu_cls))
         traffic = read_traffic()
+        evaluation = surrogate_eval(pkg, ct, gd, args.eval_n, SEED + 41) if gd is not None else None
+        # launches per step: gated = unpack, 4 GEMMs, gate, gather, 2 contraction, scatter
+        per_step = 10 if gd is not None else 2
         line = {
             "metric": METRIC, "value": value, "unit": "syndromes/s", "n_gpus": world, "steps": K, "warmup": W,
             "ms_per_step": step_ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f32", "data": "synthetic (seeded depolarizing errors, numpy PCG64)", "config": config(B),
+            "dtype": "f32", "data": "synthetic (seeded depolarizing errors, numpy PCG64)",
+            "config": dict(config(B), decoder="gated surrogate (4x512 MLP, bf16/f32) + batched TN f32 with f64 "
+                                              "recheck" if gd is not None else "batched TN f32 with f64 recheck"),
             "e2e": {"value": e2e_value, "unit": "syndromes/s", "h2d_bytes_per_step": int(packed[0].nbytes),
                     "d2h_bytes_per_step": int(B * 4)},
             "roofline": {"bound": "tensor", "achieved": achieved_tflops, "peak": bf16_peak, "unit": "TFLOP/s",
@@ -321,13 +394,18 @@ def run_ours(args):
                          "kernel": "tn_contract_kernel<float> (SIMT float32; peak is the measured bf16 "
                                    f"tensor rate, {peak_kind})",
                          "flops_per_syndrome": flops, "kernel_ms": kernel_ms},
+            "surrogate_gemm": mlp_part,
             "cpu_baseline": cpu,
             "clocks": clk,
-            "gpu_launches": 2 * K,
+            "gpu_launches": per_step * K,
+            "batched_tn_syn_per_s": tn_rate,
             "plain_f64_gpu_syn_per_s": plain_rate,
             "speedup_vs_plain_f64_gpu": value / plain_rate,
+            "fallback_fraction_last_step": fallback / B,
             "decision_mismatch_vs_f64_oracle": mismatch,
             "recheck_fraction": rechecks / B,
+            "surrogate": sur_stats,
+            "evaluation": evaluation,
         }
         print(json.dumps(line), flush=True)
     ct.close()

@@ -222,6 +222,11 @@ int tqec_mlp_infer(tqec_mlp* mlp, const uint8_t* syndromes, int64_t n, int32_t* 
  * (tqec_decode_batch).  Writes the number of such rows. */
 int tqec_gated_decode(tqec_mlp* mlp, tqec_program* prog, float threshold, const uint8_t* syndromes,
                       int64_t n, int32_t* class_out, int64_t* n_fallback_out, void* stream);
+/* Hidden layers on the tcgen05 tensor cores (1, the default, where the shape
+ * allows: hidden a multiple of 256) or on the SIMT GEMM (0). */
+int tqec_mlp_set_gemm(tqec_mlp* mlp, int use_tensor_cores);
+/* Raw output-layer logits (n x n_out float32, host or device memory). */
+int tqec_mlp_forward_logits(tqec_mlp* mlp, const uint8_t* syndromes, int64_t n, float* logits_out);
 /* Checkpoint: one JSON header line, then the float32 parameters. */
 int tqec_mlp_save(tqec_mlp* mlp, const char* path);
 int tqec_mlp_load(tqec_mlp* mlp, const char* path);

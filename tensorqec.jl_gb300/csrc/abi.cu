@@ -134,7 +134,7 @@ int choose_shape(tqec_program* p, int precision, int G_req, int threads_req, Sha
     s.smem_arena = tqec::contract_smem_bytes(precision, nsteps, sw, G, arena, true) <= limit;
     // one syndrome per block with a wide arena: use more threads per block
     if (G == 1 && (!s.smem_arena || tqec::contract_smem_bytes(precision, nsteps, sw, 1, arena, true) > target))
-      s.threads = threads_req > 0 ? threads_req : 512;
+      s.threads = threads_req > 0 ? threads_req : 1024;
     (void)esz;
   }
   s.smem = tqec::contract_smem_bytes(precision, nsteps, sw, s.G, arena, s.smem_arena);
@@ -336,7 +336,7 @@ int tqec_program_create(const tqec_network* net, const tqec_tree* tree, const tq
   if (opts) o = *opts;
   if (o.precision != TQEC_F32 && o.precision != TQEC_F64) return fail(TQEC_ERR_INVALID, "unknown precision");
   if (o.group < 0 || (o.group & (o.group - 1)) || o.group > 1024) return fail(TQEC_ERR_INVALID, "group must be 0 or a power of two <= 1024");
-  if (o.threads < 0 || (o.threads % 32) || o.threads > 512) return fail(TQEC_ERR_INVALID, "threads must be 0 or a multiple of 32 up to 512");
+  if (o.threads < 0 || (o.threads % 32) || o.threads > 1024) return fail(TQEC_ERR_INVALID, "threads must be 0 or a multiple of 32 up to 1024");
   tqec::NetworkView v{net->n_tensors, net->ix_offsets, net->ix_labels, net->data_offsets, net->data,
                       net->n_out, net->out_labels, net->n_syndrome, net->syndrome_tensors};
   tqec::PlanLimits lim;
@@ -489,7 +489,7 @@ int tqec_program_autotune(tqec_program* p, int64_t n_probe) {
     Shape best = p->shape[prec];
     float best_ms = 1e30f;
     for (int G : {1, 2, 4, 8, 16, 32, 64, 128}) {
-      for (int th : {128, 256, 512}) {
+      for (int th : {128, 256, 512, 1024}) {
         Shape s;
         if (choose_shape(p, prec, G, th, &s) != TQEC_OK) continue;
         // a global arena bigger than 4 GB is not worth probing on a shared GPU

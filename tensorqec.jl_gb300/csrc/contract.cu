@@ -146,8 +146,135 @@ __device__ void run_step(const KArgs& a, const StepDesc& d, int st, const uint32
   }
 }
 
+template <typename T>
+__device__ __forceinline__ void load4(const T* p, T v[4]);
+template <>
+__device__ __forceinline__ void load4<float>(const float* p, float v[4]) {
+  const float4 x = *reinterpret_cast<const float4*>(p);
+  v[0] = x.x; v[1] = x.y; v[2] = x.z; v[3] = x.w;
+}
+template <>
+__device__ __forceinline__ void load4<double>(const double* p, double v[4]) {
+  const double2 x = reinterpret_cast<const double2*>(p)[0];
+  const double2 y = reinterpret_cast<const double2*>(p)[1];
+  v[0] = x.x; v[1] = x.y; v[2] = y.x; v[3] = y.y;
+}
+
+template <typename T>
+__device__ __forceinline__ void store4(T* p, const T v[4]);
+template <>
+__device__ __forceinline__ void store4<float>(float* p, const float v[4]) {
+  *reinterpret_cast<float4*>(p) = make_float4(v[0], v[1], v[2], v[3]);
+}
+template <>
+__device__ __forceinline__ void store4<double>(double* p, const double v[4]) {
+  reinterpret_cast<double2*>(p)[0] = make_double2(v[0], v[1]);
+  reinterpret_cast<double2*>(p)[1] = make_double2(v[2], v[3]);
+}
+
+// A step whose B-only group has at least 4 entries: each work item is four
+// consecutive outputs along fb, which share every A value and read B as one
+// 16-byte vector.  Operand bases, fb offsets and k strides are multiples of 4
+// elements (arena and constant offsets are planned that way), so the vector
+// accesses are aligned.
+template <typename T, bool NORM, bool APAR, bool BPAR>
+__device__ void run_step_v4(const KArgs& a, const StepDesc& d, int st, const uint32_t* s_syn,
+                            uint32_t* s_max, T* arena, const T* consts) {
+  const int lw = d.lh + d.lfa + d.lfb;
+  const int lwv = lw - 2;
+  const int total = 1 << (lwv + a.lg);
+  const int total_r = (total + 31) & ~31;
+  const int mfb = (1 << d.lfb) - 1;
+  const int mfa = (1 << d.lfa) - 1;
+  const int mwv = (1 << lwv) - 1;
+  const int K = 1 << d.lk;
+  const int abits = d.lh + d.lfa + d.lk;
+  const int bbits = d.lh + d.lk + d.lfb;
+  const int32_t* perm = d.perm_off < 0 ? nullptr : a.perm + d.perm_off;
+  const int cb0 = lw < 8 ? lw : 8;
+  for (int i = threadIdx.x; i < total_r; i += blockDim.x) {
+    const bool valid = i < total;
+    const int g = valid ? (i >> lwv) : 0;
+    const int e0 = (i & mwv) << 2;
+    T acc[4] = {T(0), T(0), T(0), T(0)};
+    if (valid) {
+      const uint32_t* syn = s_syn + g * a.syn_words;
+      T* arena_g = arena + int64_t(g) * a.arena_elems;
+      const int fb0 = e0 & mfb;
+      const int fa = (e0 >> d.lfb) & mfa;
+      const int h = e0 >> (d.lfb + d.lfa);
+      const int abase = ((h << d.lfa) | fa) << d.lk;
+      const int bbase = (h << (d.lk + d.lfb)) | fb0;
+      const T* ap = nullptr;
+      const T* bp = nullptr;
+      int as = 0, bs = 0;
+      if (APAR) as = syn_bit(syn, d.a_ref);
+      else ap = operand_ptr<T>(d.a_kind, d.a_ref, d.a_sel, abits, arena_g, consts, syn);
+      if (BPAR) bs = syn_bit(syn, d.b_ref);
+      else bp = operand_ptr<T>(d.b_kind, d.b_ref, d.b_sel, bbits, arena_g, consts, syn);
+      T fa_s = T(1), fb_s = T(1);
+      if (NORM) {
+        int ee;
+        if (!APAR && d.a_kind == OP_ARENA) fa_s = T(norm_factor(s_max[g * a.n_steps + d.a_prod], &ee));
+        if (!BPAR && d.b_kind == OP_ARENA) fb_s = T(norm_factor(s_max[g * a.n_steps + d.b_prod], &ee));
+      }
+      for (int k = 0; k < K; ++k) {
+        T av;
+        if (APAR) {
+          if (parity_val<T>(abase + k, as) == T(0)) continue;
+          av = T(1);
+        } else {
+          av = ap[abase + k];
+          if (NORM) av *= fa_s;
+        }
+        T bv[4];
+        const int bi = bbase + (k << d.lfb);
+        if (BPAR) {
+#pragma unroll
+          for (int j = 0; j < 4; ++j) bv[j] = parity_val<T>(bi + j, bs);
+        } else {
+          load4<T>(bp + bi, bv);
+        }
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[j] = fma(av, bv[j], acc[j]);
+      }
+      if (NORM && !BPAR) {
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[j] *= fb_s;
+      }
+      T* out = arena_g + d.out_off;
+      if (!perm) {
+        store4<T>(out + e0, acc);
+      } else {
+        const int4 lo = *reinterpret_cast<const int4*>(perm + (e0 & ((1 << cb0) - 1)));
+        int hi = 0;
+        int tab = 1 << cb0;
+        for (int sh = 8; sh < lw; sh += 8) {
+          const int cb = lw - sh < 8 ? lw - sh : 8;
+          hi |= __ldg(perm + tab + ((e0 >> sh) & ((1 << cb) - 1)));
+          tab += 1 << cb;
+        }
+        out[lo.x | hi] = acc[0];
+        out[lo.y | hi] = acc[1];
+        out[lo.z | hi] = acc[2];
+        out[lo.w | hi] = acc[3];
+      }
+    }
+    if (NORM) {
+      float m = fmaxf(fmaxf(float(acc[0]), float(acc[1])), fmaxf(float(acc[2]), float(acc[3])));
+      uint32_t bits = __float_as_uint(m);
+      const int seg = lwv >= 5 ? 32 : (1 << lwv);
+      for (int o = 1; o < seg; o <<= 1) {
+        uint32_t other = __shfl_xor_sync(0xffffffffu, bits, o);
+        bits = other > bits ? other : bits;
+      }
+      if (valid && (threadIdx.x & (seg - 1)) == 0) atomicMax(&s_max[g * a.n_steps + st], bits);
+    }
+  }
+}
+
 template <typename T, bool NORM>
-__global__ void __launch_bounds__(512) tn_contract_kernel(KArgs a) {
+__global__ void __launch_bounds__(1024) tn_contract_kernel(KArgs a) {
   extern __shared__ __align__(16) unsigned char smem[];
   StepDesc* s_steps = reinterpret_cast<StepDesc*>(smem);
   size_t off = size_t(a.n_steps) * sizeof(StepDesc);
@@ -187,10 +314,17 @@ __global__ void __launch_bounds__(512) tn_contract_kernel(KArgs a) {
     for (int st = 0; st < a.n_steps; ++st) {
       const StepDesc& d = s_steps[st];
       const bool ap = d.a_kind == OP_PARITY, bp = d.b_kind == OP_PARITY;
-      if (ap && bp) run_step<T, NORM, true, true>(a, d, st, s_syn, s_max, arena, consts);
-      else if (ap) run_step<T, NORM, true, false>(a, d, st, s_syn, s_max, arena, consts);
-      else if (bp) run_step<T, NORM, false, true>(a, d, st, s_syn, s_max, arena, consts);
-      else run_step<T, NORM, false, false>(a, d, st, s_syn, s_max, arena, consts);
+      if (d.lfb >= 2) {
+        if (ap && bp) run_step_v4<T, NORM, true, true>(a, d, st, s_syn, s_max, arena, consts);
+        else if (ap) run_step_v4<T, NORM, true, false>(a, d, st, s_syn, s_max, arena, consts);
+        else if (bp) run_step_v4<T, NORM, false, true>(a, d, st, s_syn, s_max, arena, consts);
+        else run_step_v4<T, NORM, false, false>(a, d, st, s_syn, s_max, arena, consts);
+      } else {
+        if (ap && bp) run_step<T, NORM, true, true>(a, d, st, s_syn, s_max, arena, consts);
+        else if (ap) run_step<T, NORM, true, false>(a, d, st, s_syn, s_max, arena, consts);
+        else if (bp) run_step<T, NORM, false, true>(a, d, st, s_syn, s_max, arena, consts);
+        else run_step<T, NORM, false, false>(a, d, st, s_syn, s_max, arena, consts);
+      }
       __syncthreads();
     }
     // epilogue: log-marginals, first argmax (Julia findmax order), recheck flag

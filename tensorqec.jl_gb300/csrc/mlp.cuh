@@ -41,6 +41,13 @@ cudaError_t transpose_bf16(const __nv_bfloat16* in, int rows, int cols, __nv_bfl
 cudaError_t gate_rows(const float* logits, int ldl, int64_t n, int n_out, float threshold, int32_t* cls,
                       float* conf, int32_t* fallback_list, int32_t* fallback_count, cudaStream_t st);
 
+// tcgen05 GEMM (umma_gemm.cu): out = relu(A * B^T + bias) as bf16.
+bool umma_gemm_supported(int M, int N, int K, int lda, int ldb, int ldo, const void* A, const void* B,
+                         const void* out);
+cudaError_t umma_gemm_bias_relu(int M, int N, int K, const __nv_bfloat16* A, int lda, const __nv_bfloat16* B,
+                                int ldb, const float* bias, __nv_bfloat16* out, int ldo, int* err,
+                                cudaStream_t st);
+
 cudaError_t gather_rows(const uint8_t* src, int row_bytes, const int32_t* list, int64_t n, uint8_t* dst,
                         cudaStream_t st);
 cudaError_t scatter_classes(const int32_t* src, const int32_t* list, int64_t n, int32_t* dst, cudaStream_t st);

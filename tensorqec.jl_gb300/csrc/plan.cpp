@@ -560,6 +560,8 @@ std::string build_plan(const NetworkView& net, int32_t n_steps, const int32_t* s
     if (ident) {
       d.perm_off = -1;
     } else {
+      // tables start on a 16-byte boundary (vector loads of the low table)
+      while (P.perm.size() % 4) P.perm.push_back(0);
       d.perm_off = (int32_t)P.perm.size();
       const int nb = (int)nat.size();
       for (int c0 = 0; c0 < nb; c0 += 8) {

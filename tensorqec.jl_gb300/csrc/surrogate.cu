@@ -77,6 +77,9 @@ struct tqec_mlp {
   uint8_t* gathered = nullptr;
   int32_t* gcls = nullptr;
   int adam_t = 0;
+  int use_tensor_cores = 1;                   // hidden layers on tcgen05 where the shape allows
+  int* d_err = nullptr;                       // timeout flag of the tcgen05 kernel
+  int* h_err = nullptr;                       // pinned
   cudaStream_t stream = nullptr;
   std::mutex mu;
 };
@@ -158,8 +161,13 @@ int forward(tqec_mlp* p, const uint8_t* dsyn, int64_t n, cudaStream_t st) {
     const __nv_bfloat16* W = p->w16 + p->w_off[l];
     const float* b = p->w32 + p->b_off[l];
     if (l < p->L - 1) {
-      SQ_CUDA(tqec::gemm_bf16(true, true, tqec::EPI_BIAS_RELU_BF16, (int)n, p->dout[l], p->din[l], x, ldx, W,
-                              p->din[l], p->H[l], p->cfg.hidden, b, nullptr, 0, 1, st));
+      if (p->use_tensor_cores &&
+          tqec::umma_gemm_supported((int)n, p->dout[l], p->din[l], ldx, p->din[l], p->cfg.hidden, x, W, p->H[l]))
+        SQ_CUDA(tqec::umma_gemm_bias_relu((int)n, p->dout[l], p->din[l], x, ldx, W, p->din[l], b, p->H[l],
+                                          p->cfg.hidden, p->d_err, st));
+      else
+        SQ_CUDA(tqec::gemm_bf16(true, true, tqec::EPI_BIAS_RELU_BF16, (int)n, p->dout[l], p->din[l], x, ldx, W,
+                                p->din[l], p->H[l], p->cfg.hidden, b, nullptr, 0, 1, st));
       x = p->H[l];
       ldx = p->cfg.hidden;
     } else {
@@ -212,9 +220,42 @@ int refresh_bf16(tqec_mlp* p, cudaStream_t st) {
   return TQEC_OK;
 }
 
+// Reports a timed-out tcgen05 wait (recorded by the kernel) as an error.
+int check_device_error(tqec_mlp* p, cudaStream_t st) {
+  SQ_CUDA(cudaMemcpyAsync(p->h_err, p->d_err, sizeof(int), cudaMemcpyDeviceToHost, st));
+  SQ_CUDA(cudaStreamSynchronize(st));
+  if (*p->h_err) {
+    cudaMemsetAsync(p->d_err, 0, sizeof(int), st);
+    return sfail(TQEC_ERR_TIMEOUT, "a tensor-core GEMM wait timed out");
+  }
+  return TQEC_OK;
+}
+
 }  // namespace
 
 extern "C" {
+
+int tqec_mlp_set_gemm(tqec_mlp* p, int use_tensor_cores) {
+  if (!p) return sfail(TQEC_ERR_INVALID, "NULL argument");
+  std::lock_guard<std::mutex> lk(p->mu);
+  p->use_tensor_cores = use_tensor_cores ? 1 : 0;
+  return TQEC_OK;
+}
+
+int tqec_mlp_forward_logits(tqec_mlp* p, const uint8_t* syn, int64_t n, float* logits_out) {
+  if (!p || !syn || !logits_out || n <= 0) return sfail(TQEC_ERR_INVALID, "bad argument");
+  std::lock_guard<std::mutex> lk(p->mu);
+  SQ_CUDA(cudaSetDevice(p->cfg.device));
+  cudaStream_t st = p->stream;
+  int rc = ensure_cap(p, n);
+  if (rc) return rc;
+  const uint8_t* ds;
+  if ((rc = stage_syn(p, syn, n, st, &ds))) return rc;
+  if ((rc = forward(p, ds, n, st))) return rc;
+  SQ_CUDA(cudaMemcpy2DAsync(logits_out, sizeof(float) * p->cfg.n_out, p->logits, sizeof(float) * p->out_pad,
+                            sizeof(float) * p->cfg.n_out, size_t(n), cudaMemcpyDeviceToHost, st));
+  return check_device_error(p, st);
+}
 
 int tqec_mlp_create(const tqec_mlp_config* cfg, tqec_mlp** out) {
   if (!cfg || !out) return sfail(TQEC_ERR_INVALID, "NULL argument");
@@ -249,8 +290,10 @@ int tqec_mlp_create(const tqec_mlp_config* cfg, tqec_mlp** out) {
       cudaMalloc(&p->m, sizeof(float) * off) || cudaMalloc(&p->v, sizeof(float) * off) ||
       cudaMalloc(&p->w16, sizeof(__nv_bfloat16) * off) || cudaMalloc(&p->loss, sizeof(float)) ||
       cudaMallocHost(&p->h_loss, sizeof(float)) || cudaMalloc(&p->count, sizeof(int32_t)) ||
-      cudaMallocHost(&p->h_count, sizeof(int32_t)))
+      cudaMallocHost(&p->h_count, sizeof(int32_t)) || cudaMalloc(&p->d_err, sizeof(int)) ||
+      cudaMallocHost(&p->h_err, sizeof(int)))
     return bail(TQEC_ERR_OOM, "surrogate parameters");
+  cudaMemset(p->d_err, 0, sizeof(int));
   cudaMemset(p->m, 0, sizeof(float) * off);
   cudaMemset(p->v, 0, sizeof(float) * off);
   // uniform(-1/sqrt(fan_in), 1/sqrt(fan_in)) weights and biases; the padded
@@ -285,6 +328,8 @@ int tqec_mlp_destroy(tqec_mlp* p) {
   cudaFree(p->loss);
   cudaFree(p->count);
   cudaFree(p->syn);
+  cudaFree(p->d_err);
+  if (p->h_err) cudaFreeHost(p->h_err);
   if (p->h_loss) cudaFreeHost(p->h_loss);
   if (p->h_count) cudaFreeHost(p->h_count);
   if (p->stream) cudaStreamDestroy(p->stream);
@@ -391,7 +436,7 @@ int tqec_mlp_infer(tqec_mlp* p, const uint8_t* syn, int64_t n, int32_t* class_ou
     if (host_conf) SQ_CUDA(cudaMemcpyAsync(conf_out + r0, p->conf, sizeof(float) * m, cudaMemcpyDeviceToHost, st));
     if (host_in || host_cls || host_conf) SQ_CUDA(cudaStreamSynchronize(st));
   }
-  if (!stream) SQ_CUDA(cudaStreamSynchronize(st));
+  if (!stream) return check_device_error(p, st);
   return TQEC_OK;
 }
 
@@ -433,8 +478,8 @@ int tqec_gated_decode(tqec_mlp* p, tqec_program* prog, float threshold, const ui
                             host_cls ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice, st));
     if (host_cls) SQ_CUDA(cudaStreamSynchronize(st));
   }
-  if (!stream) SQ_CUDA(cudaStreamSynchronize(st));
   if (n_fallback_out) *n_fallback_out = total_fb;
+  if (!stream) return check_device_error(p, st);
   return TQEC_OK;
 }
 

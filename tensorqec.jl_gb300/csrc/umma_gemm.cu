@@ -1,0 +1,276 @@
+// umma_gemm.cu -- the surrogate's hidden-layer GEMM on the 5th-generation
+// tensor cores: D[M, N] = relu(A[M, K] * B[N, K]^T + bias) in bf16, float32
+// accumulation in tensor memory.
+//
+// One CTA computes a 128 x 256 tile.  Warp 0 streams 128x64 A and 256x64 B
+// tiles (bf16, K-major, 128-byte swizzle) into a 4-stage shared-memory ring
+// with TMA; warp 1's elected thread issues tcgen05.mma (M=128, N=256, K=16,
+// four per stage) into a 256-column TMEM accumulator and frees each stage
+// with tcgen05.commit; warps 4-7 wait for the accumulator, read it back with
+// tcgen05.ld (one TMEM lane quadrant per warp), add the bias, apply ReLU and
+// store bf16.  Every mbarrier wait is bounded: on timeout the kernel records
+// an error flag, stops issuing work and still releases its TMEM.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <mutex>
+
+#include "mlp.cuh"
+
+namespace tqec {
+namespace {
+
+constexpr int UM = 128, UN = 256, UK = 64, STAGES = 4;
+constexpr int A_BYTES = UM * UK * 2;  // 16 KB
+constexpr int B_BYTES = UN * UK * 2;  // 32 KB
+constexpr int STAGE_BYTES = A_BYTES + B_BYTES;
+constexpr uint32_t TMEM_COLS = 256;
+constexpr int UMMA_THREADS = 256;
+constexpr uint32_t WAIT_LIMIT = 1u << 24;
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count));
+}
+
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
+               : "memory");
+}
+
+__device__ __forceinline__ bool mbar_test(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_addr(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// Bounded wait on a phase; false (and the error flag set) on timeout.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int* err) {
+  for (uint32_t i = 0; i < WAIT_LIMIT; ++i)
+    if (mbar_test(bar, parity)) return true;
+  atomicExch(err, 1);
+  return false;
+}
+
+__device__ __forceinline__ void tma_load_2d(const CUtensorMap* map, uint64_t* bar, void* dst, int x, int y) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4}], [%2];" ::"r"(
+          smem_addr(dst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(smem_addr(bar)), "r"(x), "r"(y)
+      : "memory");
+}
+
+// Shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row atoms
+// 1024 bytes apart.
+__device__ __forceinline__ uint64_t sdesc(uint32_t saddr) {
+  uint64_t d = 0;
+  d |= uint64_t((saddr >> 4) & 0x3FFFu);
+  d |= uint64_t(1) << 16;             // leading byte offset (unused for swizzled K-major)
+  d |= uint64_t(1024 >> 4) << 32;     // stride byte offset
+  d |= uint64_t(1) << 46;             // descriptor version
+  d |= uint64_t(2) << 61;             // 128-byte swizzle
+  return d;
+}
+
+// Instruction descriptor of kind::f16: bf16 A and B, float32 D, both K-major.
+constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | (uint32_t(UN >> 3) << 17) | (uint32_t(UM >> 4) << 24);
+
+__device__ __forceinline__ void umma(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem_d),
+      "l"(a), "l"(b), "r"(kIdesc), "r"(accumulate));
+}
+
+__device__ __forceinline__ void umma_commit(uint64_t* bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_addr(bar))
+               : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+      "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+      "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+        "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+        "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
+__global__ void __launch_bounds__(UMMA_THREADS, 1)
+    umma_gemm_relu_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensorMap map_b,
+                          int M, int N, int K, const float* __restrict__ bias, __nv_bfloat16* __restrict__ out,
+                          int ldo, int* __restrict__ err) {
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  // stage buffers on a 1024-byte boundary (the 128-byte swizzle atom)
+  unsigned char* smem = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
+                                                         ~uintptr_t(1023));
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem + STAGES * STAGE_BYTES);
+  uint64_t* empty = full + STAGES;
+  uint64_t* acc_ready = empty + STAGES;
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(acc_ready + 1);
+  volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int m0 = blockIdx.y * UM, n0 = blockIdx.x * UN;
+  const int kblocks = K / UK;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < STAGES; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], 1);
+    }
+    mbar_init(acc_ready, 1);
+    *abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(tmem_slot)),
+                 "r"(TMEM_COLS));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = *tmem_slot;
+
+  if (warp == 0 && lane == 0) {
+    // TMA producer
+    int issued = 0;
+    for (int kb = 0; kb < kblocks; ++kb) {
+      const int s = kb % STAGES;
+      if (kb >= STAGES && !mbar_wait(&empty[s], uint32_t((kb / STAGES - 1) & 1), err)) {
+        *abort_flag = 1;
+        break;
+      }
+      if (*abort_flag) break;
+      unsigned char* sa = smem + s * STAGE_BYTES;
+      mbar_arrive_expect_tx(&full[s], STAGE_BYTES);
+      tma_load_2d(&map_a, &full[s], sa, kb * UK, m0);
+      tma_load_2d(&map_b, &full[s], sa + A_BYTES, kb * UK, n0);
+      issued = kb + 1;
+    }
+    // the copies still in flight land before the block exits (bounded)
+    for (int kb = issued > STAGES ? issued - STAGES : 0; kb < issued; ++kb)
+      mbar_wait(&full[kb % STAGES], uint32_t((kb / STAGES) & 1), err);
+  } else if (warp == 1 && lane == 0) {
+    // MMA issuer
+    bool ok = true;
+    for (int kb = 0; kb < kblocks && ok; ++kb) {
+      const int s = kb % STAGES;
+      if (!mbar_wait(&full[s], uint32_t((kb / STAGES) & 1), err)) {
+        *abort_flag = 1;
+        ok = false;
+        break;
+      }
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const uint32_t sa = smem_addr(smem + s * STAGE_BYTES);
+      const uint64_t da = sdesc(sa), db = sdesc(sa + A_BYTES);
+#pragma unroll
+      for (int kk = 0; kk < UK / 16; ++kk)  // advance 16 bf16 = 32 bytes along K inside the swizzle atom
+        umma(tmem, da + uint64_t(kk * 2), db + uint64_t(kk * 2), (kb | kk) != 0 ? 1u : 0u);
+      umma_commit(&empty[s]);
+    }
+    umma_commit(acc_ready);
+  } else if (warp >= 4) {
+    // epilogue: warp w reads TMEM lanes 32*(w%4) .. +31, one output row per thread
+    const int q = warp & 3;
+    const int row = m0 + q * 32 + lane;
+    const bool waited = mbar_wait(acc_ready, 0u, err);
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    // tcgen05.ld is warp-collective: decide for the whole warp
+    const bool go = __all_sync(0xffffffffu, waited && *abort_flag == 0);
+    if (go) {
+#pragma unroll 1
+      for (int c = 0; c < UN / 32; ++c) {
+        uint32_t r[32];
+        tmem_ld32(tmem + (uint32_t(q * 32) << 16) + uint32_t(c * 32), r);
+        const int col = n0 + c * 32;
+        if (row < M && col < N) {
+          __align__(16) __nv_bfloat16 v[32];
+#pragma unroll
+          for (int j = 0; j < 32; ++j) {
+            const float x = __uint_as_float(r[j]) + bias[col + j];
+            v[j] = __float2bfloat16(x > 0.f ? x : 0.f);
+          }
+          uint4* dst = reinterpret_cast<uint4*>(out + int64_t(row) * ldo + col);
+          const uint4* src = reinterpret_cast<const uint4*>(v);
+#pragma unroll
+          for (int j = 0; j < 4; ++j) dst[j] = src[j];
+        }
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 0) {
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS));
+  }
+}
+
+PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+  });
+  return fn;
+}
+
+bool make_map(CUtensorMap* map, const __nv_bfloat16* base, int rows, int cols, int ld, int box_rows) {
+  auto fn = encode_fn();
+  if (!fn) return false;
+  const cuuint64_t dims[2] = {cuuint64_t(cols), cuuint64_t(rows)};
+  const cuuint64_t strides[1] = {cuuint64_t(ld) * 2};
+  const cuuint32_t box[2] = {cuuint32_t(UK), cuuint32_t(box_rows)};
+  const cuuint32_t estr[2] = {1, 1};
+  return fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<__nv_bfloat16*>(base), dims, strides, box, estr,
+            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+}  // namespace
+
+bool umma_gemm_supported(int M, int N, int K, int lda, int ldb, int ldo, const void* A, const void* B,
+                         const void* out) {
+  return M > 0 && N % UN == 0 && K % UK == 0 && K > 0 && lda % 8 == 0 && ldb % 8 == 0 && ldo % 8 == 0 &&
+         (reinterpret_cast<uintptr_t>(A) % 16) == 0 && (reinterpret_cast<uintptr_t>(B) % 16) == 0 &&
+         (reinterpret_cast<uintptr_t>(out) % 16) == 0 && encode_fn() != nullptr;
+}
+
+cudaError_t umma_gemm_bias_relu(int M, int N, int K, const __nv_bfloat16* A, int lda, const __nv_bfloat16* B,
+                                int ldb, const float* bias, __nv_bfloat16* out, int ldo, int* err,
+                                cudaStream_t st) {
+  CUtensorMap ma, mb;
+  if (!make_map(&ma, A, M, K, lda, UM) || !make_map(&mb, B, N, K, ldb, UN)) return cudaErrorInvalidValue;
+  const size_t smem = size_t(STAGES) * STAGE_BYTES + 1024 + 256;
+  cudaError_t e = cudaFuncSetAttribute(umma_gemm_relu_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+  if (e != cudaSuccess) return e;
+  dim3 grid(N / UN, (M + UM - 1) / UM);
+  umma_gemm_relu_kernel<<<grid, UMMA_THREADS, smem, st>>>(ma, mb, M, N, K, bias, out, ldo, err);
+  return cudaGetLastError();
+}
+
+}  // namespace tqec

@@ -33,7 +33,8 @@ def _lib():
                "tqec_mlp_train_step": [vp, vp, vp, i64, C.c_float, vp, vp],
                "tqec_mlp_infer": [vp, vp, i64, vp, vp, vp],
                "tqec_gated_decode": [vp, vp, C.c_float, vp, i64, vp, vp, vp],
-               "tqec_mlp_save": [vp, C.c_char_p], "tqec_mlp_load": [vp, C.c_char_p]}
+               "tqec_mlp_save": [vp, C.c_char_p], "tqec_mlp_load": [vp, C.c_char_p],
+               "tqec_mlp_set_gemm": [vp, C.c_int], "tqec_mlp_forward_logits": [vp, vp, i64, vp]}
         for name, args in sig.items():
             f = getattr(L, name)
             f.argtypes = args
@@ -108,6 +109,17 @@ class Surrogate:
         conf = np.empty(n, dtype=np.float32)
         native.check(_lib().tqec_mlp_infer(self._h, _p(packed), n, _p(cls), _p(conf), None))
         return cls, conf
+
+    def use_tensor_cores(self, on=True):
+        """Hidden layers on the tcgen05 GEMM (where hidden % 256 == 0) or on
+        the SIMT GEMM."""
+        native.check(_lib().tqec_mlp_set_gemm(self._h, 1 if on else 0))
+
+    def logits(self, packed):
+        packed = np.ascontiguousarray(packed, dtype=np.uint8)
+        out = np.empty((packed.shape[0], self.cfg["n_out"]), dtype=np.float32)
+        native.check(_lib().tqec_mlp_forward_logits(self._h, _p(packed), packed.shape[0], _p(out)))
+        return out
 
     def save(self, path):
         native.check(_lib().tqec_mlp_save(self._h, path.encode()))
