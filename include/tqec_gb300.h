@@ -231,6 +231,27 @@ int tqec_mlp_forward_logits(tqec_mlp* mlp, const uint8_t* syndromes, int64_t n, 
 int tqec_mlp_save(tqec_mlp* mlp, const char* path);
 int tqec_mlp_load(tqec_mlp* mlp, const char* path);
 
+/* Float64 batch decode that allocates no device memory (no counterpart in
+ * the reference).  For callers that cannot allocate while they decode: a
+ * real-time decoding loop that must not stall or fail on an allocation, or a
+ * process whose device memory is already reserved in full by another
+ * allocator.  Same results as tqec_decode_batch with TQEC_F64, whatever the
+ * program's own precision.  All pointers must be device memory (host
+ * pointers are rejected, since staging them would allocate); logp_out may be
+ * NULL.  The only scratch is a 32 MiB array inside the library, which every
+ * GPU that loads the library holds until the process exits; a program whose
+ * float64 working set exceeds it (tqec_program_info: arena_elems * 8 bytes per
+ * syndrome) is rejected with TQEC_ERR_UNSUPPORTED.  The first call on a device
+ * looks up that array's device address on the current device and caches it;
+ * make that first call before any stream capture.  All calls share the one
+ * array: calls whose kernels overlap on the GPU (concurrent streams, other
+ * threads) race on it and must be serialised by the caller.  Every scratch
+ * element a call reads it has written first, so nothing needs clearing.  With
+ * stream == NULL the call runs on the default stream and returns when done. */
+int tqec_decode_batch_noalloc(tqec_program* prog, const uint8_t* syndromes,
+                              int64_t n, int32_t* class_out, double* logp_out,
+                              void* stream);
+
 /* Message of the calling thread's last failure (always NUL-terminated). */
 int tqec_last_error(char* buf, size_t len);
 

@@ -16,6 +16,7 @@
 #include "../../include/tqec_gb300.h"
 #include "contract.cuh"
 #include "plan.h"
+#include "program_view.h"
 
 namespace tqec {
 std::string& last_error_ref() {
@@ -312,6 +313,22 @@ int decode_locked(tqec_program* p, const uint8_t* syn, int64_t n, int32_t* cls, 
 }
 
 }  // namespace
+
+namespace tqec {
+
+int program_f64_view(tqec_program* p, ProgramF64View* v) {
+  if (!p || !v) return TQEC_ERR_INVALID;
+  v->args = base_args(p, TQEC_F64);
+  v->args.arena_global = nullptr;
+  v->device = p->device;
+  v->sm_count = p->sm_count;
+  v->threads = p->shape[TQEC_F64].threads;
+  v->group = p->shape[TQEC_F64].G;
+  v->mu = &p->mu;
+  return TQEC_OK;
+}
+
+}  // namespace tqec
 
 extern "C" {
 
