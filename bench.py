@@ -306,7 +306,9 @@ def run_ours(args):
     if dist:
         dist.barrier()
     torch.cuda.synchronize()
+    torch.cuda.nvtx.range_push("bench_step")
     ms = timed(lambda i: decode(d_syn[W + i].data_ptr(), d_cls.data_ptr()), range(K))
+    torch.cuda.nvtx.range_pop()
     if dist:
         dist.barrier()
     clk = clocks.stop()
