@@ -146,7 +146,8 @@ int tqec_program_autotune(tqec_program* prog, int64_t n_probe);
  * OMEinsum.contraction_complexity(ct), tndecoder.jl:273-279).  `steps` holds
  * n_steps records of 64 bytes: int32 a_kind, b_kind, a_ref, b_ref, a_prod,
  * b_prod; int8 a_sel[4], b_sel[4]; int32 lh, lfa, lfb, lk, out_off,
- * perm_off, pad, pad.  Release the view with tqec_plan_release. */
+ * perm_off, sync_after (1 = block barrier after the step), pad.  Release the
+ * view with tqec_plan_release. */
 typedef struct {
   int32_t n_steps;
   const void* steps;
@@ -184,6 +185,26 @@ typedef struct {
 int tqec_optimize_order(const tqec_network* net, const tqec_order_options* opts,
                         int32_t* steps_out, double* log2_macs_out,
                         int32_t* width_out);
+
+/* ---- error patterns: error_pattern(pos, ct, syndrome), tndecoder.jl:167-174
+ * A syndrome-consistent (ex, ez) of the decoded class for every row, in place
+ * of the reference's integer program (ipdecoder.jl:150-169): ex = rz * sz and
+ * ez = rx * sx with precomputed GF(2) right inverses (0/1 bytes, row-major
+ * nq x n_sz and nq x n_sx), then the reference's fix-up with lx, lz (k x nq).
+ * chk_* rows (each over n_s* bits) must all have even overlap with the
+ * syndrome half for it to be reachable; ok_out gets 0 for rows that are not.
+ * Outputs are bit-packed rows of ceil(nq/8) bytes; host or device memory. */
+typedef struct tqec_patterns tqec_patterns;
+
+int tqec_patterns_create(int32_t nq, int32_t n_sx, int32_t n_sz, int32_t k,
+                         const uint8_t* rx, const uint8_t* rz, int32_t n_chk_x,
+                         const uint8_t* chk_x, int32_t n_chk_z, const uint8_t* chk_z,
+                         const uint8_t* lx, const uint8_t* lz, int32_t device,
+                         tqec_patterns** out);
+int tqec_patterns_destroy(tqec_patterns* p);
+int tqec_patterns_decode(tqec_patterns* p, const uint8_t* syndromes, const int32_t* classes,
+                         int64_t n, uint8_t* ex_out, uint8_t* ez_out, uint8_t* ok_out,
+                         void* stream);
 
 /* ---- learned surrogate (no counterpart in the reference) -----------------
  * A ReLU MLP over the syndrome bits proposes the logical class with a

@@ -66,8 +66,44 @@ __device__ __forceinline__ int perm_addr(const int32_t* __restrict__ perm, int e
   return addr;
 }
 
+// Arena addresses are stored swizzled: bits 2..4 of an element's address are
+// XOR-ed with a hash of its higher bits.  The map is a bijection inside every
+// aligned 32-element block (arena sizes are multiples of 32), keeps groups of
+// four consecutive elements together (16-byte vectors stay intact) and
+// spreads the strided writes of permuted outputs over the shared-memory banks.
+__device__ __forceinline__ int swz(int a) {
+  return a ^ ((((a >> 5) ^ (a >> 8) ^ (a >> 11) ^ (a >> 14)) & 7) << 2);
+}
+
+// An operand: arena operands are addressed through swz(base + idx), constant
+// operands directly.
+template <typename T>
+struct Operand {
+  const T* p;
+  int base;
+  bool sw;
+  __device__ __forceinline__ T ld(int idx) const { return sw ? p[swz(base + idx)] : p[base + idx]; }
+  __device__ __forceinline__ const T* vec(int idx) const { return sw ? p + swz(base + idx) : p + base + idx; }
+};
+
+template <typename T>
+__device__ __forceinline__ Operand<T> make_operand(int kind, int32_t ref, const int8_t* sel, int obits, T* arena_g,
+                                                   const T* consts, const uint32_t* syn) {
+  Operand<T> o;
+  if (kind == OP_ARENA) {
+    o.p = arena_g;
+    o.base = ref;
+    o.sw = true;
+  } else {
+    o.p = operand_ptr<T>(kind, ref, sel, obits, arena_g, consts, syn);
+    o.base = 0;
+    o.sw = false;
+  }
+  return o;
+}
+
 template <typename T, bool NORM, bool APAR, bool BPAR>
-__device__ void run_step(const KArgs& a, const StepDesc& d, int st, const uint32_t* s_syn,
+__device__ int run_step(const KArgs& a, const StepDesc& d, int st, int item_base, const uint32_t* s_syn,
                          uint32_t* s_max, T* arena, const T* consts) {
   const int lw = d.lh + d.lfa + d.lfb;
   const int total = 1 << (lw + a.lg);
@@ -78,7 +114,10 @@ __device__ void run_step(const KArgs& a, const StepDesc& d, int st, const uint32
   const int K = 1 << d.lk;
   const int abits = d.lh + d.lfa + d.lk;
   const int bbits = d.lh + d.lk + d.lfb;
-  for (int i = threadIdx.x; i < total_r; i += blockDim.x) {
+  // item i runs on thread (i + item_base) mod blockDim: steps of one barrier
+  // group start on different threads (item_base is a multiple of 32)
+  const int i0 = (int(threadIdx.x) + int(blockDim.x) - item_base % int(blockDim.x)) % int(blockDim.x);
+  for (int i = i0; i < total_r; i += blockDim.x) {
     const bool valid = i < total;
     const int g = valid ? (i >> lw) : 0;
     const int e = i & mw;
@@ -91,13 +130,12 @@ __device__ void run_step(const KArgs& a, const StepDesc& d, int st, const uint32
       const int h = e >> (d.lfb + d.lfa);
       const int abase = ((h << d.lfa) | fa) << d.lk;
       const int bbase = (h << (d.lk + d.lfb)) | fb;
-      const T* ap = nullptr;
-      const T* bp = nullptr;
+      Operand<T> A{}, B{};
       int as = 0, bs = 0;
       if (APAR) as = syn_bit(syn, d.a_ref);
-      else ap = operand_ptr<T>(d.a_kind, d.a_ref, d.a_sel, abits, arena_g, consts, syn);
+      else A = make_operand<T>(d.a_kind, d.a_ref, d.a_sel, abits, arena_g, consts, syn);
       if (BPAR) bs = syn_bit(syn, d.b_ref);
-      else bp = operand_ptr<T>(d.b_kind, d.b_ref, d.b_sel, bbits, arena_g, consts, syn);
+      else B = make_operand<T>(d.b_kind, d.b_ref, d.b_sel, bbits, arena_g, consts, syn);
       T fa_s = T(1), fb_s = T(1);
       if (NORM) {
         int ee;
@@ -109,30 +147,21 @@ __device__ void run_step(const KArgs& a, const StepDesc& d, int st, const uint32
           acc += parity_val<T>(abase + k, as) * parity_val<T>(bbase + (k << d.lfb), bs);
       } else if (APAR) {
         for (int k = 0; k < K; ++k)
-          if (parity_val<T>(abase + k, as) != T(0)) acc += bp[bbase + (k << d.lfb)];
+          if (parity_val<T>(abase + k, as) != T(0)) acc += B.ld(bbase + (k << d.lfb));
       } else if (BPAR) {
         for (int k = 0; k < K; ++k)
-          if (parity_val<T>(bbase + (k << d.lfb), bs) != T(0)) acc += ap[abase + k];
+          if (parity_val<T>(bbase + (k << d.lfb), bs) != T(0)) acc += A.ld(abase + k);
         if (NORM) acc *= fa_s;
       } else {
-        int k = 0;
-        for (; k + 4 <= K; k += 4) {
-          T a0 = ap[abase + k], a1 = ap[abase + k + 1], a2 = ap[abase + k + 2], a3 = ap[abase + k + 3];
-          if (NORM) { a0 *= fa_s; a1 *= fa_s; a2 *= fa_s; a3 *= fa_s; }
-          acc = fma(a0, bp[bbase + (k << d.lfb)], acc);
-          acc = fma(a1, bp[bbase + ((k + 1) << d.lfb)], acc);
-          acc = fma(a2, bp[bbase + ((k + 2) << d.lfb)], acc);
-          acc = fma(a3, bp[bbase + ((k + 3) << d.lfb)], acc);
-        }
-        for (; k < K; ++k) {
-          T a0 = ap[abase + k];
+        for (int k = 0; k < K; ++k) {
+          T a0 = A.ld(abase + k);
           if (NORM) a0 *= fa_s;
-          acc = fma(a0, bp[bbase + (k << d.lfb)], acc);
+          acc = fma(a0, B.ld(bbase + (k << d.lfb)), acc);
         }
       }
       if (NORM && !BPAR) acc *= fb_s;
       const int addr = d.perm_off < 0 ? e : perm_addr(a.perm + d.perm_off, e, lw);
-      arena_g[d.out_off + addr] = acc;
+      arena_g[swz(d.out_off + addr)] = acc;
     }
     if (NORM) {
       uint32_t bits = __float_as_uint(float(acc));
@@ -144,6 +173,7 @@ __device__ void run_step(const KArgs& a, const StepDesc& d, int st, const uint32
       if (valid && (threadIdx.x & (seg - 1)) == 0) atomicMax(&s_max[g * a.n_steps + st], bits);
     }
   }
+  return total_r;
 }
 
 template <typename T>
@@ -172,13 +202,19 @@ __device__ __forceinline__ void store4<double>(double* p, const double v[4]) {
   reinterpret_cast<double2*>(p)[1] = make_double2(v[2], v[3]);
 }
 
+template <typename T>
+__device__ __forceinline__ T pick4(const T v[4], int j) {
+  return j == 0 ? v[0] : (j == 1 ? v[1] : (j == 2 ? v[2] : v[3]));
+}
+
 // A step whose B-only group has at least 4 entries: each work item is four
 // consecutive outputs along fb, which share every A value and read B as one
 // 16-byte vector.  Operand bases, fb offsets and k strides are multiples of 4
 // elements (arena and constant offsets are planned that way), so the vector
-// accesses are aligned.
+// accesses are aligned.  Permuted outputs are written in a lane-rotated order
+// so that the four stores of a warp instruction hit different index bits.
 template <typename T, bool NORM, bool APAR, bool BPAR>
-__device__ void run_step_v4(const KArgs& a, const StepDesc& d, int st, const uint32_t* s_syn,
+__device__ int run_step_v4(const KArgs& a, const StepDesc& d, int st, int item_base, const uint32_t* s_syn,
                             uint32_t* s_max, T* arena, const T* consts) {
   const int lw = d.lh + d.lfa + d.lfb;
   const int lwv = lw - 2;
@@ -192,7 +228,9 @@ __device__ void run_step_v4(const KArgs& a, const StepDesc& d, int st, const uin
   const int bbits = d.lh + d.lk + d.lfb;
   const int32_t* perm = d.perm_off < 0 ? nullptr : a.perm + d.perm_off;
   const int cb0 = lw < 8 ? lw : 8;
-  for (int i = threadIdx.x; i < total_r; i += blockDim.x) {
+  const int rot = threadIdx.x & 3;
+  const int i0 = (int(threadIdx.x) + int(blockDim.x) - item_base % int(blockDim.x)) % int(blockDim.x);
+  for (int i = i0; i < total_r; i += blockDim.x) {
     const bool valid = i < total;
     const int g = valid ? (i >> lwv) : 0;
     const int e0 = (i & mwv) << 2;
@@ -205,13 +243,12 @@ __device__ void run_step_v4(const KArgs& a, const StepDesc& d, int st, const uin
       const int h = e0 >> (d.lfb + d.lfa);
       const int abase = ((h << d.lfa) | fa) << d.lk;
       const int bbase = (h << (d.lk + d.lfb)) | fb0;
-      const T* ap = nullptr;
-      const T* bp = nullptr;
+      Operand<T> A{}, B{};
       int as = 0, bs = 0;
       if (APAR) as = syn_bit(syn, d.a_ref);
-      else ap = operand_ptr<T>(d.a_kind, d.a_ref, d.a_sel, abits, arena_g, consts, syn);
+      else A = make_operand<T>(d.a_kind, d.a_ref, d.a_sel, abits, arena_g, consts, syn);
       if (BPAR) bs = syn_bit(syn, d.b_ref);
-      else bp = operand_ptr<T>(d.b_kind, d.b_ref, d.b_sel, bbits, arena_g, consts, syn);
+      else B = make_operand<T>(d.b_kind, d.b_ref, d.b_sel, bbits, arena_g, consts, syn);
       T fa_s = T(1), fb_s = T(1);
       if (NORM) {
         int ee;
@@ -224,7 +261,7 @@ __device__ void run_step_v4(const KArgs& a, const StepDesc& d, int st, const uin
           if (parity_val<T>(abase + k, as) == T(0)) continue;
           av = T(1);
         } else {
-          av = ap[abase + k];
+          av = A.ld(abase + k);
           if (NORM) av *= fa_s;
         }
         T bv[4];
@@ -233,7 +270,7 @@ __device__ void run_step_v4(const KArgs& a, const StepDesc& d, int st, const uin
 #pragma unroll
           for (int j = 0; j < 4; ++j) bv[j] = parity_val<T>(bi + j, bs);
         } else {
-          load4<T>(bp + bi, bv);
+          load4<T>(B.vec(bi), bv);
         }
 #pragma unroll
         for (int j = 0; j < 4; ++j) acc[j] = fma(av, bv[j], acc[j]);
@@ -242,9 +279,8 @@ __device__ void run_step_v4(const KArgs& a, const StepDesc& d, int st, const uin
 #pragma unroll
         for (int j = 0; j < 4; ++j) acc[j] *= fb_s;
       }
-      T* out = arena_g + d.out_off;
       if (!perm) {
-        store4<T>(out + e0, acc);
+        store4<T>(arena_g + swz(d.out_off + e0), acc);
       } else {
         const int4 lo = *reinterpret_cast<const int4*>(perm + (e0 & ((1 << cb0) - 1)));
         int hi = 0;
@@ -254,10 +290,12 @@ __device__ void run_step_v4(const KArgs& a, const StepDesc& d, int st, const uin
           hi |= __ldg(perm + tab + ((e0 >> sh) & ((1 << cb) - 1)));
           tab += 1 << cb;
         }
-        out[lo.x | hi] = acc[0];
-        out[lo.y | hi] = acc[1];
-        out[lo.z | hi] = acc[2];
-        out[lo.w | hi] = acc[3];
+        const int los[4] = {lo.x, lo.y, lo.z, lo.w};
+#pragma unroll
+        for (int s4 = 0; s4 < 4; ++s4) {
+          const int j = (s4 + rot) & 3;
+          arena_g[swz(d.out_off + (pick4(los, j) | hi))] = pick4(acc, j);
+        }
       }
     }
     if (NORM) {
@@ -271,6 +309,7 @@ __device__ void run_step_v4(const KArgs& a, const StepDesc& d, int st, const uin
       if (valid && (threadIdx.x & (seg - 1)) == 0) atomicMax(&s_max[g * a.n_steps + st], bits);
     }
   }
+  return total_r;
 }
 
 template <typename T, bool NORM>
@@ -311,21 +350,28 @@ __global__ void __launch_bounds__(1024) tn_contract_kernel(KArgs a) {
     if (NORM)
       for (int i = threadIdx.x; i < a.G * a.n_steps; i += blockDim.x) s_max[i] = 0u;
     __syncthreads();
+    int item_base = 0;
     for (int st = 0; st < a.n_steps; ++st) {
       const StepDesc& d = s_steps[st];
       const bool ap = d.a_kind == OP_PARITY, bp = d.b_kind == OP_PARITY;
+      int items;
       if (d.lfb >= 2) {
-        if (ap && bp) run_step_v4<T, NORM, true, true>(a, d, st, s_syn, s_max, arena, consts);
-        else if (ap) run_step_v4<T, NORM, true, false>(a, d, st, s_syn, s_max, arena, consts);
-        else if (bp) run_step_v4<T, NORM, false, true>(a, d, st, s_syn, s_max, arena, consts);
-        else run_step_v4<T, NORM, false, false>(a, d, st, s_syn, s_max, arena, consts);
+        if (ap && bp) items = run_step_v4<T, NORM, true, true>(a, d, st, item_base, s_syn, s_max, arena, consts);
+        else if (ap) items = run_step_v4<T, NORM, true, false>(a, d, st, item_base, s_syn, s_max, arena, consts);
+        else if (bp) items = run_step_v4<T, NORM, false, true>(a, d, st, item_base, s_syn, s_max, arena, consts);
+        else items = run_step_v4<T, NORM, false, false>(a, d, st, item_base, s_syn, s_max, arena, consts);
       } else {
-        if (ap && bp) run_step<T, NORM, true, true>(a, d, st, s_syn, s_max, arena, consts);
-        else if (ap) run_step<T, NORM, true, false>(a, d, st, s_syn, s_max, arena, consts);
-        else if (bp) run_step<T, NORM, false, true>(a, d, st, s_syn, s_max, arena, consts);
-        else run_step<T, NORM, false, false>(a, d, st, s_syn, s_max, arena, consts);
+        if (ap && bp) items = run_step<T, NORM, true, true>(a, d, st, item_base, s_syn, s_max, arena, consts);
+        else if (ap) items = run_step<T, NORM, true, false>(a, d, st, item_base, s_syn, s_max, arena, consts);
+        else if (bp) items = run_step<T, NORM, false, true>(a, d, st, item_base, s_syn, s_max, arena, consts);
+        else items = run_step<T, NORM, false, false>(a, d, st, item_base, s_syn, s_max, arena, consts);
       }
-      __syncthreads();
+      if (d.sync_after) {
+        __syncthreads();
+        item_base = 0;
+      } else {
+        item_base += items;
+      }
     }
     // epilogue: log-marginals, first argmax (Julia findmax order), recheck flag
     const StepDesc& root = s_steps[a.n_steps - 1];
@@ -333,7 +379,7 @@ __global__ void __launch_bounds__(1024) tn_contract_kernel(KArgs a) {
       const int64_t r = base + g;
       if (r >= nrows) continue;
       const int64_t row = a.list ? int64_t(a.list[r]) : r + a.row_offset;
-      const T* rv = arena + int64_t(g) * a.arena_elems + root.out_off;
+      const T* rv = arena + int64_t(g) * a.arena_elems;
       double lsc = 0.0;
       if (NORM) {
         for (int st = 0; st < a.n_steps - 1; ++st) {
@@ -346,7 +392,7 @@ __global__ void __launch_bounds__(1024) tn_contract_kernel(KArgs a) {
       double best = -INFINITY, second = -INFINITY;
       int bc = 0;
       for (int c = 0; c < a.n_classes; ++c) {
-        const double v = double(rv[c]);
+        const double v = double(rv[swz(root.out_off + c)]);
         const double lp = v > 0.0 ? log(v) + lsc : -INFINITY;
         if (a.logp_out) a.logp_out[row * a.n_classes + c] = lp;
         if (lp > best) {

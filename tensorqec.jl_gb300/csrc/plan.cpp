@@ -508,9 +508,37 @@ std::string build_plan(const NetworkView& net, int32_t n_steps, const int32_t* s
     }
     free_list.swap(merged);
   };
+  // ---- barrier groups: consecutive steps that do not read each other's
+  // outputs run between the same pair of block barriers.  Wide steps stay
+  // alone (they fill the block by themselves and dominate the arena).
+  std::vector<char> group_end(R, 0);
+  {
+    constexpr int kMaxGroup = 8;
+    constexpr int kMaxGroupedWidth = 12;
+    std::vector<char> in_group(nodes.size(), 0);
+    std::vector<int> members;
+    for (int r = 0; r < R; ++r) {
+      const int id = order[r];
+      const StepLayout& L = lay[r];
+      const bool wide = (int)nodes[id].vars.size() > kMaxGroupedWidth;
+      bool dep = false;
+      for (int op : {L.a, L.b})
+        if (nodes[op].kind == NK_RUNTIME && in_group[op]) dep = true;
+      if (r > 0 && (dep || wide || (int)members.size() >= kMaxGroup ||
+                    (int)nodes[order[r - 1]].vars.size() > kMaxGroupedWidth)) {
+        group_end[r - 1] = 1;
+        for (int m : members) in_group[m] = 0;
+        members.clear();
+      }
+      in_group[id] = 1;
+      members.push_back(id);
+    }
+    group_end[R - 1] = 1;
+  }
   int width = 0;
   double macs_rt = 0.0;
   P.steps.resize(R);
+  std::vector<int> pending_release;
   for (int r = 0; r < R; ++r) {
     const int id = order[r];
     PNode& n = nodes[id];
@@ -519,8 +547,13 @@ std::string build_plan(const NetworkView& net, int32_t n_steps, const int32_t* s
     width = std::max(width, (int)n.vars.size());
     int64_t off = alloc(osz);
     arena_off[id] = off;
+    // operands are freed when the whole barrier group has run
     for (int op : {L.a, L.b})
-      if (nodes[op].kind == NK_RUNTIME) release(arena_off[op], int64_t(1) << nodes[op].vars.size());
+      if (nodes[op].kind == NK_RUNTIME) pending_release.push_back(op);
+    if (group_end[r]) {
+      for (int op : pending_release) release(arena_off[op], int64_t(1) << nodes[op].vars.size());
+      pending_release.clear();
+    }
     macs_rt += std::ldexp(1.0, (int)(L.H.size() + L.Fa.size() + L.Fb.size() + L.K.size()));
     StepDesc d;
     std::memset(&d, 0, sizeof(d));
@@ -529,6 +562,7 @@ std::string build_plan(const NetworkView& net, int32_t n_steps, const int32_t* s
     d.lfb = (int)L.Fb.size();
     d.lk = (int)L.K.size();
     d.out_off = (int32_t)off;
+    d.sync_after = group_end[r];
     for (int side = 0; side < 2; ++side) {
       int op = side ? L.b : L.a;
       PNode& o = nodes[op];

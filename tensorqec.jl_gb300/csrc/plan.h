@@ -38,7 +38,8 @@ struct StepDesc {
   int32_t lh, lfa, lfb, lk;  // log2 sizes of the index groups
   int32_t out_off;           // arena offset of the output
   int32_t perm_off;          // output permutation tables, -1 = identity
-  int32_t pad0, pad1;
+  int32_t sync_after;        // 1: block barrier after this step (end of a barrier group)
+  int32_t pad1;
 };
 static_assert(sizeof(StepDesc) == 64, "StepDesc is 64 bytes");
 

@@ -204,6 +204,23 @@ class CompiledTNMMAP:
                 ez = ez ^ self.lz[i]
         return CSSErrorPattern(ex, ez)
 
+    def _pattern_decoder(self):
+        if getattr(self, "_patterns", None) is None:
+            self._patterns = native.PatternDecoder(self.tanner, self.lx, self.lz, self.decoder.device)
+        return self._patterns
+
+    def decode_patterns(self, syndromes, classes=None):
+        """Batched ``decode``: classes (argmax of the marginal, unless given)
+        and the rebuilt (ex, ez) error patterns of every row, all on the GPU.
+        Returns (classes, ex, ez, ok) with ex/ez as (n, nq) 0/1 arrays and
+        ok = 0 for syndromes no error produces."""
+        bits = self._bits(syndromes)
+        packed = pack_syndromes(bits)
+        if classes is None:
+            classes = self.program.decode_packed(packed)
+        ex, ez, ok = self._pattern_decoder().decode(packed, np.asarray(classes, dtype=np.int32))
+        return classes, ex, ez, ok
+
     def decode(self, syndrome: CSSSyndrome) -> DecodingResult:
         """decode(ct, syndrome), tndecoder.jl:160-165."""
         cls = int(self.decode_batch(syndrome)[0])

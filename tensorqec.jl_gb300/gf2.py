@@ -239,3 +239,34 @@ def remove_linear_dependency_rows(x_rows, z_rows, nq):
     b.eliminate(0, b.xcodenum - 1, 0, 0)
     b.eliminate(b.xcodenum, len(rows) - 1, nq, b.xcodenum)
     return [i for i, r in enumerate(b.rows) if r]
+
+
+def right_inverse(H: np.ndarray):
+    """(R, C) over GF(2) for an m x n matrix H: R (n x m) maps every
+    reachable syndrome s to an e = R s with H e = s; the rows of C (r x m)
+    all have even overlap with s exactly when s is reachable."""
+    H = np.asarray(H).astype(np.uint8)
+    m, n = H.shape
+    rows = rows_from_matrix(H)
+    rec = [1 << i for i in range(m)]
+    pivots = []
+    r = 0
+    for c in range(n):
+        piv = next((k for k in range(r, m) if (rows[k] >> c) & 1), None)
+        if piv is None:
+            continue
+        rows[r], rows[piv] = rows[piv], rows[r]
+        rec[r], rec[piv] = rec[piv], rec[r]
+        for k in range(m):
+            if k != r and (rows[k] >> c) & 1:
+                rows[k] ^= rows[r]
+                rec[k] ^= rec[r]
+        pivots.append(c)
+        r += 1
+        if r == m:
+            break
+    R = np.zeros((n, m), dtype=np.uint8)
+    for i, c in enumerate(pivots):
+        R[c] = matrix_from_rows([rec[i]], m)[0]
+    C = matrix_from_rows(rec[r:], m) if r < m else np.zeros((0, m), dtype=np.uint8)
+    return R, C

@@ -69,7 +69,7 @@ class OrderOptions(C.Structure):
 STEP_DTYPE = np.dtype([("a_kind", "<i4"), ("b_kind", "<i4"), ("a_ref", "<i4"), ("b_ref", "<i4"),
                        ("a_prod", "<i4"), ("b_prod", "<i4"), ("a_sel", "i1", (4,)), ("b_sel", "i1", (4,)),
                        ("lh", "<i4"), ("lfa", "<i4"), ("lfb", "<i4"), ("lk", "<i4"),
-                       ("out_off", "<i4"), ("perm_off", "<i4"), ("pad0", "<i4"), ("pad1", "<i4")])
+                       ("out_off", "<i4"), ("perm_off", "<i4"), ("sync_after", "<i4"), ("pad1", "<i4")])
 assert STEP_DTYPE.itemsize == 64
 
 _lib = None
@@ -97,6 +97,9 @@ def lib():
         "tqec_plan_release": [vp],
         "tqec_optimize_order": [vp, vp, vp, vp, vp],
         "tqec_last_error": [vp, C.c_size_t],
+        "tqec_patterns_create": [i32, i32, i32, i32, vp, vp, i32, vp, i32, vp, vp, vp, i32, vp],
+        "tqec_patterns_destroy": [vp],
+        "tqec_patterns_decode": [vp, vp, vp, i64, vp, vp, vp, vp],
     }
     for name, args in sig.items():
         f = getattr(L, name)
@@ -244,3 +247,43 @@ class Program:
         info = ProgramInfo()
         check(lib().tqec_program_info(self._h, C.byref(info)))
         self.info = {f: getattr(info, f) for f, _ in ProgramInfo._fields_}
+
+
+class PatternDecoder:
+    """Owner of a ``tqec_patterns`` (batched error_pattern for a CSS code)."""
+
+    def __init__(self, tanner, lx, lz, device=0):
+        from . import gf2
+
+        rx, cx = gf2.right_inverse(tanner.stgx.H)
+        rz, cz = gf2.right_inverse(tanner.stgz.H)
+        self._keep = [np.ascontiguousarray(a, dtype=np.uint8) for a in (rx, rz, cx, cz, lx, lz)]
+        rx, rz, cx, cz, lxa, lza = self._keep
+        self.nq = tanner.nq
+        h = C.c_void_p()
+        check(lib().tqec_patterns_create(tanner.nq, tanner.stgx.ns, tanner.stgz.ns, lx.shape[0], _ptr(rx),
+                                         _ptr(rz), cx.shape[0], _ptr(cx) if cx.size else None, cz.shape[0],
+                                         _ptr(cz) if cz.size else None, _ptr(lxa), _ptr(lza), device,
+                                         C.byref(h)))
+        self._h = h
+
+    def decode(self, packed, classes):
+        packed = np.ascontiguousarray(packed, dtype=np.uint8)
+        classes = np.ascontiguousarray(classes, dtype=np.int32)
+        n = packed.shape[0]
+        qb = (self.nq + 7) // 8
+        ex = np.empty((n, qb), dtype=np.uint8)
+        ez = np.empty((n, qb), dtype=np.uint8)
+        ok = np.empty(n, dtype=np.uint8)
+        check(lib().tqec_patterns_decode(self._h, _ptr(packed), _ptr(classes), n, _ptr(ex), _ptr(ez), _ptr(ok),
+                                         None))
+        unpack = lambda a: np.unpackbits(a, axis=1, count=self.nq, bitorder="little")  # noqa: E731
+        return unpack(ex), unpack(ez), ok
+
+    def __del__(self):
+        try:
+            if getattr(self, "_h", None):
+                lib().tqec_patterns_destroy(self._h)
+                self._h = None
+        except Exception:
+            pass

@@ -189,3 +189,33 @@ def test_empty_batch_and_device_pointers(pkg):
     torch.cuda.synchronize()
     assert np.array_equal(d_cls.cpu().numpy(), want)
     ct.close()
+
+
+@pytest.mark.parametrize("kind,d", [("surface", 3), ("surface", 7), ("toric", 4), ("666", 5)])
+def test_gpu_error_patterns(pkg, oracle, kind, d):
+    """error_pattern (tndecoder.jl:167-174) on the GPU: each rebuilt pattern
+    reproduces its syndrome and carries the decoded class."""
+    code = {"surface": lambda: pkg.SurfaceCode(d, d), "toric": lambda: pkg.ToricCode(d, d),
+            "666": lambda: pkg.Color666(d)}[kind]()
+    t = pkg.tanner_graph(code)
+    em = pkg.depolarizing(0.08, t.nq)
+    ct = pkg.compile(pkg.TNMMAP(precision="f32"), t, em)
+    rng = np.random.default_rng(31)
+    ep = pkg.random_error_pattern(em, rng, nsamples=2000)
+    syn = pkg.syndrome_extraction(ep, t)
+    bits = np.concatenate([syn.sx, syn.sz], axis=1)
+    forced = rng.integers(0, ct.n_classes, size=2000).astype(np.int32)
+    for classes in (None, forced):
+        cls, ex, ez, ok = ct.decode_patterns(bits, classes)
+        assert ok.all()
+        assert np.array_equal((ez.astype(np.int64) @ t.stgx.H.T) % 2, syn.sx)
+        assert np.array_equal((ex.astype(np.int64) @ t.stgz.H.T) % 2, syn.sz)
+        k = ct.lx.shape[0]
+        a = (ez.astype(np.int64) @ ct.lx.T) % 2
+        b = (ex.astype(np.int64) @ ct.lz.T) % 2
+        got = (a * (1 << np.arange(k))).sum(1) + (b * (1 << (k + np.arange(k)))).sum(1)
+        assert np.array_equal(got, cls)
+    # the single-syndrome decode path agrees with the batched one
+    res = ct.decode(pkg.CSSSyndrome(syn.sx[0], syn.sz[0]))
+    assert res.success_tag and pkg.syndrome_extraction(res.error_pattern, t) == pkg.CSSSyndrome(syn.sx[0], syn.sz[0])
+    ct.close()

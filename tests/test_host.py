@@ -158,3 +158,23 @@ def test_dem_graph_matches_oracle(pkg, oracle, kat):
     assert g.ixs == net.ixs and g.iy == net.iy and g.syndrome_positions == net.syndrome_positions
     for a, b in zip(g.tensors, net.tensors):
         np.testing.assert_array_equal(a, np.asarray(b).flatten(order="F"))
+
+
+@pytest.mark.parametrize("kind,d", [("surface", 5), ("toric", 3), ("488", 5)])
+def test_right_inverse(pkg, oracle, kind, d):
+    code, _ = _codes(pkg, oracle, kind, d)
+    t = pkg.tanner_graph(code)
+    rng = np.random.default_rng(d)
+    for H in (t.stgx.H, t.stgz.H, np.vstack([t.stgz.H, t.stgz.H[:2]])):
+        R, Cc = pkg.gf2.right_inverse(H)
+        for _ in range(20):
+            e = (rng.random(H.shape[1]) < 0.2).astype(np.int64)
+            s = (H.astype(np.int64) @ e) % 2
+            e2 = (R.astype(np.int64) @ s) % 2
+            assert np.array_equal((H.astype(np.int64) @ e2) % 2, s)
+            assert not ((Cc.astype(np.int64) @ s) % 2).any()
+        if Cc.shape[0]:
+            # a syndrome violating a consistency row is not reachable
+            s = np.zeros(H.shape[0], dtype=np.int64)
+            s[np.flatnonzero(Cc[0])[0]] = 1
+            assert ((Cc.astype(np.int64) @ s) % 2).any()
