@@ -252,6 +252,31 @@ int tqec_mlp_forward_logits(tqec_mlp* mlp, const uint8_t* syndromes, int64_t n, 
 int tqec_mlp_save(tqec_mlp* mlp, const char* path);
 int tqec_mlp_load(tqec_mlp* mlp, const char* path);
 
+/* ---- seeded sampling and the Monte-Carlo loop (no counterpart in the
+ * reference's decoder path; replaces the host loop of multi_round_qec,
+ * threshold.jl:1-19, with check_logical_error, error_model.jl:179-181).
+ * Per sample and qubit one Philox4x32-10 uniform picks the Pauli as
+ * random_error_pattern does (error_model.jl:97-117); the syndrome is
+ * [Hx ez ; Hz ex] bit-packed, the true class the Julia linear index of mar
+ * for a = lx.ez, b = lz.ex.  hx/hz are 0/1 bytes (n_s* x nq), lx/lz (k x nq),
+ * px/py/pz per qubit.  Sample i of seed s is the same for any batching. */
+typedef struct tqec_sampler tqec_sampler;
+
+int tqec_sampler_create(int32_t nq, int32_t n_sx, int32_t n_sz, const uint8_t* hx,
+                        const uint8_t* hz, int32_t k, const uint8_t* lx, const uint8_t* lz,
+                        const double* px, const double* py, const double* pz, int32_t device,
+                        tqec_sampler** out);
+int tqec_sampler_destroy(tqec_sampler* s);
+/* Samples offset .. offset+n-1 of `seed`; host or device outputs. */
+int tqec_sample(tqec_sampler* s, uint64_t seed, uint64_t offset, int64_t n,
+                uint8_t* syndromes_out, int32_t* class_out, void* stream);
+/* Samples n_total syndromes in batches on the device, decodes them with
+ * `prog` (or the gated surrogate `mlp` in front of it when not NULL) and
+ * counts decoded classes that differ from the true class (logical errors). */
+int tqec_monte_carlo(tqec_sampler* s, tqec_program* prog, tqec_mlp* mlp, float threshold,
+                     uint64_t seed, int64_t n_total, int64_t batch, int64_t* n_logical_errors,
+                     int64_t* n_fallback);
+
 /* Float64 batch decode that allocates no device memory (no counterpart in
  * the reference).  For callers that cannot allocate while they decode: a
  * real-time decoding loop that must not stall or fail on an allocation, or a

@@ -66,39 +66,19 @@ __device__ __forceinline__ int perm_addr(const int32_t* __restrict__ perm, int e
   return addr;
 }
 
-// Arena addresses are stored swizzled: bits 2..4 of an element's address are
-// XOR-ed with a hash of its higher bits.  The map is a bijection inside every
-// aligned 32-element block (arena sizes are multiples of 32), keeps groups of
-// four consecutive elements together (16-byte vectors stay intact) and
-// spreads the strided writes of permuted outputs over the shared-memory banks.
-__device__ __forceinline__ int swz(int a) {
-  return a ^ ((((a >> 5) ^ (a >> 8) ^ (a >> 11) ^ (a >> 14)) & 7) << 2);
-}
-
-// An operand: arena operands are addressed through swz(base + idx), constant
-// operands directly.
+// An operand: a base pointer (arena slice or constant table) plus offset.
 template <typename T>
 struct Operand {
   const T* p;
-  int base;
-  bool sw;
-  __device__ __forceinline__ T ld(int idx) const { return sw ? p[swz(base + idx)] : p[base + idx]; }
-  __device__ __forceinline__ const T* vec(int idx) const { return sw ? p + swz(base + idx) : p + base + idx; }
+  __device__ __forceinline__ T ld(int idx) const { return p[idx]; }
+  __device__ __forceinline__ const T* vec(int idx) const { return p + idx; }
 };
 
 template <typename T>
 __device__ __forceinline__ Operand<T> make_operand(int kind, int32_t ref, const int8_t* sel, int obits, T* arena_g,
                                                    const T* consts, const uint32_t* syn) {
   Operand<T> o;
-  if (kind == OP_ARENA) {
-    o.p = arena_g;
-    o.base = ref;
-    o.sw = true;
-  } else {
-    o.p = operand_ptr<T>(kind, ref, sel, obits, arena_g, consts, syn);
-    o.base = 0;
-    o.sw = false;
-  }
+  o.p = operand_ptr<T>(kind, ref, sel, obits, arena_g, consts, syn);
   return o;
 }
 
@@ -161,7 +141,7 @@ __device__ int run_step(const KArgs& a, const StepDesc& d, int st, int item_base
       }
       if (NORM && !BPAR) acc *= fb_s;
       const int addr = d.perm_off < 0 ? e : perm_addr(a.perm + d.perm_off, e, lw);
-      arena_g[swz(d.out_off + addr)] = acc;
+      arena_g[d.out_off + addr] = acc;
     }
     if (NORM) {
       uint32_t bits = __float_as_uint(float(acc));
@@ -280,7 +260,7 @@ __device__ int run_step_v4(const KArgs& a, const StepDesc& d, int st, int item_b
         for (int j = 0; j < 4; ++j) acc[j] *= fb_s;
       }
       if (!perm) {
-        store4<T>(arena_g + swz(d.out_off + e0), acc);
+        store4<T>(arena_g + d.out_off + e0, acc);
       } else {
         const int4 lo = *reinterpret_cast<const int4*>(perm + (e0 & ((1 << cb0) - 1)));
         int hi = 0;
@@ -294,7 +274,7 @@ __device__ int run_step_v4(const KArgs& a, const StepDesc& d, int st, int item_b
 #pragma unroll
         for (int s4 = 0; s4 < 4; ++s4) {
           const int j = (s4 + rot) & 3;
-          arena_g[swz(d.out_off + (pick4(los, j) | hi))] = pick4(acc, j);
+          arena_g[d.out_off + (pick4(los, j) | hi)] = pick4(acc, j);
         }
       }
     }
@@ -392,7 +372,7 @@ __global__ void __launch_bounds__(1024) tn_contract_kernel(KArgs a) {
       double best = -INFINITY, second = -INFINITY;
       int bc = 0;
       for (int c = 0; c < a.n_classes; ++c) {
-        const double v = double(rv[swz(root.out_off + c)]);
+        const double v = double(rv[root.out_off + c]);
         const double lp = v > 0.0 ? log(v) + lsc : -INFINITY;
         if (a.logp_out) a.logp_out[row * a.n_classes + c] = lp;
         if (lp > best) {

@@ -397,30 +397,25 @@ std::string build_plan(const NetworkView& net, int32_t n_steps, const int32_t* s
   post(root);
   const int R = (int)order.size();
 
-  // ---- layouts, top-down --------------------------------------------------
+  // ---- layouts --------------------------------------------------------------
   struct StepLayout {
     std::vector<int> H, Fa, Fb, K;  // ordered groups
     int a = -1, b = -1;             // operand node ids
     std::vector<int> out_layout;    // required layout of the output
   };
   std::vector<StepLayout> lay(R);
-  std::map<int, std::vector<int>> req;  // node id -> required layout
-  req[root] = out_vars;
-  Plan& P = *out;
-  P = Plan();
-  P.n_syndrome = net.n_syndrome;
-  P.syndrome_bytes = (net.n_syndrome + 7) / 8;
-  P.n_out = net.n_out;
-  P.n_classes = 1 << net.n_out;
-  P.n_tree_steps = n_steps;
-  P.macs_tree = macs_tree;
-  std::map<int, std::pair<int64_t, std::vector<int8_t>>> const_ref;  // node -> (offset, sel)
-  double err_terms = 0.0;
-  for (int r = R - 1; r >= 0; --r) {
+  // Group orders are assigned bottom-up: a step orders each of its index
+  // groups by the position its labels hold in the producing step's natural
+  // output order ([fb][fa][h], fb lowest), so an intermediate's lowest
+  // natural bits (the ones adjacent threads differ in when they write it)
+  // stay among the lowest address bits of the layout its consumer reads.
+  // Stores then spread over the shared-memory banks.  The root's natural
+  // order is permuted into the output order at the last step.
+  std::map<int, std::vector<int>> nat;  // runtime node id -> natural order (bit 0 first)
+  for (int r = 0; r < R; ++r) {
     const int id = order[r];
     PNode& n = nodes[id];
     StepLayout& L = lay[r];
-    L.out_layout = req.at(id);
     const std::vector<int>& lv = nodes[n.left].vars;
     const std::vector<int>& rv = nodes[n.right].vars;
     auto in = [](const std::vector<int>& s, int v) { return std::find(s.begin(), s.end(), v) != s.end(); };
@@ -442,12 +437,46 @@ std::string build_plan(const NetworkView& net, int32_t n_steps, const int32_t* s
     }
     for (int v : bv)
       if (!in(av, v)) L.Fb.push_back(v);
-    auto pos = [&](int v) { return int(std::find(L.out_layout.begin(), L.out_layout.end(), v) - L.out_layout.begin()); };
-    auto by_pos = [&](std::vector<int>& g) { std::sort(g.begin(), g.end(), [&](int p, int q) { return pos(p) < pos(q); }); };
-    by_pos(L.H);
-    by_pos(L.Fa);
-    by_pos(L.Fb);
-    std::sort(L.K.begin(), L.K.end());
+    // position of a label in an operand's natural order (leaves: label id)
+    auto natpos = [&](int node, int v) {
+      auto it = nat.find(node);
+      if (it == nat.end()) return 1000000 + v;
+      const std::vector<int>& o = it->second;
+      return int(std::find(o.begin(), o.end(), v) - o.begin());
+    };
+    auto order_by = [&](std::vector<int>& g, int node) {
+      std::sort(g.begin(), g.end(), [&](int p, int q) { return natpos(node, p) < natpos(node, q); });
+    };
+    order_by(L.Fb, L.b);
+    order_by(L.Fa, L.a);
+    order_by(L.H, L.b);
+    // contracted labels follow the larger intermediate operand's natural order
+    {
+      const bool ra = nat.count(L.a) > 0, rb = nat.count(L.b) > 0;
+      int pick = L.b;
+      if (ra && (!rb || nodes[L.a].vars.size() > nodes[L.b].vars.size())) pick = L.a;
+      order_by(L.K, pick);
+    }
+    std::vector<int> nn;
+    nn.insert(nn.end(), L.Fb.begin(), L.Fb.end());
+    nn.insert(nn.end(), L.Fa.begin(), L.Fa.end());
+    nn.insert(nn.end(), L.H.begin(), L.H.end());
+    nat[id] = nn;
+  }
+  Plan& P = *out;
+  P = Plan();
+  P.n_syndrome = net.n_syndrome;
+  P.syndrome_bytes = (net.n_syndrome + 7) / 8;
+  P.n_out = net.n_out;
+  P.n_classes = 1 << net.n_out;
+  P.n_tree_steps = n_steps;
+  P.macs_tree = macs_tree;
+  std::map<int, std::pair<int64_t, std::vector<int8_t>>> const_ref;  // node -> (offset, sel)
+  std::map<int, std::vector<int>> req;  // node id -> required (read) layout
+  double err_terms = 0.0;
+  for (int r = 0; r < R; ++r) {
+    const int id = order[r];
+    StepLayout& L = lay[r];
     std::vector<int> la, lb;
     la.insert(la.end(), L.K.begin(), L.K.end());
     la.insert(la.end(), L.Fa.begin(), L.Fa.end());
@@ -472,7 +501,10 @@ std::string build_plan(const NetworkView& net, int32_t n_steps, const int32_t* s
       const_ref[op] = {off, sel};
       err_terms += 1.0;
     }
+    (void)id;
   }
+  req[root] = out_vars;
+  for (int r = 0; r < R; ++r) lay[r].out_layout = req.at(order[r]);
   if (P.consts.size() > (size_t)INT32_MAX) {
     *unsupported = true;
     return "constant data above 2^31 entries";

@@ -100,6 +100,10 @@ def lib():
         "tqec_patterns_create": [i32, i32, i32, i32, vp, vp, i32, vp, i32, vp, vp, vp, i32, vp],
         "tqec_patterns_destroy": [vp],
         "tqec_patterns_decode": [vp, vp, vp, i64, vp, vp, vp, vp],
+        "tqec_sampler_create": [i32, i32, i32, vp, vp, i32, vp, vp, vp, vp, vp, i32, vp],
+        "tqec_sampler_destroy": [vp],
+        "tqec_sample": [vp, C.c_uint64, C.c_uint64, i64, vp, vp, vp],
+        "tqec_monte_carlo": [vp, vp, vp, C.c_float, C.c_uint64, i64, i64, vp, vp],
     }
     for name, args in sig.items():
         f = getattr(L, name)
@@ -284,6 +288,48 @@ class PatternDecoder:
         try:
             if getattr(self, "_h", None):
                 lib().tqec_patterns_destroy(self._h)
+                self._h = None
+        except Exception:
+            pass
+
+
+class Sampler:
+    """Owner of a ``tqec_sampler``: seeded code-capacity sampling on the GPU
+    and the Monte-Carlo logical-error count."""
+
+    def __init__(self, tanner, lx, lz, em, device=0):
+        arrs = [np.ascontiguousarray(a, dtype=np.uint8) for a in (tanner.stgx.H, tanner.stgz.H, lx, lz)]
+        ps = [np.ascontiguousarray(np.broadcast_to(np.asarray(v, dtype=np.float64), (tanner.nq,)))
+              for v in (em.px, em.py, em.pz)]
+        self._keep = arrs + ps
+        hx, hz, lxa, lza = arrs
+        self.ns = tanner.ns
+        self.syn_bytes = (tanner.ns + 7) // 8
+        h = C.c_void_p()
+        check(lib().tqec_sampler_create(tanner.nq, tanner.stgx.ns, tanner.stgz.ns, _ptr(hx), _ptr(hz), lx.shape[0],
+                                        _ptr(lxa), _ptr(lza), _ptr(ps[0]), _ptr(ps[1]), _ptr(ps[2]), device,
+                                        C.byref(h)))
+        self._h = h
+
+    def sample(self, seed, n, offset=0):
+        """(packed syndromes (n, syn_bytes), true classes (n,))."""
+        syn = np.empty((n, self.syn_bytes), dtype=np.uint8)
+        cls = np.empty(n, dtype=np.int32)
+        check(lib().tqec_sample(self._h, seed, offset, n, _ptr(syn), _ptr(cls), None))
+        return syn, cls
+
+    def monte_carlo(self, program, seed, n_total, batch=1 << 16, mlp=None, threshold=0.0):
+        """(logical errors, fallback rows) over n_total sampled syndromes."""
+        ne = C.c_int64()
+        nf = C.c_int64()
+        check(lib().tqec_monte_carlo(self._h, program._h, mlp, threshold, seed, n_total, batch, C.byref(ne),
+                                     C.byref(nf)))
+        return ne.value, nf.value
+
+    def __del__(self):
+        try:
+            if getattr(self, "_h", None):
+                lib().tqec_sampler_destroy(self._h)
                 self._h = None
         except Exception:
             pass
