@@ -53,6 +53,9 @@ extern "C" {
 /* Option flags. */
 #define TQEC_FLAG_PLAIN 1u   /* decode one syndrome per kernel launch (drop-in form) */
 #define TQEC_FLAG_NORECHECK 2u /* TQEC_F32: skip the float64 recheck of low margins */
+#define TQEC_FLAG_MAP 4u      /* most probable configuration (TNMAP): the network's
+                                 out_labels name the variables whose values are
+                                 reported; the contraction maximises over all */
 
 /* The factor graph, as built by compile(::TNMMAP, ...) (tndecoder.jl:97-146
  * for CSS codes, :186-219 for detector error models). */
@@ -134,6 +137,16 @@ int tqec_contract_batch(tqec_program* prog, const uint8_t* syndromes,
                         int64_t n, int32_t precision, double* logp_out,
                         void* stream);
 
+/* decode(ct::CompiledTNMAP, syndrome) over a batch (tndecoder.jl:53-57,
+ * TensorInference's most_probable_config): for a program created with
+ * TQEC_FLAG_MAP, the values of the reported variables in the most probable
+ * configuration consistent with each syndrome (bit-packed rows of
+ * ceil(n_out/8) bytes in out_labels order; ties go to the configuration
+ * whose maximised labels read smallest as binary numbers, step by step) and
+ * the natural log of its probability (n doubles, may be NULL). */
+int tqec_map_decode_batch(tqec_program* prog, const uint8_t* syndromes, int64_t n,
+                          uint8_t* assignment_out, double* logp_out, void* stream);
+
 /* Count of syndromes the last TQEC_F32 decode call sent to the float64
  * recheck (a measure of how often the rounding bound was not enough). */
 int tqec_last_recheck_count(const tqec_program* prog, int64_t* count);
@@ -162,10 +175,23 @@ typedef struct {
   double flops_per_syndrome;
   double flops_tree;
   double err_terms;
+  /* TQEC_FLAG_MAP programs: per-step variable ids (fb, fa, h, k bits; the
+   * step record's last field is its offset here), reported variables, and
+   * per-variable values fixed on the host (-1 = decided by the search) */
+  int32_t map_mode;
+  int32_t n_vars;
+  int64_t n_vartab;
+  const int32_t* vartab;
+  int32_t n_report;
+  const int32_t* report;
+  const int8_t* fixed;
 } tqec_plan_view;
 
 int tqec_plan_inspect(const tqec_network* net, const tqec_tree* tree,
                       tqec_plan_view* view, void** handle);
+/* The same for a program compiled with option flags (TQEC_FLAG_MAP). */
+int tqec_plan_inspect_flags(const tqec_network* net, const tqec_tree* tree, uint32_t flags,
+                            tqec_plan_view* view, void** handle);
 int tqec_plan_release(void* handle);
 
 /* Contraction-order search, in place of OMEinsum's

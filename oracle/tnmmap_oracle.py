@@ -18,6 +18,8 @@ the TensorQEC.jl project root):
 * DEM network            -- src/decoding/tndecoder.jl:186-271,
                            src/decoding/dem.jl:150-160,
                            src/stim_parser/stim_parser.jl:342-375
+* TNMAP (most probable   -- src/decoding/tndecoder.jl:33-57,
+  configuration)           src/decoding/general_decoding.jl:24-32
 
 The contraction itself lives in OMEinsum (a Julia dependency, compat "0.9",
 not vendored with the reference).  Its published semantics are plain einsum:
@@ -779,3 +781,57 @@ def contraction_cost(ixs, iy, order):
         nodes[nid] = keep
         nid += 1
     return macs, width
+
+
+# ---------------------------------------------------------------------------
+# TNMAP: most probable configuration (src/decoding/tndecoder.jl:33-57)
+# ---------------------------------------------------------------------------
+
+
+def most_probable_configs(H, prior_ixs, prior_tensors, syndromes):
+    """The reference's TNMAP answer by enumeration: for each syndrome row,
+    the maximum over all bit configurations e with H e = s (mod 2) of the
+    product of the prior tensors (stg2uaimodel, tndecoder.jl:33-40, with the
+    syndrome as evidence, :46-57; TensorInference's most_probable_config is a
+    max-product contraction of that model).  Returns (natural log of the
+    maximum, mask of all maximisers) per row; only for nq <= 22 bits.
+
+    ``prior_tensors`` are flattened in Julia column-major order over their
+    labels (1-based bits)."""
+    H = np.asarray(H, dtype=np.int64)
+    nq = H.shape[1]
+    if nq > 22:
+        raise ValueError("enumeration is limited to 22 bits")
+    cfg = (np.arange(1 << nq, dtype=np.int64)[:, None] >> np.arange(nq)) & 1
+    logw = np.zeros(1 << nq)
+    with np.errstate(divide="ignore"):
+        for ix, t in zip(prior_ixs, prior_tensors):
+            flat = np.asarray(t, dtype=np.float64).ravel(order="F")
+            idx = np.zeros(1 << nq, dtype=np.int64)
+            for j, v in enumerate(ix):
+                idx |= cfg[:, v - 1] << j
+            logw += np.log(flat[idx])
+    syn = (cfg @ H.T) % 2
+    key = (syn * (1 << np.arange(H.shape[0]))).sum(1)
+    out = []
+    for s in np.atleast_2d(syndromes):
+        k = int((np.asarray(s, dtype=np.int64) * (1 << np.arange(H.shape[0]))).sum())
+        m = key == k
+        best = logw[m].max() if m.any() else -np.inf
+        out.append((best, cfg[m & (logw == best)] if np.isfinite(best) else cfg[:0]))
+    return out
+
+
+def config_log_probability(prior_ixs, prior_tensors, cfg):
+    """Natural log of the product of the prior tensors at configurations
+    ``cfg`` (rows of 0/1 over all bits)."""
+    cfg = np.atleast_2d(np.asarray(cfg, dtype=np.int64))
+    out = np.zeros(cfg.shape[0])
+    with np.errstate(divide="ignore"):
+        for ix, t in zip(prior_ixs, prior_tensors):
+            flat = np.asarray(t, dtype=np.float64).ravel(order="F")
+            idx = np.zeros(cfg.shape[0], dtype=np.int64)
+            for j, v in enumerate(ix):
+                idx |= cfg[:, v - 1] << j
+            out += np.log(flat[idx])
+    return out

@@ -82,6 +82,9 @@ struct tqec_program {
   cudaStream_t stream = nullptr;
   tqec::StepDesc* d_steps = nullptr;
   int32_t* d_perm = nullptr;
+  int32_t* d_vartab = nullptr;   // MAP mode tables
+  int32_t* d_report = nullptr;
+  int8_t* d_fixed = nullptr;
   double* d_c64 = nullptr;
   float* d_c32 = nullptr;
   Shape shape[2];  // indexed by precision
@@ -112,6 +115,8 @@ double err_bound(const tqec_program* p, int precision) {
 
 int syn_words(const tqec_program* p) { return std::max(1, (p->plan.n_syndrome + 31) / 32); }
 
+int var_words(const tqec_program* p) { return p->plan.map_mode ? (p->plan.n_vars + 31) / 32 : 0; }
+
 // Picks (G, threads) for one precision: the largest group whose arena fits
 // about half of the shared memory (two blocks per SM), else a global arena.
 int choose_shape(tqec_program* p, int precision, int G_req, int threads_req, Shape* out) {
@@ -120,27 +125,28 @@ int choose_shape(tqec_program* p, int precision, int G_req, int threads_req, Sha
   const int64_t arena = p->plan.arena_elems;
   const int nsteps = (int)p->plan.steps.size();
   const int sw = syn_words(p);
+  const int vw = var_words(p);
   Shape s;
   s.threads = threads_req > 0 ? threads_req : 256;
   if (G_req > 0) {
     s.G = G_req;
-    s.smem_arena = tqec::contract_smem_bytes(precision, nsteps, sw, s.G, arena, true) <= limit;
+    s.smem_arena = tqec::contract_smem_bytes(precision, nsteps, sw, s.G, arena, true, vw) <= limit;
   } else {
     const size_t target = limit / 2 - 1024;
     int G = 1;
-    while (G < 256 && tqec::contract_smem_bytes(precision, nsteps, sw, G * 2, arena, true) <= target &&
+    while (G < 256 && tqec::contract_smem_bytes(precision, nsteps, sw, G * 2, arena, true, vw) <= target &&
            (int64_t(G) * 2 << p->plan.width) <= 16 * 4096)
       G *= 2;
     s.G = G;
-    s.smem_arena = tqec::contract_smem_bytes(precision, nsteps, sw, G, arena, true) <= limit;
+    s.smem_arena = tqec::contract_smem_bytes(precision, nsteps, sw, G, arena, true, vw) <= limit;
     // one syndrome per block with a wide arena: use more threads per block
-    if (G == 1 && (!s.smem_arena || tqec::contract_smem_bytes(precision, nsteps, sw, 1, arena, true) > target))
+    if (G == 1 && (!s.smem_arena || tqec::contract_smem_bytes(precision, nsteps, sw, 1, arena, true, vw) > target))
       s.threads = threads_req > 0 ? threads_req : 1024;
     (void)esz;
   }
-  s.smem = tqec::contract_smem_bytes(precision, nsteps, sw, s.G, arena, s.smem_arena);
+  s.smem = tqec::contract_smem_bytes(precision, nsteps, sw, s.G, arena, s.smem_arena, vw);
   if (s.smem > limit) return fail(TQEC_ERR_UNSUPPORTED, "program does not fit shared memory even with a global arena");
-  int occ = tqec::contract_occupancy(precision, s.threads, s.smem);
+  int occ = tqec::contract_occupancy(precision, s.threads, s.smem, p->plan.map_mode);
   if (occ < 1) return fail(TQEC_ERR_UNSUPPORTED, "launch shape cannot be resident on this device");
   s.grid_cap = occ * p->sm_count;
   *out = s;
@@ -174,6 +180,15 @@ tqec::KArgs base_args(tqec_program* p, int precision) {
   a.n_classes = p->plan.n_classes;
   a.err_bound = (float)err_bound(p, precision);
   a.recheck_margin = -1.0;
+  if (p->plan.map_mode) {
+    a.map_mode = 1;
+    a.vartab = p->d_vartab;
+    a.n_vars = p->plan.n_vars;
+    a.var_words = var_words(p);
+    a.fixed = p->d_fixed;
+    a.report = p->d_report;
+    a.n_report = (int32_t)p->plan.report.size();
+  }
   return a;
 }
 
@@ -196,8 +211,10 @@ int launch_plain(tqec_program* p, int precision, tqec::KArgs a, int64_t n, cudaS
   Shape one;
   one.G = 1;
   one.threads = s.threads;
-  one.smem_arena = tqec::contract_smem_bytes(precision, nsteps, syn_words(p), 1, p->plan.arena_elems, true) <= limit;
-  one.smem = tqec::contract_smem_bytes(precision, nsteps, syn_words(p), 1, p->plan.arena_elems, one.smem_arena);
+  one.smem_arena =
+      tqec::contract_smem_bytes(precision, nsteps, syn_words(p), 1, p->plan.arena_elems, true, var_words(p)) <= limit;
+  one.smem = tqec::contract_smem_bytes(precision, nsteps, syn_words(p), 1, p->plan.arena_elems, one.smem_arena,
+                                       var_words(p));
   a.G = 1;
   a.lg = 0;
   if (!one.smem_arena) {
@@ -357,6 +374,7 @@ int tqec_program_create(const tqec_network* net, const tqec_tree* tree, const tq
   tqec::NetworkView v{net->n_tensors, net->ix_offsets, net->ix_labels, net->data_offsets, net->data,
                       net->n_out, net->out_labels, net->n_syndrome, net->syndrome_tensors};
   tqec::PlanLimits lim;
+  lim.map_mode = (o.flags & TQEC_FLAG_MAP) != 0;
   auto* p = new tqec_program();
   bool unsupported = false;
   std::string err = tqec::build_plan(v, tree->n_steps, tree->steps, lim, &p->plan, &unsupported);
@@ -392,6 +410,15 @@ int tqec_program_create(const tqec_network* net, const tqec_tree* tree, const tq
     cudaMemcpy(p->d_c64, P.consts.data(), P.consts.size() * sizeof(double), cudaMemcpyHostToDevice);
     cudaMemcpy(p->d_c32, c32.data(), c32.size() * sizeof(float), cudaMemcpyHostToDevice);
   }
+  if (P.map_mode) {
+    const size_t nv = std::max<size_t>(P.vartab.size(), 1), nr = std::max<size_t>(P.report.size(), 1);
+    if (cudaMalloc(&p->d_vartab, nv * 4) != cudaSuccess || cudaMalloc(&p->d_report, nr * 4) != cudaSuccess ||
+        cudaMalloc(&p->d_fixed, std::max<size_t>(P.fixed.size(), 1)) != cudaSuccess)
+      return bail(TQEC_ERR_OOM, "MAP tables");
+    if (!P.vartab.empty()) cudaMemcpy(p->d_vartab, P.vartab.data(), P.vartab.size() * 4, cudaMemcpyHostToDevice);
+    if (!P.report.empty()) cudaMemcpy(p->d_report, P.report.data(), P.report.size() * 4, cudaMemcpyHostToDevice);
+    if (!P.fixed.empty()) cudaMemcpy(p->d_fixed, P.fixed.data(), P.fixed.size(), cudaMemcpyHostToDevice);
+  }
   if ((e = cudaMallocHost(&p->h_count, sizeof(int32_t))) != cudaSuccess) return bail(TQEC_ERR_OOM, "pinned count");
   *p->h_count = 0;
   if ((e = cudaGetLastError()) != cudaSuccess) return bail(TQEC_ERR_CUDA, cudaGetErrorString(e));
@@ -416,6 +443,9 @@ int tqec_program_destroy(tqec_program* p) {
   cudaFree(p->d_perm);
   cudaFree(p->d_c64);
   cudaFree(p->d_c32);
+  cudaFree(p->d_vartab);
+  cudaFree(p->d_report);
+  cudaFree(p->d_fixed);
   if (p->h_count) cudaFreeHost(p->h_count);
   for (auto* b : {&p->arena[0], &p->arena[1], &p->syn, &p->cls, &p->logp, &p->err, &p->list, &p->count}) b->release();
   if (p->stream) cudaStreamDestroy(p->stream);
@@ -450,6 +480,7 @@ int tqec_program_info(const tqec_program* p, tqec_program_info_t* info) {
 int tqec_decode_batch(tqec_program* p, const uint8_t* syndromes, int64_t n, int32_t* class_out, double* logp_out,
                       float* err_bound_out, void* stream) {
   if (!p || n < 0 || (n > 0 && !syndromes)) return fail(TQEC_ERR_INVALID, "bad argument");
+  if (p->plan.map_mode) return fail(TQEC_ERR_INVALID, "a TQEC_FLAG_MAP program decodes with tqec_map_decode_batch");
   std::lock_guard<std::mutex> lk(p->mu);
   TQ_CUDA(cudaSetDevice(p->device));
   cudaStream_t st = stream ? (cudaStream_t)stream : p->stream;
@@ -476,6 +507,39 @@ int tqec_contract_batch(tqec_program* p, const uint8_t* syndromes, int64_t n, in
   int rc = decode_locked(p, syndromes, n, nullptr, logp_out, nullptr, precision, false, plain, st);
   if (rc) return rc;
   if (!stream || !is_device_ptr(logp_out)) TQ_CUDA(cudaStreamSynchronize(st));
+  return TQEC_OK;
+}
+
+int tqec_map_decode_batch(tqec_program* p, const uint8_t* syndromes, int64_t n, uint8_t* assignment_out,
+                          double* logp_out, void* stream) {
+  if (!p || n < 0 || (n > 0 && (!syndromes || !assignment_out))) return fail(TQEC_ERR_INVALID, "bad argument");
+  if (!p->plan.map_mode) return fail(TQEC_ERR_INVALID, "program was not created with TQEC_FLAG_MAP");
+  std::lock_guard<std::mutex> lk(p->mu);
+  TQ_CUDA(cudaSetDevice(p->device));
+  cudaStream_t st = stream ? (cudaStream_t)stream : p->stream;
+  Staged s;
+  int rc = stage_inputs(p, syndromes, n, nullptr, logp_out, nullptr, st, &s);
+  if (rc) return rc;
+  const size_t rb = (p->plan.report.size() + 7) / 8;
+  const bool host_asg = !is_device_ptr(assignment_out);
+  uint8_t* d_asg = assignment_out;
+  if (host_asg) {
+    TQ_CUDA(p->err.ensure(std::max<size_t>(rb * size_t(n), 16)));
+    d_asg = static_cast<uint8_t*>(p->err.p);
+  }
+  if (n > 0) {
+    tqec::KArgs a = base_args(p, p->precision);
+    a.syn = s.d_syn;
+    a.n = n;
+    a.logp_out = s.d_logp;
+    a.assign_out = d_asg;
+    const bool plain = (p->flags & TQEC_FLAG_PLAIN) != 0;
+    rc = plain ? launch_plain(p, p->precision, a, n, st) : launch_rows(p, p->precision, a, n, st);
+    if (rc) return rc;
+    if (host_asg) TQ_CUDA(cudaMemcpyAsync(assignment_out, d_asg, rb * size_t(n), cudaMemcpyDeviceToHost, st));
+    if (s.host_logp) TQ_CUDA(cudaMemcpyAsync(logp_out, s.d_logp, sizeof(double) * n, cudaMemcpyDeviceToHost, st));
+  }
+  if (!stream || host_asg || s.host_logp) TQ_CUDA(cudaStreamSynchronize(st));
   return TQEC_OK;
 }
 
@@ -544,13 +608,20 @@ int tqec_program_autotune(tqec_program* p, int64_t n_probe) {
 }
 
 int tqec_plan_inspect(const tqec_network* net, const tqec_tree* tree, tqec_plan_view* view, void** handle) {
+  return tqec_plan_inspect_flags(net, tree, 0u, view, handle);
+}
+
+int tqec_plan_inspect_flags(const tqec_network* net, const tqec_tree* tree, uint32_t flags, tqec_plan_view* view,
+                            void** handle) {
   if (!net || !tree || !view || !handle) return fail(TQEC_ERR_INVALID, "NULL argument");
   *handle = nullptr;
   tqec::NetworkView v{net->n_tensors, net->ix_offsets, net->ix_labels, net->data_offsets, net->data,
                       net->n_out, net->out_labels, net->n_syndrome, net->syndrome_tensors};
   auto* P = new tqec::Plan();
   bool unsupported = false;
-  std::string err = tqec::build_plan(v, tree->n_steps, tree->steps, tqec::PlanLimits(), P, &unsupported);
+  tqec::PlanLimits lim;
+  lim.map_mode = (flags & TQEC_FLAG_MAP) != 0;
+  std::string err = tqec::build_plan(v, tree->n_steps, tree->steps, lim, P, &unsupported);
   if (!err.empty()) {
     delete P;
     return fail(unsupported ? TQEC_ERR_UNSUPPORTED : TQEC_ERR_INVALID, err);
@@ -569,6 +640,13 @@ int tqec_plan_inspect(const tqec_network* net, const tqec_tree* tree, tqec_plan_
   view->flops_per_syndrome = 2.0 * P->macs_runtime;
   view->flops_tree = 2.0 * P->macs_tree;
   view->err_terms = P->err_terms;
+  view->map_mode = P->map_mode ? 1 : 0;
+  view->n_vars = P->n_vars;
+  view->n_vartab = (int64_t)P->vartab.size();
+  view->vartab = P->vartab.data();
+  view->n_report = (int32_t)P->report.size();
+  view->report = P->report.data();
+  view->fixed = P->fixed.data();
   *handle = P;
   return TQEC_OK;
 }

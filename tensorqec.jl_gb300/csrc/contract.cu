@@ -82,7 +82,7 @@ __device__ __forceinline__ Operand<T> make_operand(int kind, int32_t ref, const 
   return o;
 }
 
-template <typename T, bool NORM, bool APAR, bool BPAR>
+template <typename T, bool NORM, bool APAR, bool BPAR, bool MAXP>
 __device__ int run_step(const KArgs& a, const StepDesc& d, int st, int item_base, const uint32_t* s_syn,
                          uint32_t* s_max, T* arena, const T* consts) {
   const int lw = d.lh + d.lfa + d.lfb;
@@ -123,20 +123,33 @@ __device__ int run_step(const KArgs& a, const StepDesc& d, int st, int item_base
         if (!BPAR && d.b_kind == OP_ARENA) fb_s = T(norm_factor(s_max[g * a.n_steps + d.b_prod], &ee));
       }
       if (APAR && BPAR) {
-        for (int k = 0; k < K; ++k)
-          acc += parity_val<T>(abase + k, as) * parity_val<T>(bbase + (k << d.lfb), bs);
+        for (int k = 0; k < K; ++k) {
+          const T v = parity_val<T>(abase + k, as) * parity_val<T>(bbase + (k << d.lfb), bs);
+          acc = MAXP ? (v > acc ? v : acc) : acc + v;
+        }
       } else if (APAR) {
         for (int k = 0; k < K; ++k)
-          if (parity_val<T>(abase + k, as) != T(0)) acc += B.ld(bbase + (k << d.lfb));
+          if (parity_val<T>(abase + k, as) != T(0)) {
+            const T v = B.ld(bbase + (k << d.lfb));
+            acc = MAXP ? (v > acc ? v : acc) : acc + v;
+          }
       } else if (BPAR) {
         for (int k = 0; k < K; ++k)
-          if (parity_val<T>(bbase + (k << d.lfb), bs) != T(0)) acc += A.ld(abase + k);
+          if (parity_val<T>(bbase + (k << d.lfb), bs) != T(0)) {
+            const T v = A.ld(abase + k);
+            acc = MAXP ? (v > acc ? v : acc) : acc + v;
+          }
         if (NORM) acc *= fa_s;
       } else {
         for (int k = 0; k < K; ++k) {
           T a0 = A.ld(abase + k);
           if (NORM) a0 *= fa_s;
-          acc = fma(a0, B.ld(bbase + (k << d.lfb)), acc);
+          if (MAXP) {
+            const T v = a0 * B.ld(bbase + (k << d.lfb));
+            acc = v > acc ? v : acc;
+          } else {
+            acc = fma(a0, B.ld(bbase + (k << d.lfb)), acc);
+          }
         }
       }
       if (NORM && !BPAR) acc *= fb_s;
@@ -193,7 +206,7 @@ __device__ __forceinline__ T pick4(const T v[4], int j) {
 // elements (arena and constant offsets are planned that way), so the vector
 // accesses are aligned.  Permuted outputs are written in a lane-rotated order
 // so that the four stores of a warp instruction hit different index bits.
-template <typename T, bool NORM, bool APAR, bool BPAR>
+template <typename T, bool NORM, bool APAR, bool BPAR, bool MAXP>
 __device__ int run_step_v4(const KArgs& a, const StepDesc& d, int st, int item_base, const uint32_t* s_syn,
                             uint32_t* s_max, T* arena, const T* consts) {
   const int lw = d.lh + d.lfa + d.lfb;
@@ -253,7 +266,14 @@ __device__ int run_step_v4(const KArgs& a, const StepDesc& d, int st, int item_b
           load4<T>(B.vec(bi), bv);
         }
 #pragma unroll
-        for (int j = 0; j < 4; ++j) acc[j] = fma(av, bv[j], acc[j]);
+        for (int j = 0; j < 4; ++j) {
+          if (MAXP) {
+            const T v = av * bv[j];
+            acc[j] = v > acc[j] ? v : acc[j];
+          } else {
+            acc[j] = fma(av, bv[j], acc[j]);
+          }
+        }
       }
       if (NORM && !BPAR) {
 #pragma unroll
@@ -292,7 +312,97 @@ __device__ int run_step_v4(const KArgs& a, const StepDesc& d, int st, int item_b
   return total_r;
 }
 
-template <typename T, bool NORM>
+// Most probable configuration: after the max-product pass every runtime
+// step's output is still in the arena.  Walking the steps from the root
+// down, the values of a step's output labels are known (set by its
+// consumer), which fixes (h, fa, fb); the k maximising A[h,fa,k] B[h,k,fb]
+// (first maximum) gives the values of the labels the step maximised over.
+// One warp per syndrome; lanes split the k range.
+template <typename T>
+__device__ void backtrack(const KArgs& a, const StepDesc* s_steps, const uint32_t* s_syn, uint32_t* s_asg, T* arena,
+                          const T* consts, int64_t base, int64_t nrows) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int nwarps = blockDim.x >> 5;
+  for (int g = warp; g < a.G; g += nwarps) {
+    const int64_t r = base + g;
+    if (r >= nrows) continue;
+    uint32_t* asg = s_asg + g * a.var_words;
+    const uint32_t* syn = s_syn + g * a.syn_words;
+    T* arena_g = arena + int64_t(g) * a.arena_elems;
+    for (int w = lane; w < a.var_words; w += 32) {
+      uint32_t v = 0;
+      for (int b = 0; b < 32; ++b) {
+        const int id = w * 32 + b;
+        if (id < a.n_vars && a.fixed[id] == 1) v |= 1u << b;
+      }
+      asg[w] = v;
+    }
+    __syncwarp();
+    for (int st = a.n_steps - 1; st >= 0; --st) {
+      const StepDesc& d = s_steps[st];
+      const int32_t* vt = a.vartab + d.var_off;
+      auto bit = [&](int id) { return int((asg[id >> 5] >> (id & 31)) & 1u); };
+      int fb = 0, fa = 0, h = 0;
+      for (int j = 0; j < d.lfb; ++j) fb |= bit(vt[j]) << j;
+      for (int j = 0; j < d.lfa; ++j) fa |= bit(vt[d.lfb + j]) << j;
+      for (int j = 0; j < d.lh; ++j) h |= bit(vt[d.lfb + d.lfa + j]) << j;
+      const int abase = ((h << d.lfa) | fa) << d.lk;
+      const int bbase = (h << (d.lk + d.lfb)) | fb;
+      const int abits = d.lh + d.lfa + d.lk, bbits = d.lh + d.lk + d.lfb;
+      const bool apar = d.a_kind == OP_PARITY, bpar = d.b_kind == OP_PARITY;
+      const T* ap = apar ? nullptr : operand_ptr<T>(d.a_kind, d.a_ref, d.a_sel, abits, arena_g, consts, syn);
+      const T* bp = bpar ? nullptr : operand_ptr<T>(d.b_kind, d.b_ref, d.b_sel, bbits, arena_g, consts, syn);
+      const int as = apar ? syn_bit(syn, d.a_ref) : 0, bs = bpar ? syn_bit(syn, d.b_ref) : 0;
+      T best = T(-1);
+      int bk = 0;
+      for (int k = lane; k < (1 << d.lk); k += 32) {
+        const int ai = abase + k, bi = bbase + (k << d.lfb);
+        const T av = apar ? parity_val<T>(ai, as) : ap[ai];
+        const T bv = bpar ? parity_val<T>(bi, bs) : bp[bi];
+        const T v = av * bv;
+        if (v > best) {
+          best = v;
+          bk = k;
+        }
+      }
+      for (int o = 16; o > 0; o >>= 1) {
+        const T ob = __shfl_xor_sync(0xffffffffu, best, o);
+        const int okk = __shfl_xor_sync(0xffffffffu, bk, o);
+        if (ob > best || (ob == best && okk < bk)) {
+          best = ob;
+          bk = okk;
+        }
+      }
+      if (lane == 0) {
+        const int32_t* kv = vt + d.lfb + d.lfa + d.lh;
+        for (int j = 0; j < d.lk; ++j) {
+          const int id = kv[j];
+          const uint32_t m = 1u << (id & 31);
+          if ((bk >> j) & 1) asg[id >> 5] |= m;
+          else asg[id >> 5] &= ~m;
+        }
+      }
+      __syncwarp();
+    }
+    if (a.assign_out) {
+      const int rb = (a.n_report + 7) / 8;
+      const int64_t row = a.list ? int64_t(a.list[r]) : r + a.row_offset;
+      for (int byte = lane; byte < rb; byte += 32) {
+        uint32_t v = 0;
+        for (int b = 0; b < 8; ++b) {
+          const int i = byte * 8 + b;
+          if (i < a.n_report) {
+            const int id = a.report[i];
+            v |= ((asg[id >> 5] >> (id & 31)) & 1u) << b;
+          }
+        }
+        a.assign_out[row * rb + byte] = uint8_t(v);
+      }
+    }
+  }
+}
+
+template <typename T, bool NORM, bool MAXP>
 __global__ void __launch_bounds__(1024) tn_contract_kernel(KArgs a) {
   extern __shared__ __align__(16) unsigned char smem[];
   StepDesc* s_steps = reinterpret_cast<StepDesc*>(smem);
@@ -301,6 +411,8 @@ __global__ void __launch_bounds__(1024) tn_contract_kernel(KArgs a) {
   off += size_t(a.G) * a.syn_words * 4;
   uint32_t* s_max = reinterpret_cast<uint32_t*>(smem + off);
   if (NORM) off += size_t(a.G) * a.n_steps * 4;
+  uint32_t* s_asg = reinterpret_cast<uint32_t*>(smem + off);
+  if (MAXP) off += size_t(a.G) * a.var_words * 4;
   off = (off + 15) & ~size_t(15);
   T* arena = a.arena_global
                  ? reinterpret_cast<T*>(a.arena_global) + int64_t(blockIdx.x) * a.G * a.arena_elems
@@ -336,15 +448,15 @@ __global__ void __launch_bounds__(1024) tn_contract_kernel(KArgs a) {
       const bool ap = d.a_kind == OP_PARITY, bp = d.b_kind == OP_PARITY;
       int items;
       if (d.lfb >= 2) {
-        if (ap && bp) items = run_step_v4<T, NORM, true, true>(a, d, st, item_base, s_syn, s_max, arena, consts);
-        else if (ap) items = run_step_v4<T, NORM, true, false>(a, d, st, item_base, s_syn, s_max, arena, consts);
-        else if (bp) items = run_step_v4<T, NORM, false, true>(a, d, st, item_base, s_syn, s_max, arena, consts);
-        else items = run_step_v4<T, NORM, false, false>(a, d, st, item_base, s_syn, s_max, arena, consts);
+        if (ap && bp) items = run_step_v4<T, NORM, true, true, MAXP>(a, d, st, item_base, s_syn, s_max, arena, consts);
+        else if (ap) items = run_step_v4<T, NORM, true, false, MAXP>(a, d, st, item_base, s_syn, s_max, arena, consts);
+        else if (bp) items = run_step_v4<T, NORM, false, true, MAXP>(a, d, st, item_base, s_syn, s_max, arena, consts);
+        else items = run_step_v4<T, NORM, false, false, MAXP>(a, d, st, item_base, s_syn, s_max, arena, consts);
       } else {
-        if (ap && bp) items = run_step<T, NORM, true, true>(a, d, st, item_base, s_syn, s_max, arena, consts);
-        else if (ap) items = run_step<T, NORM, true, false>(a, d, st, item_base, s_syn, s_max, arena, consts);
-        else if (bp) items = run_step<T, NORM, false, true>(a, d, st, item_base, s_syn, s_max, arena, consts);
-        else items = run_step<T, NORM, false, false>(a, d, st, item_base, s_syn, s_max, arena, consts);
+        if (ap && bp) items = run_step<T, NORM, true, true, MAXP>(a, d, st, item_base, s_syn, s_max, arena, consts);
+        else if (ap) items = run_step<T, NORM, true, false, MAXP>(a, d, st, item_base, s_syn, s_max, arena, consts);
+        else if (bp) items = run_step<T, NORM, false, true, MAXP>(a, d, st, item_base, s_syn, s_max, arena, consts);
+        else items = run_step<T, NORM, false, false, MAXP>(a, d, st, item_base, s_syn, s_max, arena, consts);
       }
       if (d.sync_after) {
         __syncthreads();
@@ -352,6 +464,10 @@ __global__ void __launch_bounds__(1024) tn_contract_kernel(KArgs a) {
       } else {
         item_base += items;
       }
+    }
+    if (MAXP) {
+      backtrack<T>(a, s_steps, s_syn, s_asg, arena, consts, base, nrows);
+      __syncthreads();
     }
     // epilogue: log-marginals, first argmax (Julia findmax order), recheck flag
     const StepDesc& root = s_steps[a.n_steps - 1];
@@ -400,10 +516,11 @@ __global__ void __launch_bounds__(1024) tn_contract_kernel(KArgs a) {
 }  // namespace
 
 size_t contract_smem_bytes(int precision, int32_t n_steps, int32_t syn_words, int G,
-                           int64_t arena_elems, bool arena_in_smem) {
+                           int64_t arena_elems, bool arena_in_smem, int32_t var_words) {
   const bool norm = precision == 1;
   size_t off = size_t(n_steps) * sizeof(StepDesc) + size_t(G) * syn_words * 4;
   if (norm) off += size_t(G) * n_steps * 4;
+  off += size_t(G) * var_words * 4;
   off = (off + 15) & ~size_t(15);
   if (arena_in_smem) off += size_t(G) * size_t(arena_elems) * (precision == 1 ? 4 : 8);
   return off;
@@ -415,37 +532,40 @@ size_t contract_smem_limit(int device) {
   return size_t(v);
 }
 
-int contract_occupancy(int precision, int threads, size_t smem) {
+template <typename K>
+int occupancy_of(K kernel, int threads, size_t smem) {
   int blocks = 0;
-  cudaError_t e;
-  if (precision == 1) {
-    cudaFuncSetAttribute(tn_contract_kernel<float, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, tn_contract_kernel<float, true>, threads, smem);
-  } else {
-    cudaFuncSetAttribute(tn_contract_kernel<double, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, tn_contract_kernel<double, false>, threads, smem);
-  }
-  if (e != cudaSuccess) {
+  cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, kernel, threads, smem) != cudaSuccess) {
     cudaGetLastError();
     return 0;
   }
   return blocks;
 }
 
+int contract_occupancy(int precision, int threads, size_t smem, bool map_mode) {
+  if (precision == 1)
+    return map_mode ? occupancy_of(tn_contract_kernel<float, true, true>, threads, smem)
+                    : occupancy_of(tn_contract_kernel<float, true, false>, threads, smem);
+  return map_mode ? occupancy_of(tn_contract_kernel<double, false, true>, threads, smem)
+                  : occupancy_of(tn_contract_kernel<double, false, false>, threads, smem);
+}
+
+template <typename K>
+cudaError_t launch_with(K kernel, const KArgs& a, int grid, int threads, size_t smem, cudaStream_t stream) {
+  cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+  if (e != cudaSuccess) return e;
+  kernel<<<grid, threads, smem, stream>>>(a);
+  return cudaGetLastError();
+}
+
 cudaError_t contract_launch(int precision, const KArgs& a, int grid, int threads, size_t smem,
                             cudaStream_t stream) {
-  if (precision == 1) {
-    cudaError_t e = cudaFuncSetAttribute(tn_contract_kernel<float, true>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
-    if (e != cudaSuccess) return e;
-    tn_contract_kernel<float, true><<<grid, threads, smem, stream>>>(a);
-  } else {
-    cudaError_t e = cudaFuncSetAttribute(tn_contract_kernel<double, false>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
-    if (e != cudaSuccess) return e;
-    tn_contract_kernel<double, false><<<grid, threads, smem, stream>>>(a);
-  }
-  return cudaGetLastError();
+  if (precision == 1)
+    return a.map_mode ? launch_with(tn_contract_kernel<float, true, true>, a, grid, threads, smem, stream)
+                      : launch_with(tn_contract_kernel<float, true, false>, a, grid, threads, smem, stream);
+  return a.map_mode ? launch_with(tn_contract_kernel<double, false, true>, a, grid, threads, smem, stream)
+                    : launch_with(tn_contract_kernel<double, false, false>, a, grid, threads, smem, stream);
 }
 
 }  // namespace tqec

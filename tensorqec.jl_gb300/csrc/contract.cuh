@@ -35,17 +35,26 @@ struct KArgs {
   double recheck_margin;  // < 0: never flag
   int32_t* recheck_list;
   int32_t* recheck_count;
+  // most probable configuration (max-product contraction + back-tracking)
+  int32_t map_mode;
+  const int32_t* vartab;  // per step: variable ids of fb, fa, h, k bits
+  int32_t n_vars;
+  int32_t var_words;      // ceil(n_vars / 32)
+  const int8_t* fixed;    // per variable: -1, or the value decided on the host
+  const int32_t* report;  // variables whose values are returned
+  int32_t n_report;
+  uint8_t* assign_out;    // n x ceil(n_report / 8) bit-packed values
 };
 
 // Shared memory a launch needs (bytes).
 size_t contract_smem_bytes(int precision, int32_t n_steps, int32_t syn_words, int G,
-                           int64_t arena_elems, bool arena_in_smem);
+                           int64_t arena_elems, bool arena_in_smem, int32_t var_words = 0);
 
 // Largest dynamic shared memory a block may use on this device.
 size_t contract_smem_limit(int device);
 
 // Resident blocks per SM for a launch shape (0 if it cannot launch).
-int contract_occupancy(int precision, int threads, size_t smem);
+int contract_occupancy(int precision, int threads, size_t smem, bool map_mode = false);
 
 cudaError_t contract_launch(int precision, const KArgs& a, int grid, int threads, size_t smem,
                             cudaStream_t stream);

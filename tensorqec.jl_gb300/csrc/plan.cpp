@@ -170,7 +170,7 @@ std::string build_plan(const NetworkView& net, int32_t n_steps, const int32_t* s
   if (T < 1) return "network has no tensors";
   if (!net.ix_offsets || !net.ix_labels || !net.data_offsets || !net.data)
     return "network arrays must not be NULL";
-  if (net.n_out < 0 || net.n_out > 16) {
+  if (net.n_out < 0 || (!lim.map_mode && net.n_out > 16)) {
     *unsupported = net.n_out > 16;
     return "n_out must be in [0, 16]";
   }
@@ -228,22 +228,28 @@ std::string build_plan(const NetworkView& net, int32_t n_steps, const int32_t* s
     n.kind = NK_TABLE;
     n.data.assign(net.data + da, net.data + db);
   }
-  std::vector<int> out_vars;
+  const bool map_mode = lim.map_mode;
+  std::vector<int> out_vars, report_vars;
   for (int i = 0; i < net.n_out; ++i) {
     auto it = var_of.find(net.out_labels[i]);
     if (it == var_of.end()) {
       *unsupported = true;
       return "output label does not appear in any tensor";
     }
-    if (std::find(out_vars.begin(), out_vars.end(), it->second) != out_vars.end())
-      return "repeated output label";
-    out_vars.push_back(it->second);
+    std::vector<int>& dst = map_mode ? report_vars : out_vars;
+    if (std::find(dst.begin(), dst.end(), it->second) != dst.end()) return "repeated output label";
+    dst.push_back(it->second);
   }
   const int V = (int)var_of.size();
   std::vector<int> cnt(V, 0);
   for (int i = 0; i < T; ++i)
     for (int v : nodes[i].vars) cnt[v]++;
   for (int v : out_vars) cnt[v]++;
+  // labels of the syndrome leaves: evidence, never reported
+  std::vector<char> is_syn_var(V, 0);
+  for (int i = 0; i < T; ++i)
+    if (syn_bit_of[i] >= 0) is_syn_var[nodes[i].vars[0]] = 1;
+  std::vector<int8_t> fixed(V, -1);
 
   // ---- dead labels inside a single leaf are summed right away -------------
   for (int i = 0; i < T; ++i) {
@@ -255,6 +261,29 @@ std::string build_plan(const NetworkView& net, int32_t n_steps, const int32_t* s
       else dead = true;
     }
     if (!dead) continue;
+    if (map_mode) {
+      // maximising over a label only this leaf carries: a one-label prior
+      // decides its value on the host; anything else needs the search
+      if (n.kind == NK_PARITY && n.vars.size() == 1 && is_syn_var[n.vars[0]]) {
+        cnt[n.vars[0]]--;
+        n.kind = NK_TABLE;
+        n.vars.clear();
+        n.data.assign(1, 1.0);
+        n.par_bit = -1;
+        continue;
+      }
+      if (n.kind == NK_TABLE && n.vars.size() == 1) {
+        const int v = n.vars[0];
+        fixed[v] = n.data[1] > n.data[0] ? 1 : 0;
+        const double m = std::max(n.data[0], n.data[1]);
+        cnt[v]--;
+        n.vars.clear();
+        n.data.assign(1, m);
+        continue;
+      }
+      *unsupported = true;
+      return "MAP mode: a label occurs in a single multi-label tensor";
+    }
     if (n.kind == NK_PARITY) {
       // summing a parity indicator over one of its labels gives all ones
       for (int v : n.vars)
@@ -318,7 +347,12 @@ std::string build_plan(const NetworkView& net, int32_t n_steps, const int32_t* s
         }
       }
     }
-    if (!folded && nx.kind != NK_RUNTIME && ny.kind != NK_RUNTIME) {
+    // MAP mode folds only products that eliminate nothing but evidence
+    bool fold_ok = true;
+    if (map_mode)
+      for (int v : uni)
+        if (std::find(keep.begin(), keep.end(), v) == keep.end() && !is_syn_var[v]) fold_ok = false;
+    if (!folded && fold_ok && nx.kind != NK_RUNTIME && ny.kind != NK_RUNTIME) {
       PNode tx = nx.kind == NK_PARITY ? parity_as_table(nx) : nx;
       PNode ty = ny.kind == NK_PARITY ? parity_as_table(ny) : ny;
       std::set<int> sb(tx.sel.begin(), tx.sel.end());
@@ -331,7 +365,7 @@ std::string build_plan(const NetworkView& net, int32_t n_steps, const int32_t* s
       if (ok) {
         c = fold_tables(tx, ty, keep);
         folded = true;
-      } else if (nsel == 0) {
+      } else if (nsel == 0 && !map_mode) {
         *unsupported = true;
         return "syndrome-independent intermediate too wide to fold on the host";
       }
@@ -467,8 +501,8 @@ std::string build_plan(const NetworkView& net, int32_t n_steps, const int32_t* s
   P = Plan();
   P.n_syndrome = net.n_syndrome;
   P.syndrome_bytes = (net.n_syndrome + 7) / 8;
-  P.n_out = net.n_out;
-  P.n_classes = 1 << net.n_out;
+  P.n_out = map_mode ? 0 : net.n_out;
+  P.n_classes = map_mode ? 1 : 1 << net.n_out;
   P.n_tree_steps = n_steps;
   P.macs_tree = macs_tree;
   std::map<int, std::pair<int64_t, std::vector<int8_t>>> const_ref;  // node -> (offset, sel)
@@ -571,6 +605,7 @@ std::string build_plan(const NetworkView& net, int32_t n_steps, const int32_t* s
   double macs_rt = 0.0;
   P.steps.resize(R);
   std::vector<int> pending_release;
+  int32_t d_var_off = 0;
   for (int r = 0; r < R; ++r) {
     const int id = order[r];
     PNode& n = nodes[id];
@@ -583,8 +618,13 @@ std::string build_plan(const NetworkView& net, int32_t n_steps, const int32_t* s
     for (int op : {L.a, L.b})
       if (nodes[op].kind == NK_RUNTIME) pending_release.push_back(op);
     if (group_end[r]) {
-      for (int op : pending_release) release(arena_off[op], int64_t(1) << nodes[op].vars.size());
+      if (!map_mode)  // MAP back-tracking reads every intermediate again
+        for (int op : pending_release) release(arena_off[op], int64_t(1) << nodes[op].vars.size());
       pending_release.clear();
+    }
+    if (map_mode) {
+      d_var_off = (int32_t)P.vartab.size();
+      for (const std::vector<int>* g : {&L.Fb, &L.Fa, &L.H, &L.K}) P.vartab.insert(P.vartab.end(), g->begin(), g->end());
     }
     macs_rt += std::ldexp(1.0, (int)(L.H.size() + L.Fa.size() + L.Fb.size() + L.K.size()));
     StepDesc d;
@@ -595,6 +635,7 @@ std::string build_plan(const NetworkView& net, int32_t n_steps, const int32_t* s
     d.lk = (int)L.K.size();
     d.out_off = (int32_t)off;
     d.sync_after = group_end[r];
+    d.var_off = map_mode ? d_var_off : 0;
     for (int side = 0; side < 2; ++side) {
       int op = side ? L.b : L.a;
       PNode& o = nodes[op];
@@ -647,6 +688,23 @@ std::string build_plan(const NetworkView& net, int32_t n_steps, const int32_t* s
     P.steps[r] = d;
   }
   P.width = width;
+  if (map_mode) {
+    P.map_mode = true;
+    P.n_vars = V;
+    P.fixed = fixed;
+    P.report.assign(report_vars.begin(), report_vars.end());
+    // every reported label is decided by some step's k group or on the host
+    std::vector<char> decided(V, 0);
+    for (int r = 0; r < R; ++r)
+      for (int v : lay[r].K) decided[v] = 1;
+    for (int v = 0; v < V; ++v)
+      if (fixed[v] >= 0) decided[v] = 1;
+    for (int v : report_vars)
+      if (!decided[v]) {
+        *unsupported = true;
+        return "MAP mode: a reported label is never maximised over (is it an output of the tree?)";
+      }
+  }
   P.arena_elems = std::max<int64_t>((arena_top + 31) & ~int64_t(31), 32);
   P.root_step = R - 1;
   P.macs_runtime = macs_rt;

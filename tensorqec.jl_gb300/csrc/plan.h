@@ -39,7 +39,7 @@ struct StepDesc {
   int32_t out_off;           // arena offset of the output
   int32_t perm_off;          // output permutation tables, -1 = identity
   int32_t sync_after;        // 1: block barrier after this step (end of a barrier group)
-  int32_t pad1;
+  int32_t var_off;           // MAP mode: offset of the step's labels in Plan::vartab
 };
 static_assert(sizeof(StepDesc) == 64, "StepDesc is 64 bytes");
 
@@ -55,6 +55,15 @@ struct Plan {
   double macs_runtime = 0.0;       // multiply-adds per syndrome, runtime steps
   double macs_tree = 0.0;          // multiply-adds of the tree as given
   double err_terms = 0.0;          // sum over runtime steps of (K + 1) plus leaves
+  // MAP mode (most probable configuration): every runtime step keeps its
+  // output; vartab lists, per step, the variable ids of its fb, fa, h and k
+  // index bits (lowest first); report lists the variables whose values are
+  // returned; fixed holds values decided on the host (-1: from the search).
+  bool map_mode = false;
+  int32_t n_vars = 0;
+  std::vector<int32_t> vartab;
+  std::vector<int32_t> report;
+  std::vector<int8_t> fixed;
   std::vector<StepDesc> steps;
   std::vector<int32_t> perm;       // concatenated permutation tables
   std::vector<double> consts;      // constant operand data (all variants)
@@ -76,6 +85,7 @@ struct PlanLimits {
   int max_sel_bits = 2;       // fold syndrome-dependent leaves up to this many bits
   int max_sel_rank = 8;       // ... and up to this many labels
   int max_width = 30;         // refuse intermediates wider than 2^max_width
+  bool map_mode = false;      // max-product contraction + back-tracking (TNMAP)
 };
 
 // Builds the program; returns "" on success or an error message.

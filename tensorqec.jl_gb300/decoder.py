@@ -17,8 +17,8 @@ from . import gf2, native
 from .codes import CSSTannerGraph, SimpleTannerGraph
 from .dem import DetectorErrorModel, dem2tanner, logical_map
 from .error_model import (CSSErrorPattern, CSSSyndrome, DecodingResult, IndependentDepolarizingError,
-                          SimpleSyndrome, iid_error, pack_syndromes)
-from .network import FactorGraph, tnmmap_css_graph, tnmmap_dem_graph
+                          IndependentFlipError, SimpleSyndrome, iid_error, pack_syndromes)
+from .network import FactorGraph, reduce2general, tnmap_graph, tnmmap_css_graph, tnmmap_dem_graph
 
 
 # ---------------------------------------------------------------------------
@@ -52,6 +52,9 @@ class NoOptimizer:
 
 def optimize_code(graph: FactorGraph, optimizer) -> np.ndarray:
     """Returns the tree as an (n_tensors - 1, 2) array of node ids."""
+    if graph.map_mode:
+        # the root of a most-probable-configuration contraction is a scalar
+        return optimize_code(FactorGraph(graph.ixs, graph.tensors, [], graph.syndrome_positions), optimizer)
     n = graph.n_tensors
     if isinstance(optimizer, NoOptimizer) or n == 1:
         steps = np.zeros((max(n - 1, 0), 2), dtype=np.int32)
@@ -315,12 +318,137 @@ class CompiledDEMTNMMAP:
         self.program.close()
 
 
+@dataclass
+class TNMAP:
+    """Most-probable-configuration decoder (tndecoder.jl:9-11): max-product
+    contraction of the general decoding problem's factor graph on the GPU,
+    then back-tracking of the maximising values from the root down.
+
+    ``precision``: "f64" (default) or "f32" (power-of-two renormalised; the
+    maximiser can differ from f64 only between configurations whose
+    probabilities agree to float32 rounding)."""
+    optimizer: object = field(default_factory=TreeSA)
+    precision: str = "f64"
+    device: int = 0
+    group: int = 0
+    threads: int = 0
+
+    def _native_precision(self):
+        return {"f64": native.TQEC_F64, "f32": native.TQEC_F32}[self.precision]
+
+
+class CompiledTNMAP:
+    """CompiledTNMAP (tndecoder.jl:16-19, compile at :46-50) for a
+    GeneralDecodingProblem: a SimpleTannerGraph plus one prior tensor per
+    ``prior_ixs`` entry (labels are 1-based bits)."""
+
+    def __init__(self, decoder: TNMAP, tanner: SimpleTannerGraph, prior_ixs, prior_tensors):
+        self.decoder = decoder
+        self.tanner = tanner
+        self.prior_ixs = [list(ix) for ix in prior_ixs]
+        self.prior_tensors = [np.asarray(t, dtype=np.float64) for t in prior_tensors]
+        self.graph = tnmap_graph(tanner, self.prior_ixs, self.prior_tensors)
+        self.steps = optimize_code(self.graph, decoder.optimizer)
+        self.program = native.Program(self.graph, self.steps, decoder._native_precision(), native.TQEC_FLAG_MAP,
+                                      decoder.device, decoder.group, decoder.threads, -1.0)
+
+    @property
+    def n_syndrome(self):
+        return self.tanner.ns
+
+    @property
+    def qubit_num(self):
+        return self.tanner.nq
+
+    def decode_batch(self, syndromes, return_logp=False):
+        """Most probable bit configuration for each syndrome row: an
+        (n, nq) 0/1 array (and the natural log of its probability)."""
+        bits = np.atleast_2d(np.asarray(syndromes, dtype=np.uint8)) & 1
+        cfg, logp = self.program.map_decode_packed(pack_syndromes(bits), self.tanner.nq)
+        return (cfg, logp) if return_logp else cfg
+
+    def log_probability(self, config):
+        """Natural log of the unnormalised probability of full bit
+        configurations (rows of 0/1), from the prior tensors (host)."""
+        config = np.atleast_2d(np.asarray(config, dtype=np.int64))
+        out = np.zeros(config.shape[0])
+        with np.errstate(divide="ignore"):
+            for ix, t in zip(self.prior_ixs, self.prior_tensors):
+                flat = t.ravel(order="F")
+                idx = np.zeros(config.shape[0], dtype=np.int64)
+                for j, v in enumerate(ix):
+                    idx |= config[:, v - 1] << j
+                out += np.log(flat[idx])
+        return out
+
+    def decode(self, syndrome: SimpleSyndrome) -> DecodingResult:
+        """decode(ct::CompiledTNMAP, syndrome), tndecoder.jl:53-57."""
+        cfg = self.decode_batch(np.asarray(syndrome.s)[None, :])[0]
+        return DecodingResult(True, cfg.astype(np.uint8))
+
+    def close(self):
+        self.program.close()
+
+
+class CompiledGeneralTNMAP:
+    """CompiledGeneralDecoder (interfaces.jl:124-137): TNMAP on the CSS
+    problem reduced by reduce2general; decode returns a CSSErrorPattern."""
+
+    def __init__(self, decoder: TNMAP, tanner: CSSTannerGraph, em):
+        self.css = tanner
+        self.em = em
+        general, ixs, ts = reduce2general(tanner, em)
+        self.cd = CompiledTNMAP(decoder, general, ixs, ts)
+
+    @property
+    def program(self):
+        return self.cd.program
+
+    def decode_batch(self, syndromes, return_logp=False):
+        """(ex, ez) rows for syndrome rows [sx..., sz...]."""
+        if isinstance(syndromes, CSSSyndrome):
+            syndromes = syndromes.bits()[None, :]
+        cfg, logp = self.cd.decode_batch(syndromes, return_logp=True)
+        nq = self.css.nq
+        out = (cfg[:, :nq], cfg[:, nq:])
+        return (out, logp) if return_logp else out
+
+    def decode(self, syndrome: CSSSyndrome) -> DecodingResult:
+        """extract_decoding (general_decoding.jl:9-12) of the general decode."""
+        cfg = self.cd.decode_batch(syndrome.bits()[None, :])[0].astype(np.uint8)
+        nq = self.css.nq
+        return DecodingResult(True, CSSErrorPattern(cfg[:nq], cfg[nq:]))
+
+    def close(self):
+        self.cd.close()
+
+
 def compile(decoder, problem, em=None):
     """compile(decoder, tanner[, em]) / compile(decoder, dem)
     (interfaces.jl:74-79, tndecoder.jl:97, :186).  Without ``em`` a CSS code
-    gets the reference's default ``iid_error(0.05, tanner)``."""
+    gets the reference's default ``iid_error(0.05, tanner)``.  TNMAP takes a
+    CSS code (reduced by reduce2general, interfaces.jl:129-133), a
+    SimpleTannerGraph with an IndependentFlipError (:139-142) or a
+    GeneralDecodingProblem given as (tanner, prior_ixs, prior_tensors)."""
+    if isinstance(decoder, TNMAP):
+        if isinstance(problem, CSSTannerGraph):
+            if em is None:
+                em = iid_error(0.05, problem)
+            return CompiledGeneralTNMAP(decoder, problem, em)
+        if isinstance(problem, SimpleTannerGraph):
+            if em is None:
+                em = iid_error(0.05, problem.nq)
+            if isinstance(em, IndependentFlipError):
+                p = em.p
+            else:
+                p = np.broadcast_to(np.asarray(em, dtype=np.float64), (problem.nq,))
+            return CompiledTNMAP(decoder, problem, [[i + 1] for i in range(problem.nq)],
+                                 [np.array([1 - q, q]) for q in p])
+        if isinstance(problem, tuple) and len(problem) == 3:
+            return CompiledTNMAP(decoder, *problem)
+        raise TypeError(f"TNMAP cannot compile for {type(problem).__name__}")
     if not isinstance(decoder, TNMMAP):
-        raise TypeError("compile supports TNMMAP")
+        raise TypeError("compile supports TNMMAP and TNMAP")
     if isinstance(problem, DetectorErrorModel):
         return CompiledDEMTNMMAP(decoder, problem)
     if isinstance(problem, CSSTannerGraph):
@@ -333,7 +461,7 @@ def compile(decoder, problem, em=None):
 def decode(ct_or_decoder, *args):
     """decode(ct, syndrome) or decode(decoder, tanner, syndrome[, em])
     (interfaces.jl:96-105)."""
-    if isinstance(ct_or_decoder, (CompiledTNMMAP, CompiledDEMTNMMAP)):
+    if isinstance(ct_or_decoder, (CompiledTNMMAP, CompiledDEMTNMMAP, CompiledTNMAP, CompiledGeneralTNMAP)):
         return ct_or_decoder.decode(*args)
     decoder, tanner, syndrome = ct_or_decoder, args[0], args[1]
     em = args[2] if len(args) > 2 else None

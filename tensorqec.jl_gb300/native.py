@@ -18,6 +18,7 @@ TQEC_F64 = 0
 TQEC_F32 = 1
 TQEC_FLAG_PLAIN = 1
 TQEC_FLAG_NORECHECK = 2
+TQEC_FLAG_MAP = 4
 
 ERRORS = {-1: "invalid argument", -2: "CUDA error", -3: "out of device memory",
           -4: "unsupported network", -5: "timeout", -6: "I/O error"}
@@ -58,7 +59,9 @@ class PlanView(C.Structure):
                 ("perm", C.c_void_p), ("n_consts", C.c_int64), ("consts", C.c_void_p),
                 ("arena_elems", C.c_int64), ("width", C.c_int32), ("n_classes", C.c_int32),
                 ("n_syndrome", C.c_int32), ("flops_per_syndrome", C.c_double), ("flops_tree", C.c_double),
-                ("err_terms", C.c_double)]
+                ("err_terms", C.c_double), ("map_mode", C.c_int32), ("n_vars", C.c_int32),
+                ("n_vartab", C.c_int64), ("vartab", C.c_void_p), ("n_report", C.c_int32), ("report", C.c_void_p),
+                ("fixed", C.c_void_p)]
 
 
 class OrderOptions(C.Structure):
@@ -69,7 +72,7 @@ class OrderOptions(C.Structure):
 STEP_DTYPE = np.dtype([("a_kind", "<i4"), ("b_kind", "<i4"), ("a_ref", "<i4"), ("b_ref", "<i4"),
                        ("a_prod", "<i4"), ("b_prod", "<i4"), ("a_sel", "i1", (4,)), ("b_sel", "i1", (4,)),
                        ("lh", "<i4"), ("lfa", "<i4"), ("lfb", "<i4"), ("lk", "<i4"),
-                       ("out_off", "<i4"), ("perm_off", "<i4"), ("sync_after", "<i4"), ("pad1", "<i4")])
+                       ("out_off", "<i4"), ("perm_off", "<i4"), ("sync_after", "<i4"), ("var_off", "<i4")])
 assert STEP_DTYPE.itemsize == 64
 
 _lib = None
@@ -94,6 +97,8 @@ def lib():
         "tqec_last_recheck_count": [vp, vp],
         "tqec_program_autotune": [vp, i64],
         "tqec_plan_inspect": [vp, vp, vp, vp],
+        "tqec_plan_inspect_flags": [vp, vp, C.c_uint32, vp, vp],
+        "tqec_map_decode_batch": [vp, vp, i64, vp, vp, vp],
         "tqec_plan_release": [vp],
         "tqec_optimize_order": [vp, vp, vp, vp, vp],
         "tqec_last_error": [vp, C.c_size_t],
@@ -154,24 +159,30 @@ def optimize_order(graph, trials=32, sweeps=60, target_width=0, width_penalty=1.
     return steps, lm.value, w.value
 
 
-def inspect_plan(graph, steps):
+def inspect_plan(graph, steps, flags=0):
     """The compiled program as numpy arrays (no GPU needed)."""
     na = NetworkArrays(graph)
     steps = np.ascontiguousarray(steps, dtype=np.int32)
     tree = Tree(steps.shape[0], _ptr(steps))
     view = PlanView()
     h = C.c_void_p()
-    check(lib().tqec_plan_inspect(C.byref(na.struct), C.byref(tree), C.byref(view), C.byref(h)))
+    check(lib().tqec_plan_inspect_flags(C.byref(na.struct), C.byref(tree), flags, C.byref(view), C.byref(h)))
     try:
         st = np.frombuffer(C.string_at(view.steps, 64 * view.n_steps), dtype=STEP_DTYPE).copy()
         perm = (np.frombuffer(C.string_at(view.perm, 4 * view.n_perm), dtype=np.int32).copy()
                 if view.n_perm else np.zeros(0, np.int32))
         consts = (np.frombuffer(C.string_at(view.consts, 8 * view.n_consts), dtype=np.float64).copy()
                   if view.n_consts else np.zeros(0))
-        return {"steps": st, "perm": perm, "consts": consts, "arena_elems": view.arena_elems,
-                "width": view.width, "n_classes": view.n_classes, "n_syndrome": view.n_syndrome,
-                "flops_per_syndrome": view.flops_per_syndrome, "flops_tree": view.flops_tree,
-                "err_terms": view.err_terms}
+        out = {"steps": st, "perm": perm, "consts": consts, "arena_elems": view.arena_elems,
+               "width": view.width, "n_classes": view.n_classes, "n_syndrome": view.n_syndrome,
+               "flops_per_syndrome": view.flops_per_syndrome, "flops_tree": view.flops_tree,
+               "err_terms": view.err_terms, "map_mode": bool(view.map_mode)}
+        if view.map_mode:
+            out["n_vars"] = view.n_vars
+            out["vartab"] = np.frombuffer(C.string_at(view.vartab, 4 * view.n_vartab), dtype=np.int32).copy()
+            out["report"] = np.frombuffer(C.string_at(view.report, 4 * view.n_report), dtype=np.int32).copy()
+            out["fixed"] = np.frombuffer(C.string_at(view.fixed, view.n_vars), dtype=np.int8).copy()
+        return out
     finally:
         lib().tqec_plan_release(h)
 
@@ -240,6 +251,17 @@ class Program:
     def contract_ptrs(self, syn_ptr, n, precision, logp_ptr, stream=None):
         check(lib().tqec_contract_batch(self._h, C.c_void_p(syn_ptr), n, precision, C.c_void_p(logp_ptr),
                                         C.c_void_p(stream) if stream else None))
+
+    def map_decode_packed(self, packed, n_report):
+        """TQEC_FLAG_MAP programs: (values of the reported variables as an
+        (n, n_report) 0/1 array, log-probability of the configuration)."""
+        packed = np.ascontiguousarray(packed, dtype=np.uint8)
+        n = packed.shape[0]
+        rb = (n_report + 7) // 8
+        asg = np.empty((n, rb), dtype=np.uint8)
+        logp = np.empty(n, dtype=np.float64)
+        check(lib().tqec_map_decode_batch(self._h, _ptr(packed), n, _ptr(asg), _ptr(logp), None))
+        return np.unpackbits(asg, axis=1, count=n_report, bitorder="little"), logp
 
     def last_recheck_count(self):
         c = C.c_int64(0)

@@ -34,6 +34,9 @@ class FactorGraph:
     tensors: list
     iy: list
     syndrome_positions: list
+    # most-probable-configuration graphs: ``iy`` lists the reported labels
+    # and the contraction reduces everything to a scalar
+    map_mode: bool = False
 
     @property
     def n_tensors(self):
@@ -127,3 +130,46 @@ def tnmmap_dem_graph(tanner, l2q, error_rates, n_logicals, factorize=True) -> Fa
         ixs.append([v])
         tensors.append(np.array([1.0, 0.0]))
     return FactorGraph(ixs, tensors, iy, synd)
+
+
+def tnmap_graph(tanner, prior_ixs, prior_tensors) -> FactorGraph:
+    """stg2uaimodel (tndecoder.jl:33-40) with the syndrome evidence of
+    compile(::TNMAP, ...) (:46-50) as one-hot leaves.  Labels: bits
+    1..nq, syndromes nq+1..nq+ns; every bit label is reported (the root is a
+    scalar: the probability of the most probable configuration)."""
+    nq, ns = tanner.nq, tanner.ns
+    ixs, tensors = [], []
+    for s, c in enumerate(tanner.s2q, 1):
+        ixs.append(list(c) + [s + nq])
+        tensors.append(parity_tensor(len(c) + 1))
+    for ix, t in zip(prior_ixs, prior_tensors):
+        ixs.append(list(ix))
+        tensors.append(np.asarray(t, dtype=np.float64).ravel(order="F"))
+    synd = []
+    for v in range(nq + 1, nq + ns + 1):
+        synd.append(len(ixs))
+        ixs.append([v])
+        tensors.append(np.array([1.0, 0.0]))
+    return FactorGraph(ixs, tensors, list(range(1, nq + 1)), synd, map_mode=True)
+
+
+def reduce2general(tanner, em):
+    """reduce2general(tanner::CSSTannerGraph, pvec) (general_decoding.jl:
+    24-32): a SimpleTannerGraph over 2nq bits (x errors 1..nq, z errors
+    nq+1..2nq) whose checks are the X checks on the z-error bits followed by
+    the Z checks on the x-error bits, and one prior [1-p pz; px py] over
+    (x_i, z_i) per qubit.  ``em`` may instead be a tensor network given as
+    (ixs, tensors) over those 2nq labels (general_decoding.jl:29-32)."""
+    from .codes import SimpleTannerGraph
+    nq = tanner.nq
+    general = SimpleTannerGraph(2 * nq, [[q + nq for q in c] for c in tanner.stgx.s2q] +
+                                [list(c) for c in tanner.stgz.s2q])
+    if isinstance(em, tuple):
+        ixs, ts = em
+        return general, [list(ix) for ix in ixs], [np.asarray(t, dtype=np.float64) for t in ts]
+    ixs = [[i + 1, i + 1 + nq] for i in range(nq)]
+    ts = []
+    for i in range(nq):
+        px, py, pz = float(em.px[i]), float(em.py[i]), float(em.pz[i])
+        ts.append(np.array([1 - px - py - pz, px, pz, py], dtype=np.float64))
+    return general, ixs, ts

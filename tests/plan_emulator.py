@@ -33,8 +33,10 @@ def _perm_addr(perm, off, e, lw):
     return addr
 
 
-def run_plan(plan, bits, dtype=np.float64):
-    """bits: (n, n_syndrome) 0/1.  Returns (n, n_classes) marginals."""
+def run_plan(plan, bits, dtype=np.float64, return_arena=False):
+    """bits: (n, n_syndrome) 0/1.  Returns (n, n_classes) marginals (for a
+    MAP-mode plan: the max-product value, shape (n, 1))."""
+    maxp = plan.get("map_mode", False)
     bits = np.atleast_2d(np.asarray(bits, dtype=np.int64))
     n = bits.shape[0]
     steps = plan["steps"]
@@ -67,8 +69,52 @@ def run_plan(plan, bits, dtype=np.float64):
 
         av = operand(int(d["a_kind"]), int(d["a_ref"]), d["a_sel"], aidx, lh + lfa + lk)
         bv = operand(int(d["b_kind"]), int(d["b_ref"]), d["b_sel"], bidx, lh + lk + lfb)
-        acc = (av * bv).sum(axis=2)
+        acc = (av * bv).max(axis=2) if maxp else (av * bv).sum(axis=2)
         addr = e if int(d["perm_off"]) < 0 else _perm_addr(perm, int(d["perm_off"]), e, lw)
         arena[:, int(d["out_off"]) + addr] = acc
     root = steps[-1]
-    return arena[:, int(root["out_off"]): int(root["out_off"]) + plan["n_classes"]]
+    out = arena[:, int(root["out_off"]): int(root["out_off"]) + plan["n_classes"]]
+    return (out, arena) if return_arena else out
+
+
+def map_backtrack(plan, bits, arena):
+    """Most probable configuration from a MAP-mode plan's arena: walks the
+    steps from the root down (as the kernel does) and returns the values of
+    the reported variables, (n, n_report)."""
+    bits = np.atleast_2d(np.asarray(bits, dtype=np.int64))
+    n = bits.shape[0]
+    consts = plan["consts"]
+    vt = plan["vartab"]
+    out = np.zeros((n, len(plan["report"])), dtype=np.uint8)
+    for r in range(n):
+        asg = np.where(plan["fixed"] == 1, 1, 0).astype(np.int64)
+        for d in plan["steps"][::-1]:
+            lh, lfa, lfb, lk = int(d["lh"]), int(d["lfa"]), int(d["lfb"]), int(d["lk"])
+            o = int(d["var_off"])
+            fb = sum(int(asg[vt[o + j]]) << j for j in range(lfb))
+            fa = sum(int(asg[vt[o + lfb + j]]) << j for j in range(lfa))
+            h = sum(int(asg[vt[o + lfb + lfa + j]]) << j for j in range(lh))
+            abase = ((h << lfa) | fa) << lk
+            bbase = (h << (lk + lfb)) | fb
+
+            def val(kind, ref, sel, idx, obits):
+                if kind == OP_PARITY:
+                    return 1.0 if ((bin(idx).count("1") ^ int(bits[r, ref])) & 1) == 0 else 0.0
+                if kind == OP_ARENA:
+                    return arena[r, ref + idx]
+                v = 0
+                for i, b in enumerate(sel):
+                    if b >= 0:
+                        v |= int(bits[r, b]) << i
+                return consts[ref + (v << obits) + idx]
+
+            best, bk = -1.0, 0
+            for k in range(1 << lk):
+                v = (val(int(d["a_kind"]), int(d["a_ref"]), d["a_sel"], abase + k, lh + lfa + lk)
+                     * val(int(d["b_kind"]), int(d["b_ref"]), d["b_sel"], bbase + (k << lfb), lh + lk + lfb))
+                if v > best:
+                    best, bk = v, k
+            for j in range(lk):
+                asg[vt[o + lfb + lfa + lh + j]] = (bk >> j) & 1
+        out[r] = asg[plan["report"]]
+    return out
