@@ -45,7 +45,7 @@ def parse():
                     help="one float32 contraction launch of --batch syndromes (for ncu), no timing")
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--no-surrogate", action="store_true", help="time the batched exact decoder alone")
-    ap.add_argument("--train-n", type=int, default=1 << 22, help="surrogate training syndromes")
+    ap.add_argument("--train-n", type=int, default=1 << 24, help="surrogate training syndromes")
     ap.add_argument("--calib-n", type=int, default=1 << 20, help="surrogate calibration syndromes")
     ap.add_argument("--eval-n", type=int, default=1 << 20, help="fresh syndromes for the evaluation")
     return ap.parse_args()
@@ -262,7 +262,7 @@ def run_ours(args):
     sur_stats = None
     if not args.no_surrogate:
         t0 = time.time()
-        sur, tstats = train_surrogate(ct, n_train=args.train_n, batch=8192, epochs=2, lr=2e-3, hidden=512,
+        sur, tstats = train_surrogate(ct, n_train=args.train_n, batch=16384, epochs=4, lr=3e-3, hidden=512,
                                       n_layers=4, seed=SEED + 17 + rank)
         # calibrated at half the 1e-4 budget so fresh syndromes stay under it
         thr, cstats = calibrate(sur, ct, n_val=args.calib_n, target_mismatch=5e-5, seed=SEED + 29 + rank)

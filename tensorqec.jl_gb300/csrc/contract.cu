@@ -82,9 +82,25 @@ __device__ __forceinline__ Operand<T> make_operand(int kind, int32_t ref, const 
   return o;
 }
 
-template <typename T, bool NORM, bool APAR, bool BPAR, bool MAXP>
-__device__ int run_step(const KArgs& a, const StepDesc& d, int st, int item_base, const uint32_t* s_syn,
+// Folds a thread's running maximum into the step's per-syndrome maximum
+// (one warp reduction and one shared atomic per warp that had work).
+__device__ __forceinline__ void flush_max(bool had_items, uint32_t bits, uint32_t* slot) {
+  if (!__any_sync(0xffffffffu, had_items)) return;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t other = __shfl_xor_sync(0xffffffffu, bits, o);
+    bits = other > bits ? other : bits;
+  }
+  if ((threadIdx.x & 31) == 0) atomicMax(slot, bits);
+}
+
+// G1: the block owns one syndrome, so the syndrome bits, the arena slice, the
+// operand bases and the normalisers are step invariants computed once.
+template <typename T, bool NORM, bool APAR, bool BPAR, bool MAXP, bool G1>
+__device__ int run_step(const KArgs& a, const StepDesc& dref, int st, int item_base, const uint32_t* s_syn,
                          uint32_t* s_max, T* arena, const T* consts) {
+  // a register copy: arena stores (same shared array) cannot alias it
+  const StepDesc d = dref;
   const int lw = d.lh + d.lfa + d.lfb;
   const int total = 1 << (lw + a.lg);
   const int total_r = (total + 31) & ~31;
@@ -97,30 +113,48 @@ __device__ int run_step(const KArgs& a, const StepDesc& d, int st, int item_base
   // item i runs on thread (i + item_base) mod blockDim: steps of one barrier
   // group start on different threads (item_base is a multiple of 32)
   const int i0 = (int(threadIdx.x) + int(blockDim.x) - item_base % int(blockDim.x)) % int(blockDim.x);
-  for (int i = i0; i < total_r; i += blockDim.x) {
-    const bool valid = i < total;
-    const int g = valid ? (i >> lw) : 0;
+  // step invariants of a one-syndrome block
+  Operand<T> A1{}, B1{};
+  int as1 = 0, bs1 = 0;
+  T fa1 = T(1), fb1 = T(1);
+  if (G1) {
+    if (APAR) as1 = syn_bit(s_syn, d.a_ref);
+    else A1 = make_operand<T>(d.a_kind, d.a_ref, d.a_sel, abits, arena, consts, s_syn);
+    if (BPAR) bs1 = syn_bit(s_syn, d.b_ref);
+    else B1 = make_operand<T>(d.b_kind, d.b_ref, d.b_sel, bbits, arena, consts, s_syn);
+    if (NORM) {
+      int ee;
+      if (!APAR && d.a_kind == OP_ARENA) fa1 = T(norm_factor(s_max[d.a_prod], &ee));
+      if (!BPAR && d.b_kind == OP_ARENA) fb1 = T(norm_factor(s_max[d.b_prod], &ee));
+    }
+  }
+  uint32_t run_bits = 0u;
+  for (int i = i0; i < (G1 ? total : total_r); i += blockDim.x) {
+    const bool valid = G1 || i < total;
+    const int g = G1 ? 0 : (valid ? (i >> lw) : 0);
     const int e = i & mw;
     T acc = T(0);
     if (valid) {
-      const uint32_t* syn = s_syn + g * a.syn_words;
-      T* arena_g = arena + int64_t(g) * a.arena_elems;
+      T* arena_g = G1 ? arena : arena + int64_t(g) * a.arena_elems;
       const int fb = e & mfb;
       const int fa = (e >> d.lfb) & mfa;
       const int h = e >> (d.lfb + d.lfa);
       const int abase = ((h << d.lfa) | fa) << d.lk;
       const int bbase = (h << (d.lk + d.lfb)) | fb;
-      Operand<T> A{}, B{};
-      int as = 0, bs = 0;
-      if (APAR) as = syn_bit(syn, d.a_ref);
-      else A = make_operand<T>(d.a_kind, d.a_ref, d.a_sel, abits, arena_g, consts, syn);
-      if (BPAR) bs = syn_bit(syn, d.b_ref);
-      else B = make_operand<T>(d.b_kind, d.b_ref, d.b_sel, bbits, arena_g, consts, syn);
-      T fa_s = T(1), fb_s = T(1);
-      if (NORM) {
-        int ee;
-        if (!APAR && d.a_kind == OP_ARENA) fa_s = T(norm_factor(s_max[g * a.n_steps + d.a_prod], &ee));
-        if (!BPAR && d.b_kind == OP_ARENA) fb_s = T(norm_factor(s_max[g * a.n_steps + d.b_prod], &ee));
+      Operand<T> A = A1, B = B1;
+      int as = as1, bs = bs1;
+      T fa_s = fa1, fb_s = fb1;
+      if (!G1) {
+        const uint32_t* syn = s_syn + g * a.syn_words;
+        if (APAR) as = syn_bit(syn, d.a_ref);
+        else A = make_operand<T>(d.a_kind, d.a_ref, d.a_sel, abits, arena_g, consts, syn);
+        if (BPAR) bs = syn_bit(syn, d.b_ref);
+        else B = make_operand<T>(d.b_kind, d.b_ref, d.b_sel, bbits, arena_g, consts, syn);
+        if (NORM) {
+          int ee;
+          if (!APAR && d.a_kind == OP_ARENA) fa_s = T(norm_factor(s_max[g * a.n_steps + d.a_prod], &ee));
+          if (!BPAR && d.b_kind == OP_ARENA) fb_s = T(norm_factor(s_max[g * a.n_steps + d.b_prod], &ee));
+        }
       }
       if (APAR && BPAR) {
         for (int k = 0; k < K; ++k) {
@@ -156,7 +190,10 @@ __device__ int run_step(const KArgs& a, const StepDesc& d, int st, int item_base
       const int addr = d.perm_off < 0 ? e : perm_addr(a.perm + d.perm_off, e, lw);
       arena_g[d.out_off + addr] = acc;
     }
-    if (NORM) {
+    if (NORM && G1) {
+      const uint32_t bits = __float_as_uint(float(acc));
+      run_bits = bits > run_bits ? bits : run_bits;
+    } else if (NORM) {
       uint32_t bits = __float_as_uint(float(acc));
       const int seg = lw >= 5 ? 32 : (1 << lw);
       for (int o = 1; o < seg; o <<= 1) {
@@ -166,6 +203,7 @@ __device__ int run_step(const KArgs& a, const StepDesc& d, int st, int item_base
       if (valid && (threadIdx.x & (seg - 1)) == 0) atomicMax(&s_max[g * a.n_steps + st], bits);
     }
   }
+  if (NORM && G1) flush_max(i0 < total, run_bits, &s_max[st]);
   return total_r;
 }
 
@@ -195,78 +233,100 @@ __device__ __forceinline__ void store4<double>(double* p, const double v[4]) {
   reinterpret_cast<double2*>(p)[1] = make_double2(v[2], v[3]);
 }
 
-template <typename T>
-__device__ __forceinline__ T pick4(const T v[4], int j) {
-  return j == 0 ? v[0] : (j == 1 ? v[1] : (j == 2 ? v[2] : v[3]));
-}
-
-// A step whose B-only group has at least 4 entries: each work item is four
-// consecutive outputs along fb, which share every A value and read B as one
-// 16-byte vector.  Operand bases, fb offsets and k strides are multiples of 4
-// elements (arena and constant offsets are planned that way), so the vector
-// accesses are aligned.  Permuted outputs are written in a lane-rotated order
-// so that the four stores of a warp instruction hit different index bits.
-template <typename T, bool NORM, bool APAR, bool BPAR, bool MAXP>
-__device__ int run_step_v4(const KArgs& a, const StepDesc& d, int st, int item_base, const uint32_t* s_syn,
+// A step whose B-only group has at least log2(VW) bits: each work item is VW
+// (4 or 8) consecutive outputs along fb, which share every A value and read
+// B as 16-byte vectors.  Operand bases, fb offsets and k strides are
+// multiples of 8 elements (arena and constant offsets are planned that way),
+// so the vector accesses are aligned.  Permuted outputs are written in a
+// lane-rotated order so that the stores of one warp instruction hit
+// different index bits.
+template <typename T, int VW, bool NORM, bool APAR, bool BPAR, bool MAXP, bool G1>
+__device__ int run_step_vec(const KArgs& a, const StepDesc& dref, int st, int item_base, const uint32_t* s_syn,
                             uint32_t* s_max, T* arena, const T* consts) {
+  constexpr int LV = VW == 8 ? 3 : 2;
+  const StepDesc d = dref;
   const int lw = d.lh + d.lfa + d.lfb;
-  const int lwv = lw - 2;
+  const int lwv = lw - LV;
   const int total = 1 << (lwv + a.lg);
   const int total_r = (total + 31) & ~31;
   const int mfb = (1 << d.lfb) - 1;
   const int mfa = (1 << d.lfa) - 1;
   const int mwv = (1 << lwv) - 1;
   const int K = 1 << d.lk;
+  const int bstride = 1 << d.lfb;
   const int abits = d.lh + d.lfa + d.lk;
   const int bbits = d.lh + d.lk + d.lfb;
   const int32_t* perm = d.perm_off < 0 ? nullptr : a.perm + d.perm_off;
   const int cb0 = lw < 8 ? lw : 8;
-  const int rot = threadIdx.x & 3;
+  const int rot = threadIdx.x & (VW - 1);
   const int i0 = (int(threadIdx.x) + int(blockDim.x) - item_base % int(blockDim.x)) % int(blockDim.x);
-  for (int i = i0; i < total_r; i += blockDim.x) {
-    const bool valid = i < total;
-    const int g = valid ? (i >> lwv) : 0;
-    const int e0 = (i & mwv) << 2;
-    T acc[4] = {T(0), T(0), T(0), T(0)};
+  Operand<T> A1{}, B1{};
+  int as1 = 0, bs1 = 0;
+  T fa1 = T(1), fb1 = T(1);
+  if (G1) {
+    if (APAR) as1 = syn_bit(s_syn, d.a_ref);
+    else A1 = make_operand<T>(d.a_kind, d.a_ref, d.a_sel, abits, arena, consts, s_syn);
+    if (BPAR) bs1 = syn_bit(s_syn, d.b_ref);
+    else B1 = make_operand<T>(d.b_kind, d.b_ref, d.b_sel, bbits, arena, consts, s_syn);
+    if (NORM) {
+      int ee;
+      if (!APAR && d.a_kind == OP_ARENA) fa1 = T(norm_factor(s_max[d.a_prod], &ee));
+      if (!BPAR && d.b_kind == OP_ARENA) fb1 = T(norm_factor(s_max[d.b_prod], &ee));
+    }
+  }
+  uint32_t run_bits = 0u;
+  for (int i = i0; i < (G1 ? total : total_r); i += blockDim.x) {
+    const bool valid = G1 || i < total;
+    const int g = G1 ? 0 : (valid ? (i >> lwv) : 0);
+    const int e0 = (i & mwv) << LV;
+    T acc[VW];
+#pragma unroll
+    for (int j = 0; j < VW; ++j) acc[j] = T(0);
     if (valid) {
-      const uint32_t* syn = s_syn + g * a.syn_words;
-      T* arena_g = arena + int64_t(g) * a.arena_elems;
+      T* arena_g = G1 ? arena : arena + int64_t(g) * a.arena_elems;
       const int fb0 = e0 & mfb;
       const int fa = (e0 >> d.lfb) & mfa;
       const int h = e0 >> (d.lfb + d.lfa);
       const int abase = ((h << d.lfa) | fa) << d.lk;
       const int bbase = (h << (d.lk + d.lfb)) | fb0;
-      Operand<T> A{}, B{};
-      int as = 0, bs = 0;
-      if (APAR) as = syn_bit(syn, d.a_ref);
-      else A = make_operand<T>(d.a_kind, d.a_ref, d.a_sel, abits, arena_g, consts, syn);
-      if (BPAR) bs = syn_bit(syn, d.b_ref);
-      else B = make_operand<T>(d.b_kind, d.b_ref, d.b_sel, bbits, arena_g, consts, syn);
-      T fa_s = T(1), fb_s = T(1);
-      if (NORM) {
-        int ee;
-        if (!APAR && d.a_kind == OP_ARENA) fa_s = T(norm_factor(s_max[g * a.n_steps + d.a_prod], &ee));
-        if (!BPAR && d.b_kind == OP_ARENA) fb_s = T(norm_factor(s_max[g * a.n_steps + d.b_prod], &ee));
+      Operand<T> A = A1, B = B1;
+      int as = as1, bs = bs1;
+      T fa_s = fa1, fb_s = fb1;
+      if (!G1) {
+        const uint32_t* syn = s_syn + g * a.syn_words;
+        if (APAR) as = syn_bit(syn, d.a_ref);
+        else A = make_operand<T>(d.a_kind, d.a_ref, d.a_sel, abits, arena_g, consts, syn);
+        if (BPAR) bs = syn_bit(syn, d.b_ref);
+        else B = make_operand<T>(d.b_kind, d.b_ref, d.b_sel, bbits, arena_g, consts, syn);
+        if (NORM) {
+          int ee;
+          if (!APAR && d.a_kind == OP_ARENA) fa_s = T(norm_factor(s_max[g * a.n_steps + d.a_prod], &ee));
+          if (!BPAR && d.b_kind == OP_ARENA) fb_s = T(norm_factor(s_max[g * a.n_steps + d.b_prod], &ee));
+        }
       }
-      for (int k = 0; k < K; ++k) {
+      const T* pa = APAR ? nullptr : A.p + abase;
+      const T* pb = BPAR ? nullptr : B.p + bbase;
+      auto body = [&](int k) {
         T av;
         if (APAR) {
-          if (parity_val<T>(abase + k, as) == T(0)) continue;
+          if (parity_val<T>(abase + k, as) == T(0)) return;
           av = T(1);
         } else {
-          av = A.ld(abase + k);
+          av = pa[k];
           if (NORM) av *= fa_s;
         }
-        T bv[4];
-        const int bi = bbase + (k << d.lfb);
+        T bv[VW];
         if (BPAR) {
+          const int bi = bbase + k * bstride;
 #pragma unroll
-          for (int j = 0; j < 4; ++j) bv[j] = parity_val<T>(bi + j, bs);
+          for (int j = 0; j < VW; ++j) bv[j] = parity_val<T>(bi + j, bs);
         } else {
-          load4<T>(B.vec(bi), bv);
+          const T* q = pb + k * bstride;
+          load4<T>(q, bv);
+          if (VW == 8) load4<T>(q + 4, bv + 4);
         }
 #pragma unroll
-        for (int j = 0; j < 4; ++j) {
+        for (int j = 0; j < VW; ++j) {
           if (MAXP) {
             const T v = av * bv[j];
             acc[j] = v > acc[j] ? v : acc[j];
@@ -274,15 +334,32 @@ __device__ int run_step_v4(const KArgs& a, const StepDesc& d, int st, int item_b
             acc[j] = fma(av, bv[j], acc[j]);
           }
         }
+      };
+      if (K == 1) {
+        body(0);
+      } else {
+        for (int k = 0; k < K; k += 2) {
+          body(k);
+          body(k + 1);
+        }
       }
       if (NORM && !BPAR) {
 #pragma unroll
-        for (int j = 0; j < 4; ++j) acc[j] *= fb_s;
+        for (int j = 0; j < VW; ++j) acc[j] *= fb_s;
       }
       if (!perm) {
         store4<T>(arena_g + d.out_off + e0, acc);
+        if (VW == 8) store4<T>(arena_g + d.out_off + e0 + 4, acc + 4);
       } else {
-        const int4 lo = *reinterpret_cast<const int4*>(perm + (e0 & ((1 << cb0) - 1)));
+        int los[VW];
+        {
+          const int4 l0 = *reinterpret_cast<const int4*>(perm + (e0 & ((1 << cb0) - 1)));
+          los[0] = l0.x; los[1] = l0.y; los[2] = l0.z; los[3] = l0.w;
+          if (VW == 8) {
+            const int4 l1 = *reinterpret_cast<const int4*>(perm + (e0 & ((1 << cb0) - 1)) + 4);
+            los[4] = l1.x; los[5] = l1.y; los[6] = l1.z; los[7] = l1.w;
+          }
+        }
         int hi = 0;
         int tab = 1 << cb0;
         for (int sh = 8; sh < lw; sh += 8) {
@@ -290,25 +367,50 @@ __device__ int run_step_v4(const KArgs& a, const StepDesc& d, int st, int item_b
           hi |= __ldg(perm + tab + ((e0 >> sh) & ((1 << cb) - 1)));
           tab += 1 << cb;
         }
-        const int los[4] = {lo.x, lo.y, lo.z, lo.w};
+        T* out = arena_g + d.out_off;
+        if (d.flags & (VW == 8 ? kStepRotate8 : kStepRotate4)) {
+          // barrel rotation: lane r stores its outputs starting at r mod VW,
+          // so the lanes of one store instruction differ in the low bits too
 #pragma unroll
-        for (int s4 = 0; s4 < 4; ++s4) {
-          const int j = (s4 + rot) & 3;
-          arena_g[d.out_off + (pick4(los, j) | hi)] = pick4(acc, j);
+          for (int b = 1; b < VW; b <<= 1) {
+            if (rot & b) {
+              int tl[VW];
+              T tv[VW];
+#pragma unroll
+              for (int j = 0; j < VW; ++j) {
+                tl[j] = los[(j + b) & (VW - 1)];
+                tv[j] = acc[(j + b) & (VW - 1)];
+              }
+#pragma unroll
+              for (int j = 0; j < VW; ++j) {
+                los[j] = tl[j];
+                acc[j] = tv[j];
+              }
+            }
+          }
         }
+#pragma unroll
+        for (int j = 0; j < VW; ++j) out[los[j] | hi] = acc[j];
       }
     }
     if (NORM) {
-      float m = fmaxf(fmaxf(float(acc[0]), float(acc[1])), fmaxf(float(acc[2]), float(acc[3])));
+      float m = float(acc[0]);
+#pragma unroll
+      for (int j = 1; j < VW; ++j) m = fmaxf(m, float(acc[j]));
       uint32_t bits = __float_as_uint(m);
-      const int seg = lwv >= 5 ? 32 : (1 << lwv);
-      for (int o = 1; o < seg; o <<= 1) {
-        uint32_t other = __shfl_xor_sync(0xffffffffu, bits, o);
-        bits = other > bits ? other : bits;
+      if (G1) {
+        run_bits = bits > run_bits ? bits : run_bits;
+      } else {
+        const int seg = lwv >= 5 ? 32 : (1 << lwv);
+        for (int o = 1; o < seg; o <<= 1) {
+          uint32_t other = __shfl_xor_sync(0xffffffffu, bits, o);
+          bits = other > bits ? other : bits;
+        }
+        if (valid && (threadIdx.x & (seg - 1)) == 0) atomicMax(&s_max[g * a.n_steps + st], bits);
       }
-      if (valid && (threadIdx.x & (seg - 1)) == 0) atomicMax(&s_max[g * a.n_steps + st], bits);
     }
   }
+  if (NORM && G1) flush_max(i0 < total, run_bits, &s_max[st]);
   return total_r;
 }
 
@@ -402,6 +504,30 @@ __device__ void backtrack(const KArgs& a, const StepDesc* s_steps, const uint32_
   }
 }
 
+template <typename T, bool NORM, bool MAXP, bool G1>
+__device__ __forceinline__ int dispatch_step(const KArgs& a, const StepDesc& d, bool ap, bool bp, int st,
+                                             int item_base, const uint32_t* s_syn, uint32_t* s_max, T* arena,
+                                             const T* consts) {
+  // eight outputs per item where that still gives every thread an item
+  const int lw = d.lh + d.lfa + d.lfb;
+  if (sizeof(T) == 4 && d.lfb >= 3 && (int64_t(1) << (lw - 3 + a.lg)) >= int64_t(blockDim.x)) {
+    if (ap && bp) return run_step_vec<T, 8, NORM, true, true, MAXP, G1>(a, d, st, item_base, s_syn, s_max, arena, consts);
+    if (ap) return run_step_vec<T, 8, NORM, true, false, MAXP, G1>(a, d, st, item_base, s_syn, s_max, arena, consts);
+    if (bp) return run_step_vec<T, 8, NORM, false, true, MAXP, G1>(a, d, st, item_base, s_syn, s_max, arena, consts);
+    return run_step_vec<T, 8, NORM, false, false, MAXP, G1>(a, d, st, item_base, s_syn, s_max, arena, consts);
+  }
+  if (d.lfb >= 2) {
+    if (ap && bp) return run_step_vec<T, 4, NORM, true, true, MAXP, G1>(a, d, st, item_base, s_syn, s_max, arena, consts);
+    if (ap) return run_step_vec<T, 4, NORM, true, false, MAXP, G1>(a, d, st, item_base, s_syn, s_max, arena, consts);
+    if (bp) return run_step_vec<T, 4, NORM, false, true, MAXP, G1>(a, d, st, item_base, s_syn, s_max, arena, consts);
+    return run_step_vec<T, 4, NORM, false, false, MAXP, G1>(a, d, st, item_base, s_syn, s_max, arena, consts);
+  }
+  if (ap && bp) return run_step<T, NORM, true, true, MAXP, G1>(a, d, st, item_base, s_syn, s_max, arena, consts);
+  if (ap) return run_step<T, NORM, true, false, MAXP, G1>(a, d, st, item_base, s_syn, s_max, arena, consts);
+  if (bp) return run_step<T, NORM, false, true, MAXP, G1>(a, d, st, item_base, s_syn, s_max, arena, consts);
+  return run_step<T, NORM, false, false, MAXP, G1>(a, d, st, item_base, s_syn, s_max, arena, consts);
+}
+
 template <typename T, bool NORM, bool MAXP>
 __global__ void __launch_bounds__(1024) tn_contract_kernel(KArgs a) {
   extern __shared__ __align__(16) unsigned char smem[];
@@ -447,18 +573,11 @@ __global__ void __launch_bounds__(1024) tn_contract_kernel(KArgs a) {
       const StepDesc& d = s_steps[st];
       const bool ap = d.a_kind == OP_PARITY, bp = d.b_kind == OP_PARITY;
       int items;
-      if (d.lfb >= 2) {
-        if (ap && bp) items = run_step_v4<T, NORM, true, true, MAXP>(a, d, st, item_base, s_syn, s_max, arena, consts);
-        else if (ap) items = run_step_v4<T, NORM, true, false, MAXP>(a, d, st, item_base, s_syn, s_max, arena, consts);
-        else if (bp) items = run_step_v4<T, NORM, false, true, MAXP>(a, d, st, item_base, s_syn, s_max, arena, consts);
-        else items = run_step_v4<T, NORM, false, false, MAXP>(a, d, st, item_base, s_syn, s_max, arena, consts);
-      } else {
-        if (ap && bp) items = run_step<T, NORM, true, true, MAXP>(a, d, st, item_base, s_syn, s_max, arena, consts);
-        else if (ap) items = run_step<T, NORM, true, false, MAXP>(a, d, st, item_base, s_syn, s_max, arena, consts);
-        else if (bp) items = run_step<T, NORM, false, true, MAXP>(a, d, st, item_base, s_syn, s_max, arena, consts);
-        else items = run_step<T, NORM, false, false, MAXP>(a, d, st, item_base, s_syn, s_max, arena, consts);
-      }
-      if (d.sync_after) {
+      if (a.G == 1)
+        items = dispatch_step<T, NORM, MAXP, true>(a, d, ap, bp, st, item_base, s_syn, s_max, arena, consts);
+      else
+        items = dispatch_step<T, NORM, MAXP, false>(a, d, ap, bp, st, item_base, s_syn, s_max, arena, consts);
+      if (d.flags & kStepSync) {
         __syncthreads();
         item_base = 0;
       } else {

@@ -11,6 +11,7 @@
 #include <cmath>
 #include <cstdint>
 #include <cstring>
+#include <functional>
 #include <queue>
 #include <random>
 #include <string>
@@ -250,11 +251,12 @@ void anneal(const Problem& P, Tree* t, std::mt19937_64& rng, int sweeps, int tar
 }
 
 // Emits steps in post-order (children before parents); node ids follow the
-// tqec_tree convention.
-void emit(const Tree& t, int T, int32_t* steps) {
+// tqec_tree convention.  `leaf_id` maps the search's leaves to node ids of
+// the caller's network and `next` is the first free step index (steps before
+// it were emitted by the caller).
+void emit(const Tree& t, int T, const std::vector<int>& leaf_id, int next, int n_net, int32_t* steps) {
   std::vector<int> id(t.l.size(), -1);
-  for (int i = 0; i < T; ++i) id[i] = i;
-  int next = 0;
+  for (int i = 0; i < T; ++i) id[i] = leaf_id[i];
   std::vector<std::pair<int, int>> stack = {{t.root, 0}};
   while (!stack.empty()) {
     auto [n, state] = stack.back();
@@ -267,7 +269,7 @@ void emit(const Tree& t, int T, int32_t* steps) {
     } else {
       steps[2 * next] = id[t.l[n]];
       steps[2 * next + 1] = id[t.r[n]];
-      id[n] = T + next;
+      id[n] = n_net + next;
       ++next;
     }
   }
@@ -286,11 +288,10 @@ extern "C" int tqec_optimize_order(const tqec_network* net, const tqec_order_opt
   o.width_penalty = 1.0;
   o.seed = 1;
   if (opts) o = *opts;
-  Problem P;
-  P.T = net->n_tensors;
+  const int NT = net->n_tensors;
   std::unordered_map<int32_t, int> var_of;
-  P.leaf.resize(P.T);
-  for (int i = 0; i < P.T; ++i)
+  std::vector<std::vector<int>> net_leaf(NT);
+  for (int i = 0; i < NT; ++i)
     for (int32_t q = net->ix_offsets[i]; q < net->ix_offsets[i + 1]; ++q) {
       auto it = var_of.find(net->ix_labels[q]);
       int v;
@@ -300,16 +301,76 @@ extern "C" int tqec_optimize_order(const tqec_network* net, const tqec_order_opt
       } else {
         v = it->second;
       }
-      P.leaf[i].push_back(v);
+      net_leaf[i].push_back(v);
     }
-  P.V = (int)var_of.size();
-  P.total.assign(P.V, 0);
-  P.is_out.assign(P.V, 0);
-  for (int i = 0; i < P.T; ++i)
-    for (int v : P.leaf[i]) P.total[v]++;
+  const int V = (int)var_of.size();
+  std::vector<int> total(V, 0);
+  std::vector<char> is_out(V, 0);
+  for (int i = 0; i < NT; ++i)
+    for (int v : net_leaf[i]) total[v]++;
   for (int i = 0; i < net->n_out; ++i) {
     auto it = var_of.find(net->out_labels[i]);
-    if (it != var_of.end()) P.is_out[it->second] = 1;
+    if (it != var_of.end()) is_out[it->second] = 1;
+  }
+  // A one-hot syndrome leaf whose label one other tensor carries is merged
+  // with that tensor before the search: the planner folds the pair into a
+  // parity or selected-table operand, so the syndrome label never becomes a
+  // runtime dimension and must not count in the search's cost or width.
+  std::vector<int> group(NT);
+  for (int i = 0; i < NT; ++i) group[i] = i;
+  std::function<int(int)> find = [&](int x) { return group[x] == x ? x : group[x] = find(group[x]); };
+  std::vector<std::pair<int, int>> pre;  // (syndrome leaf, partner)
+  if (net->syndrome_tensors)
+    for (int j = 0; j < net->n_syndrome; ++j) {
+      const int sl = net->syndrome_tensors[j];
+      if (sl < 0 || sl >= NT || net_leaf[sl].size() != 1) continue;
+      const int v = net_leaf[sl][0];
+      if (total[v] != 2 || is_out[v]) continue;
+      int partner = -1;
+      for (int i = 0; i < NT; ++i)
+        if (i != sl && std::find(net_leaf[i].begin(), net_leaf[i].end(), v) != net_leaf[i].end()) partner = i;
+      if (partner < 0 || find(partner) == find(sl)) continue;
+      pre.push_back({sl, partner});
+      group[find(sl)] = find(partner);
+    }
+  // the search's leaves: one per group, carrying the labels that leave it
+  Problem P;
+  std::vector<int> rep_leaf(NT, -1);
+  std::vector<std::vector<int>> members;
+  for (int i = 0; i < NT; ++i) {
+    const int g = find(i);
+    if (rep_leaf[g] < 0) {
+      rep_leaf[g] = (int)members.size();
+      members.push_back({});
+    }
+    members[rep_leaf[g]].push_back(i);
+  }
+  P.T = (int)members.size();
+  P.V = V;
+  P.total = total;
+  P.is_out = is_out;
+  P.leaf.resize(P.T);
+  for (int k = 0; k < P.T; ++k) {
+    std::unordered_map<int, int> c;
+    for (int i : members[k])
+      for (int v : net_leaf[i]) c[v]++;
+    for (auto& [v, n] : c)
+      if (n < total[v] || is_out[v]) P.leaf[k].push_back(v);
+    for (auto& [v, n] : c)
+      if (n == total[v] && !is_out[v]) P.total[v] = 0;  // contracted inside the group
+  }
+  // pre-merge steps: the members of each group, left to right
+  std::vector<int> leaf_id(P.T);
+  int next_step = 0;
+  for (int k = 0; k < P.T; ++k) {
+    int acc = members[k][0];
+    for (size_t m = 1; m < members[k].size(); ++m) {
+      steps_out[2 * next_step] = acc;
+      steps_out[2 * next_step + 1] = members[k][m];
+      acc = NT + next_step;
+      ++next_step;
+    }
+    leaf_id[k] = acc;
   }
   if (P.T == 1) {
     if (log2_macs_out) *log2_macs_out = 0;
@@ -334,7 +395,7 @@ extern "C" int tqec_optimize_order(const tqec_network* net, const tqec_order_opt
     double E = energy(tree_macs(t, P.T), tree_width(t, P.T), target, o.width_penalty);
     if (E < bestE) { bestE = E; best = t; }
   }
-  emit(best, P.T, steps_out);
+  emit(best, P.T, leaf_id, next_step, NT, steps_out);
   if (log2_macs_out) *log2_macs_out = std::log2(tree_macs(best, P.T));
   if (width_out) *width_out = tree_width(best, P.T);
   return TQEC_OK;

@@ -163,6 +163,41 @@ std::vector<double> permute_table(const PNode& n, const std::vector<int>& layout
 
 }  // namespace
 
+// Shared-memory store wavefronts of one warp's permuted output stores
+// (items of `vw` consecutive outputs, lane l owning item l), with or without
+// the kernel's lane rotation; rotation pays when it saves more wavefronts
+// than its register selects cost.
+static int store_wavefronts(const std::vector<int32_t>& perm, int32_t off, int lw, int vw, bool rotate) {
+  const int lv = vw == 8 ? 3 : 2;
+  if (lw < lv) return 0;
+  auto addr = [&](int e) {
+    int a = 0, tab = off;
+    for (int sh = 0; sh < lw; sh += 8) {
+      const int cb = std::min(8, lw - sh);
+      a |= perm[tab + ((e >> sh) & ((1 << cb) - 1))];
+      tab += 1 << cb;
+    }
+    return a;
+  };
+  const int lanes = std::min(32, 1 << (lw - lv));
+  int total = 0;
+  for (int s = 0; s < vw; ++s) {
+    int count[32] = {0};
+    for (int l = 0; l < lanes; ++l) {
+      const int j = rotate ? (s + l) & (vw - 1) : s;
+      count[addr((l << lv) + j) & 31]++;
+    }
+    total += *std::max_element(count, count + 32);
+  }
+  return total;
+}
+
+static bool rotation_pays(const std::vector<int32_t>& perm, int32_t off, int lw, int vw) {
+  const int plain = store_wavefronts(perm, off, lw, vw, false);
+  const int rot = store_wavefronts(perm, off, lw, vw, true);
+  return plain - rot > (vw == 8 ? 24 : 8);
+}
+
 std::string build_plan(const NetworkView& net, int32_t n_steps, const int32_t* steps,
                        const PlanLimits& lim, Plan* out, bool* unsupported) {
   *unsupported = false;
@@ -634,7 +669,7 @@ std::string build_plan(const NetworkView& net, int32_t n_steps, const int32_t* s
     d.lfb = (int)L.Fb.size();
     d.lk = (int)L.K.size();
     d.out_off = (int32_t)off;
-    d.sync_after = group_end[r];
+    d.flags = group_end[r] ? kStepSync : 0;
     d.var_off = map_mode ? d_var_off : 0;
     for (int side = 0; side < 2; ++side) {
       int op = side ? L.b : L.a;
@@ -684,6 +719,8 @@ std::string build_plan(const NetworkView& net, int32_t n_steps, const int32_t* s
           P.perm.push_back(a);
         }
       }
+      for (int vw : {4, 8})
+        if (rotation_pays(P.perm, d.perm_off, nb, vw)) d.flags |= vw == 4 ? kStepRotate4 : kStepRotate8;
     }
     P.steps[r] = d;
   }

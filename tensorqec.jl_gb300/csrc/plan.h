@@ -29,6 +29,11 @@ enum OperandKind : int32_t {
 
 constexpr int kMaxSel = 4;
 
+// StepDesc::flags
+constexpr int32_t kStepSync = 1;     // block barrier after this step (end of a barrier group)
+constexpr int32_t kStepRotate4 = 2;  // permuted stores of 4-output items are lane-rotated
+constexpr int32_t kStepRotate8 = 4;  // the same for 8-output items
+
 struct StepDesc {
   int32_t a_kind, b_kind;
   int32_t a_ref, b_ref;      // arena offset | const offset | syndrome bit
@@ -38,7 +43,7 @@ struct StepDesc {
   int32_t lh, lfa, lfb, lk;  // log2 sizes of the index groups
   int32_t out_off;           // arena offset of the output
   int32_t perm_off;          // output permutation tables, -1 = identity
-  int32_t sync_after;        // 1: block barrier after this step (end of a barrier group)
+  int32_t flags;             // kStepSync | kStepRotate4 | kStepRotate8
   int32_t var_off;           // MAP mode: offset of the step's labels in Plan::vartab
 };
 static_assert(sizeof(StepDesc) == 64, "StepDesc is 64 bytes");

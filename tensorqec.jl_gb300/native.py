@@ -72,7 +72,7 @@ class OrderOptions(C.Structure):
 STEP_DTYPE = np.dtype([("a_kind", "<i4"), ("b_kind", "<i4"), ("a_ref", "<i4"), ("b_ref", "<i4"),
                        ("a_prod", "<i4"), ("b_prod", "<i4"), ("a_sel", "i1", (4,)), ("b_sel", "i1", (4,)),
                        ("lh", "<i4"), ("lfa", "<i4"), ("lfb", "<i4"), ("lk", "<i4"),
-                       ("out_off", "<i4"), ("perm_off", "<i4"), ("sync_after", "<i4"), ("var_off", "<i4")])
+                       ("out_off", "<i4"), ("perm_off", "<i4"), ("flags", "<i4"), ("var_off", "<i4")])
 assert STEP_DTYPE.itemsize == 64
 
 _lib = None
@@ -348,10 +348,13 @@ class Sampler:
                                      C.byref(nf)))
         return ne.value, nf.value
 
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().tqec_sampler_destroy(self._h)
+            self._h = None
+
     def __del__(self):
         try:
-            if getattr(self, "_h", None):
-                lib().tqec_sampler_destroy(self._h)
-                self._h = None
+            self.close()
         except Exception:
             pass

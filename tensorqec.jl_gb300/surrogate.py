@@ -143,20 +143,30 @@ def sample_bits(ct, n, rng):
     return np.concatenate([s.sx, s.sz], axis=1)
 
 
-def train_surrogate(ct, n_train=1 << 22, batch=8192, epochs=2, lr=2e-3, hidden=512, n_layers=4, seed=1,
-                    rng=None, log=None):
+def train_surrogate(ct, n_train=1 << 24, batch=16384, epochs=4, lr=3e-3, hidden=512, n_layers=4, seed=1,
+                    rng=None, log=None, gpu_sampler=True):
     """Trains a surrogate for a compiled CSS decoder on n_train sampled
     syndromes labelled by the exact contraction (float32 with its rounding
-    bound).  Returns (surrogate, stats)."""
+    bound).  Syndromes come from the GPU sampler (Philox, seeded by `seed`)
+    or, with gpu_sampler=False, from the host sampler.  Returns (surrogate,
+    stats)."""
     rng = np.random.default_rng(seed) if rng is None else rng
     t0 = time.time()
-    bits = sample_bits(ct, n_train, rng)
-    packed = pack_syndromes(bits)
-    logp = np.empty((n_train, ct.n_classes), dtype=np.float64)
-    chunk = 1 << 18
-    for i in range(0, n_train, chunk):
-        logp[i:i + chunk] = ct.program.contract_packed(packed[i:i + chunk], native.TQEC_F32)
-    targets = soft_labels(logp)
+    chunk = 1 << 20
+    packed = np.empty((n_train, (ct.n_syndrome + 7) // 8), dtype=np.uint8)
+    targets = np.empty((n_train, ct.n_classes), dtype=np.float32)
+    sampler = native.Sampler(ct.tanner, ct.lx, ct.lz, ct.em, ct.decoder.device) if gpu_sampler else None
+    try:
+        for i in range(0, n_train, chunk):
+            m = min(chunk, n_train - i)
+            if sampler is not None:
+                packed[i:i + m], _ = sampler.sample(seed, m, offset=i)
+            else:
+                packed[i:i + m] = pack_syndromes(sample_bits(ct, m, rng))
+            targets[i:i + m] = soft_labels(ct.program.contract_packed(packed[i:i + m], native.TQEC_F32))
+    finally:
+        if sampler is not None:
+            sampler.close()
     t_label = time.time() - t0
     sur = Surrogate(ct.n_syndrome, ct.n_classes, hidden, n_layers, seed, ct.decoder.device)
     steps = epochs * (n_train // batch)
