@@ -44,6 +44,8 @@ def parse():
     ap.add_argument("--profile", action="store_true",
                     help="one float32 contraction launch of --batch syndromes (for ncu), no timing")
     ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--group", type=int, default=0, help="--profile: syndromes per block (0: default shape)")
+    ap.add_argument("--threads", type=int, default=0, help="--profile: threads per block (0: default shape)")
     ap.add_argument("--no-surrogate", action="store_true", help="time the batched exact decoder alone")
     ap.add_argument("--train-n", type=int, default=1 << 24, help="surrogate training syndromes")
     ap.add_argument("--calib-n", type=int, default=1 << 20, help="surrogate calibration syndromes")
@@ -426,7 +428,7 @@ def run_profile(args):
 
     pkg = G.load_package()
     t, em, bits = workload(pkg, 0, 1, args.batch)
-    ct = pkg.compile(pkg.TNMMAP(precision="f32"), t, em)
+    ct = pkg.compile(pkg.TNMMAP(precision="f32", group=args.group, threads=args.threads), t, em)
     d_syn = torch.from_numpy(pkg.pack_syndromes(bits[0])).cuda()
     d_lp = torch.empty((args.batch, ct.n_classes), dtype=torch.float64, device="cuda")
     sptr = torch.cuda.current_stream().cuda_stream

@@ -47,6 +47,7 @@ struct Shape {
   int G = 1;
   int threads = 256;
   bool smem_arena = true;
+  bool smem_tables = false;  // constants and permutation tables staged in shared memory
   size_t smem = 0;
   int grid_cap = 1;  // blocks resident on the whole device
 };
@@ -82,6 +83,8 @@ struct tqec_program {
   cudaStream_t stream = nullptr;
   tqec::StepDesc* d_steps = nullptr;
   int32_t* d_perm = nullptr;
+  uint16_t* d_perm16 = nullptr;  // the same tables as uint16 (programs of width <= 16)
+  int64_t n_perm_padded = 0;     // entries, a multiple of 8
   int32_t* d_vartab = nullptr;   // MAP mode tables
   int32_t* d_report = nullptr;
   int8_t* d_fixed = nullptr;
@@ -117,34 +120,53 @@ int syn_words(const tqec_program* p) { return std::max(1, (p->plan.n_syndrome + 
 
 int var_words(const tqec_program* p) { return p->plan.map_mode ? (p->plan.n_vars + 31) / 32 : 0; }
 
+size_t table_bytes(const tqec_program* p, int precision) {
+  return tqec::contract_table_bytes(precision == TQEC_F32 ? 1 : 0, (int64_t)p->plan.consts.size(), p->n_perm_padded,
+                                    p->d_perm16 != nullptr);
+}
+
 // Picks (G, threads) for one precision: the largest group whose arena fits
 // about half of the shared memory (two blocks per SM), else a global arena.
-int choose_shape(tqec_program* p, int precision, int G_req, int threads_req, Shape* out) {
+// tables_req: 1 stages the constant and permutation tables in shared memory
+// (unless that would push a one-syndrome arena out of it), 0 keeps them in
+// global memory, -1 stages them only next to a shared-memory arena (a
+// global-arena shape wants small blocks, many per SM).
+int choose_shape(tqec_program* p, int precision, int G_req, int threads_req, int tables_req, Shape* out) {
   const size_t limit = tqec::contract_smem_limit(p->device);
-  const size_t esz = precision == TQEC_F32 ? 4 : 8;
   const int64_t arena = p->plan.arena_elems;
   const int nsteps = (int)p->plan.steps.size();
   const int sw = syn_words(p);
   const int vw = var_words(p);
+  const size_t tb_all = table_bytes(p, precision);
+  auto bytes = [&](int G, bool arena_smem, size_t tb) {
+    return tqec::contract_smem_bytes(precision, nsteps, sw, G, arena, arena_smem, vw, tb);
+  };
   Shape s;
   s.threads = threads_req > 0 ? threads_req : 256;
+  size_t tb = tb_all;
   if (G_req > 0) {
     s.G = G_req;
-    s.smem_arena = tqec::contract_smem_bytes(precision, nsteps, sw, s.G, arena, true, vw) <= limit;
+    s.smem_arena = bytes(s.G, true, tb) <= limit;
+    if (!s.smem_arena && bytes(s.G, true, 0) <= limit) {
+      tb = 0;
+      s.smem_arena = true;
+    }
   } else {
     const size_t target = limit / 2 - 1024;
+    if (bytes(1, true, tb) > limit && bytes(1, true, 0) <= limit) tb = 0;
     int G = 1;
-    while (G < 256 && tqec::contract_smem_bytes(precision, nsteps, sw, G * 2, arena, true, vw) <= target &&
-           (int64_t(G) * 2 << p->plan.width) <= 16 * 4096)
-      G *= 2;
+    while (G < 256 && bytes(G * 2, true, tb) <= target && (int64_t(G) * 2 << p->plan.width) <= 16 * 4096) G *= 2;
     s.G = G;
-    s.smem_arena = tqec::contract_smem_bytes(precision, nsteps, sw, G, arena, true, vw) <= limit;
+    s.smem_arena = bytes(G, true, tb) <= limit;
     // one syndrome per block with a wide arena: use more threads per block
-    if (G == 1 && (!s.smem_arena || tqec::contract_smem_bytes(precision, nsteps, sw, 1, arena, true, vw) > target))
+    if (G == 1 && (!s.smem_arena || bytes(1, true, tb) > target))
       s.threads = threads_req > 0 ? threads_req : 1024;
-    (void)esz;
   }
-  s.smem = tqec::contract_smem_bytes(precision, nsteps, sw, s.G, arena, s.smem_arena, vw);
+  s.threads = std::min(s.threads, tqec::contract_max_threads(precision));
+  if (bytes(s.G, s.smem_arena, tb) > limit) tb = 0;
+  if (tables_req == 0 || (tables_req < 0 && !s.smem_arena)) tb = 0;
+  s.smem_tables = tb > 0;
+  s.smem = bytes(s.G, s.smem_arena, tb);
   if (s.smem > limit) return fail(TQEC_ERR_UNSUPPORTED, "program does not fit shared memory even with a global arena");
   int occ = tqec::contract_occupancy(precision, s.threads, s.smem, p->plan.map_mode);
   if (occ < 1) return fail(TQEC_ERR_UNSUPPORTED, "launch shape cannot be resident on this device");
@@ -172,6 +194,10 @@ tqec::KArgs base_args(tqec_program* p, int precision) {
   a.syn_bytes = p->plan.syndrome_bytes;
   a.syn_words = syn_words(p);
   const Shape& s = p->shape[precision];
+  a.tables_smem = s.smem_tables ? 1 : 0;
+  a.n_consts = (int32_t)p->plan.consts.size();
+  a.n_perm = (int32_t)p->n_perm_padded;
+  a.perm16 = s.smem_tables ? p->d_perm16 : nullptr;
   a.G = s.G;
   a.lg = 0;
   while ((1 << a.lg) < s.G) a.lg++;
@@ -211,10 +237,16 @@ int launch_plain(tqec_program* p, int precision, tqec::KArgs a, int64_t n, cudaS
   Shape one;
   one.G = 1;
   one.threads = s.threads;
-  one.smem_arena =
-      tqec::contract_smem_bytes(precision, nsteps, syn_words(p), 1, p->plan.arena_elems, true, var_words(p)) <= limit;
-  one.smem = tqec::contract_smem_bytes(precision, nsteps, syn_words(p), 1, p->plan.arena_elems, one.smem_arena,
-                                       var_words(p));
+  const size_t tb = table_bytes(p, precision);
+  auto bytes = [&](bool arena_smem, size_t t) {
+    return tqec::contract_smem_bytes(precision, nsteps, syn_words(p), 1, p->plan.arena_elems, arena_smem,
+                                     var_words(p), t);
+  };
+  one.smem_arena = bytes(true, 0) <= limit;
+  one.smem_tables = bytes(one.smem_arena, tb) <= limit;
+  one.smem = bytes(one.smem_arena, one.smem_tables ? tb : 0);
+  a.tables_smem = one.smem_tables ? 1 : 0;
+  a.perm16 = one.smem_tables ? p->d_perm16 : nullptr;
   a.G = 1;
   a.lg = 0;
   if (!one.smem_arena) {
@@ -337,6 +369,9 @@ int program_f64_view(tqec_program* p, ProgramF64View* v) {
   if (!p || !v) return TQEC_ERR_INVALID;
   v->args = base_args(p, TQEC_F64);
   v->args.arena_global = nullptr;
+  // the view's launches size their own shared memory: tables stay global
+  v->args.tables_smem = 0;
+  v->args.perm16 = nullptr;
   v->device = p->device;
   v->sm_count = p->sm_count;
   v->threads = p->shape[TQEC_F64].threads;
@@ -395,13 +430,29 @@ int tqec_program_create(const tqec_network* net, const tqec_tree* tree, const tq
   cudaDeviceGetAttribute(&p->sm_count, cudaDevAttrMultiProcessorCount, o.device);
   if ((e = cudaStreamCreateWithFlags(&p->stream, cudaStreamNonBlocking)) != cudaSuccess)
     return bail(TQEC_ERR_CUDA, cudaGetErrorString(e));
+  for (const tqec::StepDesc& d : p->plan.steps)
+    if (d.a_kind == tqec::OP_PARITY || d.b_kind == tqec::OP_PARITY)
+      return bail(TQEC_ERR_INVALID, "internal: the kernel reads no parity operands");
   const tqec::Plan& P = p->plan;
   size_t nst = P.steps.size();
   if ((e = cudaMalloc(&p->d_steps, nst * sizeof(tqec::StepDesc))) != cudaSuccess) return bail(TQEC_ERR_OOM, "steps");
   cudaMemcpy(p->d_steps, P.steps.data(), nst * sizeof(tqec::StepDesc), cudaMemcpyHostToDevice);
-  size_t np = std::max<size_t>(P.perm.size(), 1);
-  if ((e = cudaMalloc(&p->d_perm, np * sizeof(int32_t))) != cudaSuccess) return bail(TQEC_ERR_OOM, "perm");
-  if (!P.perm.empty()) cudaMemcpy(p->d_perm, P.perm.data(), P.perm.size() * sizeof(int32_t), cudaMemcpyHostToDevice);
+  {
+    // both copies padded to a multiple of 8 entries (16-byte staging copies)
+    std::vector<int32_t> perm(P.perm);
+    while (perm.size() % 8) perm.push_back(0);
+    p->n_perm_padded = (int64_t)perm.size();
+    const size_t np = std::max<size_t>(perm.size(), 8);
+    if ((e = cudaMalloc(&p->d_perm, np * sizeof(int32_t))) != cudaSuccess) return bail(TQEC_ERR_OOM, "perm");
+    if (!perm.empty()) cudaMemcpy(p->d_perm, perm.data(), perm.size() * sizeof(int32_t), cudaMemcpyHostToDevice);
+    bool fits16 = true;
+    for (int32_t v : perm) fits16 = fits16 && v >= 0 && v < 65536;
+    if (fits16) {
+      std::vector<uint16_t> p16(perm.begin(), perm.end());
+      if ((e = cudaMalloc(&p->d_perm16, np * sizeof(uint16_t))) != cudaSuccess) return bail(TQEC_ERR_OOM, "perm");
+      if (!p16.empty()) cudaMemcpy(p->d_perm16, p16.data(), p16.size() * sizeof(uint16_t), cudaMemcpyHostToDevice);
+    }
+  }
   size_t nc = std::max<size_t>(P.consts.size(), 4);
   if ((e = cudaMalloc(&p->d_c64, nc * sizeof(double))) != cudaSuccess) return bail(TQEC_ERR_OOM, "consts");
   if ((e = cudaMalloc(&p->d_c32, nc * sizeof(float))) != cudaSuccess) return bail(TQEC_ERR_OOM, "consts");
@@ -423,11 +474,11 @@ int tqec_program_create(const tqec_network* net, const tqec_tree* tree, const tq
   *p->h_count = 0;
   if ((e = cudaGetLastError()) != cudaSuccess) return bail(TQEC_ERR_CUDA, cudaGetErrorString(e));
   int rc;
-  if ((rc = choose_shape(p, TQEC_F32, o.group, o.threads, &p->shape[TQEC_F32])) != TQEC_OK) {
+  if ((rc = choose_shape(p, TQEC_F32, o.group, o.threads, -1, &p->shape[TQEC_F32])) != TQEC_OK) {
     std::string m = g_last_error;
     return bail(rc, m);
   }
-  if ((rc = choose_shape(p, TQEC_F64, o.group, o.threads, &p->shape[TQEC_F64])) != TQEC_OK) {
+  if ((rc = choose_shape(p, TQEC_F64, o.group, o.threads, -1, &p->shape[TQEC_F64])) != TQEC_OK) {
     std::string m = g_last_error;
     return bail(rc, m);
   }
@@ -441,6 +492,7 @@ int tqec_program_destroy(tqec_program* p) {
   if (p->stream) cudaStreamSynchronize(p->stream);
   cudaFree(p->d_steps);
   cudaFree(p->d_perm);
+  cudaFree(p->d_perm16);
   cudaFree(p->d_c64);
   cudaFree(p->d_c32);
   cudaFree(p->d_vartab);
@@ -571,8 +623,11 @@ int tqec_program_autotune(tqec_program* p, int64_t n_probe) {
     float best_ms = 1e30f;
     for (int G : {1, 2, 4, 8, 16, 32, 64, 128}) {
       for (int th : {128, 256, 512, 1024}) {
+       if (th > tqec::contract_max_threads(prec)) continue;
+       for (int tables : {0, 1}) {
         Shape s;
-        if (choose_shape(p, prec, G, th, &s) != TQEC_OK) continue;
+        if (choose_shape(p, prec, G, th, tables, &s) != TQEC_OK) continue;
+        if (tables && !s.smem_tables) continue;
         // a global arena bigger than 4 GB is not worth probing on a shared GPU
         const size_t esz = prec == TQEC_F32 ? 4 : 8;
         if (!s.smem_arena && (G > 8 || size_t(s.grid_cap) * G * size_t(p->plan.arena_elems) * esz > (size_t(4) << 30)))
@@ -597,6 +652,7 @@ int tqec_program_autotune(tqec_program* p, int64_t n_probe) {
           best_ms = ms;
           best = s;
         }
+       }
       }
     }
     p->shape[prec] = best;

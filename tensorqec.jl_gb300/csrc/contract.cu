@@ -55,12 +55,55 @@ __device__ __forceinline__ const T* operand_ptr(int kind, int32_t ref, const int
   return consts + ref + (int64_t(v) << obits);
 }
 
-__device__ __forceinline__ int perm_addr(const int32_t* __restrict__ perm, int e, int lw) {
+// Permutation tables: int32 entries (global or shared memory) or uint16
+// entries (shared memory, programs of width <= 16).
+struct PermTab {
+  const void* base;
+  bool is16;
+  __device__ __forceinline__ int at(int idx) const {
+    return is16 ? int(static_cast<const uint16_t*>(base)[idx]) : static_cast<const int32_t*>(base)[idx];
+  }
+  // VW consecutive entries starting at idx (idx a multiple of VW, tables
+  // 16-byte aligned)
+  template <int VW>
+  __device__ __forceinline__ void vec(int idx, int out[VW]) const {
+    if (is16) {
+      const uint16_t* p = static_cast<const uint16_t*>(base) + idx;
+      if (VW == 8) {
+        const uint4 x = *reinterpret_cast<const uint4*>(p);
+        const uint32_t w[4] = {x.x, x.y, x.z, x.w};
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          out[2 * j] = int(w[j] & 0xffffu);
+          out[2 * j + 1] = int(w[j] >> 16);
+        }
+      } else {
+        const uint2 x = *reinterpret_cast<const uint2*>(p);
+        out[0] = int(x.x & 0xffffu);
+        out[1] = int(x.x >> 16);
+        out[2] = int(x.y & 0xffffu);
+        out[3] = int(x.y >> 16);
+      }
+    } else {
+      const int32_t* p = static_cast<const int32_t*>(base) + idx;
+#pragma unroll
+      for (int j = 0; j < VW; j += 4) {
+        const int4 x = *reinterpret_cast<const int4*>(p + j);
+        out[j] = x.x;
+        out[j + 1] = x.y;
+        out[j + 2] = x.z;
+        out[j + 3] = x.w;
+      }
+    }
+  }
+};
+
+__device__ __forceinline__ int perm_addr(const PermTab& perm, int off, int e, int lw) {
   int addr = 0;
-  int tab = 0;
+  int tab = off;
   for (int sh = 0; sh < lw; sh += 8) {
     const int cb = lw - sh < 8 ? lw - sh : 8;
-    addr |= __ldg(perm + tab + ((e >> sh) & ((1 << cb) - 1)));
+    addr |= perm.at(tab + ((e >> sh) & ((1 << cb) - 1)));
     tab += 1 << cb;
   }
   return addr;
@@ -94,15 +137,16 @@ __device__ __forceinline__ void flush_max(bool had_items, uint32_t bits, uint32_
   if ((threadIdx.x & 31) == 0) atomicMax(slot, bits);
 }
 
-// G1: the block owns one syndrome, so the syndrome bits, the arena slice, the
-// operand bases and the normalisers are step invariants computed once.
+// G1: the step runs for one syndrome (the block's only one, or one of its G
+// in turn), so the syndrome bits, the arena slice, the operand bases and the
+// normalisers are step invariants computed once.
 template <typename T, bool NORM, bool APAR, bool BPAR, bool MAXP, bool G1>
 __device__ int run_step(const KArgs& a, const StepDesc& dref, int st, int item_base, const uint32_t* s_syn,
-                         uint32_t* s_max, T* arena, const T* consts) {
+                         uint32_t* s_max, T* arena, const T* consts, const PermTab& ptab) {
   // a register copy: arena stores (same shared array) cannot alias it
   const StepDesc d = dref;
   const int lw = d.lh + d.lfa + d.lfb;
-  const int total = 1 << (lw + a.lg);
+  const int total = 1 << (lw + (G1 ? 0 : a.lg));
   const int total_r = (total + 31) & ~31;
   const int mfb = (1 << d.lfb) - 1;
   const int mfa = (1 << d.lfa) - 1;
@@ -187,7 +231,7 @@ __device__ int run_step(const KArgs& a, const StepDesc& dref, int st, int item_b
         }
       }
       if (NORM && !BPAR) acc *= fb_s;
-      const int addr = d.perm_off < 0 ? e : perm_addr(a.perm + d.perm_off, e, lw);
+      const int addr = d.perm_off < 0 ? e : perm_addr(ptab, d.perm_off, e, lw);
       arena_g[d.out_off + addr] = acc;
     }
     if (NORM && G1) {
@@ -242,12 +286,12 @@ __device__ __forceinline__ void store4<double>(double* p, const double v[4]) {
 // different index bits.
 template <typename T, int VW, bool NORM, bool APAR, bool BPAR, bool MAXP, bool G1>
 __device__ int run_step_vec(const KArgs& a, const StepDesc& dref, int st, int item_base, const uint32_t* s_syn,
-                            uint32_t* s_max, T* arena, const T* consts) {
+                            uint32_t* s_max, T* arena, const T* consts, const PermTab& ptab) {
   constexpr int LV = VW == 8 ? 3 : 2;
   const StepDesc d = dref;
   const int lw = d.lh + d.lfa + d.lfb;
   const int lwv = lw - LV;
-  const int total = 1 << (lwv + a.lg);
+  const int total = 1 << (lwv + (G1 ? 0 : a.lg));
   const int total_r = (total + 31) & ~31;
   const int mfb = (1 << d.lfb) - 1;
   const int mfa = (1 << d.lfa) - 1;
@@ -256,7 +300,7 @@ __device__ int run_step_vec(const KArgs& a, const StepDesc& dref, int st, int it
   const int bstride = 1 << d.lfb;
   const int abits = d.lh + d.lfa + d.lk;
   const int bbits = d.lh + d.lk + d.lfb;
-  const int32_t* perm = d.perm_off < 0 ? nullptr : a.perm + d.perm_off;
+  const bool permuted = d.perm_off >= 0;
   const int cb0 = lw < 8 ? lw : 8;
   const int rot = threadIdx.x & (VW - 1);
   const int i0 = (int(threadIdx.x) + int(blockDim.x) - item_base % int(blockDim.x)) % int(blockDim.x);
@@ -347,24 +391,17 @@ __device__ int run_step_vec(const KArgs& a, const StepDesc& dref, int st, int it
 #pragma unroll
         for (int j = 0; j < VW; ++j) acc[j] *= fb_s;
       }
-      if (!perm) {
+      if (!permuted) {
         store4<T>(arena_g + d.out_off + e0, acc);
         if (VW == 8) store4<T>(arena_g + d.out_off + e0 + 4, acc + 4);
       } else {
         int los[VW];
-        {
-          const int4 l0 = *reinterpret_cast<const int4*>(perm + (e0 & ((1 << cb0) - 1)));
-          los[0] = l0.x; los[1] = l0.y; los[2] = l0.z; los[3] = l0.w;
-          if (VW == 8) {
-            const int4 l1 = *reinterpret_cast<const int4*>(perm + (e0 & ((1 << cb0) - 1)) + 4);
-            los[4] = l1.x; los[5] = l1.y; los[6] = l1.z; los[7] = l1.w;
-          }
-        }
+        ptab.vec<VW>(d.perm_off + (e0 & ((1 << cb0) - 1)), los);
         int hi = 0;
-        int tab = 1 << cb0;
+        int tab = d.perm_off + (1 << cb0);
         for (int sh = 8; sh < lw; sh += 8) {
           const int cb = lw - sh < 8 ? lw - sh : 8;
-          hi |= __ldg(perm + tab + ((e0 >> sh) & ((1 << cb) - 1)));
+          hi |= ptab.at(tab + ((e0 >> sh) & ((1 << cb) - 1)));
           tab += 1 << cb;
         }
         T* out = arena_g + d.out_off;
@@ -411,6 +448,86 @@ __device__ int run_step_vec(const KArgs& a, const StepDesc& dref, int st, int it
     }
   }
   if (NORM && G1) flush_max(i0 < total, run_bits, &s_max[st]);
+  return total_r;
+}
+
+// A step with few outputs and a long k range: TPO (a power of two, at most
+// 32) consecutive lanes share one output, each summing every TPO-th k, and
+// combine their partial sums with shuffles (maxima in max-product mode).
+template <typename T, bool NORM, bool APAR, bool BPAR, bool MAXP, bool G1>
+__device__ int run_step_splitk(const KArgs& a, const StepDesc& dref, int st, int item_base, int lt,
+                               const uint32_t* s_syn, uint32_t* s_max, T* arena, const T* consts,
+                               const PermTab& ptab) {
+  const StepDesc d = dref;
+  const int tpo = 1 << lt;
+  const int lw = d.lh + d.lfa + d.lfb;
+  const int outs = 1 << (lw + (G1 ? 0 : a.lg));
+  const int total = outs << lt;
+  const int total_r = (total + 31) & ~31;
+  const int mfb = (1 << d.lfb) - 1;
+  const int mfa = (1 << d.lfa) - 1;
+  const int mw = (1 << lw) - 1;
+  const int K = 1 << d.lk;
+  const int abits = d.lh + d.lfa + d.lk;
+  const int bbits = d.lh + d.lk + d.lfb;
+  const int vt0 = (int(threadIdx.x) + int(blockDim.x) - item_base % int(blockDim.x)) % int(blockDim.x);
+  uint32_t run_bits = 0u;
+  // whole warps iterate together (the shuffles below need every lane)
+  for (int vt = vt0; vt < total_r; vt += blockDim.x) {
+    const bool valid = vt < total;
+    const int item = vt >> lt, sub = vt & (tpo - 1);
+    const int g = G1 ? 0 : (valid ? (item >> lw) : 0);
+    const int e = item & mw;
+    T acc = T(0);
+    T* arena_g = G1 ? arena : arena + int64_t(g) * a.arena_elems;
+    if (valid) {
+      const uint32_t* syn = s_syn + g * a.syn_words;
+      const int fb = e & mfb;
+      const int fa = (e >> d.lfb) & mfa;
+      const int h = e >> (d.lfb + d.lfa);
+      const int abase = ((h << d.lfa) | fa) << d.lk;
+      const int bbase = (h << (d.lk + d.lfb)) | fb;
+      Operand<T> A{}, B{};
+      int as = 0, bs = 0;
+      if (APAR) as = syn_bit(syn, d.a_ref);
+      else A = make_operand<T>(d.a_kind, d.a_ref, d.a_sel, abits, arena_g, consts, syn);
+      if (BPAR) bs = syn_bit(syn, d.b_ref);
+      else B = make_operand<T>(d.b_kind, d.b_ref, d.b_sel, bbits, arena_g, consts, syn);
+      T fa_s = T(1);
+      if (NORM && !APAR && d.a_kind == OP_ARENA) {
+        int ee;
+        fa_s = T(norm_factor(s_max[g * a.n_steps + d.a_prod], &ee));
+      }
+      for (int k = sub; k < K; k += tpo) {
+        const T av = APAR ? parity_val<T>(abase + k, as) : A.ld(abase + k) * fa_s;
+        const T bv = BPAR ? parity_val<T>(bbase + (k << d.lfb), bs) : B.ld(bbase + (k << d.lfb));
+        if (MAXP) {
+          const T v = av * bv;
+          acc = v > acc ? v : acc;
+        } else {
+          acc = fma(av, bv, acc);
+        }
+      }
+    }
+    for (int o = 1; o < tpo; o <<= 1) {
+      const T other = __shfl_xor_sync(0xffffffffu, acc, o);
+      acc = MAXP ? (other > acc ? other : acc) : acc + other;
+    }
+    if (valid && sub == 0) {
+      if (NORM && !BPAR && d.b_kind == OP_ARENA) {
+        int ee;
+        acc *= T(norm_factor(s_max[g * a.n_steps + d.b_prod], &ee));
+      }
+      const int addr = d.perm_off < 0 ? e : perm_addr(ptab, d.perm_off, e, lw);
+      arena_g[d.out_off + addr] = acc;
+      if (NORM) {
+        const uint32_t bits = __float_as_uint(float(acc));
+        if (G1) run_bits = bits > run_bits ? bits : run_bits;
+        else atomicMax(&s_max[g * a.n_steps + st], bits);
+      }
+    }
+  }
+  if (NORM && G1) flush_max(vt0 < total, run_bits, &s_max[st]);
   return total_r;
 }
 
@@ -504,32 +621,66 @@ __device__ void backtrack(const KArgs& a, const StepDesc* s_steps, const uint32_
   }
 }
 
-template <typename T, bool NORM, bool MAXP, bool G1>
-__device__ __forceinline__ int dispatch_step(const KArgs& a, const StepDesc& d, bool ap, bool bp, int st,
-                                             int item_base, const uint32_t* s_syn, uint32_t* s_max, T* arena,
-                                             const T* consts) {
-  // eight outputs per item where that still gives every thread an item
-  const int lw = d.lh + d.lfa + d.lfb;
-  if (sizeof(T) == 4 && d.lfb >= 3 && (int64_t(1) << (lw - 3 + a.lg)) >= int64_t(blockDim.x)) {
-    if (ap && bp) return run_step_vec<T, 8, NORM, true, true, MAXP, G1>(a, d, st, item_base, s_syn, s_max, arena, consts);
-    if (ap) return run_step_vec<T, 8, NORM, true, false, MAXP, G1>(a, d, st, item_base, s_syn, s_max, arena, consts);
-    if (bp) return run_step_vec<T, 8, NORM, false, true, MAXP, G1>(a, d, st, item_base, s_syn, s_max, arena, consts);
-    return run_step_vec<T, 8, NORM, false, false, MAXP, G1>(a, d, st, item_base, s_syn, s_max, arena, consts);
+// How a step is executed and how many work items it has (rounded up to a
+// warp): several lanes per output for few outputs over a long k range,
+// eight or four outputs per item along fb, else one output per item.
+enum StepKind { SK_SPLITK, SK_VEC8, SK_VEC4, SK_SCALAR };
+struct StepShape {
+  int kind;
+  int lt;       // SK_SPLITK: log2 of the lanes per output
+  int total_r;  // work items (threads for SK_SPLITK), a multiple of 32
+};
+
+template <typename T>
+__device__ __forceinline__ StepShape step_shape(int lh, int lfa, int lfb, int lk, int lg) {
+  const int lw = lh + lfa + lfb;
+  const int64_t outs = int64_t(1) << (lw + lg);
+  const int64_t bd = blockDim.x;
+  StepShape sh;
+  int lt = 0;
+  while (lt < 5 && (outs << (lt + 1)) <= bd && (lt + 1) + 2 <= lk) ++lt;
+  int64_t total;
+  if (lt >= 2) {
+    sh.kind = SK_SPLITK;
+    total = outs << lt;
+  } else if (sizeof(T) == 4 && lfb >= 3 && (outs >> 3) >= bd) {
+    sh.kind = SK_VEC8;
+    total = outs >> 3;
+  } else if (lfb >= 2) {
+    sh.kind = SK_VEC4;
+    total = outs >> 2;
+  } else {
+    sh.kind = SK_SCALAR;
+    total = outs;
   }
-  if (d.lfb >= 2) {
-    if (ap && bp) return run_step_vec<T, 4, NORM, true, true, MAXP, G1>(a, d, st, item_base, s_syn, s_max, arena, consts);
-    if (ap) return run_step_vec<T, 4, NORM, true, false, MAXP, G1>(a, d, st, item_base, s_syn, s_max, arena, consts);
-    if (bp) return run_step_vec<T, 4, NORM, false, true, MAXP, G1>(a, d, st, item_base, s_syn, s_max, arena, consts);
-    return run_step_vec<T, 4, NORM, false, false, MAXP, G1>(a, d, st, item_base, s_syn, s_max, arena, consts);
-  }
-  if (ap && bp) return run_step<T, NORM, true, true, MAXP, G1>(a, d, st, item_base, s_syn, s_max, arena, consts);
-  if (ap) return run_step<T, NORM, true, false, MAXP, G1>(a, d, st, item_base, s_syn, s_max, arena, consts);
-  if (bp) return run_step<T, NORM, false, true, MAXP, G1>(a, d, st, item_base, s_syn, s_max, arena, consts);
-  return run_step<T, NORM, false, false, MAXP, G1>(a, d, st, item_base, s_syn, s_max, arena, consts);
+  sh.lt = lt;
+  sh.total_r = int((total + 31) & ~int64_t(31));
+  return sh;
 }
 
+// The planner hands the kernel arena and constant operands only (parity
+// operands become syndrome-selected tables), so each step shape has one code
+// path: the kernel stays small enough for the instruction caches.
+template <typename T, bool NORM, bool MAXP, bool G1>
+__device__ __forceinline__ int dispatch_step(const KArgs& a, const StepDesc& d, const StepShape& sh, int st,
+                                             int item_base, const uint32_t* s_syn, uint32_t* s_max, T* arena,
+                                             const T* consts, const PermTab& ptab) {
+  switch (sh.kind) {
+    case SK_SPLITK:
+      return run_step_splitk<T, NORM, false, false, MAXP, G1>(a, d, st, item_base, sh.lt, s_syn, s_max, arena, consts,
+                                                              ptab);
+    case SK_VEC8:
+      return run_step_vec<T, 8, NORM, false, false, MAXP, G1>(a, d, st, item_base, s_syn, s_max, arena, consts, ptab);
+    case SK_VEC4:
+      return run_step_vec<T, 4, NORM, false, false, MAXP, G1>(a, d, st, item_base, s_syn, s_max, arena, consts, ptab);
+    default:
+      return run_step<T, NORM, false, false, MAXP, G1>(a, d, st, item_base, s_syn, s_max, arena, consts, ptab);
+  }
+}
+
+// float64 blocks are capped at 512 threads, which leaves them 128 registers
 template <typename T, bool NORM, bool MAXP>
-__global__ void __launch_bounds__(1024) tn_contract_kernel(KArgs a) {
+__global__ void __launch_bounds__(sizeof(T) == 8 ? 512 : 1024) tn_contract_kernel(KArgs a) {
   extern __shared__ __align__(16) unsigned char smem[];
   StepDesc* s_steps = reinterpret_cast<StepDesc*>(smem);
   size_t off = size_t(a.n_steps) * sizeof(StepDesc);
@@ -540,10 +691,33 @@ __global__ void __launch_bounds__(1024) tn_contract_kernel(KArgs a) {
   uint32_t* s_asg = reinterpret_cast<uint32_t*>(smem + off);
   if (MAXP) off += size_t(a.G) * a.var_words * 4;
   off = (off + 15) & ~size_t(15);
+  const T* consts = reinterpret_cast<const T*>(a.consts);
+  PermTab ptab{a.perm, false};
+  if (a.tables_smem) {
+    // constants and permutation tables move to shared memory once per block
+    T* s_consts = reinterpret_cast<T*>(smem + off);
+    off += (size_t(a.n_consts) * sizeof(T) + 15) & ~size_t(15);
+    void* s_perm = smem + off;
+    const size_t perm_bytes = size_t(a.n_perm) * (a.perm16 ? 2 : 4);
+    off += (perm_bytes + 15) & ~size_t(15);
+    {
+      const int4* src = reinterpret_cast<const int4*>(a.consts);
+      int4* dst = reinterpret_cast<int4*>(s_consts);
+      const int n16 = int(size_t(a.n_consts) * sizeof(T) / 16);
+      for (int i = threadIdx.x; i < n16; i += blockDim.x) dst[i] = src[i];
+    }
+    {
+      const int4* src = a.perm16 ? reinterpret_cast<const int4*>(a.perm16) : reinterpret_cast<const int4*>(a.perm);
+      int4* dst = reinterpret_cast<int4*>(s_perm);
+      const int n16 = int(perm_bytes / 16);
+      for (int i = threadIdx.x; i < n16; i += blockDim.x) dst[i] = src[i];
+    }
+    consts = s_consts;
+    ptab = PermTab{s_perm, a.perm16 != nullptr};
+  }
   T* arena = a.arena_global
                  ? reinterpret_cast<T*>(a.arena_global) + int64_t(blockIdx.x) * a.G * a.arena_elems
                  : reinterpret_cast<T*>(smem + off);
-  const T* consts = reinterpret_cast<const T*>(a.consts);
   {
     const int4* src = reinterpret_cast<const int4*>(a.steps);
     int4* dst = reinterpret_cast<int4*>(s_steps);
@@ -571,12 +745,30 @@ __global__ void __launch_bounds__(1024) tn_contract_kernel(KArgs a) {
     int item_base = 0;
     for (int st = 0; st < a.n_steps; ++st) {
       const StepDesc& d = s_steps[st];
-      const bool ap = d.a_kind == OP_PARITY, bp = d.b_kind == OP_PARITY;
-      int items;
-      if (a.G == 1)
-        items = dispatch_step<T, NORM, MAXP, true>(a, d, ap, bp, st, item_base, s_syn, s_max, arena, consts);
-      else
-        items = dispatch_step<T, NORM, MAXP, false>(a, d, ap, bp, st, item_base, s_syn, s_max, arena, consts);
+      const int4 q = *reinterpret_cast<const int4*>(&d.lh);  // lh, lfa, lfb, lk
+      const int bd = int(blockDim.x);
+      const StepShape sh = step_shape<T>(q.x, q.y, q.z, q.w, a.lg);
+      // a step that fills the block for each syndrome alone runs the block's
+      // syndromes one after another with hoisted invariants (every thread
+      // takes part)
+      const StepShape sh1 = a.G > 1 ? step_shape<T>(q.x, q.y, q.z, q.w, 0) : sh;
+      const bool per_syndrome = a.G > 1 && sh1.total_r >= bd;
+      const int items = per_syndrome ? bd : sh.total_r;
+      // first virtual thread of this warp (steps of a barrier group start on
+      // different warps); a warp past the step's items goes to the barrier
+      const int vt_warp = (int(threadIdx.x & ~31u) + bd - item_base % bd) % bd;
+      if (vt_warp < items) {
+        if (a.G == 1) {
+          dispatch_step<T, NORM, MAXP, true>(a, d, sh, st, item_base, s_syn, s_max, arena, consts, ptab);
+        } else if (per_syndrome) {
+          for (int g = 0; g < a.G; ++g)
+            dispatch_step<T, NORM, MAXP, true>(a, d, sh1, st, item_base, s_syn + g * a.syn_words,
+                                               s_max + g * a.n_steps, arena + int64_t(g) * a.arena_elems, consts,
+                                               ptab);
+        } else {
+          dispatch_step<T, NORM, MAXP, false>(a, d, sh, st, item_base, s_syn, s_max, arena, consts, ptab);
+        }
+      }
       if (d.flags & kStepSync) {
         __syncthreads();
         item_base = 0;
@@ -635,14 +827,21 @@ __global__ void __launch_bounds__(1024) tn_contract_kernel(KArgs a) {
 }  // namespace
 
 size_t contract_smem_bytes(int precision, int32_t n_steps, int32_t syn_words, int G,
-                           int64_t arena_elems, bool arena_in_smem, int32_t var_words) {
+                           int64_t arena_elems, bool arena_in_smem, int32_t var_words, size_t table_bytes) {
   const bool norm = precision == 1;
   size_t off = size_t(n_steps) * sizeof(StepDesc) + size_t(G) * syn_words * 4;
   if (norm) off += size_t(G) * n_steps * 4;
   off += size_t(G) * var_words * 4;
   off = (off + 15) & ~size_t(15);
+  off += table_bytes;
   if (arena_in_smem) off += size_t(G) * size_t(arena_elems) * (precision == 1 ? 4 : 8);
   return off;
+}
+
+size_t contract_table_bytes(int precision, int64_t n_consts, int64_t n_perm, bool perm16) {
+  const size_t c = (size_t(n_consts) * (precision == 1 ? 4 : 8) + 15) & ~size_t(15);
+  const size_t p = (size_t(n_perm) * (perm16 ? 2 : 4) + 15) & ~size_t(15);
+  return c + p;
 }
 
 size_t contract_smem_limit(int device) {

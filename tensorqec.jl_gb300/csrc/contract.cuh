@@ -17,6 +17,13 @@ struct KArgs {
   int32_t n_steps;
   const int32_t* perm;
   const void* consts;  // float or double, matching the kernel
+  // tables staged in shared memory at kernel start: the constants (n_consts,
+  // a multiple of 4) and the permutation tables (n_perm entries, a multiple
+  // of 8), the latter from perm16 (uint16 entries) when it is set
+  int32_t tables_smem;
+  int32_t n_consts;
+  int32_t n_perm;
+  const uint16_t* perm16;
   const uint8_t* syn;
   int32_t syn_bytes;
   int32_t syn_words;  // 32-bit words per syndrome in shared memory (>= 1)
@@ -48,10 +55,17 @@ struct KArgs {
 
 // Shared memory a launch needs (bytes).
 size_t contract_smem_bytes(int precision, int32_t n_steps, int32_t syn_words, int G,
-                           int64_t arena_elems, bool arena_in_smem, int32_t var_words = 0);
+                           int64_t arena_elems, bool arena_in_smem, int32_t var_words = 0,
+                           size_t table_bytes = 0);
+
+// Shared-memory bytes of the staged constant and permutation tables.
+size_t contract_table_bytes(int precision, int64_t n_consts, int64_t n_perm, bool perm16);
 
 // Largest dynamic shared memory a block may use on this device.
 size_t contract_smem_limit(int device);
+
+// Most threads a block of the given precision may have.
+constexpr int contract_max_threads(int precision) { return precision == 1 ? 1024 : 512; }
 
 // Resident blocks per SM for a launch shape (0 if it cannot launch).
 int contract_occupancy(int precision, int threads, size_t smem, bool map_mode = false);

@@ -465,6 +465,12 @@ std::string build_plan(const NetworkView& net, int32_t n_steps, const int32_t* s
   };
   post(root);
   const int R = (int)order.size();
+  // A parity operand of a runtime step becomes a two-variant table selected
+  // by its syndrome bit: the kernel then reads only arena and constant
+  // operands (one code path per step shape, a smaller kernel).
+  for (int id : order)
+    for (int op : {nodes[id].left, nodes[id].right})
+      if (nodes[op].kind == NK_PARITY) nodes[op] = parity_as_table(nodes[op]);
 
   // ---- layouts --------------------------------------------------------------
   struct StepLayout {
@@ -702,8 +708,9 @@ std::string build_plan(const NetworkView& net, int32_t n_steps, const int32_t* s
     if (ident) {
       d.perm_off = -1;
     } else {
-      // tables start on a 16-byte boundary (vector loads of the low table)
-      while (P.perm.size() % 4) P.perm.push_back(0);
+      // tables start on a multiple of 8 entries (16-byte vector loads of the
+      // low table, as int32 or as uint16)
+      while (P.perm.size() % 8) P.perm.push_back(0);
       d.perm_off = (int32_t)P.perm.size();
       const int nb = (int)nat.size();
       for (int c0 = 0; c0 < nb; c0 += 8) {

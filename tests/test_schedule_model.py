@@ -1,0 +1,103 @@
+"""A CPU model of how the contraction kernel spreads a step over a block.
+
+It restates the kernel's step-shape choice (several lanes per output, eight
+or four outputs per work item, or one), its per-warp entry test, the
+rotation of barrier-group members over the block and the per-syndrome loop
+of multi-syndrome blocks (csrc/contract.cu: step_shape, the step loop of
+tn_contract_kernel, run_step*, run_step_splitk), and checks on real programs
+that every output of every syndrome of every step is written exactly once for
+each launch shape the autotuner may pick.
+"""
+import numpy as np
+import pytest
+
+
+def step_shape(lh, lfa, lfb, lk, lg, bd, is_float):
+    lw = lh + lfa + lfb
+    outs = 1 << (lw + lg)
+    lt = 0
+    while lt < 5 and (outs << (lt + 1)) <= bd and (lt + 1) + 2 <= lk:
+        lt += 1
+    if lt >= 2:
+        kind, total = "splitk", outs << lt
+    elif is_float and lfb >= 3 and (outs >> 3) >= bd:
+        kind, total = "vec8", outs >> 3
+    elif lfb >= 2:
+        kind, total = "vec4", outs >> 2
+    else:
+        kind, total = "scalar", outs
+    return kind, lt, (total + 31) & ~31
+
+
+def _run(kind, lt, lw, lg, one, bd, item_base, enter, cover, gbase):
+    """Marks the outputs the block's threads write for one step (one
+    syndrome when `one`, else all G of the block)."""
+    tid = np.arange(bd)
+    vt = (tid + bd - item_base % bd) % bd
+    warp_vt = ((tid & ~31) + bd - item_base % bd) % bd
+    vt = vt[warp_vt < enter]
+    lwg = lw + (0 if one else lg)
+    if kind == "splitk":
+        total = (1 << lwg) << lt
+        tr = (total + 31) & ~31
+        for v in vt:
+            for x in range(v, tr, bd):
+                if x < total and (x & ((1 << lt) - 1)) == 0:
+                    item = x >> lt
+                    g = 0 if one else item >> lw
+                    cover[gbase + g, item & ((1 << lw) - 1)] += 1
+        return
+    lv = {"vec8": 3, "vec4": 2, "scalar": 0}[kind]
+    lwv = lw - lv
+    total = 1 << (lwv + (0 if one else lg))
+    stop = total if one else (total + 31) & ~31
+    for v in vt:
+        for i in range(v, stop, bd):
+            if i < total:
+                g = 0 if one else i >> lwv
+                e0 = (i & ((1 << lwv) - 1)) << lv
+                cover[gbase + g, e0:e0 + (1 << lv)] += 1
+
+
+def check_program(plan, is_float):
+    bad = []
+    for G in (1, 2, 4, 8):
+        lg = G.bit_length() - 1
+        for bd in (128, 256, 512, 1024):
+            if not is_float and bd > 512:
+                continue
+            item_base = 0
+            for st, d in enumerate(plan["steps"]):
+                lh, lfa, lfb, lk = int(d["lh"]), int(d["lfa"]), int(d["lfb"]), int(d["lk"])
+                lw = lh + lfa + lfb
+                kind, lt, tr = step_shape(lh, lfa, lfb, lk, lg, bd, is_float)
+                k1, lt1, tr1 = step_shape(lh, lfa, lfb, lk, 0, bd, is_float)
+                per_syndrome = G > 1 and tr1 >= bd
+                enter = bd if per_syndrome else tr
+                cover = np.zeros((G, 1 << lw), dtype=np.int64)
+                if G == 1:
+                    _run(kind, lt, lw, 0, True, bd, item_base, enter, cover, 0)
+                elif per_syndrome:
+                    for g in range(G):
+                        _run(k1, lt1, lw, 0, True, bd, item_base, enter, cover, g)
+                else:
+                    _run(kind, lt, lw, lg, False, bd, item_base, enter, cover, 0)
+                if not (cover == 1).all():
+                    bad.append((G, bd, st, kind, int(cover.min()), int(cover.max())))
+                item_base = 0 if int(d["flags"]) & 1 else item_base + enter
+    return bad
+
+
+@pytest.mark.parametrize("code", ["surface5", "color488_5", "surface7"])
+def test_every_output_written_once(pkg, code):
+    from tensorqec_gb300 import decoder, gf2, network, native
+    c = {"surface5": lambda: pkg.SurfaceCode(5, 5), "color488_5": lambda: pkg.Color488(5),
+         "surface7": lambda: pkg.SurfaceCode(7, 7)}[code]()
+    t = pkg.tanner_graph(c)
+    em = pkg.depolarizing(0.05, t.nq)
+    lx, lz = gf2.logical_operator(t)
+    graph = network.tnmmap_css_graph(t, em, lx, lz)
+    steps = decoder.optimize_code(graph, decoder.TreeSA(restarts=1))
+    plan = native.inspect_plan(graph, steps)
+    for is_float in (True, False):
+        assert check_program(plan, is_float) == []
