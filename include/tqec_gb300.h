@@ -106,6 +106,8 @@ typedef struct {
   double err_bound_f64;      /* relative error bound of a TQEC_F64 marginal */
   int32_t group_f32, threads_f32, smem_f32; /* launch shape chosen for F32 */
   int32_t group_f64, threads_f64, smem_f64; /* launch shape chosen for F64 */
+  int32_t resident_f32, resident_f64;       /* most blocks in flight on the device */
+  int32_t tables_smem_f32, tables_smem_f64; /* 1: tables staged in shared memory */
 } tqec_program_info_t;
 
 typedef struct tqec_program tqec_program;

@@ -90,7 +90,13 @@ struct tqec_program {
   int8_t* d_fixed = nullptr;
   double* d_c64 = nullptr;
   float* d_c32 = nullptr;
-  Shape shape[2];  // indexed by precision
+  Shape shape[2];  // indexed by precision: the shape of large batches
+  // shapes tuned for smaller batches: (rows they were tuned at, shape),
+  // ascending; a launch takes the one nearest its row count (log scale)
+  std::vector<std::pair<int64_t, Shape>> sized[2];
+  // float64 re-contraction of the few flagged rows: latency matters, so one
+  // syndrome per block with the most threads and the tables staged
+  Shape recheck_shape;
   DevBuf arena[2];
   DevBuf syn, cls, logp, err, list, count;
   int32_t* h_count = nullptr;  // pinned
@@ -175,8 +181,18 @@ int choose_shape(tqec_program* p, int precision, int G_req, int threads_req, int
   return TQEC_OK;
 }
 
-int ensure_arena(tqec_program* p, int precision, int grid) {
-  const Shape& s = p->shape[precision];
+// The launch shape for a batch of n rows.
+const Shape& pick_shape(const tqec_program* p, int precision, int64_t n) {
+  const auto& v = p->sized[precision];
+  for (size_t i = 0; i < v.size(); ++i) {
+    // boundary: geometric mean of this size and the next larger one
+    const double next = i + 1 < v.size() ? double(v[i + 1].first) : double(v[i].first) * 4.0;
+    if (double(n) * double(n) <= double(v[i].first) * next) return v[i].second;
+  }
+  return p->shape[precision];
+}
+
+int ensure_arena(tqec_program* p, int precision, const Shape& s, int grid) {
   if (s.smem_arena) return TQEC_OK;
   const size_t esz = precision == TQEC_F32 ? 4 : 8;
   const size_t want = size_t(grid) * s.G * size_t(p->plan.arena_elems) * esz;
@@ -218,12 +234,20 @@ tqec::KArgs base_args(tqec_program* p, int precision) {
   return a;
 }
 
-int launch_rows(tqec_program* p, int precision, tqec::KArgs a, int64_t n_rows_max, cudaStream_t st) {
-  const Shape& s = p->shape[precision];
+// Launches the batched kernel over up to n_rows_max rows with the shape
+// tuned for that many rows (`forced`: that shape instead).
+int launch_rows(tqec_program* p, int precision, tqec::KArgs a, int64_t n_rows_max, cudaStream_t st,
+                const Shape* forced = nullptr) {
+  const Shape& s = forced ? *forced : pick_shape(p, precision, n_rows_max);
   int64_t want = (n_rows_max + s.G - 1) / s.G;
   int grid = (int)std::max<int64_t>(1, std::min<int64_t>(want, s.grid_cap));
-  int rc = ensure_arena(p, precision, grid);
+  int rc = ensure_arena(p, precision, s, grid);
   if (rc) return rc;
+  a.G = s.G;
+  a.lg = 0;
+  while ((1 << a.lg) < s.G) a.lg++;
+  a.tables_smem = s.smem_tables ? 1 : 0;
+  a.perm16 = s.smem_tables ? p->d_perm16 : nullptr;
   a.arena_global = s.smem_arena ? nullptr : p->arena[precision].p;
   TQ_CUDA(tqec::contract_launch(precision, a, grid, s.threads, s.smem, st));
   return TQEC_OK;
@@ -351,7 +375,7 @@ int decode_locked(tqec_program* p, const uint8_t* syn, int64_t n, int32_t* cls, 
       b.class_out = a.class_out;
       b.logp_out = s.d_logp;
       b.err_out = s.d_err;
-      rc = launch_rows(p, TQEC_F64, b, n, st);
+      rc = launch_rows(p, TQEC_F64, b, n, st, &p->recheck_shape);
       if (rc) return rc;
       TQ_CUDA(cudaMemcpyAsync(p->h_count, p->count.p, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
     }
@@ -482,6 +506,10 @@ int tqec_program_create(const tqec_network* net, const tqec_tree* tree, const tq
     std::string m = g_last_error;
     return bail(rc, m);
   }
+  if ((rc = choose_shape(p, TQEC_F64, 1, tqec::contract_max_threads(TQEC_F64), 1, &p->recheck_shape)) != TQEC_OK) {
+    std::string m = g_last_error;
+    return bail(rc, m);
+  }
   *out = p;
   return TQEC_OK;
 }
@@ -526,6 +554,10 @@ int tqec_program_info(const tqec_program* p, tqec_program_info_t* info) {
   info->group_f64 = p->shape[TQEC_F64].G;
   info->threads_f64 = p->shape[TQEC_F64].threads;
   info->smem_f64 = (int32_t)p->shape[TQEC_F64].smem;
+  info->resident_f32 = p->shape[TQEC_F32].grid_cap;
+  info->resident_f64 = p->shape[TQEC_F64].grid_cap;
+  info->tables_smem_f32 = p->shape[TQEC_F32].smem_tables ? 1 : 0;
+  info->tables_smem_f64 = p->shape[TQEC_F64].smem_tables ? 1 : 0;
   return TQEC_OK;
 }
 
@@ -601,6 +633,58 @@ int tqec_last_recheck_count(const tqec_program* p, int64_t* count) {
   return TQEC_OK;
 }
 
+namespace {
+
+// The fastest launch shape for batches of n rows (the probe syndromes are
+// already on the device).  Returns false if a launch failed.
+bool tune_shape(tqec_program* p, int prec, int64_t n, cudaEvent_t e0, cudaEvent_t e1, Shape* out) {
+  Shape best = p->shape[prec];
+  float best_ms = 1e30f;
+  for (int G : {1, 2, 4, 8, 16, 32, 64, 128}) {
+    if (G > 1 && G > n) break;
+    for (int th : {128, 256, 512, 1024}) {
+      if (th > tqec::contract_max_threads(prec)) continue;
+      for (int tables : {0, 1}) {
+        // global-arena shapes also try fewer resident blocks per SM, so that
+        // the arenas in flight can stay in L2
+        for (int resident : {0, 8, 4, 2}) {
+          Shape s;
+          if (choose_shape(p, prec, G, th, tables, &s) != TQEC_OK) continue;
+          if (tables && !s.smem_tables) continue;
+          if (resident) {
+            if (s.smem_arena || tables || resident * p->sm_count >= s.grid_cap) continue;
+            s.grid_cap = resident * p->sm_count;
+          }
+          // a global arena bigger than 4 GB is not worth probing on a shared GPU
+          const size_t esz = prec == TQEC_F32 ? 4 : 8;
+          if (!s.smem_arena &&
+              (G > 8 || size_t(s.grid_cap) * G * size_t(p->plan.arena_elems) * esz > (size_t(4) << 30)))
+            continue;
+          tqec::KArgs a = base_args(p, prec);
+          a.syn = (const uint8_t*)p->syn.p;
+          a.n = n;
+          a.logp_out = (double*)p->logp.p;
+          if (launch_rows(p, prec, a, n, p->stream, &s) != TQEC_OK) continue;  // warm-up
+          cudaEventRecord(e0, p->stream);
+          launch_rows(p, prec, a, n, p->stream, &s);
+          cudaEventRecord(e1, p->stream);
+          if (cudaEventSynchronize(e1) != cudaSuccess) return false;
+          float ms = 0.f;
+          cudaEventElapsedTime(&ms, e0, e1);
+          if (ms < best_ms) {
+            best_ms = ms;
+            best = s;
+          }
+        }
+      }
+    }
+  }
+  *out = best;
+  return true;
+}
+
+}  // namespace
+
 int tqec_program_autotune(tqec_program* p, int64_t n_probe) {
   if (!p || n_probe <= 0) return fail(TQEC_ERR_INVALID, "bad argument");
   std::lock_guard<std::mutex> lk(p->mu);
@@ -618,47 +702,25 @@ int tqec_program_autotune(tqec_program* p, int64_t n_probe) {
   cudaEvent_t e0, e1;
   TQ_CUDA(cudaEventCreate(&e0));
   TQ_CUDA(cudaEventCreate(&e1));
+  bool ok = true;
   for (int prec : {TQEC_F32, TQEC_F64}) {
-    Shape best = p->shape[prec];
-    float best_ms = 1e30f;
-    for (int G : {1, 2, 4, 8, 16, 32, 64, 128}) {
-      for (int th : {128, 256, 512, 1024}) {
-       if (th > tqec::contract_max_threads(prec)) continue;
-       for (int tables : {0, 1}) {
-        Shape s;
-        if (choose_shape(p, prec, G, th, tables, &s) != TQEC_OK) continue;
-        if (tables && !s.smem_tables) continue;
-        // a global arena bigger than 4 GB is not worth probing on a shared GPU
-        const size_t esz = prec == TQEC_F32 ? 4 : 8;
-        if (!s.smem_arena && (G > 8 || size_t(s.grid_cap) * G * size_t(p->plan.arena_elems) * esz > (size_t(4) << 30)))
-          continue;
-        p->shape[prec] = s;
-        tqec::KArgs a = base_args(p, prec);
-        a.syn = (const uint8_t*)p->syn.p;
-        a.n = n;
-        a.logp_out = (double*)p->logp.p;
-        if (launch_rows(p, prec, a, n, p->stream) != TQEC_OK) continue;  // warm-up
-        cudaEventRecord(e0, p->stream);
-        launch_rows(p, prec, a, n, p->stream);
-        cudaEventRecord(e1, p->stream);
-        if (cudaEventSynchronize(e1) != cudaSuccess) {
-          cudaEventDestroy(e0);
-          cudaEventDestroy(e1);
-          return fail(TQEC_ERR_CUDA, "autotune launch failed");
-        }
-        float ms = 0.f;
-        cudaEventElapsedTime(&ms, e0, e1);
-        if (ms < best_ms) {
-          best_ms = ms;
-          best = s;
-        }
-       }
-      }
+    // large batches at n rows; smaller batches (down to 1/64 of it, at
+    // least 256 rows) get shapes of their own
+    Shape big;
+    ok = ok && tune_shape(p, prec, n, e0, e1, &big);
+    std::vector<std::pair<int64_t, Shape>> sized;
+    for (int64_t m = n / 4; ok && m >= 256 && m >= n / 64; m /= 4) {
+      Shape sm;
+      ok = ok && tune_shape(p, prec, m, e0, e1, &sm);
+      sized.insert(sized.begin(), {m, sm});
     }
-    p->shape[prec] = best;
+    if (!ok) break;
+    p->shape[prec] = big;
+    p->sized[prec] = sized;
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
+  if (!ok) return fail(TQEC_ERR_CUDA, "autotune launch failed");
   g_last_error.clear();
   return TQEC_OK;
 }

@@ -188,6 +188,58 @@ __global__ void gate_kernel(const float* __restrict__ logits, int ldl, int64_t n
   if (list && !(p >= thr)) list[atomicAdd(count, 1)] = int32_t(r);
 }
 
+// One warp per row: lanes split k in chunks of 8 (one 16-byte load of the
+// activation row per chunk), every class's partial sum is reduced over the
+// warp.  The weights (N x K) sit in shared memory.
+template <int NC>
+__global__ void __launch_bounds__(256) small_out_kernel(int M, int N, int K, const __nv_bfloat16* __restrict__ A,
+                                                        int lda, const __nv_bfloat16* __restrict__ W, int ldw,
+                                                        const float* __restrict__ bias, float* __restrict__ C,
+                                                        int ldc) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __nv_bfloat16* sw = reinterpret_cast<__nv_bfloat16*>(smem_raw);
+  for (int i = threadIdx.x; i < N * (K / 8); i += blockDim.x) {
+    const int c = i / (K / 8), j = i % (K / 8);
+    reinterpret_cast<uint4*>(sw + c * K)[j] = *reinterpret_cast<const uint4*>(W + int64_t(c) * ldw + 8 * j);
+  }
+  __syncthreads();
+  const int lane = threadIdx.x & 31;
+  const int64_t warps = int64_t(gridDim.x) * (blockDim.x >> 5);
+  for (int64_t r = int64_t(blockIdx.x) * (blockDim.x >> 5) + (threadIdx.x >> 5); r < M; r += warps) {
+    float acc[NC];
+#pragma unroll
+    for (int c = 0; c < NC; ++c) acc[c] = 0.f;
+    const __nv_bfloat16* a = A + r * lda;
+    for (int k0 = 8 * lane; k0 < K; k0 += 256) {
+      const uint4 av = *reinterpret_cast<const uint4*>(a + k0);
+      const __nv_bfloat162* a2 = reinterpret_cast<const __nv_bfloat162*>(&av);
+      float2 af[4];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) af[j] = __bfloat1622float2(a2[j]);
+#pragma unroll
+      for (int c = 0; c < NC; ++c) {
+        if (c >= N) break;
+        const uint4 wv = *reinterpret_cast<const uint4*>(sw + c * K + k0);
+        const __nv_bfloat162* w2 = reinterpret_cast<const __nv_bfloat162*>(&wv);
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          const float2 wf = __bfloat1622float2(w2[j]);
+          acc[c] = fmaf(af[j].x, wf.x, acc[c]);
+          acc[c] = fmaf(af[j].y, wf.y, acc[c]);
+        }
+      }
+    }
+#pragma unroll
+    for (int c = 0; c < NC; ++c) {
+      if (c >= N) break;
+      float v = acc[c];
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+      if (lane == c) C[r * ldc + c] = v + (bias ? bias[c] : 0.f);
+    }
+  }
+}
+
 __global__ void gather_kernel(const uint8_t* __restrict__ src, int row_bytes, const int32_t* __restrict__ list,
                               int64_t n, uint8_t* __restrict__ dst) {
   const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
@@ -232,6 +284,29 @@ cudaError_t gemm_bf16(bool a_kmajor, bool b_kmajor, int epi, int M, int N, int K
     return cudaErrorInvalidValue;
   }
 #undef TQ_GEMM
+  return cudaGetLastError();
+}
+
+bool small_out_supported(int N, int K, int lda, int ldw) {
+  return N >= 1 && N <= 16 && K % 8 == 0 && lda % 8 == 0 && ldw % 8 == 0 && size_t(N) * K * 2 <= 96 * 1024;
+}
+
+cudaError_t small_out_gemm(int M, int N, int K, const __nv_bfloat16* A, int lda, const __nv_bfloat16* W, int ldw,
+                           const float* bias, float* C, int ldc, cudaStream_t st) {
+  if (M <= 0) return cudaSuccess;
+  if (!small_out_supported(N, K, lda, ldw)) return cudaErrorInvalidValue;
+  const size_t smem = size_t(N) * K * 2;
+  int dev = 0, sms = 1;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const unsigned grid = unsigned(std::min<int64_t>((int64_t(M) + 7) / 8, int64_t(sms) * 8));
+  if (N <= 4) {
+    cudaFuncSetAttribute(small_out_kernel<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+    small_out_kernel<4><<<grid, 256, smem, st>>>(M, N, K, A, lda, W, ldw, bias, C, ldc);
+  } else {
+    cudaFuncSetAttribute(small_out_kernel<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+    small_out_kernel<16><<<grid, 256, smem, st>>>(M, N, K, A, lda, W, ldw, bias, C, ldc);
+  }
   return cudaGetLastError();
 }
 

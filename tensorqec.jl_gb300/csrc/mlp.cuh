@@ -22,6 +22,13 @@ cudaError_t gemm_bf16(bool a_kmajor, bool b_kmajor, int epi, int M, int N, int K
                       int lda, const __nv_bfloat16* B, int ldb, void* C, int ldc, const float* bias,
                       const __nv_bfloat16* H, int ldh, int split_k, cudaStream_t st);
 
+// Output layer with few classes: C[m, c] = bias[c] + sum_k A[m*lda + k] *
+// W[c*ldw + k] (float), one warp per row, W staged in shared memory.
+// Needs N <= 16, K a multiple of 8 and lda, ldw multiples of 8.
+bool small_out_supported(int N, int K, int lda, int ldw);
+cudaError_t small_out_gemm(int M, int N, int K, const __nv_bfloat16* A, int lda, const __nv_bfloat16* W, int ldw,
+                           const float* bias, float* C, int ldc, cudaStream_t st);
+
 cudaError_t unpack_syndromes_bf16(const uint8_t* syn, int64_t n, int syn_bytes, int n_bits, __nv_bfloat16* X,
                                   int ldx, cudaStream_t st);
 

@@ -170,6 +170,10 @@ int forward(tqec_mlp* p, const uint8_t* dsyn, int64_t n, cudaStream_t st) {
                                 p->din[l], p->H[l], p->cfg.hidden, b, nullptr, 0, 1, st));
       x = p->H[l];
       ldx = p->cfg.hidden;
+    } else if (tqec::small_out_supported(p->dout[l], p->din[l], ldx, p->din[l])) {
+      // few classes: a row-per-warp kernel instead of a mostly empty GEMM tile
+      SQ_CUDA(tqec::small_out_gemm((int)n, p->dout[l], p->din[l], x, ldx, W, p->din[l], b, p->logits, p->out_pad,
+                                   st));
     } else {
       SQ_CUDA(tqec::gemm_bf16(true, true, tqec::EPI_BIAS_F32, (int)n, p->dout[l], p->din[l], x, ldx, W, p->din[l],
                               p->logits, p->out_pad, b, nullptr, 0, 1, st));

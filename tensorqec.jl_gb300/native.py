@@ -51,7 +51,9 @@ class ProgramInfo(C.Structure):
                 ("arena_elems", C.c_int64), ("flops_per_syndrome", C.c_double), ("flops_tree", C.c_double),
                 ("err_bound_f32", C.c_double), ("err_bound_f64", C.c_double),
                 ("group_f32", C.c_int32), ("threads_f32", C.c_int32), ("smem_f32", C.c_int32),
-                ("group_f64", C.c_int32), ("threads_f64", C.c_int32), ("smem_f64", C.c_int32)]
+                ("group_f64", C.c_int32), ("threads_f64", C.c_int32), ("smem_f64", C.c_int32),
+                ("resident_f32", C.c_int32), ("resident_f64", C.c_int32), ("tables_smem_f32", C.c_int32),
+                ("tables_smem_f64", C.c_int32)]
 
 
 class PlanView(C.Structure):
