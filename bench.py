@@ -383,6 +383,8 @@ def run_ours(args):
         gpu_cls = gd.decode_packed(sub) if gd is not None else ct.program.decode_packed(sub)
         mismatch = float(np.mean(gpu_cls != cpu_cls))
         traffic = read_traffic()
+        sm_count = torch.cuda.get_device_properties(local).multi_processor_count
+        fp32_peak = sm_count * 128 * 2 * (clk.get("sm_mhz") or 2070.0) * 1e6 / 1e12
         evaluation = surrogate_eval(pkg, ct, gd, args.eval_n, SEED + 41) if gd is not None else None
         # launches per step: gated = unpack, 4 GEMMs, gate, gather, 2 contraction, scatter
         per_step = 10 if gd is not None else 2
@@ -398,7 +400,13 @@ def run_ours(args):
                          "frac": achieved_tflops / bf16_peak, "traffic": traffic,
                          "kernel": "tn_contract_kernel<float> (SIMT float32; peak is the measured bf16 "
                                    f"tensor rate, {peak_kind})",
-                         "flops_per_syndrome": flops, "kernel_ms": kernel_ms},
+                         "flops_per_syndrome": flops, "kernel_ms": kernel_ms,
+                         # the float32 FMA pipes this kernel actually runs on: 152 SMs x 128 lanes x 2
+                         # flops per cycle at the sampled SM clock (nominal, not measured)
+                         "fp32_simt_peak_tflops": fp32_peak,
+                         "frac_of_fp32_simt_peak": achieved_tflops / fp32_peak,
+                         "traffic_note": "dram read+write of the autotuned global-arena shape, per 65,536 "
+                                         "syndromes (ncu, scaled from 16,384)"},
             "surrogate_gemm": mlp_part,
             "cpu_baseline": cpu,
             "clocks": clk,
