@@ -44,6 +44,9 @@ def parse():
     ap.add_argument("--profile", action="store_true",
                     help="one float32 contraction launch of --batch syndromes (for ncu), no timing")
     ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--precision-sweep", action="store_true",
+                    help="float32 vs float64 log-probability error and decision mismatch over d in {5,7} and "
+                         "p in {0.02,0.05,0.08,0.11}, one JSON line per (d,p)")
     ap.add_argument("--group", type=int, default=0, help="--profile: syndromes per block (0: default shape)")
     ap.add_argument("--threads", type=int, default=0, help="--profile: threads per block (0: default shape)")
     ap.add_argument("--no-surrogate", action="store_true", help="time the batched exact decoder alone")
@@ -447,9 +450,76 @@ def run_profile(args):
     ct.close()
 
 
+def run_precision_sweep(args):
+    """Per (d, p): --batch seeded syndromes contracted in one float32 launch
+    (power-of-two renormalised) and in float64; reports the class
+    log-probability error of float32 against float64, its bound, the decision
+    mismatch before and after the float64 recheck, and float32 syndromes/s."""
+    import torch
+
+    import __graft_entry__ as G
+
+    pkg = G.load_package()
+    native = pkg.native
+    B = args.batch
+    stream = torch.cuda.current_stream()
+    for d in (5, 7):
+        for p in (0.02, 0.05, 0.08, 0.11):
+            t = pkg.tanner_graph(pkg.SurfaceCode(d, d))
+            em = pkg.depolarizing(p, t.nq)
+            rng = np.random.default_rng(SEED + 1000 * d + int(round(p * 100)))
+            ep = pkg.random_error_pattern(em, rng, nsamples=B)
+            s = pkg.syndrome_extraction(ep, t)
+            packed = pkg.pack_syndromes(np.concatenate([s.sx, s.sz], axis=1))
+            ct = pkg.compile(pkg.TNMMAP(precision="f32"), t, em)
+            ct.program.autotune(min(B, 16384))
+            info = ct.program.info
+            d_syn = torch.from_numpy(packed).cuda()
+            lp = {}
+            ms = {}
+            for prec, code in (("f32", native.TQEC_F32), ("f64", native.TQEC_F64)):
+                d_lp = torch.empty((B, info["n_classes"]), dtype=torch.float64, device="cuda")
+                ct.program.contract_ptrs(d_syn.data_ptr(), B, code, d_lp.data_ptr(), stream.cuda_stream)
+                torch.cuda.synchronize()
+                a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                a.record(stream)
+                ct.program.contract_ptrs(d_syn.data_ptr(), B, code, d_lp.data_ptr(), stream.cuda_stream)
+                b.record(stream)
+                torch.cuda.synchronize()
+                ms[prec] = a.elapsed_time(b)
+                lp[prec] = d_lp.cpu().numpy()
+            l32, l64 = lp["f32"], lp["f64"]
+            fin = np.isfinite(l64)
+            # error relative to the row's largest class probability, in log space
+            err = np.abs(np.where(fin, l32 - l64, 0.0))
+            top = np.max(np.where(fin, l64, -np.inf), axis=1, keepdims=True)
+            rel = np.where(fin, np.abs(np.exp(l32 - top) - np.exp(l64 - top)), 0.0)
+            c32 = np.argmax(l32, axis=1)
+            c64 = np.argmax(l64, axis=1)
+            srt = np.sort(l64, axis=1)
+            tie = (srt[:, -1] - srt[:, -2]) <= 1e-9
+            gated = ct.program.decode_packed(packed)  # float32 + float64 recheck
+            line = {"sweep": "precision", "d": d, "p": p, "syndromes": B, "flops_per_syndrome": info["flops_per_syndrome"],
+                    "f32_ms": ms["f32"], "f32_syn_per_s": B / (ms["f32"] / 1e3), "f64_ms": ms["f64"],
+                    "f64_syn_per_s": B / (ms["f64"] / 1e3),
+                    "max_abs_logp_err_f32": float(err[fin].max()) if fin.any() else 0.0,
+                    "max_rel_prob_err_f32": float(rel.max()),
+                    "rounding_bound_f32": info["err_bound_f32"],
+                    "mismatch_f32_no_recheck": float(np.mean((c32 != c64) & ~tie)),
+                    "mismatch_after_recheck": float(np.mean((gated != c64) & ~tie)),
+                    "recheck_fraction": ct.program.last_recheck_count() / B,
+                    "ties": float(np.mean(tie)),
+                    "bf16": "not offered: an 8-bit significand puts the rounding bound "
+                            f"{info['err_bound_f32'] * 2 ** 16:.2f} (relative) above any class margin"}
+            print(json.dumps(line), flush=True)
+            ct.close()
+
+
 def main():
     args = parse()
-    if args.profile:
+    if args.precision_sweep:
+        run_precision_sweep(args)
+    elif args.profile:
         run_profile(args)
     elif args.impl == "reference":
         run_reference(args)
