@@ -332,6 +332,33 @@ int tqec_last_error(char* buf, size_t len);
 /* Library version string, e.g. "tqec-gb300 0.1.0 sm_103a". */
 const char* tqec_version(void);
 
+/* ---- several programs in one persistent launch (uneven code sizes) ------
+ * No reference counterpart (the reference decodes one syndrome of one code at
+ * a time).  A batch is a set of rows of every program; decoding it is one
+ * float32 persistent launch over all programs' row groups (largest programs
+ * first), one float64 launch over the rows whose margin is inside the float32
+ * bound, and a counter update, with no host synchronisation and no
+ * allocation: one tqec_multi_launch can be captured into a CUDA graph and the
+ * graph replayed once per batch.  The programs' own launch shapes are not
+ * used; MAP programs are rejected. */
+typedef struct tqec_multi tqec_multi;
+
+int tqec_multi_create(tqec_program* const* progs, int32_t n_progs, tqec_multi** out);
+int tqec_multi_destroy(tqec_multi* m);
+/* batch_end_rows[b * n_progs + i]: end (exclusive) of batch b's rows of
+ * program i, non-decreasing in b (batch 0 starts at row 0).  syndromes[i]:
+ * device pointer to program i's bit-packed rows; class_out[i]: device int32
+ * per row.  The buffers must stay valid while batches are decoded. */
+int tqec_multi_set_work(tqec_multi* m, int32_t n_batches, const int64_t* batch_end_rows,
+                        const uint8_t* const* syndromes, int32_t* const* class_out);
+/* the next launch decodes batch 0 (stream-ordered) */
+int tqec_multi_reset(tqec_multi* m, void* stream);
+/* decodes the next batch on `stream`; past the last batch it does nothing */
+int tqec_multi_launch(tqec_multi* m, void* stream);
+/* per program: syndromes per block and whether its arena is in shared memory;
+ * and the float32 grid */
+int tqec_multi_info(const tqec_multi* m, int32_t* groups, int32_t* arena_in_smem, int32_t* grid);
+
 #ifdef __cplusplus
 }
 #endif

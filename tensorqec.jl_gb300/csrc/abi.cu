@@ -404,6 +404,29 @@ int program_f64_view(tqec_program* p, ProgramF64View* v) {
   return TQEC_OK;
 }
 
+int program_multi_view(tqec_program* p, ProgramMultiView* v) {
+  if (!p || !v) return TQEC_ERR_INVALID;
+  for (int prec : {TQEC_F32, TQEC_F64}) {
+    KArgs a = base_args(p, prec);
+    a.arena_global = nullptr;
+    a.tables_smem = 0;
+    a.perm16 = nullptr;
+    (prec == TQEC_F32 ? v->args32 : v->args64) = a;
+  }
+  v->device = p->device;
+  v->sm_count = p->sm_count;
+  v->arena_elems = p->plan.arena_elems;
+  v->width = p->plan.width;
+  v->n_steps = (int)p->plan.steps.size();
+  v->syn_words = syn_words(p);
+  v->syndrome_bytes = p->plan.syndrome_bytes;
+  v->n_classes = p->plan.n_classes;
+  v->map_mode = p->plan.map_mode;
+  v->flops_per_syndrome = 2.0 * p->plan.macs_runtime;
+  v->recheck_margin = p->margin >= 0.0 ? p->margin : 2.0 * err_bound(p, TQEC_F32);
+  return TQEC_OK;
+}
+
 }  // namespace tqec
 
 extern "C" {
@@ -647,7 +670,7 @@ bool tune_shape(tqec_program* p, int prec, int64_t n, cudaEvent_t e0, cudaEvent_
       for (int tables : {0, 1}) {
         // global-arena shapes also try fewer resident blocks per SM, so that
         // the arenas in flight can stay in L2
-        for (int resident : {0, 8, 4, 2}) {
+        for (int resident : {0, 8, 4, 2, 1}) {
           Shape s;
           if (choose_shape(p, prec, G, th, tables, &s) != TQEC_OK) continue;
           if (tables && !s.smem_tables) continue;

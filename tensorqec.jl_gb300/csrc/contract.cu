@@ -679,149 +679,250 @@ __device__ __forceinline__ int dispatch_step(const KArgs& a, const StepDesc& d, 
 }
 
 // float64 blocks are capped at 512 threads, which leaves them 128 registers
+// Shared-memory layout of a block working on program `a`: step records,
+// syndrome words, per-step maxima (float32), MAP assignments, then the
+// staged tables (if any) and the arena (if in shared memory).
+struct BlockSmem {
+  StepDesc* steps;
+  uint32_t* syn;
+  uint32_t* max;
+  uint32_t* asg;
+  size_t tail;  // first free byte (16-byte aligned)
+};
+
+template <bool NORM, bool MAXP>
+__device__ __forceinline__ BlockSmem carve_smem(const KArgs& a, unsigned char* smem) {
+  BlockSmem b;
+  b.steps = reinterpret_cast<StepDesc*>(smem);
+  size_t off = size_t(a.n_steps) * sizeof(StepDesc);
+  b.syn = reinterpret_cast<uint32_t*>(smem + off);
+  off += size_t(a.G) * a.syn_words * 4;
+  b.max = reinterpret_cast<uint32_t*>(smem + off);
+  if (NORM) off += size_t(a.G) * a.n_steps * 4;
+  b.asg = reinterpret_cast<uint32_t*>(smem + off);
+  if (MAXP) off += size_t(a.G) * a.var_words * 4;
+  b.tail = (off + 15) & ~size_t(15);
+  return b;
+}
+
+__device__ __forceinline__ void copy16(void* dst, const void* src, size_t bytes) {
+  const int4* s = reinterpret_cast<const int4*>(src);
+  int4* d = reinterpret_cast<int4*>(dst);
+  const int n16 = int(bytes / 16);
+  for (int i = threadIdx.x; i < n16; i += blockDim.x) d[i] = s[i];
+}
+
+// One group of up to G syndromes (rows base .. base+G-1 below nrows) through
+// the whole program: load the syndrome words, run every step, back-track
+// (MAP), then the epilogue.  Ends with a block barrier.
+template <typename T, bool NORM, bool MAXP>
+__device__ void contract_group(const KArgs& a, int64_t base, int64_t nrows, const BlockSmem& sm, T* arena,
+                               const T* consts, const PermTab& ptab) {
+  const StepDesc* s_steps = sm.steps;
+  uint32_t* s_syn = sm.syn;
+  uint32_t* s_max = sm.max;
+  for (int i = threadIdx.x; i < a.G * a.syn_words; i += blockDim.x) {
+    const int g = i / a.syn_words, w = i - g * a.syn_words;
+    const int64_t r = base + g;
+    uint32_t word = 0;
+    if (r < nrows) {
+      const int64_t row = a.list ? int64_t(a.list[r]) : r + a.row_offset;
+      const uint8_t* p = a.syn + row * a.syn_bytes;
+      for (int b = 0; b < 4; ++b) {
+        const int byte = 4 * w + b;
+        if (byte < a.syn_bytes) word |= uint32_t(p[byte]) << (8 * b);
+      }
+    }
+    s_syn[i] = word;
+  }
+  if (NORM)
+    for (int i = threadIdx.x; i < a.G * a.n_steps; i += blockDim.x) s_max[i] = 0u;
+  __syncthreads();
+  int item_base = 0;
+  for (int st = 0; st < a.n_steps; ++st) {
+    const StepDesc& d = s_steps[st];
+    const int4 q = *reinterpret_cast<const int4*>(&d.lh);  // lh, lfa, lfb, lk
+    const int bd = int(blockDim.x);
+    const StepShape sh = step_shape<T>(q.x, q.y, q.z, q.w, a.lg);
+    // a step that fills the block for each syndrome alone runs the block's
+    // syndromes one after another with hoisted invariants (every thread
+    // takes part)
+    const StepShape sh1 = a.G > 1 ? step_shape<T>(q.x, q.y, q.z, q.w, 0) : sh;
+    const bool per_syndrome = a.G > 1 && sh1.total_r >= bd;
+    const int items = per_syndrome ? bd : sh.total_r;
+    // first virtual thread of this warp (steps of a barrier group start on
+    // different warps); a warp past the step's items goes to the barrier
+    const int vt_warp = (int(threadIdx.x & ~31u) + bd - item_base % bd) % bd;
+    if (vt_warp < items) {
+      if (a.G == 1) {
+        dispatch_step<T, NORM, MAXP, true>(a, d, sh, st, item_base, s_syn, s_max, arena, consts, ptab);
+      } else if (per_syndrome) {
+        for (int g = 0; g < a.G; ++g)
+          dispatch_step<T, NORM, MAXP, true>(a, d, sh1, st, item_base, s_syn + g * a.syn_words,
+                                             s_max + g * a.n_steps, arena + int64_t(g) * a.arena_elems, consts,
+                                             ptab);
+      } else {
+        dispatch_step<T, NORM, MAXP, false>(a, d, sh, st, item_base, s_syn, s_max, arena, consts, ptab);
+      }
+    }
+    if (d.flags & kStepSync) {
+      __syncthreads();
+      item_base = 0;
+    } else {
+      item_base += items;
+    }
+  }
+  if (MAXP) {
+    backtrack<T>(a, s_steps, s_syn, sm.asg, arena, consts, base, nrows);
+    __syncthreads();
+  }
+  // epilogue: log-marginals, first argmax (Julia findmax order), recheck flag
+  const StepDesc& root = s_steps[a.n_steps - 1];
+  for (int g = threadIdx.x; g < a.G; g += blockDim.x) {
+    const int64_t r = base + g;
+    if (r >= nrows) continue;
+    const int64_t row = a.list ? int64_t(a.list[r]) : r + a.row_offset;
+    const T* rv = arena + int64_t(g) * a.arena_elems;
+    double lsc = 0.0;
+    if (NORM) {
+      for (int st = 0; st < a.n_steps - 1; ++st) {
+        int ee;
+        norm_factor(s_max[g * a.n_steps + st], &ee);
+        lsc += double(ee);
+      }
+      lsc *= 0.69314718055994530942;
+    }
+    double best = -INFINITY, second = -INFINITY;
+    int bc = 0;
+    for (int c = 0; c < a.n_classes; ++c) {
+      const double v = double(rv[root.out_off + c]);
+      const double lp = v > 0.0 ? log(v) + lsc : -INFINITY;
+      if (a.logp_out) a.logp_out[row * a.n_classes + c] = lp;
+      if (lp > best) {
+        second = best;
+        best = lp;
+        bc = c;
+      } else if (lp > second) {
+        second = lp;
+      }
+    }
+    if (a.class_out) a.class_out[row] = bc;
+    if (a.err_out) a.err_out[row] = a.err_bound;
+    if (a.recheck_margin >= 0.0) {
+      const double margin = best - second;
+      if (!(margin >= a.recheck_margin) || best == -INFINITY) {
+        const int slot = atomicAdd(a.recheck_count, 1);
+        a.recheck_list[slot] = int32_t(row);
+      }
+    }
+  }
+  __syncthreads();
+}
+
+// Stages the program's tables (if requested) after the fixed layout; returns
+// the constants, the permutation tables and the shared arena pointer.
+template <typename T>
+__device__ __forceinline__ void stage_tables(const KArgs& a, unsigned char* smem, size_t* off, const T** consts,
+                                             PermTab* ptab) {
+  *consts = reinterpret_cast<const T*>(a.consts);
+  *ptab = PermTab{a.perm, false};
+  if (!a.tables_smem) return;
+  T* s_consts = reinterpret_cast<T*>(smem + *off);
+  *off += (size_t(a.n_consts) * sizeof(T) + 15) & ~size_t(15);
+  void* s_perm = smem + *off;
+  const size_t perm_bytes = size_t(a.n_perm) * (a.perm16 ? 2 : 4);
+  *off += (perm_bytes + 15) & ~size_t(15);
+  copy16(s_consts, a.consts, size_t(a.n_consts) * sizeof(T));
+  copy16(s_perm, a.perm16 ? static_cast<const void*>(a.perm16) : static_cast<const void*>(a.perm), perm_bytes);
+  *consts = s_consts;
+  *ptab = PermTab{s_perm, a.perm16 != nullptr};
+}
+
+// float64 blocks are capped at 512 threads, which leaves them 128 registers
 template <typename T, bool NORM, bool MAXP>
 __global__ void __launch_bounds__(sizeof(T) == 8 ? 512 : 1024) tn_contract_kernel(KArgs a) {
   extern __shared__ __align__(16) unsigned char smem[];
-  StepDesc* s_steps = reinterpret_cast<StepDesc*>(smem);
-  size_t off = size_t(a.n_steps) * sizeof(StepDesc);
-  uint32_t* s_syn = reinterpret_cast<uint32_t*>(smem + off);
-  off += size_t(a.G) * a.syn_words * 4;
-  uint32_t* s_max = reinterpret_cast<uint32_t*>(smem + off);
-  if (NORM) off += size_t(a.G) * a.n_steps * 4;
-  uint32_t* s_asg = reinterpret_cast<uint32_t*>(smem + off);
-  if (MAXP) off += size_t(a.G) * a.var_words * 4;
-  off = (off + 15) & ~size_t(15);
-  const T* consts = reinterpret_cast<const T*>(a.consts);
-  PermTab ptab{a.perm, false};
-  if (a.tables_smem) {
-    // constants and permutation tables move to shared memory once per block
-    T* s_consts = reinterpret_cast<T*>(smem + off);
-    off += (size_t(a.n_consts) * sizeof(T) + 15) & ~size_t(15);
-    void* s_perm = smem + off;
-    const size_t perm_bytes = size_t(a.n_perm) * (a.perm16 ? 2 : 4);
-    off += (perm_bytes + 15) & ~size_t(15);
-    {
-      const int4* src = reinterpret_cast<const int4*>(a.consts);
-      int4* dst = reinterpret_cast<int4*>(s_consts);
-      const int n16 = int(size_t(a.n_consts) * sizeof(T) / 16);
-      for (int i = threadIdx.x; i < n16; i += blockDim.x) dst[i] = src[i];
-    }
-    {
-      const int4* src = a.perm16 ? reinterpret_cast<const int4*>(a.perm16) : reinterpret_cast<const int4*>(a.perm);
-      int4* dst = reinterpret_cast<int4*>(s_perm);
-      const int n16 = int(perm_bytes / 16);
-      for (int i = threadIdx.x; i < n16; i += blockDim.x) dst[i] = src[i];
-    }
-    consts = s_consts;
-    ptab = PermTab{s_perm, a.perm16 != nullptr};
-  }
+  const BlockSmem sm = carve_smem<NORM, MAXP>(a, smem);
+  size_t off = sm.tail;
+  const T* consts;
+  PermTab ptab;
+  stage_tables<T>(a, smem, &off, &consts, &ptab);
   T* arena = a.arena_global
                  ? reinterpret_cast<T*>(a.arena_global) + int64_t(blockIdx.x) * a.G * a.arena_elems
                  : reinterpret_cast<T*>(smem + off);
-  {
-    const int4* src = reinterpret_cast<const int4*>(a.steps);
-    int4* dst = reinterpret_cast<int4*>(s_steps);
-    for (int i = threadIdx.x; i < a.n_steps * int(sizeof(StepDesc) / 16); i += blockDim.x) dst[i] = src[i];
-  }
+  copy16(sm.steps, a.steps, size_t(a.n_steps) * sizeof(StepDesc));
   const int64_t nrows = a.list ? int64_t(*a.list_count) : a.n;
-  for (int64_t base = int64_t(blockIdx.x) * a.G; base < nrows; base += int64_t(gridDim.x) * a.G) {
-    for (int i = threadIdx.x; i < a.G * a.syn_words; i += blockDim.x) {
-      const int g = i / a.syn_words, w = i - g * a.syn_words;
-      const int64_t r = base + g;
-      uint32_t word = 0;
-      if (r < nrows) {
-        const int64_t row = a.list ? int64_t(a.list[r]) : r + a.row_offset;
-        const uint8_t* p = a.syn + row * a.syn_bytes;
-        for (int b = 0; b < 4; ++b) {
-          const int byte = 4 * w + b;
-          if (byte < a.syn_bytes) word |= uint32_t(p[byte]) << (8 * b);
-        }
-      }
-      s_syn[i] = word;
-    }
-    if (NORM)
-      for (int i = threadIdx.x; i < a.G * a.n_steps; i += blockDim.x) s_max[i] = 0u;
-    __syncthreads();
-    int item_base = 0;
-    for (int st = 0; st < a.n_steps; ++st) {
-      const StepDesc& d = s_steps[st];
-      const int4 q = *reinterpret_cast<const int4*>(&d.lh);  // lh, lfa, lfb, lk
-      const int bd = int(blockDim.x);
-      const StepShape sh = step_shape<T>(q.x, q.y, q.z, q.w, a.lg);
-      // a step that fills the block for each syndrome alone runs the block's
-      // syndromes one after another with hoisted invariants (every thread
-      // takes part)
-      const StepShape sh1 = a.G > 1 ? step_shape<T>(q.x, q.y, q.z, q.w, 0) : sh;
-      const bool per_syndrome = a.G > 1 && sh1.total_r >= bd;
-      const int items = per_syndrome ? bd : sh.total_r;
-      // first virtual thread of this warp (steps of a barrier group start on
-      // different warps); a warp past the step's items goes to the barrier
-      const int vt_warp = (int(threadIdx.x & ~31u) + bd - item_base % bd) % bd;
-      if (vt_warp < items) {
-        if (a.G == 1) {
-          dispatch_step<T, NORM, MAXP, true>(a, d, sh, st, item_base, s_syn, s_max, arena, consts, ptab);
-        } else if (per_syndrome) {
-          for (int g = 0; g < a.G; ++g)
-            dispatch_step<T, NORM, MAXP, true>(a, d, sh1, st, item_base, s_syn + g * a.syn_words,
-                                               s_max + g * a.n_steps, arena + int64_t(g) * a.arena_elems, consts,
-                                               ptab);
-        } else {
-          dispatch_step<T, NORM, MAXP, false>(a, d, sh, st, item_base, s_syn, s_max, arena, consts, ptab);
-        }
-      }
-      if (d.flags & kStepSync) {
-        __syncthreads();
-        item_base = 0;
-      } else {
-        item_base += items;
-      }
-    }
-    if (MAXP) {
-      backtrack<T>(a, s_steps, s_syn, s_asg, arena, consts, base, nrows);
+  for (int64_t base = int64_t(blockIdx.x) * a.G; base < nrows; base += int64_t(gridDim.x) * a.G)
+    contract_group<T, NORM, MAXP>(a, base, nrows, sm, arena, consts, ptab);
+}
+
+// Several programs in one persistent launch.  Work units (program, first
+// row) of the current batch are claimed from a device counter; each unit's
+// program descriptor and steps are copied into shared memory, then one group
+// of its rows is contracted.  With `list_mode` every program instead
+// contracts the rows of its own device-side list (the float64 recheck), block
+// by block in a grid-stride loop.
+template <typename T, bool NORM>
+__global__ void __launch_bounds__(kMultiThreads) tn_contract_multi_kernel(MultiArgs m) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  __shared__ __align__(16) KArgs s_ka;
+  __shared__ int64_t s_unit;
+  const int32_t b = *m.batch;
+  const KArgs* progs = m.progs;
+  T* gslice = m.arena_global ? reinterpret_cast<T*>(m.arena_global) + int64_t(blockIdx.x) * m.arena_per_block
+                             : nullptr;
+  auto run_unit = [&](int32_t prog, int64_t base, int64_t nrows, bool first) {
+    if (first) {
+      copy16(&s_ka, progs + prog, sizeof(KArgs));
       __syncthreads();
     }
-    // epilogue: log-marginals, first argmax (Julia findmax order), recheck flag
-    const StepDesc& root = s_steps[a.n_steps - 1];
-    for (int g = threadIdx.x; g < a.G; g += blockDim.x) {
-      const int64_t r = base + g;
-      if (r >= nrows) continue;
-      const int64_t row = a.list ? int64_t(a.list[r]) : r + a.row_offset;
-      const T* rv = arena + int64_t(g) * a.arena_elems;
-      double lsc = 0.0;
-      if (NORM) {
-        for (int st = 0; st < a.n_steps - 1; ++st) {
-          int ee;
-          norm_factor(s_max[g * a.n_steps + st], &ee);
-          lsc += double(ee);
-        }
-        lsc *= 0.69314718055994530942;
-      }
-      double best = -INFINITY, second = -INFINITY;
-      int bc = 0;
-      for (int c = 0; c < a.n_classes; ++c) {
-        const double v = double(rv[root.out_off + c]);
-        const double lp = v > 0.0 ? log(v) + lsc : -INFINITY;
-        if (a.logp_out) a.logp_out[row * a.n_classes + c] = lp;
-        if (lp > best) {
-          second = best;
-          best = lp;
-          bc = c;
-        } else if (lp > second) {
-          second = lp;
-        }
-      }
-      if (a.class_out) a.class_out[row] = bc;
-      if (a.err_out) a.err_out[row] = a.err_bound;
-      if (a.recheck_margin >= 0.0) {
-        const double margin = best - second;
-        if (!(margin >= a.recheck_margin) || best == -INFINITY) {
-          const int slot = atomicAdd(a.recheck_count, 1);
-          a.recheck_list[slot] = int32_t(row);
-        }
-      }
+    const KArgs& a = s_ka;
+    const BlockSmem sm = carve_smem<NORM, false>(a, smem);
+    if (first) {
+      copy16(sm.steps, a.steps, size_t(a.n_steps) * sizeof(StepDesc));
+      __syncthreads();
     }
-    __syncthreads();
+    T* arena = a.arena_global ? gslice : reinterpret_cast<T*>(smem + sm.tail);
+    contract_group<T, NORM, false>(a, base, nrows, sm, arena, reinterpret_cast<const T*>(a.consts),
+                                   PermTab{a.perm, false});
+  };
+  if (m.list_mode) {
+    for (int32_t prog = 0; prog < m.n_progs; ++prog) {
+      __syncthreads();
+      copy16(&s_ka, progs + prog, sizeof(KArgs));
+      __syncthreads();
+      const int64_t nrows = int64_t(*s_ka.list_count);
+      if (int64_t(blockIdx.x) * s_ka.G >= nrows) continue;  // block-uniform
+      const BlockSmem sm = carve_smem<NORM, false>(s_ka, smem);
+      copy16(sm.steps, s_ka.steps, size_t(s_ka.n_steps) * sizeof(StepDesc));
+      __syncthreads();
+      for (int64_t base = int64_t(blockIdx.x) * s_ka.G; base < nrows; base += int64_t(gridDim.x) * s_ka.G)
+        run_unit(prog, base, nrows, false);
+    }
+    return;
   }
+  if (b < 0 || b >= m.n_batches) return;
+  const int64_t u0 = m.unit_offsets[b], u1 = m.unit_offsets[b + 1];
+  int32_t cur = -1;
+  for (;;) {
+    if (threadIdx.x == 0) s_unit = u0 + atomicAdd(m.next_unit, 1);
+    __syncthreads();
+    const int64_t u = s_unit;
+    if (u >= u1) break;
+    const MultiUnit w = m.units[u];
+    const int64_t nrows = m.batch_rows[int64_t(b) * m.n_progs + w.prog];
+    run_unit(w.prog, w.first_row, nrows, w.prog != cur);
+    cur = w.prog;
+  }
+}
+
+__global__ void multi_advance_kernel(int32_t* batch, int32_t* next_unit, int32_t* counts, int32_t n_progs) {
+  const int i = threadIdx.x;
+  if (i == 0) {
+    *batch += 1;
+    *next_unit = 0;
+  }
+  for (int p = i; p < n_progs; p += blockDim.x) counts[p] = 0;
 }
 
 }  // namespace
@@ -884,6 +985,29 @@ cudaError_t contract_launch(int precision, const KArgs& a, int grid, int threads
                       : launch_with(tn_contract_kernel<float, true, false>, a, grid, threads, smem, stream);
   return a.map_mode ? launch_with(tn_contract_kernel<double, false, true>, a, grid, threads, smem, stream)
                     : launch_with(tn_contract_kernel<double, false, false>, a, grid, threads, smem, stream);
+}
+
+// Sets the shared-memory limit (outside any stream capture) and returns the
+// resident blocks per SM.
+int contract_multi_occupancy(int precision, int threads, size_t smem) {
+  return precision == 1 ? occupancy_of(tn_contract_multi_kernel<float, true>, threads, smem)
+                        : occupancy_of(tn_contract_multi_kernel<double, false>, threads, smem);
+}
+
+// No attribute calls here: the launch may be captured into a CUDA graph.
+cudaError_t contract_multi_launch(int precision, const MultiArgs& m, int grid, int threads, size_t smem,
+                                  cudaStream_t stream) {
+  if (precision == 1)
+    tn_contract_multi_kernel<float, true><<<grid, threads, smem, stream>>>(m);
+  else
+    tn_contract_multi_kernel<double, false><<<grid, threads, smem, stream>>>(m);
+  return cudaGetLastError();
+}
+
+cudaError_t contract_multi_advance(int32_t* batch, int32_t* next_unit, int32_t* counts, int32_t n_progs,
+                                   cudaStream_t stream) {
+  multi_advance_kernel<<<1, 256, 0, stream>>>(batch, next_unit, counts, n_progs);
+  return cudaGetLastError();
 }
 
 }  // namespace tqec

@@ -51,6 +51,37 @@ struct KArgs {
   const int32_t* report;  // variables whose values are returned
   int32_t n_report;
   uint8_t* assign_out;    // n x ceil(n_report / 8) bit-packed values
+  int64_t pad_;           // keeps the size a multiple of 16 bytes (staged with 16-byte copies)
+};
+static_assert(sizeof(KArgs) % 16 == 0, "KArgs is copied in 16-byte units");
+
+// Threads per block of the multi-program kernel (128 registers each).
+constexpr int kMultiThreads = 512;
+
+// A work unit of a multi-program launch: up to G rows of one program.
+struct MultiUnit {
+  int32_t prog;
+  int32_t pad;
+  int64_t first_row;
+};
+
+// One persistent launch over several programs (each a KArgs in device memory
+// with its own syndromes and outputs).  Batch b owns units
+// [unit_offsets[b], unit_offsets[b+1]); its rows of program i end at
+// batch_rows[b * n_progs + i].  A program whose KArgs.arena_global is set
+// uses the block's slice of arena_global (arena_per_block elements).
+struct MultiArgs {
+  const KArgs* progs;
+  int32_t n_progs;
+  int32_t list_mode;  // 1: each program contracts the rows of its list (recheck)
+  const MultiUnit* units;
+  const int64_t* unit_offsets;
+  const int64_t* batch_rows;
+  int32_t n_batches;   // a launch past the last batch does nothing
+  int32_t* batch;      // device: the current batch
+  int32_t* next_unit;  // device: units claimed in the current batch
+  void* arena_global;
+  int64_t arena_per_block;
 };
 
 // Shared memory a launch needs (bytes).
@@ -72,5 +103,13 @@ int contract_occupancy(int precision, int threads, size_t smem, bool map_mode = 
 
 cudaError_t contract_launch(int precision, const KArgs& a, int grid, int threads, size_t smem,
                             cudaStream_t stream);
+
+// The multi-program kernel (float32 normalised, or float64), and the
+// per-batch advance (batch + 1, unit counter and recheck counts to zero).
+cudaError_t contract_multi_launch(int precision, const MultiArgs& m, int grid, int threads, size_t smem,
+                                  cudaStream_t stream);
+int contract_multi_occupancy(int precision, int threads, size_t smem);
+cudaError_t contract_multi_advance(int32_t* batch, int32_t* next_unit, int32_t* counts, int32_t n_progs,
+                                   cudaStream_t stream);
 
 }  // namespace tqec

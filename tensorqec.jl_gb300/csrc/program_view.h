@@ -20,4 +20,23 @@ struct ProgramF64View {
 
 int program_f64_view(tqec_program* p, ProgramF64View* v);
 
+// What a multi-program launch needs of one program: its float32 and float64
+// launch descriptions (global tables, no buffers) and its sizes.
+struct ProgramMultiView {
+  KArgs args32, args64;
+  int device;
+  int sm_count;
+  int64_t arena_elems;
+  int width;
+  int n_steps;
+  int syn_words;
+  int syndrome_bytes;
+  int n_classes;
+  bool map_mode;
+  double flops_per_syndrome;
+  double recheck_margin;  // float32 log-margin below which a row is re-contracted
+};
+
+int program_multi_view(tqec_program* p, ProgramMultiView* v);
+
 }  // namespace tqec

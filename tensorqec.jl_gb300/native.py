@@ -99,6 +99,12 @@ def lib():
         "tqec_last_recheck_count": [vp, vp],
         "tqec_program_autotune": [vp, i64],
         "tqec_plan_inspect": [vp, vp, vp, vp],
+        "tqec_multi_create": [vp, i32, vp],
+        "tqec_multi_destroy": [vp],
+        "tqec_multi_set_work": [vp, i32, vp, vp, vp],
+        "tqec_multi_reset": [vp, vp],
+        "tqec_multi_launch": [vp, vp],
+        "tqec_multi_info": [vp, vp, vp, vp],
         "tqec_plan_inspect_flags": [vp, vp, C.c_uint32, vp, vp],
         "tqec_map_decode_batch": [vp, vp, i64, vp, vp, vp],
         "tqec_plan_release": [vp],
@@ -353,6 +359,55 @@ class Sampler:
     def close(self):
         if getattr(self, "_h", None):
             lib().tqec_sampler_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class MultiDecoder:
+    """Owner of a ``tqec_multi``: several programs decoded by one persistent
+    launch per batch (float32 + float64 recheck), capturable in a CUDA graph.
+
+    ``set_work(batch_end_rows, syn_ptrs, cls_ptrs)``: batch_end_rows is an
+    (n_batches, n_programs) array of cumulative end rows; the pointers are
+    device buffers of each program's packed syndromes and int32 classes."""
+
+    def __init__(self, programs):
+        self.programs = list(programs)
+        arr = (C.c_void_p * len(self.programs))(*[p._h for p in self.programs])
+        h = C.c_void_p()
+        check(lib().tqec_multi_create(arr, len(self.programs), C.byref(h)))
+        self._h = h
+
+    def set_work(self, batch_end_rows, syn_ptrs, cls_ptrs):
+        rows = np.ascontiguousarray(batch_end_rows, dtype=np.int64)
+        n = len(self.programs)
+        assert rows.ndim == 2 and rows.shape[1] == n
+        syn = (C.c_void_p * n)(*syn_ptrs)
+        cls = (C.c_void_p * n)(*cls_ptrs)
+        check(lib().tqec_multi_set_work(self._h, rows.shape[0], _ptr(rows), syn, cls))
+
+    def reset(self, stream=None):
+        check(lib().tqec_multi_reset(self._h, C.c_void_p(stream) if stream else None))
+
+    def launch(self, stream=None):
+        check(lib().tqec_multi_launch(self._h, C.c_void_p(stream) if stream else None))
+
+    def info(self):
+        n = len(self.programs)
+        g = np.zeros(n, dtype=np.int32)
+        sm = np.zeros(n, dtype=np.int32)
+        grid = C.c_int32()
+        check(lib().tqec_multi_info(self._h, _ptr(g), _ptr(sm), C.byref(grid)))
+        return {"groups": g.tolist(), "arena_in_smem": sm.tolist(), "grid": grid.value}
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().tqec_multi_destroy(self._h)
             self._h = None
 
     def __del__(self):

@@ -1,0 +1,83 @@
+"""Several programs in one persistent launch per batch (csrc/multi.cu).
+
+Uneven code sizes (surface d=3/5/7, colour 4.8.8 d=5, toric L=4 with 16
+classes) with their own noise rates are decoded batch by batch, directly and
+through a captured CUDA graph replayed once per batch; every class must equal
+the single-program decoder's (float32 + float64 recheck) except on exact ties.
+"""
+import numpy as np
+import pytest
+
+from conftest import gpu_available
+
+pytestmark = [pytest.mark.gpu, pytest.mark.skipif(not gpu_available(), reason="needs a CUDA GPU")]
+
+
+def _setup(pkg):
+    specs = [(pkg.SurfaceCode(3, 3), 0.08, 500), (pkg.SurfaceCode(5, 5), 0.05, 700), (pkg.Color488(5), 0.06, 300),
+             (pkg.ToricCode(4, 4), 0.04, 200), (pkg.SurfaceCode(7, 7), 0.05, 150)]
+    progs = []
+    for i, (code, p, n) in enumerate(specs):
+        t = pkg.tanner_graph(code)
+        em = pkg.depolarizing(p, t.nq)
+        ct = pkg.compile(pkg.TNMMAP(precision="f32"), t, em)
+        rng = np.random.default_rng(40 + i)
+        ep = pkg.random_error_pattern(em, rng, nsamples=n)
+        s = pkg.syndrome_extraction(ep, t)
+        bits = np.concatenate([s.sx, s.sz], axis=1)
+        progs.append((ct, bits))
+    return progs
+
+
+def _check(pkg, progs, got):
+    for (ct, bits), cls in zip(progs, got):
+        want = ct.decode_batch(bits)
+        lp = ct.class_logprobs(bits, precision="f64")
+        srt = np.sort(lp, axis=1)
+        tie = (srt[:, -1] - srt[:, -2]) <= 1e-9
+        bad = (cls != want) & ~tie
+        assert not bad.any(), (np.flatnonzero(bad)[:10], cls[bad][:10], want[bad][:10])
+
+
+def test_multi_program_batches_match_single_program(pkg):
+    import torch
+
+    progs = _setup(pkg)
+    md = pkg.native.MultiDecoder([ct.program for ct, _ in progs])
+    info = md.info()
+    assert info["grid"] > 0 and len(info["groups"]) == len(progs)
+    syn = [torch.from_numpy(pkg.pack_syndromes(b)).cuda() for _, b in progs]
+    cls = [torch.full((b.shape[0],), -1, dtype=torch.int32, device="cuda") for _, b in progs]
+    # three uneven batches: cumulative end rows per program
+    n = np.array([b.shape[0] for _, b in progs])
+    ends = np.stack([n * 1 // 5, n * 3 // 5, n])
+    md.set_work(ends, [x.data_ptr() for x in syn], [x.data_ptr() for x in cls])
+    stream = torch.cuda.current_stream()
+    md.reset(stream.cuda_stream)
+    for _ in range(ends.shape[0] + 1):  # one launch past the last batch does nothing
+        md.launch(stream.cuda_stream)
+    torch.cuda.synchronize()
+    got = [c.cpu().numpy() for c in cls]
+    assert all((g >= 0).all() for g in got)
+    _check(pkg, progs, got)
+
+    # the same work through a CUDA graph replayed once per batch
+    for c in cls:
+        c.fill_(-1)
+    side = torch.cuda.Stream()
+    side.wait_stream(stream)
+    with torch.cuda.stream(side):
+        md.reset(side.cuda_stream)
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g, stream=side):
+            md.launch(side.cuda_stream)
+        md.reset(side.cuda_stream)
+        for _ in range(ends.shape[0]):
+            g.replay()
+    torch.cuda.synchronize()
+    got = [c.cpu().numpy() for c in cls]
+    assert all((g_ >= 0).all() for g_ in got)
+    _check(pkg, progs, got)
+    md.close()
+    for ct, _ in progs:
+        ct.close()
