@@ -86,7 +86,7 @@ typedef struct {
   uint32_t flags;         /* TQEC_FLAG_* */
   int32_t device;         /* CUDA device ordinal */
   int32_t group;          /* syndromes per thread block (power of two); 0 = auto */
-  int32_t threads;        /* threads per block (multiple of 32); 0 = auto */
+  int32_t threads;        /* threads per block (rounded down to a power of two, >= 32); 0 = auto */
   double margin;          /* TQEC_F32: recheck when the log-probability margin
                              of the top class is below this; < 0 = the
                              rounding-error bound the planner derives */

@@ -169,6 +169,9 @@ int choose_shape(tqec_program* p, int precision, int G_req, int threads_req, int
       s.threads = threads_req > 0 ? threads_req : 1024;
   }
   s.threads = std::min(s.threads, tqec::contract_max_threads(precision));
+  // the kernel's thread rotation needs a power-of-two block (at least a warp)
+  while (s.threads & (s.threads - 1)) s.threads &= s.threads - 1;
+  s.threads = std::max(s.threads, 32);
   if (bytes(s.G, s.smem_arena, tb) > limit) tb = 0;
   if (tables_req == 0 || (tables_req < 0 && !s.smem_arena)) tb = 0;
   s.smem_tables = tb > 0;

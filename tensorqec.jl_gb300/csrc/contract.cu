@@ -129,13 +129,13 @@ __device__ __forceinline__ Operand<T> make_operand(int kind, int32_t ref, const 
 // (one warp reduction and one shared atomic per warp that had work).
 __device__ __forceinline__ void flush_max(bool had_items, uint32_t bits, uint32_t* slot) {
   if (!__any_sync(0xffffffffu, had_items)) return;
-#pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    const uint32_t other = __shfl_xor_sync(0xffffffffu, bits, o);
-    bits = other > bits ? other : bits;
-  }
+  bits = __reduce_max_sync(0xffffffffu, bits);
   if ((threadIdx.x & 31) == 0) atomicMax(slot, bits);
 }
+
+// Thread t's position in a step whose items start item_base threads into the
+// block (block sizes are powers of two; item_base is a multiple of 32).
+__device__ __forceinline__ int rotated(int t, int item_base) { return (t - item_base) & int(blockDim.x - 1); }
 
 // G1: the step runs for one syndrome (the block's only one, or one of its G
 // in turn), so the syndrome bits, the arena slice, the operand bases and the
@@ -156,7 +156,7 @@ __device__ int run_step(const KArgs& a, const StepDesc& dref, int st, int item_b
   const int bbits = d.lh + d.lk + d.lfb;
   // item i runs on thread (i + item_base) mod blockDim: steps of one barrier
   // group start on different threads (item_base is a multiple of 32)
-  const int i0 = (int(threadIdx.x) + int(blockDim.x) - item_base % int(blockDim.x)) % int(blockDim.x);
+  const int i0 = rotated(int(threadIdx.x), item_base);
   // step invariants of a one-syndrome block
   Operand<T> A1{}, B1{};
   int as1 = 0, bs1 = 0;
@@ -303,7 +303,7 @@ __device__ int run_step_vec(const KArgs& a, const StepDesc& dref, int st, int it
   const bool permuted = d.perm_off >= 0;
   const int cb0 = lw < 8 ? lw : 8;
   const int rot = threadIdx.x & (VW - 1);
-  const int i0 = (int(threadIdx.x) + int(blockDim.x) - item_base % int(blockDim.x)) % int(blockDim.x);
+  const int i0 = rotated(int(threadIdx.x), item_base);
   Operand<T> A1{}, B1{};
   int as1 = 0, bs1 = 0;
   T fa1 = T(1), fb1 = T(1);
@@ -470,7 +470,7 @@ __device__ int run_step_splitk(const KArgs& a, const StepDesc& dref, int st, int
   const int K = 1 << d.lk;
   const int abits = d.lh + d.lfa + d.lk;
   const int bbits = d.lh + d.lk + d.lfb;
-  const int vt0 = (int(threadIdx.x) + int(blockDim.x) - item_base % int(blockDim.x)) % int(blockDim.x);
+  const int vt0 = rotated(int(threadIdx.x), item_base);
   uint32_t run_bits = 0u;
   // whole warps iterate together (the shuffles below need every lane)
   for (int vt = vt0; vt < total_r; vt += blockDim.x) {
@@ -684,6 +684,7 @@ __device__ __forceinline__ int dispatch_step(const KArgs& a, const StepDesc& d, 
 // staged tables (if any) and the arena (if in shared memory).
 struct BlockSmem {
   StepDesc* steps;
+  int2* plan;  // per step: x = kind | lt << 8 | per-syndrome << 16, y = items (see fill_step_plan)
   uint32_t* syn;
   uint32_t* max;
   uint32_t* asg;
@@ -695,6 +696,8 @@ __device__ __forceinline__ BlockSmem carve_smem(const KArgs& a, unsigned char* s
   BlockSmem b;
   b.steps = reinterpret_cast<StepDesc*>(smem);
   size_t off = size_t(a.n_steps) * sizeof(StepDesc);
+  b.plan = reinterpret_cast<int2*>(smem + off);
+  off += size_t(a.n_steps) * sizeof(int2);
   b.syn = reinterpret_cast<uint32_t*>(smem + off);
   off += size_t(a.G) * a.syn_words * 4;
   b.max = reinterpret_cast<uint32_t*>(smem + off);
@@ -710,6 +713,24 @@ __device__ __forceinline__ void copy16(void* dst, const void* src, size_t bytes)
   int4* d = reinterpret_cast<int4*>(dst);
   const int n16 = int(bytes / 16);
   for (int i = threadIdx.x; i < n16; i += blockDim.x) d[i] = s[i];
+}
+
+// Each step's execution plan for this block size and group: its shape (kind
+// and lanes per output), whether it runs syndrome by syndrome (a step that
+// fills the block for one syndrome alone, in a block of several), and how
+// many items (threads' worth) it takes, which also rotates the next member of
+// its barrier group.  One thread per step; the caller synchronises.
+template <typename T>
+__device__ __forceinline__ void fill_step_plan(const KArgs& a, const StepDesc* steps, int2* plan) {
+  const int bd = int(blockDim.x);
+  for (int st = threadIdx.x; st < a.n_steps; st += blockDim.x) {
+    const StepDesc& d = steps[st];
+    const StepShape sh = step_shape<T>(d.lh, d.lfa, d.lfb, d.lk, a.lg);
+    const StepShape sh1 = a.G > 1 ? step_shape<T>(d.lh, d.lfa, d.lfb, d.lk, 0) : sh;
+    const bool per_syndrome = a.G > 1 && sh1.total_r >= bd;
+    const StepShape& use = per_syndrome ? sh1 : sh;
+    plan[st] = make_int2(use.kind | (use.lt << 8) | (int(per_syndrome) << 16), per_syndrome ? bd : sh.total_r);
+  }
 }
 
 // One group of up to G syndromes (rows base .. base+G-1 below nrows) through
@@ -741,24 +762,23 @@ __device__ void contract_group(const KArgs& a, int64_t base, int64_t nrows, cons
   int item_base = 0;
   for (int st = 0; st < a.n_steps; ++st) {
     const StepDesc& d = s_steps[st];
-    const int4 q = *reinterpret_cast<const int4*>(&d.lh);  // lh, lfa, lfb, lk
-    const int bd = int(blockDim.x);
-    const StepShape sh = step_shape<T>(q.x, q.y, q.z, q.w, a.lg);
-    // a step that fills the block for each syndrome alone runs the block's
-    // syndromes one after another with hoisted invariants (every thread
-    // takes part)
-    const StepShape sh1 = a.G > 1 ? step_shape<T>(q.x, q.y, q.z, q.w, 0) : sh;
-    const bool per_syndrome = a.G > 1 && sh1.total_r >= bd;
-    const int items = per_syndrome ? bd : sh.total_r;
+    const int2 pl = sm.plan[st];
+    StepShape sh;
+    sh.kind = pl.x & 0xff;
+    sh.lt = (pl.x >> 8) & 0xff;
+    sh.total_r = pl.y;
+    const bool per_syndrome = (pl.x >> 16) & 1;
+    const int items = pl.y;
     // first virtual thread of this warp (steps of a barrier group start on
     // different warps); a warp past the step's items goes to the barrier
-    const int vt_warp = (int(threadIdx.x & ~31u) + bd - item_base % bd) % bd;
+    const int vt_warp = rotated(int(threadIdx.x & ~31u), item_base);
     if (vt_warp < items) {
       if (a.G == 1) {
         dispatch_step<T, NORM, MAXP, true>(a, d, sh, st, item_base, s_syn, s_max, arena, consts, ptab);
       } else if (per_syndrome) {
+        // the block's syndromes one after another with hoisted invariants
         for (int g = 0; g < a.G; ++g)
-          dispatch_step<T, NORM, MAXP, true>(a, d, sh1, st, item_base, s_syn + g * a.syn_words,
+          dispatch_step<T, NORM, MAXP, true>(a, d, sh, st, item_base, s_syn + g * a.syn_words,
                                              s_max + g * a.n_steps, arena + int64_t(g) * a.arena_elems, consts,
                                              ptab);
       } else {
@@ -851,6 +871,8 @@ __global__ void __launch_bounds__(sizeof(T) == 8 ? 512 : 1024) tn_contract_kerne
                  ? reinterpret_cast<T*>(a.arena_global) + int64_t(blockIdx.x) * a.G * a.arena_elems
                  : reinterpret_cast<T*>(smem + off);
   copy16(sm.steps, a.steps, size_t(a.n_steps) * sizeof(StepDesc));
+  __syncthreads();
+  fill_step_plan<T>(a, sm.steps, sm.plan);
   const int64_t nrows = a.list ? int64_t(*a.list_count) : a.n;
   for (int64_t base = int64_t(blockIdx.x) * a.G; base < nrows; base += int64_t(gridDim.x) * a.G)
     contract_group<T, NORM, MAXP>(a, base, nrows, sm, arena, consts, ptab);
@@ -881,6 +903,8 @@ __global__ void __launch_bounds__(kMultiThreads) tn_contract_multi_kernel(MultiA
     if (first) {
       copy16(sm.steps, a.steps, size_t(a.n_steps) * sizeof(StepDesc));
       __syncthreads();
+      fill_step_plan<T>(a, sm.steps, sm.plan);
+      __syncthreads();
     }
     T* arena = a.arena_global ? gslice : reinterpret_cast<T*>(smem + sm.tail);
     contract_group<T, NORM, false>(a, base, nrows, sm, arena, reinterpret_cast<const T*>(a.consts),
@@ -895,6 +919,8 @@ __global__ void __launch_bounds__(kMultiThreads) tn_contract_multi_kernel(MultiA
       if (int64_t(blockIdx.x) * s_ka.G >= nrows) continue;  // block-uniform
       const BlockSmem sm = carve_smem<NORM, false>(s_ka, smem);
       copy16(sm.steps, s_ka.steps, size_t(s_ka.n_steps) * sizeof(StepDesc));
+      __syncthreads();
+      fill_step_plan<T>(s_ka, sm.steps, sm.plan);
       __syncthreads();
       for (int64_t base = int64_t(blockIdx.x) * s_ka.G; base < nrows; base += int64_t(gridDim.x) * s_ka.G)
         run_unit(prog, base, nrows, false);
@@ -930,7 +956,7 @@ __global__ void multi_advance_kernel(int32_t* batch, int32_t* next_unit, int32_t
 size_t contract_smem_bytes(int precision, int32_t n_steps, int32_t syn_words, int G,
                            int64_t arena_elems, bool arena_in_smem, int32_t var_words, size_t table_bytes) {
   const bool norm = precision == 1;
-  size_t off = size_t(n_steps) * sizeof(StepDesc) + size_t(G) * syn_words * 4;
+  size_t off = size_t(n_steps) * (sizeof(StepDesc) + 8) + size_t(G) * syn_words * 4;
   if (norm) off += size_t(G) * n_steps * 4;
   off += size_t(G) * var_words * 4;
   off = (off + 15) & ~size_t(15);
