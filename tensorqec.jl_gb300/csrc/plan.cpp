@@ -400,10 +400,9 @@ std::string build_plan(const NetworkView& net, int32_t n_steps, const int32_t* s
       if (ok) {
         c = fold_tables(tx, ty, keep);
         folded = true;
-      } else if (nsel == 0 && !map_mode) {
-        *unsupported = true;
-        return "syndrome-independent intermediate too wide to fold on the host";
       }
+      // too wide to fold on the host: contracted at run time like any other
+      // step (its operands are constant tables)
     }
     if (!folded) {
       c.kind = NK_RUNTIME;

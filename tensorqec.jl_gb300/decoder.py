@@ -67,7 +67,7 @@ def optimize_code(graph: FactorGraph, optimizer) -> np.ndarray:
         steps, _, _ = native.optimize_order(graph, trials=optimizer.trials, sweeps=0, seed=optimizer.seed)
         return steps
     if isinstance(optimizer, TreeSA):
-        if optimizer.target_width or optimizer.restarts <= 1:
+        if optimizer.restarts <= 1:
             steps, _, _ = native.optimize_order(graph, trials=optimizer.trials, sweeps=optimizer.sweeps,
                                                 target_width=optimizer.target_width,
                                                 width_penalty=optimizer.width_penalty, seed=optimizer.seed)
@@ -90,19 +90,20 @@ def _estimated_cost(plan):
 
 def _search_fitting(graph, opt):
     """Several annealing restarts (and narrower width targets) scored by the
-    planner's own flops and working-set size; the cheapest tree wins."""
+    planner's own flops and working-set size; the cheapest tree wins.  A
+    given target width is searched at that width only."""
     best = None
-    widths = [0]
+    widths = [opt.target_width] if opt.target_width else [0]
     for r in range(opt.restarts):
         for tw in widths:
             steps, _, w = native.optimize_order(graph, trials=opt.trials, sweeps=opt.sweeps, target_width=tw,
-                                                width_penalty=2.0 if tw else opt.width_penalty,
+                                                width_penalty=max(2.0, opt.width_penalty) if tw else opt.width_penalty,
                                                 seed=opt.seed + r)
             plan = native.inspect_plan(graph, steps)
             cost = _estimated_cost(plan)
             if best is None or cost < best[0]:
                 best = (cost, steps, plan)
-        if best[2]["arena_elems"] * 4 > _SMEM_ARENA_BYTES and len(widths) == 1:
+        if best[2]["arena_elems"] * 4 > _SMEM_ARENA_BYTES and len(widths) == 1 and not opt.target_width:
             widths.append(best[2]["width"] - 1)
     return best[1]
 
