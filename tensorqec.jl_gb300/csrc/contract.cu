@@ -44,10 +44,27 @@ __device__ __forceinline__ float norm_factor(uint32_t m, int* e) {
   return __uint_as_float(uint32_t(254 - be) << 23);
 }
 
+// A syndrome's intermediates: offsets below `split` live in `small` (the
+// whole arena, or the pool of small tensors kept in shared memory), the rest
+// in `big` (the pool of large tensors in global memory; `big` is biased by
+// -split so that big + offset addresses it).  of(g) steps to syndrome g of
+// the block.
+template <typename T>
+struct Arena {
+  T* small;
+  T* big;
+  int32_t split;
+  int32_t ss, bs;  // per-syndrome strides of the two pools
+  __device__ __forceinline__ Arena of(int g) const {
+    return Arena{small + int64_t(g) * ss, big + int64_t(g) * bs, split, ss, bs};
+  }
+  __device__ __forceinline__ T* at(int32_t off) const { return off < split ? small + off : big + off; }
+};
+
 template <typename T>
 __device__ __forceinline__ const T* operand_ptr(int kind, int32_t ref, const int8_t* sel, int obits,
-                                                T* arena_g, const T* consts, const uint32_t* syn) {
-  if (kind == OP_ARENA) return arena_g + ref;
+                                                const Arena<T>& arena_g, const T* consts, const uint32_t* syn) {
+  if (kind == OP_ARENA) return arena_g.at(ref);
   int v = 0;
 #pragma unroll
   for (int i = 0; i < kMaxSel; ++i)
@@ -110,19 +127,30 @@ __device__ __forceinline__ int perm_addr(const PermTab& perm, int off, int e, in
 }
 
 // An operand: a base pointer (arena slice or constant table) plus offset.
+// A step's operand and output bases for one syndrome: select tables chosen
+// by its syndrome bits, arena tensors located in their pool.  Filled once
+// per syndrome group (fill_step_ptrs), so steps start with plain loads.
 template <typename T>
-struct Operand {
-  const T* p;
-  __device__ __forceinline__ T ld(int idx) const { return p[idx]; }
-  __device__ __forceinline__ const T* vec(int idx) const { return p + idx; }
+struct StepPtrs {
+  const T* a;
+  const T* b;
+  T* out;
 };
 
 template <typename T>
-__device__ __forceinline__ Operand<T> make_operand(int kind, int32_t ref, const int8_t* sel, int obits, T* arena_g,
-                                                   const T* consts, const uint32_t* syn) {
-  Operand<T> o;
-  o.p = operand_ptr<T>(kind, ref, sel, obits, arena_g, consts, syn);
-  return o;
+__device__ void fill_step_ptrs(const KArgs& a, const StepDesc* steps, const uint32_t* s_syn, const Arena<T>& arena,
+                               const T* consts, StepPtrs<T>* ptrs) {
+  for (int i = threadIdx.x; i < a.G * a.n_steps; i += blockDim.x) {
+    const int g = i / a.n_steps, st = i - g * a.n_steps;
+    const StepDesc& d = steps[st];
+    const Arena<T> ag = arena.of(g);
+    const uint32_t* syn = s_syn + g * a.syn_words;
+    StepPtrs<T> p;
+    p.a = operand_ptr<T>(d.a_kind, d.a_ref, d.a_sel, d.lh + d.lfa + d.lk, ag, consts, syn);
+    p.b = operand_ptr<T>(d.b_kind, d.b_ref, d.b_sel, d.lh + d.lk + d.lfb, ag, consts, syn);
+    p.out = ag.at(d.out_off);
+    ptrs[i] = p;
+  }
 }
 
 // Folds a thread's running maximum into the step's per-syndrome maximum
@@ -137,12 +165,35 @@ __device__ __forceinline__ void flush_max(bool had_items, uint32_t bits, uint32_
 // block (block sizes are powers of two; item_base is a multiple of 32).
 __device__ __forceinline__ int rotated(int t, int item_base) { return (t - item_base) & int(blockDim.x - 1); }
 
-// G1: the step runs for one syndrome (the block's only one, or one of its G
-// in turn), so the syndrome bits, the arena slice, the operand bases and the
-// normalisers are step invariants computed once.
-template <typename T, bool NORM, bool APAR, bool BPAR, bool MAXP, bool G1>
-__device__ int run_step(const KArgs& a, const StepDesc& dref, int st, int item_base, const uint32_t* s_syn,
-                         uint32_t* s_max, T* arena, const T* consts, const PermTab& ptab) {
+// The normalisers of a step's arena operands (1 for constant operands).
+template <typename T, bool NORM>
+__device__ __forceinline__ void step_norms(const StepDesc& d, const uint32_t* s_max, T* fa, T* fb) {
+  *fa = T(1);
+  *fb = T(1);
+  if (NORM) {
+    int ee;
+    if (d.a_kind == OP_ARENA) *fa = T(norm_factor(s_max[d.a_prod], &ee));
+    if (d.b_kind == OP_ARENA) *fb = T(norm_factor(s_max[d.b_prod], &ee));
+  }
+}
+
+// Segmented warp maximum of multi-syndrome work items (items of one syndrome
+// are consecutive lanes).
+__device__ __forceinline__ void segment_max(bool valid, uint32_t bits, int lw_items, uint32_t* slot) {
+  const int seg = lw_items >= 5 ? 32 : (1 << lw_items);
+  for (int o = 1; o < seg; o <<= 1) {
+    const uint32_t other = __shfl_xor_sync(0xffffffffu, bits, o);
+    bits = other > bits ? other : bits;
+  }
+  if (valid && (threadIdx.x & (seg - 1)) == 0) atomicMax(slot, bits);
+}
+
+// One output per work item.  G1: the step runs for one syndrome (the
+// block's only one, or one of its G in turn), so its bases and normalisers
+// are step invariants.
+template <typename T, bool NORM, bool MAXP, bool G1>
+__device__ void run_step(const KArgs& a, const StepDesc& dref, int st, int item_base, uint32_t* s_max,
+                         const StepPtrs<T>* ptrs, const PermTab& ptab) {
   // a register copy: arena stores (same shared array) cannot alias it
   const StepDesc d = dref;
   const int lw = d.lh + d.lfa + d.lfb;
@@ -152,25 +203,12 @@ __device__ int run_step(const KArgs& a, const StepDesc& dref, int st, int item_b
   const int mfa = (1 << d.lfa) - 1;
   const int mw = (1 << lw) - 1;
   const int K = 1 << d.lk;
-  const int abits = d.lh + d.lfa + d.lk;
-  const int bbits = d.lh + d.lk + d.lfb;
-  // item i runs on thread (i + item_base) mod blockDim: steps of one barrier
-  // group start on different threads (item_base is a multiple of 32)
   const int i0 = rotated(int(threadIdx.x), item_base);
-  // step invariants of a one-syndrome block
-  Operand<T> A1{}, B1{};
-  int as1 = 0, bs1 = 0;
+  StepPtrs<T> p1{};
   T fa1 = T(1), fb1 = T(1);
   if (G1) {
-    if (APAR) as1 = syn_bit(s_syn, d.a_ref);
-    else A1 = make_operand<T>(d.a_kind, d.a_ref, d.a_sel, abits, arena, consts, s_syn);
-    if (BPAR) bs1 = syn_bit(s_syn, d.b_ref);
-    else B1 = make_operand<T>(d.b_kind, d.b_ref, d.b_sel, bbits, arena, consts, s_syn);
-    if (NORM) {
-      int ee;
-      if (!APAR && d.a_kind == OP_ARENA) fa1 = T(norm_factor(s_max[d.a_prod], &ee));
-      if (!BPAR && d.b_kind == OP_ARENA) fb1 = T(norm_factor(s_max[d.b_prod], &ee));
-    }
+    p1 = ptrs[st];
+    step_norms<T, NORM>(d, s_max, &fa1, &fb1);
   }
   uint32_t run_bits = 0u;
   for (int i = i0; i < (G1 ? total : total_r); i += blockDim.x) {
@@ -179,76 +217,40 @@ __device__ int run_step(const KArgs& a, const StepDesc& dref, int st, int item_b
     const int e = i & mw;
     T acc = T(0);
     if (valid) {
-      T* arena_g = G1 ? arena : arena + int64_t(g) * a.arena_elems;
+      StepPtrs<T> p = p1;
+      T fa_s = fa1, fb_s = fb1;
+      if (!G1) {
+        p = ptrs[g * a.n_steps + st];
+        step_norms<T, NORM>(d, s_max + g * a.n_steps, &fa_s, &fb_s);
+      }
       const int fb = e & mfb;
       const int fa = (e >> d.lfb) & mfa;
       const int h = e >> (d.lfb + d.lfa);
-      const int abase = ((h << d.lfa) | fa) << d.lk;
-      const int bbase = (h << (d.lk + d.lfb)) | fb;
-      Operand<T> A = A1, B = B1;
-      int as = as1, bs = bs1;
-      T fa_s = fa1, fb_s = fb1;
-      if (!G1) {
-        const uint32_t* syn = s_syn + g * a.syn_words;
-        if (APAR) as = syn_bit(syn, d.a_ref);
-        else A = make_operand<T>(d.a_kind, d.a_ref, d.a_sel, abits, arena_g, consts, syn);
-        if (BPAR) bs = syn_bit(syn, d.b_ref);
-        else B = make_operand<T>(d.b_kind, d.b_ref, d.b_sel, bbits, arena_g, consts, syn);
-        if (NORM) {
-          int ee;
-          if (!APAR && d.a_kind == OP_ARENA) fa_s = T(norm_factor(s_max[g * a.n_steps + d.a_prod], &ee));
-          if (!BPAR && d.b_kind == OP_ARENA) fb_s = T(norm_factor(s_max[g * a.n_steps + d.b_prod], &ee));
+      const T* pa = p.a + (((h << d.lfa) | fa) << d.lk);
+      const T* pb = p.b + ((h << (d.lk + d.lfb)) | fb);
+      for (int k = 0; k < K; ++k) {
+        T a0 = pa[k];
+        if (NORM) a0 *= fa_s;
+        if (MAXP) {
+          const T v = a0 * pb[k << d.lfb];
+          acc = v > acc ? v : acc;
+        } else {
+          acc = fma(a0, pb[k << d.lfb], acc);
         }
       }
-      if (APAR && BPAR) {
-        for (int k = 0; k < K; ++k) {
-          const T v = parity_val<T>(abase + k, as) * parity_val<T>(bbase + (k << d.lfb), bs);
-          acc = MAXP ? (v > acc ? v : acc) : acc + v;
-        }
-      } else if (APAR) {
-        for (int k = 0; k < K; ++k)
-          if (parity_val<T>(abase + k, as) != T(0)) {
-            const T v = B.ld(bbase + (k << d.lfb));
-            acc = MAXP ? (v > acc ? v : acc) : acc + v;
-          }
-      } else if (BPAR) {
-        for (int k = 0; k < K; ++k)
-          if (parity_val<T>(bbase + (k << d.lfb), bs) != T(0)) {
-            const T v = A.ld(abase + k);
-            acc = MAXP ? (v > acc ? v : acc) : acc + v;
-          }
-        if (NORM) acc *= fa_s;
-      } else {
-        for (int k = 0; k < K; ++k) {
-          T a0 = A.ld(abase + k);
-          if (NORM) a0 *= fa_s;
-          if (MAXP) {
-            const T v = a0 * B.ld(bbase + (k << d.lfb));
-            acc = v > acc ? v : acc;
-          } else {
-            acc = fma(a0, B.ld(bbase + (k << d.lfb)), acc);
-          }
-        }
-      }
-      if (NORM && !BPAR) acc *= fb_s;
+      if (NORM) acc *= fb_s;
       const int addr = d.perm_off < 0 ? e : perm_addr(ptab, d.perm_off, e, lw);
-      arena_g[d.out_off + addr] = acc;
+      p.out[addr] = acc;
     }
     if (NORM && G1) {
       const uint32_t bits = __float_as_uint(float(acc));
       run_bits = bits > run_bits ? bits : run_bits;
     } else if (NORM) {
-      uint32_t bits = __float_as_uint(float(acc));
-      const int seg = lw >= 5 ? 32 : (1 << lw);
-      for (int o = 1; o < seg; o <<= 1) {
-        uint32_t other = __shfl_xor_sync(0xffffffffu, bits, o);
-        bits = other > bits ? other : bits;
-      }
-      if (valid && (threadIdx.x & (seg - 1)) == 0) atomicMax(&s_max[g * a.n_steps + st], bits);
+      segment_max(valid, __float_as_uint(float(acc)), lw, &s_max[g * a.n_steps + st]);
     }
   }
   if (NORM && G1) flush_max(i0 < total, run_bits, &s_max[st]);
-  return total_r;
+  return;
 }
 
 template <typename T>
@@ -282,11 +284,11 @@ __device__ __forceinline__ void store4<double>(double* p, const double v[4]) {
 // B as 16-byte vectors.  Operand bases, fb offsets and k strides are
 // multiples of 8 elements (arena and constant offsets are planned that way),
 // so the vector accesses are aligned.  Permuted outputs are written in a
-// lane-rotated order so that the stores of one warp instruction hit
-// different index bits.
-template <typename T, int VW, bool NORM, bool APAR, bool BPAR, bool MAXP, bool G1>
-__device__ int run_step_vec(const KArgs& a, const StepDesc& dref, int st, int item_base, const uint32_t* s_syn,
-                            uint32_t* s_max, T* arena, const T* consts, const PermTab& ptab) {
+// lane-rotated order where the planner found that it spreads the stores of
+// one warp instruction over more shared-memory banks.
+template <typename T, int VW, bool NORM, bool MAXP, bool G1>
+__device__ void run_step_vec(const KArgs& a, const StepDesc& dref, int st, int item_base, uint32_t* s_max,
+                             const StepPtrs<T>* ptrs, const PermTab& ptab) {
   constexpr int LV = VW == 8 ? 3 : 2;
   const StepDesc d = dref;
   const int lw = d.lh + d.lfa + d.lfb;
@@ -298,25 +300,15 @@ __device__ int run_step_vec(const KArgs& a, const StepDesc& dref, int st, int it
   const int mwv = (1 << lwv) - 1;
   const int K = 1 << d.lk;
   const int bstride = 1 << d.lfb;
-  const int abits = d.lh + d.lfa + d.lk;
-  const int bbits = d.lh + d.lk + d.lfb;
   const bool permuted = d.perm_off >= 0;
   const int cb0 = lw < 8 ? lw : 8;
   const int rot = threadIdx.x & (VW - 1);
   const int i0 = rotated(int(threadIdx.x), item_base);
-  Operand<T> A1{}, B1{};
-  int as1 = 0, bs1 = 0;
+  StepPtrs<T> p1{};
   T fa1 = T(1), fb1 = T(1);
   if (G1) {
-    if (APAR) as1 = syn_bit(s_syn, d.a_ref);
-    else A1 = make_operand<T>(d.a_kind, d.a_ref, d.a_sel, abits, arena, consts, s_syn);
-    if (BPAR) bs1 = syn_bit(s_syn, d.b_ref);
-    else B1 = make_operand<T>(d.b_kind, d.b_ref, d.b_sel, bbits, arena, consts, s_syn);
-    if (NORM) {
-      int ee;
-      if (!APAR && d.a_kind == OP_ARENA) fa1 = T(norm_factor(s_max[d.a_prod], &ee));
-      if (!BPAR && d.b_kind == OP_ARENA) fb1 = T(norm_factor(s_max[d.b_prod], &ee));
-    }
+    p1 = ptrs[st];
+    step_norms<T, NORM>(d, s_max, &fa1, &fb1);
   }
   uint32_t run_bits = 0u;
   for (int i = i0; i < (G1 ? total : total_r); i += blockDim.x) {
@@ -327,48 +319,24 @@ __device__ int run_step_vec(const KArgs& a, const StepDesc& dref, int st, int it
 #pragma unroll
     for (int j = 0; j < VW; ++j) acc[j] = T(0);
     if (valid) {
-      T* arena_g = G1 ? arena : arena + int64_t(g) * a.arena_elems;
+      StepPtrs<T> p = p1;
+      T fa_s = fa1, fb_s = fb1;
+      if (!G1) {
+        p = ptrs[g * a.n_steps + st];
+        step_norms<T, NORM>(d, s_max + g * a.n_steps, &fa_s, &fb_s);
+      }
       const int fb0 = e0 & mfb;
       const int fa = (e0 >> d.lfb) & mfa;
       const int h = e0 >> (d.lfb + d.lfa);
-      const int abase = ((h << d.lfa) | fa) << d.lk;
-      const int bbase = (h << (d.lk + d.lfb)) | fb0;
-      Operand<T> A = A1, B = B1;
-      int as = as1, bs = bs1;
-      T fa_s = fa1, fb_s = fb1;
-      if (!G1) {
-        const uint32_t* syn = s_syn + g * a.syn_words;
-        if (APAR) as = syn_bit(syn, d.a_ref);
-        else A = make_operand<T>(d.a_kind, d.a_ref, d.a_sel, abits, arena_g, consts, syn);
-        if (BPAR) bs = syn_bit(syn, d.b_ref);
-        else B = make_operand<T>(d.b_kind, d.b_ref, d.b_sel, bbits, arena_g, consts, syn);
-        if (NORM) {
-          int ee;
-          if (!APAR && d.a_kind == OP_ARENA) fa_s = T(norm_factor(s_max[g * a.n_steps + d.a_prod], &ee));
-          if (!BPAR && d.b_kind == OP_ARENA) fb_s = T(norm_factor(s_max[g * a.n_steps + d.b_prod], &ee));
-        }
-      }
-      const T* pa = APAR ? nullptr : A.p + abase;
-      const T* pb = BPAR ? nullptr : B.p + bbase;
+      const T* pa = p.a + (((h << d.lfa) | fa) << d.lk);
+      const T* pb = p.b + ((h << (d.lk + d.lfb)) | fb0);
       auto body = [&](int k) {
-        T av;
-        if (APAR) {
-          if (parity_val<T>(abase + k, as) == T(0)) return;
-          av = T(1);
-        } else {
-          av = pa[k];
-          if (NORM) av *= fa_s;
-        }
+        T av = pa[k];
+        if (NORM) av *= fa_s;
         T bv[VW];
-        if (BPAR) {
-          const int bi = bbase + k * bstride;
-#pragma unroll
-          for (int j = 0; j < VW; ++j) bv[j] = parity_val<T>(bi + j, bs);
-        } else {
-          const T* q = pb + k * bstride;
-          load4<T>(q, bv);
-          if (VW == 8) load4<T>(q + 4, bv + 4);
-        }
+        const T* q = pb + k * bstride;
+        load4<T>(q, bv);
+        if (VW == 8) load4<T>(q + 4, bv + 4);
 #pragma unroll
         for (int j = 0; j < VW; ++j) {
           if (MAXP) {
@@ -387,13 +355,14 @@ __device__ int run_step_vec(const KArgs& a, const StepDesc& dref, int st, int it
           body(k + 1);
         }
       }
-      if (NORM && !BPAR) {
+      if (NORM) {
 #pragma unroll
         for (int j = 0; j < VW; ++j) acc[j] *= fb_s;
       }
       if (!permuted) {
-        store4<T>(arena_g + d.out_off + e0, acc);
-        if (VW == 8) store4<T>(arena_g + d.out_off + e0 + 4, acc + 4);
+        T* out = p.out + e0;
+        store4<T>(out, acc);
+        if (VW == 8) store4<T>(out + 4, acc + 4);
       } else {
         int los[VW];
         ptab.vec<VW>(d.perm_off + (e0 & ((1 << cb0) - 1)), los);
@@ -404,7 +373,7 @@ __device__ int run_step_vec(const KArgs& a, const StepDesc& dref, int st, int it
           hi |= ptab.at(tab + ((e0 >> sh) & ((1 << cb) - 1)));
           tab += 1 << cb;
         }
-        T* out = arena_g + d.out_off;
+        T* out = p.out;
         if (d.flags & (VW == 8 ? kStepRotate8 : kStepRotate4)) {
           // barrel rotation: lane r stores its outputs starting at r mod VW,
           // so the lanes of one store instruction differ in the low bits too
@@ -434,30 +403,20 @@ __device__ int run_step_vec(const KArgs& a, const StepDesc& dref, int st, int it
       float m = float(acc[0]);
 #pragma unroll
       for (int j = 1; j < VW; ++j) m = fmaxf(m, float(acc[j]));
-      uint32_t bits = __float_as_uint(m);
-      if (G1) {
-        run_bits = bits > run_bits ? bits : run_bits;
-      } else {
-        const int seg = lwv >= 5 ? 32 : (1 << lwv);
-        for (int o = 1; o < seg; o <<= 1) {
-          uint32_t other = __shfl_xor_sync(0xffffffffu, bits, o);
-          bits = other > bits ? other : bits;
-        }
-        if (valid && (threadIdx.x & (seg - 1)) == 0) atomicMax(&s_max[g * a.n_steps + st], bits);
-      }
+      const uint32_t bits = __float_as_uint(m);
+      if (G1) run_bits = bits > run_bits ? bits : run_bits;
+      else segment_max(valid, bits, lwv, &s_max[g * a.n_steps + st]);
     }
   }
   if (NORM && G1) flush_max(i0 < total, run_bits, &s_max[st]);
-  return total_r;
 }
 
 // A step with few outputs and a long k range: TPO (a power of two, at most
 // 32) consecutive lanes share one output, each summing every TPO-th k, and
 // combine their partial sums with shuffles (maxima in max-product mode).
-template <typename T, bool NORM, bool APAR, bool BPAR, bool MAXP, bool G1>
-__device__ int run_step_splitk(const KArgs& a, const StepDesc& dref, int st, int item_base, int lt,
-                               const uint32_t* s_syn, uint32_t* s_max, T* arena, const T* consts,
-                               const PermTab& ptab) {
+template <typename T, bool NORM, bool MAXP, bool G1>
+__device__ void run_step_splitk(const KArgs& a, const StepDesc& dref, int st, int item_base, int lt,
+                                uint32_t* s_max, const StepPtrs<T>* ptrs, const PermTab& ptab) {
   const StepDesc d = dref;
   const int tpo = 1 << lt;
   const int lw = d.lh + d.lfa + d.lfb;
@@ -468,8 +427,6 @@ __device__ int run_step_splitk(const KArgs& a, const StepDesc& dref, int st, int
   const int mfa = (1 << d.lfa) - 1;
   const int mw = (1 << lw) - 1;
   const int K = 1 << d.lk;
-  const int abits = d.lh + d.lfa + d.lk;
-  const int bbits = d.lh + d.lk + d.lfb;
   const int vt0 = rotated(int(threadIdx.x), item_base);
   uint32_t run_bits = 0u;
   // whole warps iterate together (the shuffles below need every lane)
@@ -479,28 +436,19 @@ __device__ int run_step_splitk(const KArgs& a, const StepDesc& dref, int st, int
     const int g = G1 ? 0 : (valid ? (item >> lw) : 0);
     const int e = item & mw;
     T acc = T(0);
-    T* arena_g = G1 ? arena : arena + int64_t(g) * a.arena_elems;
+    StepPtrs<T> p{};
+    T fa_s = T(1), fb_s = T(1);
     if (valid) {
-      const uint32_t* syn = s_syn + g * a.syn_words;
+      p = ptrs[g * a.n_steps + st];
+      step_norms<T, NORM>(d, s_max + g * a.n_steps, &fa_s, &fb_s);
       const int fb = e & mfb;
       const int fa = (e >> d.lfb) & mfa;
       const int h = e >> (d.lfb + d.lfa);
-      const int abase = ((h << d.lfa) | fa) << d.lk;
-      const int bbase = (h << (d.lk + d.lfb)) | fb;
-      Operand<T> A{}, B{};
-      int as = 0, bs = 0;
-      if (APAR) as = syn_bit(syn, d.a_ref);
-      else A = make_operand<T>(d.a_kind, d.a_ref, d.a_sel, abits, arena_g, consts, syn);
-      if (BPAR) bs = syn_bit(syn, d.b_ref);
-      else B = make_operand<T>(d.b_kind, d.b_ref, d.b_sel, bbits, arena_g, consts, syn);
-      T fa_s = T(1);
-      if (NORM && !APAR && d.a_kind == OP_ARENA) {
-        int ee;
-        fa_s = T(norm_factor(s_max[g * a.n_steps + d.a_prod], &ee));
-      }
+      const T* pa = p.a + (((h << d.lfa) | fa) << d.lk);
+      const T* pb = p.b + ((h << (d.lk + d.lfb)) | fb);
       for (int k = sub; k < K; k += tpo) {
-        const T av = APAR ? parity_val<T>(abase + k, as) : A.ld(abase + k) * fa_s;
-        const T bv = BPAR ? parity_val<T>(bbase + (k << d.lfb), bs) : B.ld(bbase + (k << d.lfb));
+        const T av = pa[k] * fa_s;
+        const T bv = pb[k << d.lfb];
         if (MAXP) {
           const T v = av * bv;
           acc = v > acc ? v : acc;
@@ -514,12 +462,9 @@ __device__ int run_step_splitk(const KArgs& a, const StepDesc& dref, int st, int
       acc = MAXP ? (other > acc ? other : acc) : acc + other;
     }
     if (valid && sub == 0) {
-      if (NORM && !BPAR && d.b_kind == OP_ARENA) {
-        int ee;
-        acc *= T(norm_factor(s_max[g * a.n_steps + d.b_prod], &ee));
-      }
+      if (NORM) acc *= fb_s;
       const int addr = d.perm_off < 0 ? e : perm_addr(ptab, d.perm_off, e, lw);
-      arena_g[d.out_off + addr] = acc;
+      p.out[addr] = acc;
       if (NORM) {
         const uint32_t bits = __float_as_uint(float(acc));
         if (G1) run_bits = bits > run_bits ? bits : run_bits;
@@ -528,7 +473,6 @@ __device__ int run_step_splitk(const KArgs& a, const StepDesc& dref, int st, int
     }
   }
   if (NORM && G1) flush_max(vt0 < total, run_bits, &s_max[st]);
-  return total_r;
 }
 
 // Most probable configuration: after the max-product pass every runtime
@@ -538,7 +482,8 @@ __device__ int run_step_splitk(const KArgs& a, const StepDesc& dref, int st, int
 // (first maximum) gives the values of the labels the step maximised over.
 // One warp per syndrome; lanes split the k range.
 template <typename T>
-__device__ void backtrack(const KArgs& a, const StepDesc* s_steps, const uint32_t* s_syn, uint32_t* s_asg, T* arena,
+__device__ void backtrack(const KArgs& a, const StepDesc* s_steps, const uint32_t* s_syn, uint32_t* s_asg,
+                          const Arena<T>& arena,
                           const T* consts, int64_t base, int64_t nrows) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int nwarps = blockDim.x >> 5;
@@ -547,7 +492,7 @@ __device__ void backtrack(const KArgs& a, const StepDesc* s_steps, const uint32_
     if (r >= nrows) continue;
     uint32_t* asg = s_asg + g * a.var_words;
     const uint32_t* syn = s_syn + g * a.syn_words;
-    T* arena_g = arena + int64_t(g) * a.arena_elems;
+    const Arena<T> arena_g = arena.of(g);
     for (int w = lane; w < a.var_words; w += 32) {
       uint32_t v = 0;
       for (int b = 0; b < 32; ++b) {
@@ -662,29 +607,31 @@ __device__ __forceinline__ StepShape step_shape(int lh, int lfa, int lfb, int lk
 // operands become syndrome-selected tables), so each step shape has one code
 // path: the kernel stays small enough for the instruction caches.
 template <typename T, bool NORM, bool MAXP, bool G1>
-__device__ __forceinline__ int dispatch_step(const KArgs& a, const StepDesc& d, const StepShape& sh, int st,
-                                             int item_base, const uint32_t* s_syn, uint32_t* s_max, T* arena,
-                                             const T* consts, const PermTab& ptab) {
+__device__ __forceinline__ void dispatch_step(const KArgs& a, const StepDesc& d, const StepShape& sh, int st,
+                                              int item_base, uint32_t* s_max, const StepPtrs<T>* ptrs,
+                                              const PermTab& ptab) {
   switch (sh.kind) {
     case SK_SPLITK:
-      return run_step_splitk<T, NORM, false, false, MAXP, G1>(a, d, st, item_base, sh.lt, s_syn, s_max, arena, consts,
-                                                              ptab);
+      run_step_splitk<T, NORM, MAXP, G1>(a, d, st, item_base, sh.lt, s_max, ptrs, ptab);
+      break;
     case SK_VEC8:
-      return run_step_vec<T, 8, NORM, false, false, MAXP, G1>(a, d, st, item_base, s_syn, s_max, arena, consts, ptab);
+      run_step_vec<T, 8, NORM, MAXP, G1>(a, d, st, item_base, s_max, ptrs, ptab);
+      break;
     case SK_VEC4:
-      return run_step_vec<T, 4, NORM, false, false, MAXP, G1>(a, d, st, item_base, s_syn, s_max, arena, consts, ptab);
+      run_step_vec<T, 4, NORM, MAXP, G1>(a, d, st, item_base, s_max, ptrs, ptab);
+      break;
     default:
-      return run_step<T, NORM, false, false, MAXP, G1>(a, d, st, item_base, s_syn, s_max, arena, consts, ptab);
+      run_step<T, NORM, MAXP, G1>(a, d, st, item_base, s_max, ptrs, ptab);
   }
 }
 
-// float64 blocks are capped at 512 threads, which leaves them 128 registers
 // Shared-memory layout of a block working on program `a`: step records,
 // syndrome words, per-step maxima (float32), MAP assignments, then the
 // staged tables (if any) and the arena (if in shared memory).
 struct BlockSmem {
   StepDesc* steps;
   int2* plan;  // per step: x = kind | lt << 8 | per-syndrome << 16, y = items (see fill_step_plan)
+  void* ptrs;  // per syndrome and step: StepPtrs (operand and output bases)
   uint32_t* syn;
   uint32_t* max;
   uint32_t* asg;
@@ -698,6 +645,8 @@ __device__ __forceinline__ BlockSmem carve_smem(const KArgs& a, unsigned char* s
   size_t off = size_t(a.n_steps) * sizeof(StepDesc);
   b.plan = reinterpret_cast<int2*>(smem + off);
   off += size_t(a.n_steps) * sizeof(int2);
+  b.ptrs = smem + off;
+  off += size_t(a.G) * a.n_steps * 3 * sizeof(void*);
   b.syn = reinterpret_cast<uint32_t*>(smem + off);
   off += size_t(a.G) * a.syn_words * 4;
   b.max = reinterpret_cast<uint32_t*>(smem + off);
@@ -737,11 +686,13 @@ __device__ __forceinline__ void fill_step_plan(const KArgs& a, const StepDesc* s
 // the whole program: load the syndrome words, run every step, back-track
 // (MAP), then the epilogue.  Ends with a block barrier.
 template <typename T, bool NORM, bool MAXP>
-__device__ void contract_group(const KArgs& a, int64_t base, int64_t nrows, const BlockSmem& sm, T* arena,
+__device__ void contract_group(const KArgs& a, int64_t base, int64_t nrows, const BlockSmem& sm,
+                               const Arena<T>& arena,
                                const T* consts, const PermTab& ptab) {
   const StepDesc* s_steps = sm.steps;
   uint32_t* s_syn = sm.syn;
   uint32_t* s_max = sm.max;
+  StepPtrs<T>* s_ptrs = static_cast<StepPtrs<T>*>(sm.ptrs);
   for (int i = threadIdx.x; i < a.G * a.syn_words; i += blockDim.x) {
     const int g = i / a.syn_words, w = i - g * a.syn_words;
     const int64_t r = base + g;
@@ -759,6 +710,8 @@ __device__ void contract_group(const KArgs& a, int64_t base, int64_t nrows, cons
   if (NORM)
     for (int i = threadIdx.x; i < a.G * a.n_steps; i += blockDim.x) s_max[i] = 0u;
   __syncthreads();
+  fill_step_ptrs<T>(a, s_steps, s_syn, arena, consts, s_ptrs);
+  __syncthreads();
   int item_base = 0;
   for (int st = 0; st < a.n_steps; ++st) {
     const StepDesc& d = s_steps[st];
@@ -774,15 +727,14 @@ __device__ void contract_group(const KArgs& a, int64_t base, int64_t nrows, cons
     const int vt_warp = rotated(int(threadIdx.x & ~31u), item_base);
     if (vt_warp < items) {
       if (a.G == 1) {
-        dispatch_step<T, NORM, MAXP, true>(a, d, sh, st, item_base, s_syn, s_max, arena, consts, ptab);
+        dispatch_step<T, NORM, MAXP, true>(a, d, sh, st, item_base, s_max, s_ptrs, ptab);
       } else if (per_syndrome) {
         // the block's syndromes one after another with hoisted invariants
         for (int g = 0; g < a.G; ++g)
-          dispatch_step<T, NORM, MAXP, true>(a, d, sh, st, item_base, s_syn + g * a.syn_words,
-                                             s_max + g * a.n_steps, arena + int64_t(g) * a.arena_elems, consts,
-                                             ptab);
+          dispatch_step<T, NORM, MAXP, true>(a, d, sh, st, item_base, s_max + g * a.n_steps,
+                                             s_ptrs + g * a.n_steps, ptab);
       } else {
-        dispatch_step<T, NORM, MAXP, false>(a, d, sh, st, item_base, s_syn, s_max, arena, consts, ptab);
+        dispatch_step<T, NORM, MAXP, false>(a, d, sh, st, item_base, s_max, s_ptrs, ptab);
       }
     }
     if (d.flags & kStepSync) {
@@ -797,12 +749,11 @@ __device__ void contract_group(const KArgs& a, int64_t base, int64_t nrows, cons
     __syncthreads();
   }
   // epilogue: log-marginals, first argmax (Julia findmax order), recheck flag
-  const StepDesc& root = s_steps[a.n_steps - 1];
   for (int g = threadIdx.x; g < a.G; g += blockDim.x) {
     const int64_t r = base + g;
     if (r >= nrows) continue;
     const int64_t row = a.list ? int64_t(a.list[r]) : r + a.row_offset;
-    const T* rv = arena + int64_t(g) * a.arena_elems;
+    const T* rv = s_ptrs[g * a.n_steps + a.n_steps - 1].out;
     double lsc = 0.0;
     if (NORM) {
       for (int st = 0; st < a.n_steps - 1; ++st) {
@@ -815,7 +766,7 @@ __device__ void contract_group(const KArgs& a, int64_t base, int64_t nrows, cons
     double best = -INFINITY, second = -INFINITY;
     int bc = 0;
     for (int c = 0; c < a.n_classes; ++c) {
-      const double v = double(rv[root.out_off + c]);
+      const double v = double(rv[c]);
       const double lp = v > 0.0 ? log(v) + lsc : -INFINITY;
       if (a.logp_out) a.logp_out[row * a.n_classes + c] = lp;
       if (lp > best) {
@@ -858,6 +809,21 @@ __device__ __forceinline__ void stage_tables(const KArgs& a, unsigned char* smem
   *ptab = PermTab{s_perm, a.perm16 != nullptr};
 }
 
+// The block's arenas: all in shared memory (smem_tail) or all in global
+// memory, or -- with a.arena_small set -- the small-tensor pools in shared
+// memory and the big-tensor pools in global memory.
+template <typename T>
+__device__ __forceinline__ Arena<T> block_arena(const KArgs& a, unsigned char* smem_tail, void* global) {
+  T* sm = reinterpret_cast<T*>(smem_tail);
+  if (a.arena_small > 0) {
+    const int64_t big = a.arena_elems - a.arena_small;
+    T* gb = reinterpret_cast<T*>(global) + int64_t(blockIdx.x) * a.G * big;
+    return Arena<T>{sm, gb - a.arena_small, int32_t(a.arena_small), int32_t(a.arena_small), int32_t(big)};
+  }
+  T* base = global ? reinterpret_cast<T*>(global) + int64_t(blockIdx.x) * a.G * a.arena_elems : sm;
+  return Arena<T>{base, base, INT32_MAX, int32_t(a.arena_elems), int32_t(a.arena_elems)};
+}
+
 // float64 blocks are capped at 512 threads, which leaves them 128 registers
 template <typename T, bool NORM, bool MAXP>
 __global__ void __launch_bounds__(sizeof(T) == 8 ? 512 : 1024) tn_contract_kernel(KArgs a) {
@@ -867,9 +833,7 @@ __global__ void __launch_bounds__(sizeof(T) == 8 ? 512 : 1024) tn_contract_kerne
   const T* consts;
   PermTab ptab;
   stage_tables<T>(a, smem, &off, &consts, &ptab);
-  T* arena = a.arena_global
-                 ? reinterpret_cast<T*>(a.arena_global) + int64_t(blockIdx.x) * a.G * a.arena_elems
-                 : reinterpret_cast<T*>(smem + off);
+  const Arena<T> arena = block_arena<T>(a, smem + off, a.arena_global);
   copy16(sm.steps, a.steps, size_t(a.n_steps) * sizeof(StepDesc));
   __syncthreads();
   fill_step_plan<T>(a, sm.steps, sm.plan);
@@ -906,7 +870,8 @@ __global__ void __launch_bounds__(kMultiThreads) tn_contract_multi_kernel(MultiA
       fill_step_plan<T>(a, sm.steps, sm.plan);
       __syncthreads();
     }
-    T* arena = a.arena_global ? gslice : reinterpret_cast<T*>(smem + sm.tail);
+    T* abase = a.arena_global ? gslice : reinterpret_cast<T*>(smem + sm.tail);
+    const Arena<T> arena{abase, abase, INT32_MAX, int32_t(a.arena_elems), int32_t(a.arena_elems)};
     contract_group<T, NORM, false>(a, base, nrows, sm, arena, reinterpret_cast<const T*>(a.consts),
                                    PermTab{a.perm, false});
   };
@@ -956,7 +921,8 @@ __global__ void multi_advance_kernel(int32_t* batch, int32_t* next_unit, int32_t
 size_t contract_smem_bytes(int precision, int32_t n_steps, int32_t syn_words, int G,
                            int64_t arena_elems, bool arena_in_smem, int32_t var_words, size_t table_bytes) {
   const bool norm = precision == 1;
-  size_t off = size_t(n_steps) * (sizeof(StepDesc) + 8) + size_t(G) * syn_words * 4;
+  size_t off = size_t(n_steps) * (sizeof(StepDesc) + 8) + size_t(G) * n_steps * 3 * sizeof(void*) +
+               size_t(G) * syn_words * 4;
   if (norm) off += size_t(G) * n_steps * 4;
   off += size_t(G) * var_words * 4;
   off = (off + 15) & ~size_t(15);

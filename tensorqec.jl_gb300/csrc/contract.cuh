@@ -34,6 +34,9 @@ struct KArgs {
   int32_t G, lg;  // syndromes per block and log2(G)
   int64_t arena_elems;
   void* arena_global;  // NULL: arena in shared memory
+  // > 0: the first arena_small elements of each arena (the small tensors)
+  // are in shared memory and the rest in arena_global
+  int64_t arena_small;
   int32_t n_classes;
   int32_t* class_out;
   double* logp_out;
@@ -51,7 +54,6 @@ struct KArgs {
   const int32_t* report;  // variables whose values are returned
   int32_t n_report;
   uint8_t* assign_out;    // n x ceil(n_report / 8) bit-packed values
-  int64_t pad_;           // keeps the size a multiple of 16 bytes (staged with 16-byte copies)
 };
 static_assert(sizeof(KArgs) % 16 == 0, "KArgs is copied in 16-byte units");
 
