@@ -56,6 +56,10 @@ extern "C" {
 #define TQEC_FLAG_MAP 4u      /* most probable configuration (TNMAP): the network's
                                  out_labels name the variables whose values are
                                  reported; the contraction maximises over all */
+/* launch shape: keep each syndrome's small intermediates (at most 4096
+ * elements) in shared memory and its large ones in global memory; only for
+ * programs that have both kinds (others keep their default shape) */
+#define TQEC_FLAG_SPLIT_ARENA 8u
 
 /* The factor graph, as built by compile(::TNMMAP, ...) (tndecoder.jl:97-146
  * for CSS codes, :186-219 for detector error models). */
@@ -108,6 +112,9 @@ typedef struct {
   int32_t group_f64, threads_f64, smem_f64; /* launch shape chosen for F64 */
   int32_t resident_f32, resident_f64;       /* most blocks in flight on the device */
   int32_t tables_smem_f32, tables_smem_f64; /* 1: tables staged in shared memory */
+  int64_t arena_small;       /* elements of the small-tensor pool (0: one pool) */
+  int32_t split_f32, split_f64;             /* 1: small pool in shared, big pool in global memory */
+  int32_t reserved_;
 } tqec_program_info_t;
 
 typedef struct tqec_program tqec_program;

@@ -48,6 +48,7 @@ struct Shape {
   int threads = 256;
   bool smem_arena = true;
   bool smem_tables = false;  // constants and permutation tables staged in shared memory
+  bool split = false;        // small-tensor pool in shared memory, big-tensor pool in global memory
   size_t smem = 0;
   int grid_cap = 1;  // blocks resident on the whole device
 };
@@ -184,6 +185,31 @@ int choose_shape(tqec_program* p, int precision, int G_req, int threads_req, int
   return TQEC_OK;
 }
 
+// A split shape: G syndromes per block with their small-tensor pools in
+// shared memory and their big-tensor pools in global memory (programs that
+// have both pools).
+int choose_split_shape(tqec_program* p, int precision, int G, int threads, int tables, Shape* out) {
+  if (p->plan.arena_small <= 0 || p->plan.map_mode) return fail(TQEC_ERR_UNSUPPORTED, "program has one pool");
+  const size_t limit = tqec::contract_smem_limit(p->device);
+  const int nsteps = (int)p->plan.steps.size();
+  Shape s;
+  s.G = G;
+  s.threads = std::min(threads, tqec::contract_max_threads(precision));
+  while (s.threads & (s.threads - 1)) s.threads &= s.threads - 1;
+  s.threads = std::max(s.threads, 32);
+  s.smem_arena = false;
+  s.split = true;
+  const size_t tb = tables ? table_bytes(p, precision) : 0;
+  s.smem_tables = tb > 0;
+  s.smem = tqec::contract_smem_bytes(precision, nsteps, syn_words(p), G, p->plan.arena_small, true, 0, tb);
+  if (s.smem > limit) return fail(TQEC_ERR_UNSUPPORTED, "program does not fit shared memory even with a global arena");
+  int occ = tqec::contract_occupancy(precision, s.threads, s.smem, p->plan.map_mode);
+  if (occ < 1) return fail(TQEC_ERR_UNSUPPORTED, "launch shape cannot be resident on this device");
+  s.grid_cap = occ * p->sm_count;
+  *out = s;
+  return TQEC_OK;
+}
+
 // The launch shape for a batch of n rows.
 const Shape& pick_shape(const tqec_program* p, int precision, int64_t n) {
   const auto& v = p->sized[precision];
@@ -198,7 +224,8 @@ const Shape& pick_shape(const tqec_program* p, int precision, int64_t n) {
 int ensure_arena(tqec_program* p, int precision, const Shape& s, int grid) {
   if (s.smem_arena) return TQEC_OK;
   const size_t esz = precision == TQEC_F32 ? 4 : 8;
-  const size_t want = size_t(grid) * s.G * size_t(p->plan.arena_elems) * esz;
+  const int64_t per = s.split ? p->plan.arena_elems - p->plan.arena_small : p->plan.arena_elems;
+  const size_t want = size_t(grid) * s.G * size_t(per) * esz;
   TQ_CUDA(p->arena[precision].ensure(want));
   return TQEC_OK;
 }
@@ -252,6 +279,7 @@ int launch_rows(tqec_program* p, int precision, tqec::KArgs a, int64_t n_rows_ma
   a.tables_smem = s.smem_tables ? 1 : 0;
   a.perm16 = s.smem_tables ? p->d_perm16 : nullptr;
   a.arena_global = s.smem_arena ? nullptr : p->arena[precision].p;
+  a.arena_small = s.split ? p->plan.arena_small : 0;
   TQ_CUDA(tqec::contract_launch(precision, a, grid, s.threads, s.smem, st));
   return TQEC_OK;
 }
@@ -524,13 +552,17 @@ int tqec_program_create(const tqec_network* net, const tqec_tree* tree, const tq
   *p->h_count = 0;
   if ((e = cudaGetLastError()) != cudaSuccess) return bail(TQEC_ERR_CUDA, cudaGetErrorString(e));
   int rc;
-  if ((rc = choose_shape(p, TQEC_F32, o.group, o.threads, -1, &p->shape[TQEC_F32])) != TQEC_OK) {
-    std::string m = g_last_error;
-    return bail(rc, m);
-  }
-  if ((rc = choose_shape(p, TQEC_F64, o.group, o.threads, -1, &p->shape[TQEC_F64])) != TQEC_OK) {
-    std::string m = g_last_error;
-    return bail(rc, m);
+  for (int prec : {TQEC_F32, TQEC_F64}) {
+    Shape sp;
+    if ((o.flags & TQEC_FLAG_SPLIT_ARENA) && p->plan.arena_small > 0 &&
+        choose_split_shape(p, prec, std::max(1, o.group), o.threads > 0 ? o.threads : 256, 0, &sp) == TQEC_OK) {
+      p->shape[prec] = sp;
+      continue;
+    }
+    if ((rc = choose_shape(p, prec, o.group, o.threads, -1, &p->shape[prec])) != TQEC_OK) {
+      std::string m = g_last_error;
+      return bail(rc, m);
+    }
   }
   if ((rc = choose_shape(p, TQEC_F64, 1, tqec::contract_max_threads(TQEC_F64), 1, &p->recheck_shape)) != TQEC_OK) {
     std::string m = g_last_error;
@@ -584,6 +616,9 @@ int tqec_program_info(const tqec_program* p, tqec_program_info_t* info) {
   info->resident_f64 = p->shape[TQEC_F64].grid_cap;
   info->tables_smem_f32 = p->shape[TQEC_F32].smem_tables ? 1 : 0;
   info->tables_smem_f64 = p->shape[TQEC_F64].smem_tables ? 1 : 0;
+  info->arena_small = p->plan.arena_small;
+  info->split_f32 = p->shape[TQEC_F32].split ? 1 : 0;
+  info->split_f64 = p->shape[TQEC_F64].split ? 1 : 0;
   return TQEC_OK;
 }
 
@@ -674,8 +709,13 @@ bool tune_shape(tqec_program* p, int prec, int64_t n, cudaEvent_t e0, cudaEvent_
         // global-arena shapes also try fewer resident blocks per SM, so that
         // the arenas in flight can stay in L2
         for (int resident : {0, 8, 4, 2, 1}) {
+         for (int split : {0, 1}) {
           Shape s;
-          if (choose_shape(p, prec, G, th, tables, &s) != TQEC_OK) continue;
+          if (split) {
+            if (choose_split_shape(p, prec, G, th, tables, &s) != TQEC_OK) continue;
+          } else if (choose_shape(p, prec, G, th, tables, &s) != TQEC_OK) {
+            continue;
+          }
           if (tables && !s.smem_tables) continue;
           if (resident) {
             if (s.smem_arena || tables || resident * p->sm_count >= s.grid_cap) continue;
@@ -701,6 +741,7 @@ bool tune_shape(tqec_program* p, int prec, int64_t n, cudaEvent_t e0, cudaEvent_
             best_ms = ms;
             best = s;
           }
+         }
         }
       }
     }

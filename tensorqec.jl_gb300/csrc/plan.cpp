@@ -584,36 +584,51 @@ std::string build_plan(const NetworkView& net, int32_t n_steps, const int32_t* s
     return "constant data above 2^31 entries";
   }
 
-  // ---- arena: first fit in execution order --------------------------------
+  // ---- arena: first fit in execution order, in two pools ------------------
+  // Intermediates of more than kBigElems elements go to the big pool, the
+  // rest to the small pool; a launch may keep the small pool in shared memory
+  // and the big pool in global memory.  Offsets: small pool [0, S), big pool
+  // [S, S + B) once S is known (patched after allocation).
+  constexpr int64_t kBigElems = 4096;
   struct Block { int64_t off, size; };
-  std::vector<Block> free_list = {{0, int64_t(1) << 40}};
-  std::vector<int64_t> arena_off(nodes.size(), -1);
-  int64_t arena_top = 0;
-  auto alloc = [&](int64_t sz) {
-    sz = (sz + 7) & ~int64_t(7);
-    for (size_t i = 0; i < free_list.size(); ++i) {
-      if (free_list[i].size >= sz) {
-        int64_t off = free_list[i].off;
-        free_list[i].off += sz;
-        free_list[i].size -= sz;
-        if (free_list[i].size == 0) free_list.erase(free_list.begin() + i);
-        arena_top = std::max(arena_top, off + sz);
-        return off;
+  struct Pool {
+    std::vector<Block> free_list = {{0, int64_t(1) << 40}};
+    int64_t top = 0;
+    int64_t alloc(int64_t sz) {
+      sz = (sz + 7) & ~int64_t(7);
+      for (size_t i = 0; i < free_list.size(); ++i) {
+        if (free_list[i].size >= sz) {
+          int64_t off = free_list[i].off;
+          free_list[i].off += sz;
+          free_list[i].size -= sz;
+          if (free_list[i].size == 0) free_list.erase(free_list.begin() + i);
+          top = std::max(top, off + sz);
+          return off;
+        }
       }
+      return int64_t(-1);
     }
-    return int64_t(-1);
-  };
-  auto release = [&](int64_t off, int64_t sz) {
-    sz = (sz + 7) & ~int64_t(7);
-    free_list.push_back({off, sz});
-    std::sort(free_list.begin(), free_list.end(), [](const Block& a, const Block& b) { return a.off < b.off; });
-    std::vector<Block> merged;
-    for (const Block& b : free_list) {
-      if (!merged.empty() && merged.back().off + merged.back().size == b.off) merged.back().size += b.size;
-      else merged.push_back(b);
+    void release(int64_t off, int64_t sz) {
+      sz = (sz + 7) & ~int64_t(7);
+      free_list.push_back({off, sz});
+      std::sort(free_list.begin(), free_list.end(), [](const Block& a, const Block& b) { return a.off < b.off; });
+      std::vector<Block> merged;
+      for (const Block& b : free_list) {
+        if (!merged.empty() && merged.back().off + merged.back().size == b.off) merged.back().size += b.size;
+        else merged.push_back(b);
+      }
+      free_list.swap(merged);
     }
-    free_list.swap(merged);
   };
+  Pool small_pool, big_pool;
+  std::vector<int64_t> arena_off(nodes.size(), -1);
+  std::vector<char> in_big(nodes.size(), 0);
+  auto alloc_node = [&](int id, int64_t sz) {
+    in_big[id] = sz > kBigElems;
+    arena_off[id] = (in_big[id] ? big_pool : small_pool).alloc(sz);
+    return arena_off[id];
+  };
+  auto release_node = [&](int id, int64_t sz) { (in_big[id] ? big_pool : small_pool).release(arena_off[id], sz); };
   // ---- barrier groups: consecutive steps that do not read each other's
   // outputs run between the same pair of block barriers.  Wide steps stay
   // alone (they fill the block by themselves and dominate the arena).
@@ -652,14 +667,13 @@ std::string build_plan(const NetworkView& net, int32_t n_steps, const int32_t* s
     StepLayout& L = lay[r];
     const int64_t osz = int64_t(1) << n.vars.size();
     width = std::max(width, (int)n.vars.size());
-    int64_t off = alloc(osz);
-    arena_off[id] = off;
+    int64_t off = alloc_node(id, osz);
     // operands are freed when the whole barrier group has run
     for (int op : {L.a, L.b})
       if (nodes[op].kind == NK_RUNTIME) pending_release.push_back(op);
     if (group_end[r]) {
       if (!map_mode)  // MAP back-tracking reads every intermediate again
-        for (int op : pending_release) release(arena_off[op], int64_t(1) << nodes[op].vars.size());
+        for (int op : pending_release) release_node(op, int64_t(1) << nodes[op].vars.size());
       pending_release.clear();
     }
     if (map_mode) {
@@ -748,7 +762,17 @@ std::string build_plan(const NetworkView& net, int32_t n_steps, const int32_t* s
         return "MAP mode: a reported label is never maximised over (is it an output of the tree?)";
       }
   }
-  P.arena_elems = std::max<int64_t>((arena_top + 31) & ~int64_t(31), 32);
+  // the big pool follows the small one: patch its tensors' offsets
+  const int64_t S = (small_pool.top + 31) & ~int64_t(31);
+  const int64_t Bg = (big_pool.top + 31) & ~int64_t(31);
+  for (int r = 0; r < R; ++r) {
+    StepDesc& d = P.steps[r];
+    if (in_big[order[r]]) d.out_off += (int32_t)S;
+    if (d.a_kind == OP_ARENA && in_big[order[d.a_prod]]) d.a_ref += (int32_t)S;
+    if (d.b_kind == OP_ARENA && in_big[order[d.b_prod]]) d.b_ref += (int32_t)S;
+  }
+  P.arena_small = Bg > 0 ? S : 0;
+  P.arena_elems = std::max<int64_t>(S + Bg, 32);
   P.root_step = R - 1;
   P.macs_runtime = macs_rt;
   P.err_terms = err_terms;

@@ -56,6 +56,7 @@ struct Plan {
   int32_t n_tree_steps = 0;
   int32_t width = 0;               // log2 of the widest runtime intermediate
   int64_t arena_elems = 0;         // per syndrome
+  int64_t arena_small = 0;         // elements of the small-tensor pool at the arena's start (0: one pool)
   int32_t root_step = -1;          // the last runtime step
   double macs_runtime = 0.0;       // multiply-adds per syndrome, runtime steps
   double macs_tree = 0.0;          // multiply-adds of the tree as given

@@ -130,12 +130,14 @@ class TNMMAP:
     device: int = 0
     group: int = 0
     threads: int = 0
+    split_arena: bool = False
 
     def _native_precision(self):
         return {"f64": native.TQEC_F64, "f32": native.TQEC_F32}[self.precision]
 
     def _flags(self):
-        return native.TQEC_FLAG_PLAIN if self.plain else 0
+        return ((native.TQEC_FLAG_PLAIN if self.plain else 0) |
+                (native.TQEC_FLAG_SPLIT_ARENA if self.split_arena else 0))
 
 
 class CompiledTNMMAP:

@@ -19,6 +19,7 @@ TQEC_F32 = 1
 TQEC_FLAG_PLAIN = 1
 TQEC_FLAG_NORECHECK = 2
 TQEC_FLAG_MAP = 4
+TQEC_FLAG_SPLIT_ARENA = 8
 
 ERRORS = {-1: "invalid argument", -2: "CUDA error", -3: "out of device memory",
           -4: "unsupported network", -5: "timeout", -6: "I/O error"}
@@ -53,7 +54,8 @@ class ProgramInfo(C.Structure):
                 ("group_f32", C.c_int32), ("threads_f32", C.c_int32), ("smem_f32", C.c_int32),
                 ("group_f64", C.c_int32), ("threads_f64", C.c_int32), ("smem_f64", C.c_int32),
                 ("resident_f32", C.c_int32), ("resident_f64", C.c_int32), ("tables_smem_f32", C.c_int32),
-                ("tables_smem_f64", C.c_int32)]
+                ("tables_smem_f64", C.c_int32), ("arena_small", C.c_int64), ("split_f32", C.c_int32),
+                ("split_f64", C.c_int32), ("reserved_", C.c_int32)]
 
 
 class PlanView(C.Structure):

@@ -219,3 +219,32 @@ def test_gpu_error_patterns(pkg, oracle, kind, d):
     res = ct.decode(pkg.CSSSyndrome(syn.sx[0], syn.sz[0]))
     assert res.success_tag and pkg.syndrome_extraction(res.error_pattern, t) == pkg.CSSSyndrome(syn.sx[0], syn.sz[0])
     ct.close()
+
+
+@pytest.mark.parametrize("group,threads", [(1, 256), (2, 128), (2, 512), (1, 1024)])
+def test_split_arena_shapes_vs_plain_f64(pkg, group, threads):
+    """Launch shapes that keep each syndrome's small intermediates in shared
+    memory and its large ones in global memory give the float64 result
+    (float32 within its bound) and the same decisions."""
+    t = pkg.tanner_graph(pkg.SurfaceCode(7, 7))
+    em = pkg.depolarizing(0.05, t.nq)
+    rng = np.random.default_rng(77)
+    ep = pkg.random_error_pattern(em, rng, nsamples=300)
+    s = pkg.syndrome_extraction(ep, t)
+    bits = np.concatenate([s.sx, s.sz], axis=1)
+    ref = pkg.compile(pkg.TNMMAP(precision="f64", plain=True), t, em)
+    want = ref.class_logprobs(bits)
+    ref.close()
+    for precision in ("f64", "f32"):
+        ct = pkg.compile(pkg.TNMMAP(precision=precision, group=group, threads=threads, split_arena=True), t, em)
+        info = ct.program.info
+        assert info["arena_small"] > 0 and info[f"split_{precision}"] == 1
+        lp = ct.class_logprobs(bits)
+        tol = 1e-10 if precision == "f64" else 2 * info["err_bound_f32"]
+        top = np.max(want, axis=1, keepdims=True)
+        assert np.max(np.abs(np.exp(lp - top) - np.exp(want - top))) <= tol
+        cls = ct.decode_batch(bits)
+        srt = np.sort(want, axis=1)
+        tie = (srt[:, -1] - srt[:, -2]) <= 1e-9
+        assert not ((cls != np.argmax(want, axis=1)) & ~tie).any()
+        ct.close()
