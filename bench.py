@@ -58,6 +58,8 @@ def parse():
     ap.add_argument("--circuit-n", type=int, default=262144)
     ap.add_argument("--group", type=int, default=0, help="--profile: syndromes per block (0: default shape)")
     ap.add_argument("--threads", type=int, default=0, help="--profile: threads per block (0: default shape)")
+    ap.add_argument("--split-arena", action="store_true",
+                    help="--profile: small intermediates in shared memory, large ones in global memory")
     ap.add_argument("--no-surrogate", action="store_true", help="time the batched exact decoder alone")
     ap.add_argument("--train-n", type=int, default=1 << 24, help="surrogate training syndromes")
     ap.add_argument("--train-epochs", type=int, default=8, help="surrogate training epochs")
@@ -418,7 +420,7 @@ def run_ours(args):
                          # flops per cycle at the sampled SM clock (nominal, not measured)
                          "fp32_simt_peak_tflops": fp32_peak,
                          "frac_of_fp32_simt_peak": achieved_tflops / fp32_peak,
-                         "traffic_note": "dram read+write of the autotuned global-arena shape, per 65,536 "
+                         "traffic_note": "dram read+write of the autotuned split-arena shape, per 65,536 "
                                          "syndromes (ncu, scaled from 16,384)"},
             "surrogate_gemm": mlp_part,
             "cpu_baseline": cpu,
@@ -449,7 +451,8 @@ def run_profile(args):
 
     pkg = G.load_package()
     t, em, bits = workload(pkg, 0, 1, args.batch)
-    ct = pkg.compile(pkg.TNMMAP(precision="f32", group=args.group, threads=args.threads), t, em)
+    ct = pkg.compile(pkg.TNMMAP(precision="f32", group=args.group, threads=args.threads,
+                                split_arena=args.split_arena), t, em)
     d_syn = torch.from_numpy(pkg.pack_syndromes(bits[0])).cuda()
     d_lp = torch.empty((args.batch, ct.n_classes), dtype=torch.float64, device="cuda")
     sptr = torch.cuda.current_stream().cuda_stream

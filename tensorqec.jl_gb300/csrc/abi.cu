@@ -564,10 +564,16 @@ int tqec_program_create(const tqec_network* net, const tqec_tree* tree, const tq
       return bail(rc, m);
     }
   }
-  if ((rc = choose_shape(p, TQEC_F64, 1, tqec::contract_max_threads(TQEC_F64), 1, &p->recheck_shape)) != TQEC_OK) {
-    std::string m = g_last_error;
-    return bail(rc, m);
+  // the recheck keeps the small intermediates and the tables in shared
+  // memory when the program has both pools and they fit
+  if (p->plan.arena_small <= 0 ||
+      choose_split_shape(p, TQEC_F64, 1, tqec::contract_max_threads(TQEC_F64), 1, &p->recheck_shape) != TQEC_OK) {
+    if ((rc = choose_shape(p, TQEC_F64, 1, tqec::contract_max_threads(TQEC_F64), 1, &p->recheck_shape)) != TQEC_OK) {
+      std::string m = g_last_error;
+      return bail(rc, m);
+    }
   }
+  g_last_error.clear();
   *out = p;
   return TQEC_OK;
 }
