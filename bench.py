@@ -71,7 +71,9 @@ def parse():
 def workload(pkg, rank, nbatches, batch):
     t = pkg.tanner_graph(pkg.SurfaceCode(D, D))
     em = pkg.depolarizing(P, t.nq)
-    rng = np.random.default_rng(SEED + rank)
+    from tensorqec_gb300.replicas import rank_seed
+
+    rng = np.random.default_rng(rank_seed(SEED, rank))
     bits = []
     for _ in range(nbatches):
         ep = pkg.random_error_pattern(em, rng, nsamples=batch)
@@ -384,13 +386,12 @@ def run_ours(args):
     plain_rate = m / (pms[0] / 1e3)
     plain.close()
 
-    # max over ranks
-    if dist:
-        tt = torch.tensor([step_ms, e2e_step], dtype=torch.float64, device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        step_ms, e2e_step = tt.tolist()
-    value = world * B / (step_ms / 1e3)
-    e2e_value = world * B / (e2e_step / 1e3)
+    # max over ranks (replicas: the slowest rank sets the step)
+    from tensorqec_gb300.replicas import job_rate, reduce_max
+
+    step_ms, e2e_step = reduce_max([step_ms, e2e_step], dist, device="cuda")
+    value = job_rate(world, B, step_ms)
+    e2e_value = job_rate(world, B, e2e_step)
 
     if rank == 0:
         cpu, cpu_cls = cpu_baseline(pkg, ct, bits[W], args.cpu_sample)
