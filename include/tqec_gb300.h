@@ -56,8 +56,8 @@ extern "C" {
 #define TQEC_FLAG_MAP 4u      /* most probable configuration (TNMAP): the network's
                                  out_labels name the variables whose values are
                                  reported; the contraction maximises over all */
-/* launch shape: keep each syndrome's small intermediates (at most 4096
- * elements) in shared memory and its large ones in global memory; only for
+/* launch shape: keep each syndrome's small intermediates (at most
+ * tqec_options.big_elems elements) in shared memory and its large ones in global memory; only for
  * programs that have both kinds (others keep their default shape) */
 #define TQEC_FLAG_SPLIT_ARENA 8u
 
@@ -94,6 +94,9 @@ typedef struct {
   double margin;          /* TQEC_F32: recheck when the log-probability margin
                              of the top class is below this; < 0 = the
                              rounding-error bound the planner derives */
+  int32_t big_elems;      /* intermediates above this many elements go to the
+                             big pool (global memory in split layouts); 0 = 1024 */
+  int32_t reserved;
 } tqec_options;
 
 typedef struct {

@@ -488,6 +488,8 @@ int tqec_program_create(const tqec_network* net, const tqec_tree* tree, const tq
                       net->n_out, net->out_labels, net->n_syndrome, net->syndrome_tensors};
   tqec::PlanLimits lim;
   lim.map_mode = (o.flags & TQEC_FLAG_MAP) != 0;
+  if (o.big_elems < 0) return fail(TQEC_ERR_INVALID, "big_elems must be >= 0");
+  if (o.big_elems > 0) lim.big_elems = o.big_elems;
   auto* p = new tqec_program();
   bool unsupported = false;
   std::string err = tqec::build_plan(v, tree->n_steps, tree->steps, lim, &p->plan, &unsupported);

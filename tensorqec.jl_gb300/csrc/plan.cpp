@@ -589,7 +589,7 @@ std::string build_plan(const NetworkView& net, int32_t n_steps, const int32_t* s
   // rest to the small pool; a launch may keep the small pool in shared memory
   // and the big pool in global memory.  Offsets: small pool [0, S), big pool
   // [S, S + B) once S is known (patched after allocation).
-  constexpr int64_t kBigElems = 4096;
+  const int64_t kBigElems = lim.big_elems > 0 ? lim.big_elems : 1024;
   struct Block { int64_t off, size; };
   struct Pool {
     std::vector<Block> free_list = {{0, int64_t(1) << 40}};

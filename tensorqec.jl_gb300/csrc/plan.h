@@ -92,6 +92,7 @@ struct PlanLimits {
   int max_sel_rank = 8;       // ... and up to this many labels
   int max_width = 30;         // refuse intermediates wider than 2^max_width
   bool map_mode = false;      // max-product contraction + back-tracking (TNMAP)
+  int64_t big_elems = 1024;   // intermediates above this size go to the big pool
 };
 
 // Builds the program; returns "" on success or an error message.

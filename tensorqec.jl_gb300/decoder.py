@@ -131,6 +131,7 @@ class TNMMAP:
     group: int = 0
     threads: int = 0
     split_arena: bool = False
+    big_elems: int = 0
 
     def _native_precision(self):
         return {"f64": native.TQEC_F64, "f32": native.TQEC_F32}[self.precision]
@@ -151,7 +152,8 @@ class CompiledTNMMAP:
         self.graph = tnmmap_css_graph(tanner, em, self.lx, self.lz)
         self.steps = optimize_code(self.graph, decoder.optimizer)
         self.program = native.Program(self.graph, self.steps, decoder._native_precision(), decoder._flags(),
-                                      decoder.device, decoder.group, decoder.threads, decoder.margin)
+                                      decoder.device, decoder.group, decoder.threads, decoder.margin,
+                                      decoder.big_elems)
         self._px = gf2.solve_particular(tanner.stgz.H)   # ex from sz
         self._pz = gf2.solve_particular(tanner.stgx.H)   # ez from sx
         self.k = self.lx.shape[0]
@@ -249,7 +251,8 @@ class CompiledDEMTNMMAP:
                                       decoder.factorize)
         self.steps = optimize_code(self.graph, decoder.optimizer)
         self.program = native.Program(self.graph, self.steps, decoder._native_precision(), decoder._flags(),
-                                      decoder.device, decoder.group, decoder.threads, decoder.margin)
+                                      decoder.device, decoder.group, decoder.threads, decoder.margin,
+                                      decoder.big_elems)
         self._part = gf2.solve_particular(self.tanner.H)
         self._logical_fix = self._logical_corrections()
 

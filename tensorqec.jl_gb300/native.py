@@ -43,7 +43,8 @@ class Tree(C.Structure):
 
 class Options(C.Structure):
     _fields_ = [("precision", C.c_int32), ("flags", C.c_uint32), ("device", C.c_int32),
-                ("group", C.c_int32), ("threads", C.c_int32), ("margin", C.c_double)]
+                ("group", C.c_int32), ("threads", C.c_int32), ("margin", C.c_double),
+                ("big_elems", C.c_int32), ("reserved", C.c_int32)]
 
 
 class ProgramInfo(C.Structure):
@@ -200,12 +201,13 @@ def inspect_plan(graph, steps, flags=0):
 class Program:
     """Owner of a ``tqec_program`` (a compiled network on one GPU)."""
 
-    def __init__(self, graph, steps, precision=TQEC_F32, flags=0, device=0, group=0, threads=0, margin=-1.0):
+    def __init__(self, graph, steps, precision=TQEC_F32, flags=0, device=0, group=0, threads=0, margin=-1.0,
+                 big_elems=0):
         L = lib()
         na = NetworkArrays(graph)
         steps = np.ascontiguousarray(steps, dtype=np.int32)
         tree = Tree(steps.shape[0], _ptr(steps))
-        opts = Options(precision, flags, device, group, threads, margin)
+        opts = Options(precision, flags, device, group, threads, margin, big_elems, 0)
         h = C.c_void_p()
         check(L.tqec_program_create(C.byref(na.struct), C.byref(tree), C.byref(opts), C.byref(h)))
         self._h = h
