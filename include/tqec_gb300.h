@@ -117,7 +117,9 @@ typedef struct {
   int32_t tables_smem_f32, tables_smem_f64; /* 1: tables staged in shared memory */
   int64_t arena_small;       /* elements of the small-tensor pool (0: one pool) */
   int32_t split_f32, split_f64;             /* 1: small pool in shared, big pool in global memory */
-  int32_t reserved_;
+  int32_t tensor_steps;      /* GEMM-shaped steps (tcgen05 tf32 in float32 launches) */
+  int32_t tensor_f32;        /* 1: the float32 shape runs them on the tensor cores */
+  int32_t reserved_[2];
 } tqec_program_info_t;
 
 typedef struct tqec_program tqec_program;

@@ -49,6 +49,7 @@ struct Shape {
   bool smem_arena = true;
   bool smem_tables = false;  // constants and permutation tables staged in shared memory
   bool split = false;        // small-tensor pool in shared memory, big-tensor pool in global memory
+  bool tensor = false;       // GEMM-shaped steps on the tensor cores (float32 programs that have them)
   size_t smem = 0;
   int grid_cap = 1;  // blocks resident on the whole device
 };
@@ -85,6 +86,7 @@ struct tqec_program {
   tqec::StepDesc* d_steps = nullptr;
   int32_t* d_perm = nullptr;
   uint16_t* d_perm16 = nullptr;  // the same tables as uint16 (programs of width <= 16)
+  int32_t* d_tc_err = nullptr;   // set by a tensor-core wait that gave up
   int64_t n_perm_padded = 0;     // entries, a multiple of 8
   int32_t* d_vartab = nullptr;   // MAP mode tables
   int32_t* d_report = nullptr;
@@ -138,6 +140,17 @@ size_t table_bytes(const tqec_program* p, int precision) {
 // (unless that would push a one-syndrome arena out of it), 0 keeps them in
 // global memory, -1 stages them only next to a shared-memory arena (a
 // global-arena shape wants small blocks, many per SM).
+bool tensor_program(const tqec_program* p, int precision) {
+  return precision == TQEC_F32 && p->plan.tensor_steps > 0 && !p->plan.map_mode;
+}
+
+// Tensor-core shapes: at most 512 threads (at least 128: four warps read the
+// 128 tensor-memory lanes) and at most four blocks per SM (128 of the 512
+// tensor-memory columns each).
+void finish_tensor_shape(const tqec_program* p, Shape* s) {
+  s->grid_cap = std::min(s->grid_cap, 4 * p->sm_count);
+}
+
 int choose_shape(tqec_program* p, int precision, int G_req, int threads_req, int tables_req, Shape* out) {
   const size_t limit = tqec::contract_smem_limit(p->device);
   const int64_t arena = p->plan.arena_elems;
@@ -145,8 +158,9 @@ int choose_shape(tqec_program* p, int precision, int G_req, int threads_req, int
   const int sw = syn_words(p);
   const int vw = var_words(p);
   const size_t tb_all = table_bytes(p, precision);
+  const bool tensor = tensor_program(p, precision);
   auto bytes = [&](int G, bool arena_smem, size_t tb) {
-    return tqec::contract_smem_bytes(precision, nsteps, sw, G, arena, arena_smem, vw, tb);
+    return tqec::contract_smem_bytes(precision, nsteps, sw, G, arena, arena_smem, vw, tb, tensor);
   };
   Shape s;
   s.threads = threads_req > 0 ? threads_req : 256;
@@ -169,18 +183,20 @@ int choose_shape(tqec_program* p, int precision, int G_req, int threads_req, int
     if (G == 1 && (!s.smem_arena || bytes(1, true, tb) > target))
       s.threads = threads_req > 0 ? threads_req : 1024;
   }
-  s.threads = std::min(s.threads, tqec::contract_max_threads(precision));
+  s.threads = std::min(s.threads, tqec::contract_max_threads(precision, tensor));
   // the kernel's thread rotation needs a power-of-two block (at least a warp)
   while (s.threads & (s.threads - 1)) s.threads &= s.threads - 1;
-  s.threads = std::max(s.threads, 32);
+  s.threads = std::max(s.threads, tensor ? 128 : 32);
+  s.tensor = tensor;
   if (bytes(s.G, s.smem_arena, tb) > limit) tb = 0;
   if (tables_req == 0 || (tables_req < 0 && !s.smem_arena)) tb = 0;
   s.smem_tables = tb > 0;
   s.smem = bytes(s.G, s.smem_arena, tb);
   if (s.smem > limit) return fail(TQEC_ERR_UNSUPPORTED, "program does not fit shared memory even with a global arena");
-  int occ = tqec::contract_occupancy(precision, s.threads, s.smem, p->plan.map_mode);
+  int occ = tqec::contract_occupancy(precision, s.threads, s.smem, p->plan.map_mode, tensor);
   if (occ < 1) return fail(TQEC_ERR_UNSUPPORTED, "launch shape cannot be resident on this device");
   s.grid_cap = occ * p->sm_count;
+  if (tensor) finish_tensor_shape(p, &s);
   *out = s;
   return TQEC_OK;
 }
@@ -192,20 +208,23 @@ int choose_split_shape(tqec_program* p, int precision, int G, int threads, int t
   if (p->plan.arena_small <= 0 || p->plan.map_mode) return fail(TQEC_ERR_UNSUPPORTED, "program has one pool");
   const size_t limit = tqec::contract_smem_limit(p->device);
   const int nsteps = (int)p->plan.steps.size();
+  const bool tensor = tensor_program(p, precision);
   Shape s;
   s.G = G;
-  s.threads = std::min(threads, tqec::contract_max_threads(precision));
+  s.threads = std::min(threads, tqec::contract_max_threads(precision, tensor));
   while (s.threads & (s.threads - 1)) s.threads &= s.threads - 1;
-  s.threads = std::max(s.threads, 32);
+  s.threads = std::max(s.threads, tensor ? 128 : 32);
   s.smem_arena = false;
   s.split = true;
+  s.tensor = tensor;
   const size_t tb = tables ? table_bytes(p, precision) : 0;
   s.smem_tables = tb > 0;
-  s.smem = tqec::contract_smem_bytes(precision, nsteps, syn_words(p), G, p->plan.arena_small, true, 0, tb);
+  s.smem = tqec::contract_smem_bytes(precision, nsteps, syn_words(p), G, p->plan.arena_small, true, 0, tb, tensor);
   if (s.smem > limit) return fail(TQEC_ERR_UNSUPPORTED, "program does not fit shared memory even with a global arena");
-  int occ = tqec::contract_occupancy(precision, s.threads, s.smem, p->plan.map_mode);
+  int occ = tqec::contract_occupancy(precision, s.threads, s.smem, p->plan.map_mode, tensor);
   if (occ < 1) return fail(TQEC_ERR_UNSUPPORTED, "launch shape cannot be resident on this device");
   s.grid_cap = occ * p->sm_count;
+  if (tensor) finish_tensor_shape(p, &s);
   *out = s;
   return TQEC_OK;
 }
@@ -280,11 +299,26 @@ int launch_rows(tqec_program* p, int precision, tqec::KArgs a, int64_t n_rows_ma
   a.perm16 = s.smem_tables ? p->d_perm16 : nullptr;
   a.arena_global = s.smem_arena ? nullptr : p->arena[precision].p;
   a.arena_small = s.split ? p->plan.arena_small : 0;
+  a.tc = s.tensor ? 1 : 0;
+  a.tc_err = p->d_tc_err;
   TQ_CUDA(tqec::contract_launch(precision, a, grid, s.threads, s.smem, st));
   return TQEC_OK;
 }
 
 // Runs the plain form: one launch (one block, one syndrome) per row.
+// After a synchronisation: a tensor-core wait that gave up makes the call fail
+// (its results are not valid); the flag is cleared for the next call.
+int check_tensor_error(tqec_program* p) {
+  if (p->plan.tensor_steps == 0 || !p->d_tc_err) return TQEC_OK;
+  int32_t e = 0;
+  TQ_CUDA(cudaMemcpy(&e, p->d_tc_err, sizeof(e), cudaMemcpyDeviceToHost));
+  if (e) {
+    TQ_CUDA(cudaMemset(p->d_tc_err, 0, sizeof(e)));
+    return fail(TQEC_ERR_TIMEOUT, "a tensor-core step timed out waiting for its MMAs");
+  }
+  return TQEC_OK;
+}
+
 int launch_plain(tqec_program* p, int precision, tqec::KArgs a, int64_t n, cudaStream_t st) {
   Shape s = p->shape[precision];
   const size_t limit = tqec::contract_smem_limit(p->device);
@@ -551,6 +585,8 @@ int tqec_program_create(const tqec_network* net, const tqec_tree* tree, const tq
     if (!P.fixed.empty()) cudaMemcpy(p->d_fixed, P.fixed.data(), P.fixed.size(), cudaMemcpyHostToDevice);
   }
   if ((e = cudaMallocHost(&p->h_count, sizeof(int32_t))) != cudaSuccess) return bail(TQEC_ERR_OOM, "pinned count");
+  if ((e = cudaMalloc(&p->d_tc_err, sizeof(int32_t))) != cudaSuccess) return bail(TQEC_ERR_OOM, "error flag");
+  cudaMemset(p->d_tc_err, 0, sizeof(int32_t));
   *p->h_count = 0;
   if ((e = cudaGetLastError()) != cudaSuccess) return bail(TQEC_ERR_CUDA, cudaGetErrorString(e));
   int rc;
@@ -587,6 +623,7 @@ int tqec_program_destroy(tqec_program* p) {
   cudaFree(p->d_steps);
   cudaFree(p->d_perm);
   cudaFree(p->d_perm16);
+  cudaFree(p->d_tc_err);
   cudaFree(p->d_c64);
   cudaFree(p->d_c32);
   cudaFree(p->d_vartab);
@@ -625,6 +662,8 @@ int tqec_program_info(const tqec_program* p, tqec_program_info_t* info) {
   info->tables_smem_f32 = p->shape[TQEC_F32].smem_tables ? 1 : 0;
   info->tables_smem_f64 = p->shape[TQEC_F64].smem_tables ? 1 : 0;
   info->arena_small = p->plan.arena_small;
+  info->tensor_steps = p->plan.tensor_steps;
+  info->tensor_f32 = p->shape[TQEC_F32].tensor ? 1 : 0;
   info->split_f32 = p->shape[TQEC_F32].split ? 1 : 0;
   info->split_f64 = p->shape[TQEC_F64].split ? 1 : 0;
   return TQEC_OK;
@@ -645,6 +684,7 @@ int tqec_decode_batch(tqec_program* p, const uint8_t* syndromes, int64_t n, int3
       (err_bound_out && !is_device_ptr(err_bound_out))) {
     TQ_CUDA(cudaStreamSynchronize(st));
     p->last_recheck = recheck ? *p->h_count : 0;
+    return check_tensor_error(p);
   }
   return TQEC_OK;
 }
@@ -659,7 +699,10 @@ int tqec_contract_batch(tqec_program* p, const uint8_t* syndromes, int64_t n, in
   const bool plain = (p->flags & TQEC_FLAG_PLAIN) != 0;
   int rc = decode_locked(p, syndromes, n, nullptr, logp_out, nullptr, precision, false, plain, st);
   if (rc) return rc;
-  if (!stream || !is_device_ptr(logp_out)) TQ_CUDA(cudaStreamSynchronize(st));
+  if (!stream || !is_device_ptr(logp_out)) {
+    TQ_CUDA(cudaStreamSynchronize(st));
+    return check_tensor_error(p);
+  }
   return TQEC_OK;
 }
 
@@ -796,6 +839,8 @@ int tqec_program_autotune(tqec_program* p, int64_t n_probe) {
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   if (!ok) return fail(TQEC_ERR_CUDA, "autotune launch failed");
+  const int te = check_tensor_error(p);
+  if (te) return te;
   g_last_error.clear();
   return TQEC_OK;
 }

@@ -16,8 +16,10 @@
 // two is exact, so the only rounding is that of the products and sums.  The
 // exponents are summed into the final log-probability.
 #include <cstdio>
+#include <type_traits>
 
 #include "contract.cuh"
+#include "tcgen05.cuh"
 
 namespace tqec {
 namespace {
@@ -203,6 +205,8 @@ __device__ void run_step(const KArgs& a, const StepDesc& dref, int st, int item_
   const int mfa = (1 << d.lfa) - 1;
   const int mw = (1 << lw) - 1;
   const int K = 1 << d.lk;
+  const bool bT = (d.flags & kStepTensor) != 0;
+  const int kstride = bT ? 1 : (1 << d.lfb);
   const int i0 = rotated(int(threadIdx.x), item_base);
   StepPtrs<T> p1{};
   T fa1 = T(1), fb1 = T(1);
@@ -227,15 +231,16 @@ __device__ void run_step(const KArgs& a, const StepDesc& dref, int st, int item_
       const int fa = (e >> d.lfb) & mfa;
       const int h = e >> (d.lfb + d.lfa);
       const T* pa = p.a + (((h << d.lfa) | fa) << d.lk);
-      const T* pb = p.b + ((h << (d.lk + d.lfb)) | fb);
+      // B is [h][k][fb], or [h][fb][k] for a GEMM-shaped step
+      const T* pb = p.b + (bT ? (((h << d.lfb) | fb) << d.lk) : ((h << (d.lk + d.lfb)) | fb));
       for (int k = 0; k < K; ++k) {
         T a0 = pa[k];
         if (NORM) a0 *= fa_s;
         if (MAXP) {
-          const T v = a0 * pb[k << d.lfb];
+          const T v = a0 * pb[k * kstride];
           acc = v > acc ? v : acc;
         } else {
-          acc = fma(a0, pb[k << d.lfb], acc);
+          acc = fma(a0, pb[k * kstride], acc);
         }
       }
       if (NORM) acc *= fb_s;
@@ -445,10 +450,12 @@ __device__ void run_step_splitk(const KArgs& a, const StepDesc& dref, int st, in
       const int fa = (e >> d.lfb) & mfa;
       const int h = e >> (d.lfb + d.lfa);
       const T* pa = p.a + (((h << d.lfa) | fa) << d.lk);
-      const T* pb = p.b + ((h << (d.lk + d.lfb)) | fb);
+      const bool bT = (d.flags & kStepTensor) != 0;
+      const T* pb = p.b + (bT ? (((h << d.lfb) | fb) << d.lk) : ((h << (d.lk + d.lfb)) | fb));
+      const int kstride = bT ? 1 : (1 << d.lfb);
       for (int k = sub; k < K; k += tpo) {
         const T av = pa[k] * fa_s;
-        const T bv = pb[k << d.lfb];
+        const T bv = pb[k * kstride];
         if (MAXP) {
           const T v = av * bv;
           acc = v > acc ? v : acc;
@@ -569,7 +576,7 @@ __device__ void backtrack(const KArgs& a, const StepDesc* s_steps, const uint32_
 // How a step is executed and how many work items it has (rounded up to a
 // warp): several lanes per output for few outputs over a long k range,
 // eight or four outputs per item along fb, else one output per item.
-enum StepKind { SK_SPLITK, SK_VEC8, SK_VEC4, SK_SCALAR };
+enum StepKind { SK_SPLITK, SK_VEC8, SK_VEC4, SK_SCALAR, SK_TENSOR };
 struct StepShape {
   int kind;
   int lt;       // SK_SPLITK: log2 of the lanes per output
@@ -577,17 +584,27 @@ struct StepShape {
 };
 
 template <typename T>
-__device__ __forceinline__ StepShape step_shape(int lh, int lfa, int lfb, int lk, int lg) {
+__device__ __forceinline__ StepShape step_shape(int lh, int lfa, int lfb, int lk, int lg, int flags, bool tensor) {
   const int lw = lh + lfa + lfb;
   const int64_t outs = int64_t(1) << (lw + lg);
   const int64_t bd = blockDim.x;
   StepShape sh;
+  sh.lt = 0;
+  const bool bT = (flags & kStepTensor) != 0;
+  if (bT && tensor) {  // the tensor cores, the whole block per syndrome
+    sh.kind = SK_TENSOR;
+    sh.total_r = int(bd);
+    return sh;
+  }
   int lt = 0;
   while (lt < 5 && (outs << (lt + 1)) <= bd && (lt + 1) + 2 <= lk) ++lt;
   int64_t total;
   if (lt >= 2) {
     sh.kind = SK_SPLITK;
     total = outs << lt;
+  } else if (bT) {  // B is K-major: no vector loads along fb
+    sh.kind = SK_SCALAR;
+    total = outs;
   } else if (sizeof(T) == 4 && lfb >= 3 && (outs >> 3) >= bd) {
     sh.kind = SK_VEC8;
     total = outs >> 3;
@@ -603,13 +620,148 @@ __device__ __forceinline__ StepShape step_shape(int lh, int lfa, int lfb, int lk
   return sh;
 }
 
+// Tensor-core state of a block: the mbarrier the MMAs complete on, the
+// phase it is at, the tensor memory, and whether a wait gave up.
+struct TcState {
+  uint64_t bar;
+  uint32_t tmem;
+  uint32_t phase;
+  int32_t abort;
+  int32_t pad;
+};
+
+// Stages rows [0, rows) x k [k0, k0+32) of a K-major float32 matrix (rows
+// `ld` elements apart) into two 128-byte-swizzled tiles holding the tf32
+// high and low parts of scale * x.
+__device__ __forceinline__ void stage_split(const float* src, int rows, int ld, int k0, float scale,
+                                            unsigned char* hi, unsigned char* lo) {
+  for (int i = threadIdx.x; i < rows * 8; i += blockDim.x) {
+    const int r = i >> 3, c = i & 7;
+    const float4 v = *reinterpret_cast<const float4*>(src + int64_t(r) * ld + k0 + 4 * c);
+    float4 h, l;
+    tc::split_tf32(v.x * scale, &h.x, &l.x);
+    tc::split_tf32(v.y * scale, &h.y, &l.y);
+    tc::split_tf32(v.z * scale, &h.z, &l.z);
+    tc::split_tf32(v.w * scale, &h.w, &l.w);
+    const int off = r * 128 + ((c ^ (r & 7)) << 4);
+    *reinterpret_cast<float4*>(hi + off) = h;
+    *reinterpret_cast<float4*>(lo + off) = l;
+  }
+}
+
+// A GEMM-shaped step on the tensor cores, for one syndrome: per h, 128-row
+// tiles of A ([h][fa][k]) times up to 128-column tiles of B ([h][fb][k]),
+// k in chunks of 32 staged by the whole block as tf32 high/low parts; one
+// thread issues hi*hi + hi*lo + lo*hi per 8-element k step into tensor
+// memory (float32 accumulation); every warp then reads a quarter of the
+// tile's rows back (tcgen05.ld), scales, and stores through the step's
+// permutation.  A's normaliser is applied while staging (exact), B's on the
+// way out.
+template <typename T, bool NORM>
+__device__ void run_step_tc(const KArgs& a, const StepDesc& dref, int st, uint32_t* s_max, const StepPtrs<T>* ptrs,
+                            const PermTab& ptab, TcState* ts, unsigned char* tbuf) {
+  const StepDesc d = dref;
+  const StepPtrs<T> p = ptrs[st];
+  T fa_s, fb_s;
+  step_norms<T, NORM>(d, s_max, &fa_s, &fb_s);
+  const int M = 1 << d.lfa, N = 1 << d.lfb, K = 1 << d.lk, H = 1 << d.lh;
+  const int lw = d.lh + d.lfa + d.lfb;
+  const int n_tile = N < tc::kNMax ? N : tc::kNMax;
+  const uint32_t idesc = tc::idesc_tf32(n_tile);
+  unsigned char* a_hi = tbuf;
+  unsigned char* a_lo = tbuf + tc::kTileBytes;
+  unsigned char* b_hi = tbuf + 2 * tc::kTileBytes;
+  unsigned char* b_lo = tbuf + 3 * tc::kTileBytes;
+  const uint64_t dah = tc::sdesc(tc::smem_u32(a_hi)), dal = tc::sdesc(tc::smem_u32(a_lo));
+  const uint64_t dbh = tc::sdesc(tc::smem_u32(b_hi)), dbl = tc::sdesc(tc::smem_u32(b_lo));
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, groups = int(blockDim.x >> 7);
+  uint32_t phase = ts->phase;
+  uint32_t run_bits = 0u;
+  for (int h = 0; h < H; ++h)
+    for (int m0 = 0; m0 < M; m0 += tc::kM)
+      for (int n0 = 0; n0 < N; n0 += n_tile) {
+        const float* A = reinterpret_cast<const float*>(p.a) + (int64_t(h) * M + m0) * K;
+        const float* B = reinterpret_cast<const float*>(p.b) + (int64_t(h) * N + n0) * K;
+        for (int k0 = 0; k0 < K; k0 += tc::kK) {
+          if (ts->abort) break;  // block-uniform (written before a barrier)
+          stage_split(A, tc::kM, K, k0, float(fa_s), a_hi, a_lo);
+          stage_split(B, n_tile, K, k0, 1.0f, b_hi, b_lo);
+          tc::fence_proxy_async();
+          tc::fence_before();
+          __syncthreads();
+          tc::fence_after();
+          if (threadIdx.x == 0) {
+#pragma unroll
+            for (int kk = 0; kk < tc::kK / 8; ++kk) {  // 8 tf32 = 32 bytes along k per instruction
+              const uint64_t o = uint64_t(kk * 2);
+              tc::mma_tf32(ts->tmem, dah + o, dbh + o, idesc, (k0 | kk) != 0 ? 1u : 0u);
+              tc::mma_tf32(ts->tmem, dah + o, dbl + o, idesc, 1u);
+              tc::mma_tf32(ts->tmem, dal + o, dbh + o, idesc, 1u);
+            }
+            tc::commit(&ts->bar);
+          }
+          // the staging buffers are reused once the MMAs have read them
+          const bool ok = tc::mbar_wait(&ts->bar, phase);
+          phase ^= 1u;
+          if (!ok) {
+            ts->abort = 1;
+            atomicExch(a.tc_err, 1);
+          }
+          __syncthreads();
+        }
+        tc::fence_after();
+        if (!ts->abort) {
+          const int q = warp & 3;
+          const int m = m0 + q * 32 + lane;
+          for (int c = warp >> 2; c < n_tile / 32; c += groups) {
+            uint32_t r[32];
+            tc::ld32(ts->tmem + (uint32_t(q * 32) << 16) + uint32_t(c * 32), r);
+            // the 32 outputs differ in index bits 0-4 only: one lookup in the
+            // permutation's low table each, the higher tables once
+            const int e0 = (((h << d.lfa) | m) << d.lfb) | (n0 + c * 32);
+            int hi = 0, lo0 = 0;
+            if (d.perm_off >= 0) {
+              int tab = d.perm_off + 256;
+              for (int sh = 8; sh < lw; sh += 8) {
+                const int cb = lw - sh < 8 ? lw - sh : 8;
+                hi |= ptab.at(tab + ((e0 >> sh) & ((1 << cb) - 1)));
+                tab += 1 << cb;
+              }
+              lo0 = d.perm_off + (e0 & 0xE0);
+            }
+#pragma unroll
+            for (int j = 0; j < 32; ++j) {
+              const float v = __uint_as_float(r[j]) * float(fb_s);
+              const int addr = d.perm_off < 0 ? e0 + j : (ptab.at(lo0 + j) | hi);
+              p.out[addr] = T(v);
+              const uint32_t bits = __float_as_uint(v);
+              run_bits = bits > run_bits ? bits : run_bits;
+            }
+          }
+        }
+        // tensor-memory reads are done before the next tile's MMAs overwrite it
+        tc::fence_before();
+        __syncthreads();
+        tc::fence_after();
+      }
+  if (threadIdx.x == 0) ts->phase = phase;
+  if (NORM) flush_max(true, run_bits, &s_max[st]);
+  __syncthreads();
+}
+
 // The planner hands the kernel arena and constant operands only (parity
 // operands become syndrome-selected tables), so each step shape has one code
 // path: the kernel stays small enough for the instruction caches.
-template <typename T, bool NORM, bool MAXP, bool G1>
+template <typename T, bool NORM, bool MAXP, bool G1, bool TENSOR>
 __device__ __forceinline__ void dispatch_step(const KArgs& a, const StepDesc& d, const StepShape& sh, int st,
                                               int item_base, uint32_t* s_max, const StepPtrs<T>* ptrs,
-                                              const PermTab& ptab) {
+                                              const PermTab& ptab, TcState* ts, unsigned char* tbuf) {
+  if constexpr (TENSOR && std::is_same<T, float>::value && NORM && !MAXP && G1) {
+    if (sh.kind == SK_TENSOR) {
+      run_step_tc<T, NORM>(a, d, st, s_max, ptrs, ptab, ts, tbuf);
+      return;
+    }
+  }
   switch (sh.kind) {
     case SK_SPLITK:
       run_step_splitk<T, NORM, MAXP, G1>(a, d, st, item_base, sh.lt, s_max, ptrs, ptab);
@@ -635,6 +787,8 @@ struct BlockSmem {
   uint32_t* syn;
   uint32_t* max;
   uint32_t* asg;
+  TcState* tc;           // tensor-core state (kernels with tensor-core steps)
+  unsigned char* tbuf;   // tensor-core staging tiles, 1024-byte aligned
   size_t tail;  // first free byte (16-byte aligned)
 };
 
@@ -653,6 +807,15 @@ __device__ __forceinline__ BlockSmem carve_smem(const KArgs& a, unsigned char* s
   if (NORM) off += size_t(a.G) * a.n_steps * 4;
   b.asg = reinterpret_cast<uint32_t*>(smem + off);
   if (MAXP) off += size_t(a.G) * a.var_words * 4;
+  b.tc = nullptr;
+  b.tbuf = nullptr;
+  if (a.tc) {
+    // staging tiles on a 1024-byte boundary (the swizzle atom), then the state
+    const uintptr_t base = reinterpret_cast<uintptr_t>(smem + off);
+    b.tbuf = reinterpret_cast<unsigned char*>((base + 1023) & ~uintptr_t(1023));
+    b.tc = reinterpret_cast<TcState*>(b.tbuf + 4 * tc::kTileBytes);
+    off += tc::kSmemBytes;
+  }
   b.tail = (off + 15) & ~size_t(15);
   return b;
 }
@@ -669,13 +832,14 @@ __device__ __forceinline__ void copy16(void* dst, const void* src, size_t bytes)
 // fills the block for one syndrome alone, in a block of several), and how
 // many items (threads' worth) it takes, which also rotates the next member of
 // its barrier group.  One thread per step; the caller synchronises.
-template <typename T>
+template <typename T, bool tensor_ok>
 __device__ __forceinline__ void fill_step_plan(const KArgs& a, const StepDesc* steps, int2* plan) {
   const int bd = int(blockDim.x);
   for (int st = threadIdx.x; st < a.n_steps; st += blockDim.x) {
     const StepDesc& d = steps[st];
-    const StepShape sh = step_shape<T>(d.lh, d.lfa, d.lfb, d.lk, a.lg);
-    const StepShape sh1 = a.G > 1 ? step_shape<T>(d.lh, d.lfa, d.lfb, d.lk, 0) : sh;
+    const bool tensor = tensor_ok && a.tc != 0;
+    const StepShape sh = step_shape<T>(d.lh, d.lfa, d.lfb, d.lk, a.lg, d.flags, tensor);
+    const StepShape sh1 = a.G > 1 ? step_shape<T>(d.lh, d.lfa, d.lfb, d.lk, 0, d.flags, tensor) : sh;
     const bool per_syndrome = a.G > 1 && sh1.total_r >= bd;
     const StepShape& use = per_syndrome ? sh1 : sh;
     plan[st] = make_int2(use.kind | (use.lt << 8) | (int(per_syndrome) << 16), per_syndrome ? bd : sh.total_r);
@@ -685,7 +849,7 @@ __device__ __forceinline__ void fill_step_plan(const KArgs& a, const StepDesc* s
 // One group of up to G syndromes (rows base .. base+G-1 below nrows) through
 // the whole program: load the syndrome words, run every step, back-track
 // (MAP), then the epilogue.  Ends with a block barrier.
-template <typename T, bool NORM, bool MAXP>
+template <typename T, bool NORM, bool MAXP, bool TENSOR>
 __device__ void contract_group(const KArgs& a, int64_t base, int64_t nrows, const BlockSmem& sm,
                                const Arena<T>& arena,
                                const T* consts, const PermTab& ptab) {
@@ -727,14 +891,14 @@ __device__ void contract_group(const KArgs& a, int64_t base, int64_t nrows, cons
     const int vt_warp = rotated(int(threadIdx.x & ~31u), item_base);
     if (vt_warp < items) {
       if (a.G == 1) {
-        dispatch_step<T, NORM, MAXP, true>(a, d, sh, st, item_base, s_max, s_ptrs, ptab);
+        dispatch_step<T, NORM, MAXP, true, TENSOR>(a, d, sh, st, item_base, s_max, s_ptrs, ptab, sm.tc, sm.tbuf);
       } else if (per_syndrome) {
         // the block's syndromes one after another with hoisted invariants
         for (int g = 0; g < a.G; ++g)
-          dispatch_step<T, NORM, MAXP, true>(a, d, sh, st, item_base, s_max + g * a.n_steps,
-                                             s_ptrs + g * a.n_steps, ptab);
+          dispatch_step<T, NORM, MAXP, true, TENSOR>(a, d, sh, st, item_base, s_max + g * a.n_steps,
+                                                     s_ptrs + g * a.n_steps, ptab, sm.tc, sm.tbuf);
       } else {
-        dispatch_step<T, NORM, MAXP, false>(a, d, sh, st, item_base, s_max, s_ptrs, ptab);
+        dispatch_step<T, NORM, MAXP, false, TENSOR>(a, d, sh, st, item_base, s_max, s_ptrs, ptab, sm.tc, sm.tbuf);
       }
     }
     if (d.flags & kStepSync) {
@@ -824,9 +988,10 @@ __device__ __forceinline__ Arena<T> block_arena(const KArgs& a, unsigned char* s
   return Arena<T>{base, base, INT32_MAX, int32_t(a.arena_elems), int32_t(a.arena_elems)};
 }
 
-// float64 blocks are capped at 512 threads, which leaves them 128 registers
-template <typename T, bool NORM, bool MAXP>
-__global__ void __launch_bounds__(sizeof(T) == 8 ? 512 : 1024) tn_contract_kernel(KArgs a) {
+// float64 blocks, and blocks running tensor-core steps, are capped at 512
+// threads, which leaves them 128 registers
+template <typename T, bool NORM, bool MAXP, bool TENSOR>
+__global__ void __launch_bounds__(sizeof(T) == 8 || TENSOR ? 512 : 1024) tn_contract_kernel(KArgs a) {
   extern __shared__ __align__(16) unsigned char smem[];
   const BlockSmem sm = carve_smem<NORM, MAXP>(a, smem);
   size_t off = sm.tail;
@@ -836,10 +1001,35 @@ __global__ void __launch_bounds__(sizeof(T) == 8 ? 512 : 1024) tn_contract_kerne
   const Arena<T> arena = block_arena<T>(a, smem + off, a.arena_global);
   copy16(sm.steps, a.steps, size_t(a.n_steps) * sizeof(StepDesc));
   __syncthreads();
-  fill_step_plan<T>(a, sm.steps, sm.plan);
+  constexpr bool kTensor = TENSOR && std::is_same<T, float>::value && NORM && !MAXP;
+  fill_step_plan<T, kTensor>(a, sm.steps, sm.plan);
+  const bool tensor = kTensor && a.tc;
+  if (tensor) {
+    if (threadIdx.x == 0) {
+      tc::mbar_init(&sm.tc->bar, 1);
+      sm.tc->phase = 0;
+      sm.tc->abort = 0;
+      asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if ((threadIdx.x >> 5) == 0) tc::alloc(&sm.tc->tmem, tc::kCols);
+    tc::fence_before();
+    __syncthreads();
+    tc::fence_after();
+  }
   const int64_t nrows = a.list ? int64_t(*a.list_count) : a.n;
   for (int64_t base = int64_t(blockIdx.x) * a.G; base < nrows; base += int64_t(gridDim.x) * a.G)
-    contract_group<T, NORM, MAXP>(a, base, nrows, sm, arena, consts, ptab);
+    contract_group<T, NORM, MAXP, TENSOR>(a, base, nrows, sm, arena, consts, ptab);
+  if (tensor) {
+    tc::fence_before();
+    __syncthreads();
+    // after a wait that gave up, the MMAs still in flight finish first (bounded)
+    if (sm.tc->abort && threadIdx.x == 0) tc::mbar_wait(&sm.tc->bar, sm.tc->phase);
+    __syncthreads();
+    if ((threadIdx.x >> 5) == 0) {
+      tc::fence_after();
+      tc::dealloc(sm.tc->tmem, tc::kCols);
+    }
+  }
 }
 
 // Several programs in one persistent launch.  Work units (program, first
@@ -867,13 +1057,13 @@ __global__ void __launch_bounds__(kMultiThreads) tn_contract_multi_kernel(MultiA
     if (first) {
       copy16(sm.steps, a.steps, size_t(a.n_steps) * sizeof(StepDesc));
       __syncthreads();
-      fill_step_plan<T>(a, sm.steps, sm.plan);
+      fill_step_plan<T, false>(a, sm.steps, sm.plan);
       __syncthreads();
     }
     T* abase = a.arena_global ? gslice : reinterpret_cast<T*>(smem + sm.tail);
     const Arena<T> arena{abase, abase, INT32_MAX, int32_t(a.arena_elems), int32_t(a.arena_elems)};
-    contract_group<T, NORM, false>(a, base, nrows, sm, arena, reinterpret_cast<const T*>(a.consts),
-                                   PermTab{a.perm, false});
+    contract_group<T, NORM, false, false>(a, base, nrows, sm, arena, reinterpret_cast<const T*>(a.consts),
+                                          PermTab{a.perm, false});
   };
   if (m.list_mode) {
     for (int32_t prog = 0; prog < m.n_progs; ++prog) {
@@ -885,7 +1075,7 @@ __global__ void __launch_bounds__(kMultiThreads) tn_contract_multi_kernel(MultiA
       const BlockSmem sm = carve_smem<NORM, false>(s_ka, smem);
       copy16(sm.steps, s_ka.steps, size_t(s_ka.n_steps) * sizeof(StepDesc));
       __syncthreads();
-      fill_step_plan<T>(s_ka, sm.steps, sm.plan);
+      fill_step_plan<T, false>(s_ka, sm.steps, sm.plan);
       __syncthreads();
       for (int64_t base = int64_t(blockIdx.x) * s_ka.G; base < nrows; base += int64_t(gridDim.x) * s_ka.G)
         run_unit(prog, base, nrows, false);
@@ -919,12 +1109,14 @@ __global__ void multi_advance_kernel(int32_t* batch, int32_t* next_unit, int32_t
 }  // namespace
 
 size_t contract_smem_bytes(int precision, int32_t n_steps, int32_t syn_words, int G,
-                           int64_t arena_elems, bool arena_in_smem, int32_t var_words, size_t table_bytes) {
+                           int64_t arena_elems, bool arena_in_smem, int32_t var_words, size_t table_bytes,
+                           bool tensor) {
   const bool norm = precision == 1;
   size_t off = size_t(n_steps) * (sizeof(StepDesc) + 8) + size_t(G) * n_steps * 3 * sizeof(void*) +
                size_t(G) * syn_words * 4;
   if (norm) off += size_t(G) * n_steps * 4;
   off += size_t(G) * var_words * 4;
+  if (tensor) off += tc::kSmemBytes;
   off = (off + 15) & ~size_t(15);
   off += table_bytes;
   if (arena_in_smem) off += size_t(G) * size_t(arena_elems) * (precision == 1 ? 4 : 8);
@@ -954,12 +1146,14 @@ int occupancy_of(K kernel, int threads, size_t smem) {
   return blocks;
 }
 
-int contract_occupancy(int precision, int threads, size_t smem, bool map_mode) {
-  if (precision == 1)
-    return map_mode ? occupancy_of(tn_contract_kernel<float, true, true>, threads, smem)
-                    : occupancy_of(tn_contract_kernel<float, true, false>, threads, smem);
-  return map_mode ? occupancy_of(tn_contract_kernel<double, false, true>, threads, smem)
-                  : occupancy_of(tn_contract_kernel<double, false, false>, threads, smem);
+int contract_occupancy(int precision, int threads, size_t smem, bool map_mode, bool tensor) {
+  if (precision == 1) {
+    if (map_mode) return occupancy_of(tn_contract_kernel<float, true, true, false>, threads, smem);
+    return tensor ? occupancy_of(tn_contract_kernel<float, true, false, true>, threads, smem)
+                  : occupancy_of(tn_contract_kernel<float, true, false, false>, threads, smem);
+  }
+  return map_mode ? occupancy_of(tn_contract_kernel<double, false, true, false>, threads, smem)
+                  : occupancy_of(tn_contract_kernel<double, false, false, false>, threads, smem);
 }
 
 template <typename K>
@@ -972,11 +1166,13 @@ cudaError_t launch_with(K kernel, const KArgs& a, int grid, int threads, size_t 
 
 cudaError_t contract_launch(int precision, const KArgs& a, int grid, int threads, size_t smem,
                             cudaStream_t stream) {
-  if (precision == 1)
-    return a.map_mode ? launch_with(tn_contract_kernel<float, true, true>, a, grid, threads, smem, stream)
-                      : launch_with(tn_contract_kernel<float, true, false>, a, grid, threads, smem, stream);
-  return a.map_mode ? launch_with(tn_contract_kernel<double, false, true>, a, grid, threads, smem, stream)
-                    : launch_with(tn_contract_kernel<double, false, false>, a, grid, threads, smem, stream);
+  if (precision == 1) {
+    if (a.map_mode) return launch_with(tn_contract_kernel<float, true, true, false>, a, grid, threads, smem, stream);
+    return a.tc ? launch_with(tn_contract_kernel<float, true, false, true>, a, grid, threads, smem, stream)
+                : launch_with(tn_contract_kernel<float, true, false, false>, a, grid, threads, smem, stream);
+  }
+  return a.map_mode ? launch_with(tn_contract_kernel<double, false, true, false>, a, grid, threads, smem, stream)
+                    : launch_with(tn_contract_kernel<double, false, false, false>, a, grid, threads, smem, stream);
 }
 
 // Sets the shared-memory limit (outside any stream capture) and returns the

@@ -54,6 +54,12 @@ struct KArgs {
   const int32_t* report;  // variables whose values are returned
   int32_t n_report;
   uint8_t* assign_out;    // n x ceil(n_report / 8) bit-packed values
+  // tensor-core steps: 1 when the block allocates tensor memory and runs
+  // kStepTensor steps on tcgen05 (float32 only); tc_err is set when a wait
+  // for the tensor cores gave up
+  int32_t tc;
+  int32_t tc_pad;
+  int32_t* tc_err;
 };
 static_assert(sizeof(KArgs) % 16 == 0, "KArgs is copied in 16-byte units");
 
@@ -89,7 +95,7 @@ struct MultiArgs {
 // Shared memory a launch needs (bytes).
 size_t contract_smem_bytes(int precision, int32_t n_steps, int32_t syn_words, int G,
                            int64_t arena_elems, bool arena_in_smem, int32_t var_words = 0,
-                           size_t table_bytes = 0);
+                           size_t table_bytes = 0, bool tensor = false);
 
 // Shared-memory bytes of the staged constant and permutation tables.
 size_t contract_table_bytes(int precision, int64_t n_consts, int64_t n_perm, bool perm16);
@@ -97,11 +103,14 @@ size_t contract_table_bytes(int precision, int64_t n_consts, int64_t n_perm, boo
 // Largest dynamic shared memory a block may use on this device.
 size_t contract_smem_limit(int device);
 
-// Most threads a block of the given precision may have.
-constexpr int contract_max_threads(int precision) { return precision == 1 ? 1024 : 512; }
+// Most threads a block of the given precision may have (blocks running
+// tensor-core steps: 512).
+constexpr int contract_max_threads(int precision, bool tensor = false) {
+  return precision == 1 && !tensor ? 1024 : 512;
+}
 
 // Resident blocks per SM for a launch shape (0 if it cannot launch).
-int contract_occupancy(int precision, int threads, size_t smem, bool map_mode = false);
+int contract_occupancy(int precision, int threads, size_t smem, bool map_mode = false, bool tensor = false);
 
 cudaError_t contract_launch(int precision, const KArgs& a, int grid, int threads, size_t smem,
                             cudaStream_t stream);

@@ -476,6 +476,7 @@ std::string build_plan(const NetworkView& net, int32_t n_steps, const int32_t* s
     std::vector<int> H, Fa, Fb, K;  // ordered groups
     int a = -1, b = -1;             // operand node ids
     std::vector<int> out_layout;    // required layout of the output
+    bool tensor = false;            // GEMM-shaped (B read K-major)
   };
   std::vector<StepLayout> lay(R);
   // Group orders are assigned bottom-up: a step orders each of its index
@@ -499,8 +500,20 @@ std::string build_plan(const NetworkView& net, int32_t n_steps, const int32_t* s
     for (int v : rv)
       if (!in(lv, v)) fr.push_back(v);
     // the operand with more free labels goes innermost (B), so that adjacent
-    // threads read adjacent B elements
+    // threads read adjacent B elements -- except for a GEMM-shaped step,
+    // whose A side (the 128-row tiles) is the operand with more free labels
     bool swap = fl.size() > fr.size();
+    {
+      int nk = 0;
+      for (int v : lv)
+        if (in(rv, v) && !in(n.vars, v)) ++nk;
+      const int big = (int)std::max(fl.size(), fr.size()), small = (int)std::min(fl.size(), fr.size());
+      auto sel_free = [&](int node) { return nodes[node].kind != NK_TABLE || nodes[node].sel.empty(); };
+      L.tensor = lim.tensor_steps && !map_mode && big >= kTensorMinFa && small >= kTensorMinFb &&
+                 nk >= kTensorMinK && sel_free(n.left) && sel_free(n.right) &&
+                 nodes[n.left].kind != NK_PARITY && nodes[n.right].kind != NK_PARITY;
+      if (L.tensor) swap = fr.size() > fl.size();
+    }
     L.a = swap ? n.right : n.left;
     L.b = swap ? n.left : n.right;
     const std::vector<int>& av = nodes[L.a].vars;
@@ -555,12 +568,22 @@ std::string build_plan(const NetworkView& net, int32_t n_steps, const int32_t* s
     la.insert(la.end(), L.K.begin(), L.K.end());
     la.insert(la.end(), L.Fa.begin(), L.Fa.end());
     la.insert(la.end(), L.H.begin(), L.H.end());
-    lb.insert(lb.end(), L.Fb.begin(), L.Fb.end());
-    lb.insert(lb.end(), L.K.begin(), L.K.end());
+    if (L.tensor) {  // [h][fb][k]: K-major like A
+      lb.insert(lb.end(), L.K.begin(), L.K.end());
+      lb.insert(lb.end(), L.Fb.begin(), L.Fb.end());
+    } else {
+      lb.insert(lb.end(), L.Fb.begin(), L.Fb.end());
+      lb.insert(lb.end(), L.K.begin(), L.K.end());
+    }
     lb.insert(lb.end(), L.H.begin(), L.H.end());
     req[L.a] = la;
     req[L.b] = lb;
-    err_terms += std::ldexp(1.0, (int)L.K.size()) + 1.0;
+    // float32 rounding of the K products and sums; a tensor-core step splits
+    // each operand into two tf32 halves (three products, the dropped and
+    // truncated parts below 3 x 2^-20 of each product, i.e. 48u) and may
+    // accumulate with twice the rounding of round-to-nearest
+    const double kk = std::ldexp(1.0, (int)L.K.size());
+    err_terms += L.tensor ? 2.0 * (kk + 1.0) + 48.0 : kk + 1.0;
     for (int op : {L.a, L.b}) {
       PNode& o = nodes[op];
       if (o.kind != NK_TABLE) continue;
@@ -688,7 +711,8 @@ std::string build_plan(const NetworkView& net, int32_t n_steps, const int32_t* s
     d.lfb = (int)L.Fb.size();
     d.lk = (int)L.K.size();
     d.out_off = (int32_t)off;
-    d.flags = group_end[r] ? kStepSync : 0;
+    d.flags = (group_end[r] ? kStepSync : 0) | (L.tensor ? kStepTensor : 0);
+    if (L.tensor) P.tensor_steps++;
     d.var_off = map_mode ? d_var_off : 0;
     for (int side = 0; side < 2; ++side) {
       int op = side ? L.b : L.a;

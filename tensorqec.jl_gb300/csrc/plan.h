@@ -33,6 +33,8 @@ constexpr int kMaxSel = 4;
 constexpr int32_t kStepSync = 1;     // block barrier after this step (end of a barrier group)
 constexpr int32_t kStepRotate4 = 2;  // permuted stores of 4-output items are lane-rotated
 constexpr int32_t kStepRotate8 = 4;  // the same for 8-output items
+constexpr int32_t kStepTensor = 8;   // GEMM-shaped step: B stored [h][fb][k] (K-major);
+                                     // float32 blocks may run it on the tensor cores
 
 struct StepDesc {
   int32_t a_kind, b_kind;
@@ -57,6 +59,7 @@ struct Plan {
   int32_t width = 0;               // log2 of the widest runtime intermediate
   int64_t arena_elems = 0;         // per syndrome
   int64_t arena_small = 0;         // elements of the small-tensor pool at the arena's start (0: one pool)
+  int32_t tensor_steps = 0;        // steps marked kStepTensor
   int32_t root_step = -1;          // the last runtime step
   double macs_runtime = 0.0;       // multiply-adds per syndrome, runtime steps
   double macs_tree = 0.0;          // multiply-adds of the tree as given
@@ -93,7 +96,15 @@ struct PlanLimits {
   int max_width = 30;         // refuse intermediates wider than 2^max_width
   bool map_mode = false;      // max-product contraction + back-tracking (TNMAP)
   int64_t big_elems = 1024;   // intermediates above this size go to the big pool
+  bool tensor_steps = true;   // mark GEMM-shaped steps (kStepTensor)
 };
+
+// A step is GEMM-shaped when, per h, it multiplies a 2^lfa x 2^lk block by a
+// 2^lk x 2^lfb block with lfa >= 7 (one 128-row tile), lfb >= 5 (whole
+// 32-column tensor-memory reads) and lk >= 5 (whole 32-element k chunks), and
+// both operands are arena tensors or constant tables without syndrome
+// selection.
+constexpr int kTensorMinFa = 7, kTensorMinFb = 5, kTensorMinK = 5;
 
 // Builds the program; returns "" on success or an error message.
 // *unsupported is set when the network is valid but outside the kernels' scope.

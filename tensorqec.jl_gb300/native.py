@@ -56,7 +56,8 @@ class ProgramInfo(C.Structure):
                 ("group_f64", C.c_int32), ("threads_f64", C.c_int32), ("smem_f64", C.c_int32),
                 ("resident_f32", C.c_int32), ("resident_f64", C.c_int32), ("tables_smem_f32", C.c_int32),
                 ("tables_smem_f64", C.c_int32), ("arena_small", C.c_int64), ("split_f32", C.c_int32),
-                ("split_f64", C.c_int32), ("reserved_", C.c_int32)]
+                ("split_f64", C.c_int32), ("tensor_steps", C.c_int32), ("tensor_f32", C.c_int32),
+                ("reserved_0", C.c_int32), ("reserved_1", C.c_int32)]
 
 
 class PlanView(C.Structure):

@@ -53,7 +53,10 @@ def run_plan(plan, bits, dtype=np.float64, return_arena=False):
         h = e >> (lfb + lfa)
         k = np.arange(1 << lk, dtype=np.int64)
         aidx = (((h << lfa) | fa) << lk)[:, None] + k[None, :]
-        bidx = ((h << (lk + lfb)) | fb)[:, None] + (k[None, :] << lfb)
+        if int(d["flags"]) & 8:  # GEMM-shaped step: B stored [h][fb][k]
+            bidx = (((h << lfb) | fb) << lk)[:, None] + k[None, :]
+        else:
+            bidx = ((h << (lk + lfb)) | fb)[:, None] + (k[None, :] << lfb)
 
         def operand(kind, ref, sel, idx, obits):
             if kind == OP_PARITY:
@@ -95,7 +98,9 @@ def map_backtrack(plan, bits, arena):
             fa = sum(int(asg[vt[o + lfb + j]]) << j for j in range(lfa))
             h = sum(int(asg[vt[o + lfb + lfa + j]]) << j for j in range(lh))
             abase = ((h << lfa) | fa) << lk
-            bbase = (h << (lk + lfb)) | fb
+            bT = int(d["flags"]) & 8
+            bbase = (((h << lfb) | fb) << lk) if bT else ((h << (lk + lfb)) | fb)
+            bstep = 1 if bT else (1 << lfb)
 
             def val(kind, ref, sel, idx, obits):
                 if kind == OP_PARITY:
@@ -111,7 +116,7 @@ def map_backtrack(plan, bits, arena):
             best, bk = -1.0, 0
             for k in range(1 << lk):
                 v = (val(int(d["a_kind"]), int(d["a_ref"]), d["a_sel"], abase + k, lh + lfa + lk)
-                     * val(int(d["b_kind"]), int(d["b_ref"]), d["b_sel"], bbase + (k << lfb), lh + lk + lfb))
+                     * val(int(d["b_kind"]), int(d["b_ref"]), d["b_sel"], bbase + k * bstep, lh + lk + lfb))
                 if v > best:
                     best, bk = v, k
             for j in range(lk):

@@ -248,3 +248,28 @@ def test_split_arena_shapes_vs_plain_f64(pkg, group, threads):
         tie = (srt[:, -1] - srt[:, -2]) <= 1e-9
         assert not ((cls != np.argmax(want, axis=1)) & ~tie).any()
         ct.close()
+
+
+def test_tensor_core_steps_vs_float64(pkg):
+    """GEMM-shaped steps of a circuit-level model (rotated Z-memory d=5, 2
+    rounds) run on the tensor cores in float32 launches (tf32 high/low
+    split); the result stays within the float32 program's bound of the
+    float64 contraction (float64 runs them on the SIMT path) and decides the
+    same classes outside exact ties."""
+    from tensorqec_gb300 import circuit, dem as demmod
+
+    dm = circuit.detector_error_model(circuit.memory_z_circuit(5, 2, 0.001))
+    rng = np.random.default_rng(8)
+    _, det, _ = demmod.sample_dem(dm, 256, rng)
+    ct32 = pkg.compile(pkg.TNMMAP(precision="f32", optimizer=pkg.TreeSA(trials=16, sweeps=1000, restarts=2)), dm)
+    info = ct32.program.info
+    assert info["tensor_steps"] > 0 and info["tensor_f32"] == 1
+    lp32 = ct32.class_logprobs(det)
+    lp64 = ct32.class_logprobs(det, precision="f64")
+    top = np.max(lp64, axis=1, keepdims=True)
+    assert np.max(np.abs(np.exp(lp32 - top) - np.exp(lp64 - top))) <= 2 * info["err_bound_f32"]
+    cls = ct32.decode_batch(det)
+    srt = np.sort(lp64, axis=1)
+    tie = (srt[:, -1] - srt[:, -2]) <= 1e-9
+    assert not ((cls != np.argmax(lp64, axis=1)) & ~tie).any()
+    ct32.close()

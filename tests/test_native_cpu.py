@@ -138,3 +138,25 @@ def test_invalid_inputs_return_status(pkg):
     lib = pkg.native.lib()
     assert lib.tqec_program_create(None, None, None, None) == -1
     assert lib.tqec_decode_batch(None, None, 0, None, None, None, None) == -1
+
+
+def test_plan_emulation_tensor_steps(pkg):
+    """A circuit-level model (rotated Z-memory d=5, 2 rounds) whose program
+    has GEMM-shaped steps (B laid out K-major): the emulated program agrees
+    with the C contractor of the oracle on the same tree."""
+    from oracle.c_oracle import CContractor
+    from tensorqec_gb300 import circuit, dem as demmod
+
+    dm = circuit.detector_error_model(circuit.memory_z_circuit(5, 2, 0.001))
+    t = demmod.dem2tanner(dm)
+    g = pkg.tnmmap_dem_graph(t, demmod.logical_map(dm), dm.error_rates, len(dm.logical_list), True)
+    steps = pkg.optimize_code(g, pkg.TreeSA(trials=16, sweeps=1000, seed=1, restarts=2))
+    plan = pkg.native.inspect_plan(g, steps)
+    assert any(int(d["flags"]) & 8 for d in plan["steps"]), "expected GEMM-shaped steps"
+    rng = np.random.default_rng(5)
+    _, det, _ = demmod.sample_dem(dm, 2, rng)
+    got = run_plan(plan, det)
+    cc = CContractor(g.ixs, [np.asarray(x) for x in g.tensors], g.iy, g.syndrome_positions, steps)
+    marg, _ = cc.contract(pkg.pack_syndromes(det))
+    want = marg
+    np.testing.assert_allclose(got, want, rtol=1e-9, atol=1e-300)

@@ -12,7 +12,8 @@ import numpy as np
 import pytest
 
 
-def step_shape(lh, lfa, lfb, lk, lg, bd, is_float):
+def step_shape(lh, lfa, lfb, lk, lg, bd, is_float, flags=0):
+    """SIMT shapes (a tensor-core step covers its outputs tile by tile)."""
     lw = lh + lfa + lfb
     outs = 1 << (lw + lg)
     lt = 0
@@ -20,6 +21,8 @@ def step_shape(lh, lfa, lfb, lk, lg, bd, is_float):
         lt += 1
     if lt >= 2:
         kind, total = "splitk", outs << lt
+    elif flags & 8:  # K-major B: no vector loads along fb
+        kind, total = "scalar", outs
     elif is_float and lfb >= 3 and (outs >> 3) >= bd:
         kind, total = "vec8", outs >> 3
     elif lfb >= 2:
@@ -70,8 +73,9 @@ def check_program(plan, is_float):
             for st, d in enumerate(plan["steps"]):
                 lh, lfa, lfb, lk = int(d["lh"]), int(d["lfa"]), int(d["lfb"]), int(d["lk"])
                 lw = lh + lfa + lfb
-                kind, lt, tr = step_shape(lh, lfa, lfb, lk, lg, bd, is_float)
-                k1, lt1, tr1 = step_shape(lh, lfa, lfb, lk, 0, bd, is_float)
+                fl = int(d["flags"])
+                kind, lt, tr = step_shape(lh, lfa, lfb, lk, lg, bd, is_float, fl)
+                k1, lt1, tr1 = step_shape(lh, lfa, lfb, lk, 0, bd, is_float, fl)
                 per_syndrome = G > 1 and tr1 >= bd
                 enter = bd if per_syndrome else tr
                 cover = np.zeros((G, 1 << lw), dtype=np.int64)
