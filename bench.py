@@ -55,7 +55,10 @@ def parse():
     ap.add_argument("--circuit", action="store_true",
                     help="circuit-level rotated Z-memory d=5, 5 rounds, p=0.001: DEM from the generator, "
                          "--circuit-n seeded detector samples, float32 + float64 recheck")
-    ap.add_argument("--circuit-n", type=int, default=262144)
+    ap.add_argument("--circuit-n", type=int, default=262144,
+                    help="--circuit: detector samples (with --profile: samples in the one profiled launch)")
+    ap.add_argument("--no-tensor-cores", action="store_true",
+                    help="--circuit: run the GEMM-shaped steps on the SIMT path instead of tcgen05")
     ap.add_argument("--group", type=int, default=0, help="--profile: syndromes per block (0: default shape)")
     ap.add_argument("--threads", type=int, default=0, help="--profile: threads per block (0: default shape)")
     ap.add_argument("--split-arena", action="store_true",
@@ -637,28 +640,57 @@ def run_mixed(args):
         p_.close()
 
 
+def circuit_program(args):
+    """The Z-memory circuit (d=5, 5 rounds, p=0.001), its detector error
+    model and the compiled float32 program of its factor graph."""
+    import __graft_entry__ as G
+
+    pkg = G.load_package()
+    from tensorqec_gb300 import circuit as cz
+    from tensorqec_gb300 import decoder as dec
+
+    d, rounds, p = 5, 5, 0.001
+    circ = cz.memory_z_circuit(d, rounds, p)
+    dem = cz.detector_error_model(circ)
+    opt = dec.TreeSA(trials=32, sweeps=2000, target_width=20, width_penalty=2.0, seed=1, restarts=4)
+    ct = pkg.compile(pkg.TNMMAP(optimizer=opt, precision="f32", tensor_cores=not args.no_tensor_cores), dem)
+    return pkg, dem, ct
+
+
+def run_circuit_profile(args):
+    """W warm-up launches then one float32 contraction launch of
+    --circuit-n circuit-level samples: the case the ncu captures of the
+    tensor-core steps profile."""
+    import torch
+
+    pkg, dem, ct = circuit_program(args)
+    from tensorqec_gb300.dem import sample_dem
+
+    n = args.circuit_n
+    _, det, _ = sample_dem(dem, n, np.random.default_rng(SEED + 3))
+    d_syn = torch.from_numpy(pkg.pack_syndromes(det)).cuda()
+    d_lp = torch.empty((n, ct.n_classes), dtype=torch.float64, device="cuda")
+    sptr = torch.cuda.current_stream().cuda_stream
+    for _ in range(args.warmup + 1):
+        ct.program.contract_ptrs(d_syn.data_ptr(), n, pkg.native.TQEC_F32, d_lp.data_ptr(), sptr)
+    torch.cuda.synchronize()
+    print(json.dumps({"profile_case": "circuit d=5 r=5 p=0.001", "samples": n, "program": ct.program.info}),
+          flush=True)
+    ct.close()
+
+
 def run_circuit(args):
     """Circuit-level noise: the Z-memory circuit's detector error model
     decoded by the batched contraction of its factor graph (float32 with a
     float64 recheck of low-margin samples)."""
     import torch
 
-    import __graft_entry__ as G
-
-    pkg = G.load_package()
-    native = pkg.native
-    from tensorqec_gb300 import circuit as cz
-    from tensorqec_gb300 import decoder as dec
+    t0 = time.time()
+    pkg, dem, ct = circuit_program(args)
     from tensorqec_gb300.dem import sample_dem
 
-    d, rounds, p = 5, 5, 0.001
-    t0 = time.time()
-    circ = cz.memory_z_circuit(d, rounds, p)
-    dem = cz.detector_error_model(circ)
-    opt = dec.TreeSA(trials=32, sweeps=2000, target_width=20, width_penalty=2.0, seed=1, restarts=4)
-    ct = pkg.compile(pkg.TNMMAP(optimizer=opt, precision="f32"), dem)
-    info = ct.program.info
     ct.program.autotune(256)
+    info = ct.program.info
     compile_s = time.time() - t0
     rng = np.random.default_rng(SEED + 3)
     n = args.circuit_n
@@ -700,6 +732,7 @@ def run_circuit(args):
             "ler_ci95": [max(0.0, ler - z * se), ler + z * se],
             "decision_mismatch_vs_f64_on_sample": mism, "f64_sample": m,
             "compile_and_tune_seconds": compile_s,
+            "tensor_steps": info["tensor_steps"], "shape_f32": {k: v for k, v in info.items() if k.endswith("_f32")},
             "data": "synthetic: mechanisms sampled independently from the generated DEM (numpy PCG64)"}
     print(json.dumps(line), flush=True)
     ct.close()
@@ -707,7 +740,9 @@ def run_circuit(args):
 
 def main():
     args = parse()
-    if args.circuit:
+    if args.circuit and args.profile:
+        run_circuit_profile(args)
+    elif args.circuit:
         run_circuit(args)
     elif args.mixed:
         run_mixed(args)

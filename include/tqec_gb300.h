@@ -60,6 +60,9 @@ extern "C" {
  * tqec_options.big_elems elements) in shared memory and its large ones in global memory; only for
  * programs that have both kinds (others keep their default shape) */
 #define TQEC_FLAG_SPLIT_ARENA 8u
+/* TQEC_F32: run GEMM-shaped steps on the SIMT path instead of the tcgen05
+ * tensor cores (same results within the same error bound) */
+#define TQEC_FLAG_NO_TENSOR_CORES 16u
 
 /* The factor graph, as built by compile(::TNMMAP, ...) (tndecoder.jl:97-146
  * for CSS codes, :186-219 for detector error models). */

@@ -151,14 +151,15 @@ void finish_tensor_shape(const tqec_program* p, Shape* s) {
   s->grid_cap = std::min(s->grid_cap, 4 * p->sm_count);
 }
 
-int choose_shape(tqec_program* p, int precision, int G_req, int threads_req, int tables_req, Shape* out) {
+int choose_shape(tqec_program* p, int precision, int G_req, int threads_req, int tables_req, Shape* out,
+                 bool tensor_req = true) {
   const size_t limit = tqec::contract_smem_limit(p->device);
   const int64_t arena = p->plan.arena_elems;
   const int nsteps = (int)p->plan.steps.size();
   const int sw = syn_words(p);
   const int vw = var_words(p);
   const size_t tb_all = table_bytes(p, precision);
-  const bool tensor = tensor_program(p, precision);
+  const bool tensor = tensor_req && tensor_program(p, precision);
   auto bytes = [&](int G, bool arena_smem, size_t tb) {
     return tqec::contract_smem_bytes(precision, nsteps, sw, G, arena, arena_smem, vw, tb, tensor);
   };
@@ -204,11 +205,12 @@ int choose_shape(tqec_program* p, int precision, int G_req, int threads_req, int
 // A split shape: G syndromes per block with their small-tensor pools in
 // shared memory and their big-tensor pools in global memory (programs that
 // have both pools).
-int choose_split_shape(tqec_program* p, int precision, int G, int threads, int tables, Shape* out) {
+int choose_split_shape(tqec_program* p, int precision, int G, int threads, int tables, Shape* out,
+                       bool tensor_req = true) {
   if (p->plan.arena_small <= 0 || p->plan.map_mode) return fail(TQEC_ERR_UNSUPPORTED, "program has one pool");
   const size_t limit = tqec::contract_smem_limit(p->device);
   const int nsteps = (int)p->plan.steps.size();
-  const bool tensor = tensor_program(p, precision);
+  const bool tensor = tensor_req && tensor_program(p, precision);
   Shape s;
   s.G = G;
   s.threads = std::min(threads, tqec::contract_max_threads(precision, tensor));
@@ -522,6 +524,7 @@ int tqec_program_create(const tqec_network* net, const tqec_tree* tree, const tq
                       net->n_out, net->out_labels, net->n_syndrome, net->syndrome_tensors};
   tqec::PlanLimits lim;
   lim.map_mode = (o.flags & TQEC_FLAG_MAP) != 0;
+  lim.tensor_steps = (o.flags & TQEC_FLAG_NO_TENSOR_CORES) == 0;
   if (o.big_elems < 0) return fail(TQEC_ERR_INVALID, "big_elems must be >= 0");
   if (o.big_elems > 0) lim.big_elems = o.big_elems;
   auto* p = new tqec_program();
@@ -761,10 +764,13 @@ bool tune_shape(tqec_program* p, int prec, int64_t n, cudaEvent_t e0, cudaEvent_
         // the arenas in flight can stay in L2
         for (int resident : {0, 8, 4, 2, 1}) {
          for (int split : {0, 1}) {
+          // programs with GEMM-shaped steps also try them on the SIMT path
+          for (int tensor : {1, 0}) {
+          if (!tensor && !tensor_program(p, prec)) continue;
           Shape s;
           if (split) {
-            if (choose_split_shape(p, prec, G, th, tables, &s) != TQEC_OK) continue;
-          } else if (choose_shape(p, prec, G, th, tables, &s) != TQEC_OK) {
+            if (choose_split_shape(p, prec, G, th, tables, &s, tensor) != TQEC_OK) continue;
+          } else if (choose_shape(p, prec, G, th, tables, &s, tensor) != TQEC_OK) {
             continue;
           }
           if (tables && !s.smem_tables) continue;
@@ -791,6 +797,7 @@ bool tune_shape(tqec_program* p, int prec, int64_t n, cudaEvent_t e0, cudaEvent_
           if (ms < best_ms) {
             best_ms = ms;
             best = s;
+          }
           }
          }
         }
@@ -859,6 +866,7 @@ int tqec_plan_inspect_flags(const tqec_network* net, const tqec_tree* tree, uint
   bool unsupported = false;
   tqec::PlanLimits lim;
   lim.map_mode = (flags & TQEC_FLAG_MAP) != 0;
+  lim.tensor_steps = (flags & TQEC_FLAG_NO_TENSOR_CORES) == 0;
   std::string err = tqec::build_plan(v, tree->n_steps, tree->steps, lim, P, &unsupported);
   if (!err.empty()) {
     delete P;

@@ -198,8 +198,8 @@ static bool rotation_pays(const std::vector<int32_t>& perm, int32_t off, int lw,
   return plain - rot > (vw == 8 ? 24 : 8);
 }
 
-std::string build_plan(const NetworkView& net, int32_t n_steps, const int32_t* steps,
-                       const PlanLimits& lim, Plan* out, bool* unsupported) {
+static std::string build_plan_once(const NetworkView& net, int32_t n_steps, const int32_t* steps,
+                                   const PlanLimits& lim, Plan* out, bool* unsupported) {
   *unsupported = false;
   const int T = net.n_tensors;
   if (T < 1) return "network has no tensors";
@@ -805,6 +805,28 @@ std::string build_plan(const NetworkView& net, int32_t n_steps, const int32_t* s
     return "per-syndrome working set above 2^31 elements";
   }
   return "";
+}
+
+// Tensor-core steps pay only when they carry a good share of the work: the
+// kernel instantiation that runs them has fewer threads and registers per
+// block and holds the staging buffers in shared memory, which slows every
+// other step.  Below lim.tensor_min_share of the multiply-adds the program is
+// planned again without them.
+std::string build_plan(const NetworkView& net, int32_t n_steps, const int32_t* steps,
+                       const PlanLimits& lim, Plan* out, bool* unsupported) {
+  std::string err = build_plan_once(net, n_steps, steps, lim, out, unsupported);
+  if (!err.empty() || out->tensor_steps == 0) return err;
+  double all = 0.0, tc = 0.0;
+  for (const StepDesc& d : out->steps) {
+    const double m = std::ldexp(1.0, d.lh + d.lfa + d.lfb + d.lk);
+    all += m;
+    if (d.flags & kStepTensor) tc += m;
+  }
+  if (tc >= lim.tensor_min_share * all) return err;
+  PlanLimits simt = lim;
+  simt.tensor_steps = false;
+  *out = Plan();
+  return build_plan_once(net, n_steps, steps, simt, out, unsupported);
 }
 
 }  // namespace tqec

@@ -97,6 +97,8 @@ struct PlanLimits {
   bool map_mode = false;      // max-product contraction + back-tracking (TNMAP)
   int64_t big_elems = 1024;   // intermediates above this size go to the big pool
   bool tensor_steps = true;   // mark GEMM-shaped steps (kStepTensor)
+  // ... when they hold at least this share of the program's multiply-adds
+  double tensor_min_share = 0.25;
 };
 
 // A step is GEMM-shaped when, per h, it multiplies a 2^lfa x 2^lk block by a

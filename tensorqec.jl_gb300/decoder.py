@@ -132,13 +132,15 @@ class TNMMAP:
     threads: int = 0
     split_arena: bool = False
     big_elems: int = 0
+    tensor_cores: bool = True
 
     def _native_precision(self):
         return {"f64": native.TQEC_F64, "f32": native.TQEC_F32}[self.precision]
 
     def _flags(self):
         return ((native.TQEC_FLAG_PLAIN if self.plain else 0) |
-                (native.TQEC_FLAG_SPLIT_ARENA if self.split_arena else 0))
+                (native.TQEC_FLAG_SPLIT_ARENA if self.split_arena else 0) |
+                (0 if self.tensor_cores else native.TQEC_FLAG_NO_TENSOR_CORES))
 
 
 class CompiledTNMMAP:

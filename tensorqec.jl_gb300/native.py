@@ -20,6 +20,7 @@ TQEC_FLAG_PLAIN = 1
 TQEC_FLAG_NORECHECK = 2
 TQEC_FLAG_MAP = 4
 TQEC_FLAG_SPLIT_ARENA = 8
+TQEC_FLAG_NO_TENSOR_CORES = 16
 
 ERRORS = {-1: "invalid argument", -2: "CUDA error", -3: "out of device memory",
           -4: "unsupported network", -5: "timeout", -6: "I/O error"}

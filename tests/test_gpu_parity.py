@@ -273,3 +273,27 @@ def test_tensor_core_steps_vs_float64(pkg):
     tie = (srt[:, -1] - srt[:, -2]) <= 1e-9
     assert not ((cls != np.argmax(lp64, axis=1)) & ~tie).any()
     ct32.close()
+
+
+def test_tensor_cores_switch_and_autotune(pkg):
+    """The same circuit-level program with its GEMM-shaped steps on the SIMT
+    path (TQEC_FLAG_NO_TENSOR_CORES) and after an autotune that may pick
+    either path: both stay within the float32 bound of float64."""
+    from tensorqec_gb300 import circuit, dem as demmod
+
+    dm = circuit.detector_error_model(circuit.memory_z_circuit(5, 2, 0.001))
+    _, det, _ = demmod.sample_dem(dm, 512, np.random.default_rng(9))
+    opt = pkg.TreeSA(trials=16, sweeps=1000, restarts=2, seed=3)
+    ct_tc = pkg.compile(pkg.TNMMAP(precision="f32", optimizer=opt), dm)
+    ct_si = pkg.compile(pkg.TNMMAP(precision="f32", optimizer=opt, tensor_cores=False), dm)
+    assert ct_tc.program.info["tensor_steps"] > 0
+    assert ct_si.program.info["tensor_steps"] == 0 and ct_si.program.info["tensor_f32"] == 0
+    lp64 = ct_tc.class_logprobs(det, precision="f64")
+    top = np.max(lp64, axis=1, keepdims=True)
+    for ct in (ct_si, ct_tc):
+        ct.program.autotune(512)
+        lp32 = ct.class_logprobs(det)
+        bound = 2 * ct.program.info["err_bound_f32"]
+        assert np.max(np.abs(np.exp(lp32 - top) - np.exp(lp64 - top))) <= bound
+    ct_tc.close()
+    ct_si.close()

@@ -160,3 +160,32 @@ def test_plan_emulation_tensor_steps(pkg):
     marg, _ = cc.contract(pkg.pack_syndromes(det))
     want = marg
     np.testing.assert_allclose(got, want, rtol=1e-9, atol=1e-300)
+
+
+def test_tensor_steps_need_a_share_of_the_work(pkg):
+    """GEMM-shaped steps are planned for the tensor cores only when they hold
+    at least a quarter of the multiply-adds: the surface code d=9 program on
+    the default tree search's order (one such step, about 5% of the work) is
+    planned without them, the circuit-level
+    d=5 program keeps them; the no-tensor-cores flag plans none."""
+    from tensorqec_gb300 import circuit, dem as demmod, gf2
+    from tensorqec_gb300.network import tnmmap_css_graph
+
+    def share(plan):
+        m = np.array([1 << int(d["lh"] + d["lfa"] + d["lfb"] + d["lk"]) for d in plan["steps"]], dtype=np.float64)
+        tc = np.array([int(d["flags"]) & 8 != 0 for d in plan["steps"]])
+        return m[tc].sum() / m.sum()
+
+    t = pkg.tanner_graph(pkg.SurfaceCode(9, 9))
+    em = pkg.depolarizing(0.05, t.nq)
+    lx, lz = gf2.logical_operator(t)
+    g9 = tnmmap_css_graph(t, em, lx, lz)
+    s9 = pkg.optimize_code(g9, pkg.TreeSA())
+    assert share(pkg.native.inspect_plan(g9, s9)) == 0.0
+
+    dm = circuit.detector_error_model(circuit.memory_z_circuit(5, 2, 0.001))
+    tg = demmod.dem2tanner(dm)
+    g = pkg.tnmmap_dem_graph(tg, demmod.logical_map(dm), dm.error_rates, len(dm.logical_list), True)
+    steps = pkg.optimize_code(g, pkg.TreeSA(trials=16, sweeps=1000, seed=1, restarts=2))
+    assert share(pkg.native.inspect_plan(g, steps)) >= 0.25
+    assert share(pkg.native.inspect_plan(g, steps, pkg.native.TQEC_FLAG_NO_TENSOR_CORES)) == 0.0
