@@ -49,10 +49,15 @@ extern "C" {
 /* Arithmetic of a contraction. */
 #define TQEC_F64 0 /* float64 throughout (the reference's arithmetic) */
 #define TQEC_F32 1 /* float32 with per-tensor power-of-two renormalisation */
+/* double-float: each value a pair of float32 (hi + lo, about 48 significant
+ * bits), renormalised like TQEC_F32, on the float32 pipes (GB300 runs float64
+ * at 1/64 of the float32 rate).  The default arithmetic of the recheck;
+ * accepted by tqec_contract_batch. */
+#define TQEC_F32X2 2
 
 /* Option flags. */
 #define TQEC_FLAG_PLAIN 1u   /* decode one syndrome per kernel launch (drop-in form) */
-#define TQEC_FLAG_NORECHECK 2u /* TQEC_F32: skip the float64 recheck of low margins */
+#define TQEC_FLAG_NORECHECK 2u /* TQEC_F32: skip the recheck of low margins */
 #define TQEC_FLAG_MAP 4u      /* most probable configuration (TNMAP): the network's
                                  out_labels name the variables whose values are
                                  reported; the contraction maximises over all */
@@ -63,6 +68,8 @@ extern "C" {
 /* TQEC_F32: run GEMM-shaped steps on the SIMT path instead of the tcgen05
  * tensor cores (same results within the same error bound) */
 #define TQEC_FLAG_NO_TENSOR_CORES 16u
+/* TQEC_F32: recheck low margins in float64 instead of TQEC_F32X2 */
+#define TQEC_FLAG_RECHECK_F64 32u
 
 /* The factor graph, as built by compile(::TNMMAP, ...) (tndecoder.jl:97-146
  * for CSS codes, :186-219 for detector error models). */
@@ -122,7 +129,9 @@ typedef struct {
   int32_t split_f32, split_f64;             /* 1: small pool in shared, big pool in global memory */
   int32_t tensor_steps;      /* GEMM-shaped steps (tcgen05 tf32 in float32 launches) */
   int32_t tensor_f32;        /* 1: the float32 shape runs them on the tensor cores */
-  int32_t reserved_[2];
+  int32_t recheck_precision; /* TQEC_F32X2 or TQEC_F64: arithmetic of the recheck */
+  int32_t reserved_;
+  double err_bound_f32x2;    /* relative error bound of a TQEC_F32X2 marginal */
 } tqec_program_info_t;
 
 typedef struct tqec_program tqec_program;
@@ -141,8 +150,9 @@ int tqec_program_info(const tqec_program* prog, tqec_program_info_t* info);
  * in Julia linear order), the natural-log marginal of every class
  * (n x n_classes, Julia linear order of `mar`) and a per-syndrome relative
  * error bound.  logp_out and err_bound_out may be NULL.  With TQEC_F32 the
- * syndromes whose class margin is below the bound are contracted again in
- * float64 before the call returns. */
+ * syndromes whose class margin is below the bound are contracted again
+ * (TQEC_F32X2, or float64 with TQEC_FLAG_RECHECK_F64) before the call
+ * returns; their err_bound_out is that arithmetic's bound. */
 int tqec_decode_batch(tqec_program* prog, const uint8_t* syndromes, int64_t n,
                       int32_t* class_out, double* logp_out,
                       float* err_bound_out, void* stream);
@@ -164,7 +174,7 @@ int tqec_contract_batch(tqec_program* prog, const uint8_t* syndromes,
 int tqec_map_decode_batch(tqec_program* prog, const uint8_t* syndromes, int64_t n,
                           uint8_t* assignment_out, double* logp_out, void* stream);
 
-/* Count of syndromes the last TQEC_F32 decode call sent to the float64
+/* Count of syndromes the last TQEC_F32 decode call sent to the
  * recheck (a measure of how often the rounding bound was not enough). */
 int tqec_last_recheck_count(const tqec_program* prog, int64_t* count);
 
@@ -351,8 +361,9 @@ const char* tqec_version(void);
  * No reference counterpart (the reference decodes one syndrome of one code at
  * a time).  A batch is a set of rows of every program; decoding it is one
  * float32 persistent launch over all programs' row groups (largest programs
- * first), one float64 launch over the rows whose margin is inside the float32
- * bound, and a counter update, with no host synchronisation and no
+ * first), one recheck launch (TQEC_F32X2, or float64 when every program has
+ * TQEC_FLAG_RECHECK_F64; programs must agree) over the rows whose margin is
+ * inside the float32 bound, and a counter update, with no host synchronisation and no
  * allocation: one tqec_multi_launch can be captured into a CUDA graph and the
  * graph replayed once per batch.  The programs' own launch shapes are not
  * used; MAP programs are rejected. */

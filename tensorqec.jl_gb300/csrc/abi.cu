@@ -93,14 +93,16 @@ struct tqec_program {
   int8_t* d_fixed = nullptr;
   double* d_c64 = nullptr;
   float* d_c32 = nullptr;
-  Shape shape[2];  // indexed by precision: the shape of large batches
+  float* d_cx2 = nullptr;  // the constants as double-float pairs (hi, lo)
+  Shape shape[3];  // indexed by precision: the shape of large batches
   // shapes tuned for smaller batches: (rows they were tuned at, shape),
   // ascending; a launch takes the one nearest its row count (log scale)
-  std::vector<std::pair<int64_t, Shape>> sized[2];
-  // float64 re-contraction of the few flagged rows: latency matters, so one
-  // syndrome per block with the most threads and the tables staged
+  std::vector<std::pair<int64_t, Shape>> sized[3];
+  // re-contraction of the few flagged rows (double-float, or float64):
+  // latency matters, so one syndrome per block with the most threads and the
+  // tables staged
   Shape recheck_shape;
-  DevBuf arena[2];
+  DevBuf arena[3];
   DevBuf syn, cls, logp, err, list, count;
   int32_t* h_count = nullptr;  // pinned
   int64_t last_recheck = 0;
@@ -119,8 +121,17 @@ bool is_device_ptr(const void* p) {
   return at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged;
 }
 
+// Arithmetic of the recheck of low-margin float32 rows.
+int recheck_precision(const tqec_program* p) {
+  return (p->flags & TQEC_FLAG_RECHECK_F64) ? TQEC_F64 : TQEC_F32X2;
+}
+
 double err_bound(const tqec_program* p, int precision) {
-  const double u = precision == TQEC_F32 ? std::ldexp(1.0, -24) : std::ldexp(1.0, -53);
+  // per operation: float32 rounding, the double-float multiply-add's bound
+  // (below 2^-44, taken as 2^-43), float64 rounding
+  const double u = precision == TQEC_F32     ? std::ldexp(1.0, -24)
+                   : precision == TQEC_F32X2 ? std::ldexp(1.0, -43)
+                                             : std::ldexp(1.0, -53);
   const double b = u * p->plan.err_terms * 1.01;
   return b / (1.0 - std::min(b, 0.5));
 }
@@ -257,7 +268,9 @@ tqec::KArgs base_args(tqec_program* p, int precision) {
   a.steps = p->d_steps;
   a.n_steps = (int32_t)p->plan.steps.size();
   a.perm = p->d_perm;
-  a.consts = precision == TQEC_F32 ? (const void*)p->d_c32 : (const void*)p->d_c64;
+  a.consts = precision == TQEC_F32     ? (const void*)p->d_c32
+             : precision == TQEC_F32X2 ? (const void*)p->d_cx2
+                                       : (const void*)p->d_c64;
   a.syn_bytes = p->plan.syndrome_bytes;
   a.syn_words = syn_words(p);
   const Shape& s = p->shape[precision];
@@ -435,14 +448,15 @@ int decode_locked(tqec_program* p, const uint8_t* syn, int64_t n, int32_t* cls, 
     rc = plain ? launch_plain(p, precision, a, n, st) : launch_rows(p, precision, a, n, st);
     if (rc) return rc;
     if (recheck && precision == TQEC_F32) {
-      tqec::KArgs b = base_args(p, TQEC_F64);
+      const int rp = recheck_precision(p);
+      tqec::KArgs b = base_args(p, rp);
       b.syn = s.d_syn;
       b.list = (const int32_t*)p->list.p;
       b.list_count = (const int32_t*)p->count.p;
       b.class_out = a.class_out;
       b.logp_out = s.d_logp;
       b.err_out = s.d_err;
-      rc = launch_rows(p, TQEC_F64, b, n, st, &p->recheck_shape);
+      rc = launch_rows(p, rp, b, n, st, &p->recheck_shape);
       if (rc) return rc;
       TQ_CUDA(cudaMemcpyAsync(p->h_count, p->count.p, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
     }
@@ -473,12 +487,13 @@ int program_f64_view(tqec_program* p, ProgramF64View* v) {
 
 int program_multi_view(tqec_program* p, ProgramMultiView* v) {
   if (!p || !v) return TQEC_ERR_INVALID;
-  for (int prec : {TQEC_F32, TQEC_F64}) {
+  v->recheck_precision = recheck_precision(p);
+  for (int prec : {TQEC_F32, v->recheck_precision}) {
     KArgs a = base_args(p, prec);
     a.arena_global = nullptr;
     a.tables_smem = 0;
     a.perm16 = nullptr;
-    (prec == TQEC_F32 ? v->args32 : v->args64) = a;
+    (prec == TQEC_F32 ? v->args32 : v->args_recheck) = a;
   }
   v->device = p->device;
   v->sm_count = p->sm_count;
@@ -573,10 +588,18 @@ int tqec_program_create(const tqec_network* net, const tqec_tree* tree, const tq
   size_t nc = std::max<size_t>(P.consts.size(), 4);
   if ((e = cudaMalloc(&p->d_c64, nc * sizeof(double))) != cudaSuccess) return bail(TQEC_ERR_OOM, "consts");
   if ((e = cudaMalloc(&p->d_c32, nc * sizeof(float))) != cudaSuccess) return bail(TQEC_ERR_OOM, "consts");
+  if ((e = cudaMalloc(&p->d_cx2, nc * 2 * sizeof(float))) != cudaSuccess) return bail(TQEC_ERR_OOM, "consts");
   if (!P.consts.empty()) {
     std::vector<float> c32(P.consts.begin(), P.consts.end());
+    std::vector<float> cx2(2 * P.consts.size());
+    for (size_t i = 0; i < P.consts.size(); ++i) {
+      const float hi = float(P.consts[i]);
+      cx2[2 * i] = hi;
+      cx2[2 * i + 1] = float(P.consts[i] - double(hi));
+    }
     cudaMemcpy(p->d_c64, P.consts.data(), P.consts.size() * sizeof(double), cudaMemcpyHostToDevice);
     cudaMemcpy(p->d_c32, c32.data(), c32.size() * sizeof(float), cudaMemcpyHostToDevice);
+    cudaMemcpy(p->d_cx2, cx2.data(), cx2.size() * sizeof(float), cudaMemcpyHostToDevice);
   }
   if (P.map_mode) {
     const size_t nv = std::max<size_t>(P.vartab.size(), 1), nr = std::max<size_t>(P.report.size(), 1);
@@ -593,7 +616,8 @@ int tqec_program_create(const tqec_network* net, const tqec_tree* tree, const tq
   *p->h_count = 0;
   if ((e = cudaGetLastError()) != cudaSuccess) return bail(TQEC_ERR_CUDA, cudaGetErrorString(e));
   int rc;
-  for (int prec : {TQEC_F32, TQEC_F64}) {
+  for (int prec : {TQEC_F32, TQEC_F64, TQEC_F32X2}) {
+    if (prec == TQEC_F32X2 && P.map_mode) continue;  // max-product runs in float32 or float64
     Shape sp;
     if ((o.flags & TQEC_FLAG_SPLIT_ARENA) && p->plan.arena_small > 0 &&
         choose_split_shape(p, prec, std::max(1, o.group), o.threads > 0 ? o.threads : 256, 0, &sp) == TQEC_OK) {
@@ -607,9 +631,10 @@ int tqec_program_create(const tqec_network* net, const tqec_tree* tree, const tq
   }
   // the recheck keeps the small intermediates and the tables in shared
   // memory when the program has both pools and they fit
+  const int rp = P.map_mode ? TQEC_F64 : recheck_precision(p);
   if (p->plan.arena_small <= 0 ||
-      choose_split_shape(p, TQEC_F64, 1, tqec::contract_max_threads(TQEC_F64), 1, &p->recheck_shape) != TQEC_OK) {
-    if ((rc = choose_shape(p, TQEC_F64, 1, tqec::contract_max_threads(TQEC_F64), 1, &p->recheck_shape)) != TQEC_OK) {
+      choose_split_shape(p, rp, 1, tqec::contract_max_threads(rp), 1, &p->recheck_shape) != TQEC_OK) {
+    if ((rc = choose_shape(p, rp, 1, tqec::contract_max_threads(rp), 1, &p->recheck_shape)) != TQEC_OK) {
       std::string m = g_last_error;
       return bail(rc, m);
     }
@@ -629,11 +654,12 @@ int tqec_program_destroy(tqec_program* p) {
   cudaFree(p->d_tc_err);
   cudaFree(p->d_c64);
   cudaFree(p->d_c32);
+  cudaFree(p->d_cx2);
   cudaFree(p->d_vartab);
   cudaFree(p->d_report);
   cudaFree(p->d_fixed);
   if (p->h_count) cudaFreeHost(p->h_count);
-  for (auto* b : {&p->arena[0], &p->arena[1], &p->syn, &p->cls, &p->logp, &p->err, &p->list, &p->count}) b->release();
+  for (auto* b : {&p->arena[0], &p->arena[1], &p->arena[2], &p->syn, &p->cls, &p->logp, &p->err, &p->list, &p->count}) b->release();
   if (p->stream) cudaStreamDestroy(p->stream);
   delete p;
   return TQEC_OK;
@@ -669,6 +695,8 @@ int tqec_program_info(const tqec_program* p, tqec_program_info_t* info) {
   info->tensor_f32 = p->shape[TQEC_F32].tensor ? 1 : 0;
   info->split_f32 = p->shape[TQEC_F32].split ? 1 : 0;
   info->split_f64 = p->shape[TQEC_F64].split ? 1 : 0;
+  info->recheck_precision = P.map_mode ? TQEC_F64 : recheck_precision(p);
+  info->err_bound_f32x2 = err_bound(p, TQEC_F32X2);
   return TQEC_OK;
 }
 
@@ -695,7 +723,10 @@ int tqec_decode_batch(tqec_program* p, const uint8_t* syndromes, int64_t n, int3
 int tqec_contract_batch(tqec_program* p, const uint8_t* syndromes, int64_t n, int32_t precision, double* logp_out,
                         void* stream) {
   if (!p || n < 0 || (n > 0 && (!syndromes || !logp_out))) return fail(TQEC_ERR_INVALID, "bad argument");
-  if (precision != TQEC_F32 && precision != TQEC_F64) return fail(TQEC_ERR_INVALID, "unknown precision");
+  if (precision != TQEC_F32 && precision != TQEC_F64 && precision != TQEC_F32X2)
+    return fail(TQEC_ERR_INVALID, "unknown precision");
+  if (precision == TQEC_F32X2 && p->plan.map_mode)
+    return fail(TQEC_ERR_INVALID, "a TQEC_FLAG_MAP program contracts in TQEC_F32 or TQEC_F64");
   std::lock_guard<std::mutex> lk(p->mu);
   TQ_CUDA(cudaSetDevice(p->device));
   cudaStream_t st = stream ? (cudaStream_t)stream : p->stream;

@@ -19,6 +19,7 @@
 #include <type_traits>
 
 #include "contract.cuh"
+#include "dfloat.cuh"
 #include "tcgen05.cuh"
 
 namespace tqec {
@@ -235,15 +236,15 @@ __device__ void run_step(const KArgs& a, const StepDesc& dref, int st, int item_
       const T* pb = p.b + (bT ? (((h << d.lfb) | fb) << d.lk) : ((h << (d.lk + d.lfb)) | fb));
       for (int k = 0; k < K; ++k) {
         T a0 = pa[k];
-        if (NORM) a0 *= fa_s;
-        if (MAXP) {
+        if (NORM) a0 = scale(a0, fa_s);
+        if constexpr (MAXP) {
           const T v = a0 * pb[k * kstride];
           acc = v > acc ? v : acc;
         } else {
           acc = fma(a0, pb[k * kstride], acc);
         }
       }
-      if (NORM) acc *= fb_s;
+      if (NORM) acc = scale(acc, fb_s);
       const int addr = d.perm_off < 0 ? e : perm_addr(ptab, d.perm_off, e, lw);
       p.out[addr] = acc;
     }
@@ -272,6 +273,13 @@ __device__ __forceinline__ void load4<double>(const double* p, double v[4]) {
   v[0] = x.x; v[1] = x.y; v[2] = y.x; v[3] = y.y;
 }
 
+template <>
+__device__ __forceinline__ void load4<dfloat>(const dfloat* p, dfloat v[4]) {
+  const float4 x = reinterpret_cast<const float4*>(p)[0];
+  const float4 y = reinterpret_cast<const float4*>(p)[1];
+  v[0] = dfloat(x.x, x.y); v[1] = dfloat(x.z, x.w); v[2] = dfloat(y.x, y.y); v[3] = dfloat(y.z, y.w);
+}
+
 template <typename T>
 __device__ __forceinline__ void store4(T* p, const T v[4]);
 template <>
@@ -282,6 +290,11 @@ template <>
 __device__ __forceinline__ void store4<double>(double* p, const double v[4]) {
   reinterpret_cast<double2*>(p)[0] = make_double2(v[0], v[1]);
   reinterpret_cast<double2*>(p)[1] = make_double2(v[2], v[3]);
+}
+template <>
+__device__ __forceinline__ void store4<dfloat>(dfloat* p, const dfloat v[4]) {
+  reinterpret_cast<float4*>(p)[0] = make_float4(v[0].hi, v[0].lo, v[1].hi, v[1].lo);
+  reinterpret_cast<float4*>(p)[1] = make_float4(v[2].hi, v[2].lo, v[3].hi, v[3].lo);
 }
 
 // A step whose B-only group has at least log2(VW) bits: each work item is VW
@@ -337,14 +350,14 @@ __device__ void run_step_vec(const KArgs& a, const StepDesc& dref, int st, int i
       const T* pb = p.b + ((h << (d.lk + d.lfb)) | fb0);
       auto body = [&](int k) {
         T av = pa[k];
-        if (NORM) av *= fa_s;
+        if (NORM) av = scale(av, fa_s);
         T bv[VW];
         const T* q = pb + k * bstride;
         load4<T>(q, bv);
         if (VW == 8) load4<T>(q + 4, bv + 4);
 #pragma unroll
         for (int j = 0; j < VW; ++j) {
-          if (MAXP) {
+          if constexpr (MAXP) {
             const T v = av * bv[j];
             acc[j] = v > acc[j] ? v : acc[j];
           } else {
@@ -362,7 +375,7 @@ __device__ void run_step_vec(const KArgs& a, const StepDesc& dref, int st, int i
       }
       if (NORM) {
 #pragma unroll
-        for (int j = 0; j < VW; ++j) acc[j] *= fb_s;
+        for (int j = 0; j < VW; ++j) acc[j] = scale(acc[j], fb_s);
       }
       if (!permuted) {
         T* out = p.out + e0;
@@ -454,9 +467,9 @@ __device__ void run_step_splitk(const KArgs& a, const StepDesc& dref, int st, in
       const T* pb = p.b + (bT ? (((h << d.lfb) | fb) << d.lk) : ((h << (d.lk + d.lfb)) | fb));
       const int kstride = bT ? 1 : (1 << d.lfb);
       for (int k = sub; k < K; k += tpo) {
-        const T av = pa[k] * fa_s;
+        const T av = scale(pa[k], fa_s);
         const T bv = pb[k * kstride];
-        if (MAXP) {
+        if constexpr (MAXP) {
           const T v = av * bv;
           acc = v > acc ? v : acc;
         } else {
@@ -466,10 +479,11 @@ __device__ void run_step_splitk(const KArgs& a, const StepDesc& dref, int st, in
     }
     for (int o = 1; o < tpo; o <<= 1) {
       const T other = __shfl_xor_sync(0xffffffffu, acc, o);
-      acc = MAXP ? (other > acc ? other : acc) : acc + other;
+      if constexpr (MAXP) acc = other > acc ? other : acc;
+      else acc = acc + other;
     }
     if (valid && sub == 0) {
-      if (NORM) acc *= fb_s;
+      if (NORM) acc = scale(acc, fb_s);
       const int addr = d.perm_off < 0 ? e : perm_addr(ptab, d.perm_off, e, lw);
       p.out[addr] = acc;
       if (NORM) {
@@ -908,7 +922,7 @@ __device__ void contract_group(const KArgs& a, int64_t base, int64_t nrows, cons
       item_base += items;
     }
   }
-  if (MAXP) {
+  if constexpr (MAXP) {
     backtrack<T>(a, s_steps, s_syn, sm.asg, arena, consts, base, nrows);
     __syncthreads();
   }
@@ -1111,7 +1125,7 @@ __global__ void multi_advance_kernel(int32_t* batch, int32_t* next_unit, int32_t
 size_t contract_smem_bytes(int precision, int32_t n_steps, int32_t syn_words, int G,
                            int64_t arena_elems, bool arena_in_smem, int32_t var_words, size_t table_bytes,
                            bool tensor) {
-  const bool norm = precision == 1;
+  const bool norm = precision != 0;  // float32 and double-float keep per-step maxima
   size_t off = size_t(n_steps) * (sizeof(StepDesc) + 8) + size_t(G) * n_steps * 3 * sizeof(void*) +
                size_t(G) * syn_words * 4;
   if (norm) off += size_t(G) * n_steps * 4;
@@ -1152,6 +1166,7 @@ int contract_occupancy(int precision, int threads, size_t smem, bool map_mode, b
     return tensor ? occupancy_of(tn_contract_kernel<float, true, false, true>, threads, smem)
                   : occupancy_of(tn_contract_kernel<float, true, false, false>, threads, smem);
   }
+  if (precision == 2) return map_mode ? 0 : occupancy_of(tn_contract_kernel<dfloat, true, false, false>, threads, smem);
   return map_mode ? occupancy_of(tn_contract_kernel<double, false, true, false>, threads, smem)
                   : occupancy_of(tn_contract_kernel<double, false, false, false>, threads, smem);
 }
@@ -1171,6 +1186,10 @@ cudaError_t contract_launch(int precision, const KArgs& a, int grid, int threads
     return a.tc ? launch_with(tn_contract_kernel<float, true, false, true>, a, grid, threads, smem, stream)
                 : launch_with(tn_contract_kernel<float, true, false, false>, a, grid, threads, smem, stream);
   }
+  if (precision == 2) {
+    if (a.map_mode) return cudaErrorInvalidValue;  // max-product runs in float32 or float64
+    return launch_with(tn_contract_kernel<dfloat, true, false, false>, a, grid, threads, smem, stream);
+  }
   return a.map_mode ? launch_with(tn_contract_kernel<double, false, true, false>, a, grid, threads, smem, stream)
                     : launch_with(tn_contract_kernel<double, false, false, false>, a, grid, threads, smem, stream);
 }
@@ -1178,6 +1197,7 @@ cudaError_t contract_launch(int precision, const KArgs& a, int grid, int threads
 // Sets the shared-memory limit (outside any stream capture) and returns the
 // resident blocks per SM.
 int contract_multi_occupancy(int precision, int threads, size_t smem) {
+  if (precision == 2) return occupancy_of(tn_contract_multi_kernel<dfloat, true>, threads, smem);
   return precision == 1 ? occupancy_of(tn_contract_multi_kernel<float, true>, threads, smem)
                         : occupancy_of(tn_contract_multi_kernel<double, false>, threads, smem);
 }
@@ -1187,6 +1207,8 @@ cudaError_t contract_multi_launch(int precision, const MultiArgs& m, int grid, i
                                   cudaStream_t stream) {
   if (precision == 1)
     tn_contract_multi_kernel<float, true><<<grid, threads, smem, stream>>>(m);
+  else if (precision == 2)
+    tn_contract_multi_kernel<dfloat, true><<<grid, threads, smem, stream>>>(m);
   else
     tn_contract_multi_kernel<double, false><<<grid, threads, smem, stream>>>(m);
   return cudaGetLastError();

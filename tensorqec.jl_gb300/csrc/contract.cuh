@@ -103,6 +103,8 @@ size_t contract_table_bytes(int precision, int64_t n_consts, int64_t n_perm, boo
 // Largest dynamic shared memory a block may use on this device.
 size_t contract_smem_limit(int device);
 
+// Precisions: 0 float64, 1 float32 (normalised), 2 double-float (pairs of
+// float32, normalised; the re-contraction of low-margin rows).
 // Most threads a block of the given precision may have (blocks running
 // tensor-core steps: 512).
 constexpr int contract_max_threads(int precision, bool tensor = false) {

@@ -8,7 +8,8 @@
 //   1. the float32 multi-program kernel: blocks claim (program, row group)
 //      units of the current batch from a device counter, largest programs
 //      first, and flag rows whose class margin is inside the float32 bound;
-//   2. the float64 kernel over every program's flagged rows;
+//   2. the recheck kernel (double-float, or float64 when every program asks
+//      for it) over every program's flagged rows;
 //   3. an advance kernel: next batch, counters back to zero.
 #include <algorithm>
 #include <cstring>
@@ -102,12 +103,13 @@ struct tqec_multi {
   int n = 0;
   std::vector<tqec_program*> progs;
   std::vector<tqec::ProgramMultiView> views;
-  std::vector<Placement> pl32, pl64;
-  size_t smem32 = 0, smem64 = 0;
-  int grid32 = 1, grid64 = 1;
-  int64_t arena_block32 = 0, arena_block64 = 0;  // elements per block
-  DevArray arena32, arena64;
-  DevArray k32, k64;  // KArgs per program
+  std::vector<Placement> pl32, plr;
+  size_t smem32 = 0, smem_r = 0;
+  int grid32 = 1, grid_r = 1;
+  int64_t arena_block32 = 0, arena_block_r = 0;  // elements per block
+  DevArray arena32, arena_r;
+  DevArray k32, k_r;  // KArgs per program
+  int rprec = 2;       // arithmetic of the recheck launch (TQEC_F32X2 or TQEC_F64)
   DevArray units, unit_offsets, batch_rows, state, counts;
   std::vector<DevArray> lists;
   int32_t n_batches = 0;
@@ -131,36 +133,39 @@ int tqec_multi_create(tqec_program* const* progs, int32_t n_progs, tqec_multi** 
     if (!progs[i] || tqec::program_multi_view(progs[i], &v) != TQEC_OK) return bail(TQEC_ERR_INVALID, "bad program");
     if (v.map_mode) return bail(TQEC_ERR_INVALID, "TQEC_FLAG_MAP programs decode with tqec_map_decode_batch");
     if (i > 0 && v.device != m->views[0].device) return bail(TQEC_ERR_INVALID, "programs on different devices");
+    if (i > 0 && v.recheck_precision != m->views[0].recheck_precision)
+      return bail(TQEC_ERR_INVALID, "programs disagree on the recheck arithmetic (TQEC_FLAG_RECHECK_F64)");
     m->progs.push_back(progs[i]);
     m->views.push_back(v);
   }
   m->device = m->views[0].device;
+  m->rprec = m->views[0].recheck_precision;
   m->sm_count = m->views[0].sm_count;
   if (cudaSetDevice(m->device) != cudaSuccess) return bail(TQEC_ERR_CUDA, "cudaSetDevice");
   const size_t limit = tqec::contract_smem_limit(m->device);
   // one 512-thread block per SM (its 128 registers per thread fill the
   // register file), so a block may take all the shared memory
-  const size_t budget32 = limit - 1024, budget64 = limit - 1024;
+  const size_t budget32 = limit - 1024, budget_r = limit - 1024;
   for (const auto& v : m->views) {
     m->pl32.push_back(place(v, 1, budget32, true));
-    m->pl64.push_back(place(v, 0, budget64, false));
+    m->plr.push_back(place(v, m->rprec, budget_r, false));
   }
   for (int i = 0; i < m->n; ++i) {
     m->smem32 = std::max(m->smem32, m->pl32[i].smem);
-    m->smem64 = std::max(m->smem64, m->pl64[i].smem);
+    m->smem_r = std::max(m->smem_r, m->plr[i].smem);
     if (!m->pl32[i].arena_smem) m->arena_block32 = std::max<int64_t>(m->arena_block32, m->views[i].arena_elems);
-    if (!m->pl64[i].arena_smem) m->arena_block64 = std::max<int64_t>(m->arena_block64, m->views[i].arena_elems);
+    if (!m->plr[i].arena_smem) m->arena_block_r = std::max<int64_t>(m->arena_block_r, m->views[i].arena_elems);
   }
-  if (m->smem32 > limit || m->smem64 > limit) return bail(TQEC_ERR_UNSUPPORTED, "a program does not fit shared memory");
+  if (m->smem32 > limit || m->smem_r > limit) return bail(TQEC_ERR_UNSUPPORTED, "a program does not fit shared memory");
   const int occ32 = tqec::contract_multi_occupancy(1, tqec::kMultiThreads, m->smem32);
-  const int occ64 = tqec::contract_multi_occupancy(0, tqec::kMultiThreads, m->smem64);
-  if (occ32 < 1 || occ64 < 1) return bail(TQEC_ERR_UNSUPPORTED, "multi-program launch cannot be resident");
+  const int occ_r = tqec::contract_multi_occupancy(m->rprec, tqec::kMultiThreads, m->smem_r);
+  if (occ32 < 1 || occ_r < 1) return bail(TQEC_ERR_UNSUPPORTED, "multi-program launch cannot be resident");
   m->grid32 = occ32 * m->sm_count;
-  m->grid64 = m->sm_count;
+  m->grid_r = m->sm_count;
   if (m->arena_block32 && m->arena32.zeros(size_t(m->grid32) * m->arena_block32 * 4) != cudaSuccess)
     return bail(TQEC_ERR_OOM, "float32 arenas");
-  if (m->arena_block64 && m->arena64.zeros(size_t(m->grid64) * m->arena_block64 * 8) != cudaSuccess)
-    return bail(TQEC_ERR_OOM, "float64 arenas");
+  if (m->arena_block_r && m->arena_r.zeros(size_t(m->grid_r) * m->arena_block_r * 8) != cudaSuccess)
+    return bail(TQEC_ERR_OOM, "recheck arenas");
   if (m->state.zeros(2 * sizeof(int32_t)) != cudaSuccess || m->counts.zeros(sizeof(int32_t) * m->n) != cudaSuccess)
     return bail(TQEC_ERR_OOM, "counters");
   *out = m;
@@ -171,7 +176,7 @@ int tqec_multi_destroy(tqec_multi* m) {
   if (!m) return TQEC_OK;
   cudaSetDevice(m->device);
   cudaDeviceSynchronize();
-  for (DevArray* a : {&m->arena32, &m->arena64, &m->k32, &m->k64, &m->units, &m->unit_offsets, &m->batch_rows,
+  for (DevArray* a : {&m->arena32, &m->arena_r, &m->k32, &m->k_r, &m->units, &m->unit_offsets, &m->batch_rows,
                       &m->state, &m->counts})
     a->release();
   for (auto& l : m->lists) l.release();
@@ -210,20 +215,20 @@ int tqec_multi_set_work(tqec_multi* m, int32_t n_batches, const int64_t* batch_e
     offs.push_back((int64_t)units.size());
   }
   m->lists.resize(n);
-  std::vector<tqec::KArgs> a32(n), a64(n);
+  std::vector<tqec::KArgs> a32(n), a_r(n);
   for (int i = 0; i < n; ++i) {
     if (m->lists[i].zeros(sizeof(int32_t) * std::max<int64_t>(max_rows[i], 1)) != cudaSuccess)
       return mfail(TQEC_ERR_OOM, "recheck lists");
     int32_t* list = static_cast<int32_t*>(m->lists[i].p);
     int32_t* count = static_cast<int32_t*>(m->counts.p) + i;
-    for (int prec : {1, 0}) {
-      tqec::KArgs a = prec == 1 ? m->views[i].args32 : m->views[i].args64;
-      const Placement& pl = prec == 1 ? m->pl32[i] : m->pl64[i];
+    for (int prec : {1, m->rprec}) {
+      tqec::KArgs a = prec == 1 ? m->views[i].args32 : m->views[i].args_recheck;
+      const Placement& pl = prec == 1 ? m->pl32[i] : m->plr[i];
       a.G = pl.G;
       a.lg = 0;
       while ((1 << a.lg) < pl.G) a.lg++;
       // a non-null arena pointer marks a global arena: the kernel uses the block's slice
-      a.arena_global = pl.arena_smem ? nullptr : (prec == 1 ? m->arena32.p : m->arena64.p);
+      a.arena_global = pl.arena_smem ? nullptr : (prec == 1 ? m->arena32.p : m->arena_r.p);
       a.syn = syndromes[i];
       a.class_out = class_out[i];
       a.logp_out = nullptr;
@@ -242,12 +247,12 @@ int tqec_multi_set_work(tqec_multi* m, int32_t n_batches, const int64_t* batch_e
         a.recheck_margin = -1.0;
         a.recheck_list = nullptr;
         a.recheck_count = nullptr;
-        a64[i] = a;
+        a_r[i] = a;
       }
     }
   }
   if (m->k32.put(a32.data(), sizeof(tqec::KArgs) * n) != cudaSuccess ||
-      m->k64.put(a64.data(), sizeof(tqec::KArgs) * n) != cudaSuccess ||
+      m->k_r.put(a_r.data(), sizeof(tqec::KArgs) * n) != cudaSuccess ||
       m->units.put(units.data(), sizeof(tqec::MultiUnit) * std::max<size_t>(units.size(), 1)) != cudaSuccess ||
       m->unit_offsets.put(offs.data(), sizeof(int64_t) * offs.size()) != cudaSuccess ||
       m->batch_rows.put(batch_end_rows, sizeof(int64_t) * size_t(n_batches) * n) != cudaSuccess)
@@ -289,11 +294,11 @@ int tqec_multi_launch(tqec_multi* m, void* stream) {
   a.arena_global = m->arena32.p;
   a.arena_per_block = m->arena_block32;
   MQ_CUDA(tqec::contract_multi_launch(1, a, m->grid32, tqec::kMultiThreads, m->smem32, st));
-  a.progs = static_cast<const tqec::KArgs*>(m->k64.p);
+  a.progs = static_cast<const tqec::KArgs*>(m->k_r.p);
   a.list_mode = 1;
-  a.arena_global = m->arena64.p;
-  a.arena_per_block = m->arena_block64;
-  MQ_CUDA(tqec::contract_multi_launch(0, a, m->grid64, tqec::kMultiThreads, m->smem64, st));
+  a.arena_global = m->arena_r.p;
+  a.arena_per_block = m->arena_block_r;
+  MQ_CUDA(tqec::contract_multi_launch(m->rprec, a, m->grid_r, tqec::kMultiThreads, m->smem_r, st));
   MQ_CUDA(tqec::contract_multi_advance(batch, next, static_cast<int32_t*>(m->counts.p), m->n, st));
   return TQEC_OK;
 }

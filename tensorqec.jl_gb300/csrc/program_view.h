@@ -20,10 +20,11 @@ struct ProgramF64View {
 
 int program_f64_view(tqec_program* p, ProgramF64View* v);
 
-// What a multi-program launch needs of one program: its float32 and float64
+// What a multi-program launch needs of one program: its float32 and recheck
 // launch descriptions (global tables, no buffers) and its sizes.
 struct ProgramMultiView {
-  KArgs args32, args64;
+  KArgs args32, args_recheck;
+  int recheck_precision;  // TQEC_F32X2 or TQEC_F64
   int device;
   int sm_count;
   int64_t arena_elems;

@@ -119,9 +119,11 @@ class TNMMAP:
 
     ``precision``: "f64" contracts in float64 (the reference's arithmetic);
     "f32" contracts in float32 with power-of-two renormalisation and
-    re-contracts in float64 every syndrome whose class margin is below the
-    rounding-error bound.  ``plain`` launches one syndrome at a time (the
-    drop-in form of the reference's per-syndrome ``decode``)."""
+    re-contracts every syndrome whose class margin is below the
+    rounding-error bound, in double-float (pairs of float32, about 48
+    significant bits; GB300 runs float64 at 1/64 of the float32 rate) or, with
+    ``recheck_f64``, in float64.  ``plain`` launches one syndrome at a time
+    (the drop-in form of the reference's per-syndrome ``decode``)."""
     optimizer: object = field(default_factory=TreeSA)
     factorize: bool = True
     precision: str = "f32"
@@ -133,6 +135,7 @@ class TNMMAP:
     split_arena: bool = False
     big_elems: int = 0
     tensor_cores: bool = True
+    recheck_f64: bool = False
 
     def _native_precision(self):
         return {"f64": native.TQEC_F64, "f32": native.TQEC_F32}[self.precision]
@@ -140,7 +143,8 @@ class TNMMAP:
     def _flags(self):
         return ((native.TQEC_FLAG_PLAIN if self.plain else 0) |
                 (native.TQEC_FLAG_SPLIT_ARENA if self.split_arena else 0) |
-                (0 if self.tensor_cores else native.TQEC_FLAG_NO_TENSOR_CORES))
+                (0 if self.tensor_cores else native.TQEC_FLAG_NO_TENSOR_CORES) |
+                (native.TQEC_FLAG_RECHECK_F64 if self.recheck_f64 else 0))
 
 
 class CompiledTNMMAP:
@@ -192,7 +196,7 @@ class CompiledTNMMAP:
         (Julia linear order), contracted in the given precision."""
         packed = pack_syndromes(self._bits(syndromes))
         prec = self.decoder._native_precision() if precision is None else \
-            {"f64": native.TQEC_F64, "f32": native.TQEC_F32}[precision]
+            {"f64": native.TQEC_F64, "f32": native.TQEC_F32, "f32x2": native.TQEC_F32X2}[precision]
         return self.program.contract_packed(packed, prec)
 
     def error_pattern(self, cls: int, syndrome: CSSSyndrome):
@@ -293,7 +297,7 @@ class CompiledDEMTNMMAP:
     def class_logprobs(self, syndromes, precision=None):
         packed = pack_syndromes(np.atleast_2d(np.asarray(syndromes, dtype=np.uint8)) & 1)
         prec = self.decoder._native_precision() if precision is None else \
-            {"f64": native.TQEC_F64, "f32": native.TQEC_F32}[precision]
+            {"f64": native.TQEC_F64, "f32": native.TQEC_F32, "f32x2": native.TQEC_F32X2}[precision]
         return self.program.contract_packed(packed, prec)
 
     def error_pattern(self, cls: int, syndrome: SimpleSyndrome):

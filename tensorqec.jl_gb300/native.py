@@ -16,11 +16,13 @@ LIB_PATH = os.path.join(HERE, "libtqec_gb300.so")
 TQEC_OK = 0
 TQEC_F64 = 0
 TQEC_F32 = 1
+TQEC_F32X2 = 2
 TQEC_FLAG_PLAIN = 1
 TQEC_FLAG_NORECHECK = 2
 TQEC_FLAG_MAP = 4
 TQEC_FLAG_SPLIT_ARENA = 8
 TQEC_FLAG_NO_TENSOR_CORES = 16
+TQEC_FLAG_RECHECK_F64 = 32
 
 ERRORS = {-1: "invalid argument", -2: "CUDA error", -3: "out of device memory",
           -4: "unsupported network", -5: "timeout", -6: "I/O error"}
@@ -58,7 +60,7 @@ class ProgramInfo(C.Structure):
                 ("resident_f32", C.c_int32), ("resident_f64", C.c_int32), ("tables_smem_f32", C.c_int32),
                 ("tables_smem_f64", C.c_int32), ("arena_small", C.c_int64), ("split_f32", C.c_int32),
                 ("split_f64", C.c_int32), ("tensor_steps", C.c_int32), ("tensor_f32", C.c_int32),
-                ("reserved_0", C.c_int32), ("reserved_1", C.c_int32)]
+                ("recheck_precision", C.c_int32), ("reserved_", C.c_int32), ("err_bound_f32x2", C.c_double)]
 
 
 class PlanView(C.Structure):
@@ -376,7 +378,8 @@ class Sampler:
 
 class MultiDecoder:
     """Owner of a ``tqec_multi``: several programs decoded by one persistent
-    launch per batch (float32 + float64 recheck), capturable in a CUDA graph.
+    launch per batch (float32 + double-float or float64 recheck), capturable
+    in a CUDA graph.
 
     ``set_work(batch_end_rows, syn_ptrs, cls_ptrs)``: batch_end_rows is an
     (n_batches, n_programs) array of cumulative end rows; the pointers are

@@ -3,7 +3,7 @@
 Uneven code sizes (surface d=3/5/7, colour 4.8.8 d=5, toric L=4 with 16
 classes) with their own noise rates are decoded batch by batch, directly and
 through a captured CUDA graph replayed once per batch; every class must equal
-the single-program decoder's (float32 + float64 recheck) except on exact ties.
+the single-program decoder's (float32 + recheck) except on exact ties.
 """
 import numpy as np
 import pytest
@@ -81,3 +81,18 @@ def test_multi_program_batches_match_single_program(pkg):
     md.close()
     for ct, _ in progs:
         ct.close()
+
+
+def test_multi_programs_must_agree_on_recheck(pkg):
+    """One recheck launch serves every program: programs whose recheck
+    arithmetic differs (TQEC_FLAG_RECHECK_F64 on one of them) are refused."""
+    t = pkg.tanner_graph(pkg.SurfaceCode(3, 3))
+    em = pkg.depolarizing(0.05, t.nq)
+    a = pkg.compile(pkg.TNMMAP(precision="f32"), t, em)
+    b = pkg.compile(pkg.TNMMAP(precision="f32", recheck_f64=True), t, em)
+    with pytest.raises(pkg.native.TqecError):
+        pkg.native.MultiDecoder([a.program, b.program])
+    md = pkg.native.MultiDecoder([b.program, b.program])
+    md.close()
+    a.close()
+    b.close()

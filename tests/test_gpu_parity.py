@@ -297,3 +297,65 @@ def test_tensor_cores_switch_and_autotune(pkg):
         assert np.max(np.abs(np.exp(lp32 - top) - np.exp(lp64 - top))) <= bound
     ct_tc.close()
     ct_si.close()
+
+
+@pytest.mark.parametrize("kind,d,p,n", [("surface", 5, 0.08, 400), ("surface", 7, 0.05, 48),
+                                        ("toric", 3, 0.05, 128), ("666", 5, 0.08, 128)])
+def test_f32x2_marginals_vs_oracle(pkg, oracle, kind, d, p, n):
+    """Double-float contraction (pairs of float32, the recheck's default
+    arithmetic): marginals within its stated bound of the oracle, a bound
+    2^-19 times float32's."""
+    t, em, bits, dec = css_case(pkg, oracle, kind, d, p, n, seed=200 + d)
+    want = dec.marginals(bits)
+    ct = pkg.compile(pkg.TNMMAP(precision="f32"), t, em)
+    info = ct.program.info
+    assert info["recheck_precision"] == pkg.native.TQEC_F32X2
+    bound = info["err_bound_f32x2"]
+    assert bound <= info["err_bound_f32"] * 2.0 ** -19 * 1.001
+    assert_marginals(ct.class_logprobs(bits, precision="f32x2"), want, 2 * bound)
+    ct.close()
+
+
+@pytest.mark.parametrize("recheck_f64", [False, True])
+def test_recheck_every_row(pkg, recheck_f64):
+    """A margin no float32 result clears sends every row to the recheck:
+    decisions equal float64's outside ties, every row is counted, and each
+    row's error bound is the recheck arithmetic's."""
+    t = pkg.tanner_graph(pkg.SurfaceCode(7, 7))
+    em = pkg.depolarizing(0.08, t.nq)
+    ep = pkg.random_error_pattern(em, np.random.default_rng(13), nsamples=600)
+    syn = pkg.syndrome_extraction(ep, t)
+    bits = np.concatenate([syn.sx, syn.sz], axis=1)
+    ct = pkg.compile(pkg.TNMMAP(precision="f32", margin=1e30, recheck_f64=recheck_f64), t, em)
+    info = ct.program.info
+    want_prec = pkg.native.TQEC_F64 if recheck_f64 else pkg.native.TQEC_F32X2
+    assert info["recheck_precision"] == want_prec
+    packed = pkg.pack_syndromes(bits)
+    logp = np.empty((len(bits), ct.n_classes))
+    err = np.empty(len(bits), dtype=np.float32)
+    cls = ct.program.decode_packed(packed, logp=logp, err=err)
+    assert ct.program.last_recheck_count() == len(bits)
+    bound = info["err_bound_f64"] if recheck_f64 else info["err_bound_f32x2"]
+    np.testing.assert_allclose(err, np.float32(bound), rtol=1e-6)
+    lp64 = ct.class_logprobs(bits, precision="f64")
+    top = lp64.max(axis=1, keepdims=True)
+    assert np.max(np.abs(np.exp(logp - top) - np.exp(lp64 - top))) <= 2 * bound + 1e-15
+    srt = np.sort(lp64, axis=1)
+    tie = (srt[:, -1] - srt[:, -2]) <= 1e-9
+    assert not ((cls != np.argmax(lp64, axis=1)) & ~tie).any()
+    ct.close()
+
+
+def test_f32x2_circuit_level(pkg):
+    """Double-float on a circuit-level program (rotated Z-memory d=5, 2
+    rounds): within its bound of float64."""
+    from tensorqec_gb300 import circuit, dem as demmod
+
+    dm = circuit.detector_error_model(circuit.memory_z_circuit(5, 2, 0.001))
+    _, det, _ = demmod.sample_dem(dm, 256, np.random.default_rng(21))
+    ct = pkg.compile(pkg.TNMMAP(precision="f32", optimizer=pkg.TreeSA(trials=16, sweeps=1000, restarts=2)), dm)
+    lp2 = ct.class_logprobs(det, precision="f32x2")
+    lp64 = ct.class_logprobs(det, precision="f64")
+    top = lp64.max(axis=1, keepdims=True)
+    assert np.max(np.abs(np.exp(lp2 - top) - np.exp(lp64 - top))) <= 2 * ct.program.info["err_bound_f32x2"]
+    ct.close()
