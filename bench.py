@@ -44,6 +44,10 @@ def parse():
     ap.add_argument("--profile", action="store_true",
                     help="one float32 contraction launch of --batch syndromes (for ncu), no timing")
     ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--profile-recheck", type=int, default=0, metavar="ROWS",
+                    help="W warm-up decodes then one decode of ROWS d=7 syndromes, every one sent to the "
+                         "recheck (margin above any float32 result), for ncu; --recheck-f64: float64 recheck")
+    ap.add_argument("--recheck-f64", action="store_true")
     ap.add_argument("--precision-sweep", action="store_true",
                     help="float32 vs float64 log-probability error and decision mismatch over d in {5,7} and "
                          "p in {0.02,0.05,0.08,0.11}, one JSON line per (d,p)")
@@ -64,8 +68,8 @@ def parse():
     ap.add_argument("--split-arena", action="store_true",
                     help="--profile: small intermediates in shared memory, large ones in global memory")
     ap.add_argument("--no-surrogate", action="store_true", help="time the batched exact decoder alone")
-    ap.add_argument("--train-n", type=int, default=1 << 24, help="surrogate training syndromes")
-    ap.add_argument("--train-epochs", type=int, default=8, help="surrogate training epochs")
+    ap.add_argument("--train-n", type=int, default=1 << 25, help="surrogate training syndromes")
+    ap.add_argument("--train-epochs", type=int, default=16, help="surrogate training epochs")
     ap.add_argument("--calib-n", type=int, default=1 << 20, help="surrogate calibration syndromes")
     ap.add_argument("--eval-n", type=int, default=1 << 20, help="fresh syndromes for the evaluation")
     return ap.parse_args()
@@ -467,6 +471,28 @@ def run_profile(args):
     ct.close()
 
 
+def run_profile_recheck(args):
+    """The recheck launch on its own: ROWS d=7 syndromes decoded with a
+    margin no float32 result clears, so every row is contracted again."""
+    import torch
+
+    import __graft_entry__ as G
+
+    pkg = G.load_package()
+    rows = args.profile_recheck
+    t, em, bits = workload(pkg, 0, 1, rows)
+    ct = pkg.compile(pkg.TNMMAP(precision="f32", margin=1e30, recheck_f64=args.recheck_f64), t, em)
+    d_syn = torch.from_numpy(pkg.pack_syndromes(bits[0])).cuda()
+    d_cls = torch.empty(rows, dtype=torch.int32, device="cuda")
+    sptr = torch.cuda.current_stream().cuda_stream
+    for _ in range(args.warmup + 1):
+        ct.program.decode_ptrs(d_syn.data_ptr(), rows, d_cls.data_ptr(), None, None, sptr)
+    torch.cuda.synchronize()
+    print(json.dumps({"profile_case": "recheck", "rows": rows, "recheck": "f64" if args.recheck_f64 else "f32x2",
+                      "rechecked": ct.program.last_recheck_count()}), flush=True)
+    ct.close()
+
+
 def run_precision_sweep(args):
     """Per (d, p): --batch seeded syndromes contracted in one float32 launch
     (power-of-two renormalised) and in float64; reports the class
@@ -748,6 +774,8 @@ def main():
         run_mixed(args)
     elif args.precision_sweep:
         run_precision_sweep(args)
+    elif args.profile_recheck:
+        run_profile_recheck(args)
     elif args.profile:
         run_profile(args)
     elif args.impl == "reference":

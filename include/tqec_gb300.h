@@ -289,6 +289,13 @@ int tqec_mlp_gradients(tqec_mlp* mlp, const uint8_t* syndromes, const float* tar
 /* One Adam step (beta 0.9/0.999, eps 1e-8) on a batch; loss_out may be NULL. */
 int tqec_mlp_train_step(tqec_mlp* mlp, const uint8_t* syndromes, const float* targets, int64_t n,
                         float lr, float* loss_out, void* stream);
+/* The same step on rows[0..n) of a training set resident in device memory
+ * (n_set packed syndromes and their n_set x n_classes targets): the batch is
+ * gathered on the device, and nothing is copied to or from the host unless
+ * loss_out is given (then the call synchronises, and reports a row index
+ * outside [0, n_set) as TQEC_ERR_INVALID; such a row reads row 0). */
+int tqec_mlp_train_step_rows(tqec_mlp* mlp, const uint8_t* syndromes, const float* targets, int64_t n_set,
+                             const int32_t* rows, int64_t n, float lr, float* loss_out, void* stream);
 /* Argmax class and its softmax probability for each row. */
 int tqec_mlp_infer(tqec_mlp* mlp, const uint8_t* syndromes, int64_t n, int32_t* class_out,
                    float* conf_out, void* stream);

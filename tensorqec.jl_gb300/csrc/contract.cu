@@ -236,7 +236,9 @@ __device__ void run_step(const KArgs& a, const StepDesc& dref, int st, int item_
       const T* pb = p.b + (bT ? (((h << d.lfb) | fb) << d.lk) : ((h << (d.lk + d.lfb)) | fb));
       for (int k = 0; k < K; ++k) {
         T a0 = pa[k];
-        if (NORM) a0 = scale(a0, fa_s);
+        // both normalisers on the A value (exact powers of two): the output
+        // needs no scaling of its own
+        if (NORM) a0 = scale(scale(a0, fa_s), fb_s);
         if constexpr (MAXP) {
           const T v = a0 * pb[k * kstride];
           acc = v > acc ? v : acc;
@@ -244,7 +246,6 @@ __device__ void run_step(const KArgs& a, const StepDesc& dref, int st, int item_
           acc = fma(a0, pb[k * kstride], acc);
         }
       }
-      if (NORM) acc = scale(acc, fb_s);
       const int addr = d.perm_off < 0 ? e : perm_addr(ptab, d.perm_off, e, lw);
       p.out[addr] = acc;
     }
@@ -350,7 +351,9 @@ __device__ void run_step_vec(const KArgs& a, const StepDesc& dref, int st, int i
       const T* pb = p.b + ((h << (d.lk + d.lfb)) | fb0);
       auto body = [&](int k) {
         T av = pa[k];
-        if (NORM) av = scale(av, fa_s);
+        // both normalisers on the shared A value (exact powers of two), so
+        // the VW outputs need no scaling of their own
+        if (NORM) av = scale(scale(av, fa_s), fb_s);
         T bv[VW];
         const T* q = pb + k * bstride;
         load4<T>(q, bv);
@@ -372,10 +375,6 @@ __device__ void run_step_vec(const KArgs& a, const StepDesc& dref, int st, int i
           body(k);
           body(k + 1);
         }
-      }
-      if (NORM) {
-#pragma unroll
-        for (int j = 0; j < VW; ++j) acc[j] = scale(acc[j], fb_s);
       }
       if (!permuted) {
         T* out = p.out + e0;

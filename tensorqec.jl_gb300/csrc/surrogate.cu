@@ -80,6 +80,7 @@ struct tqec_mlp {
   int use_tensor_cores = 1;                   // hidden layers on tcgen05 where the shape allows
   int* d_err = nullptr;                       // timeout flag of the tcgen05 kernel
   int* h_err = nullptr;                       // pinned
+  int* d_bad = nullptr;                       // a gathered row index was outside the set
   cudaStream_t stream = nullptr;
   std::mutex mu;
 };
@@ -295,9 +296,10 @@ int tqec_mlp_create(const tqec_mlp_config* cfg, tqec_mlp** out) {
       cudaMalloc(&p->w16, sizeof(__nv_bfloat16) * off) || cudaMalloc(&p->loss, sizeof(float)) ||
       cudaMallocHost(&p->h_loss, sizeof(float)) || cudaMalloc(&p->count, sizeof(int32_t)) ||
       cudaMallocHost(&p->h_count, sizeof(int32_t)) || cudaMalloc(&p->d_err, sizeof(int)) ||
-      cudaMallocHost(&p->h_err, sizeof(int)))
+      cudaMallocHost(&p->h_err, sizeof(int)) || cudaMalloc(&p->d_bad, sizeof(int)))
     return bail(TQEC_ERR_OOM, "surrogate parameters");
   cudaMemset(p->d_err, 0, sizeof(int));
+  cudaMemset(p->d_bad, 0, sizeof(int));
   cudaMemset(p->m, 0, sizeof(float) * off);
   cudaMemset(p->v, 0, sizeof(float) * off);
   // uniform(-1/sqrt(fan_in), 1/sqrt(fan_in)) weights and biases; the padded
@@ -333,6 +335,7 @@ int tqec_mlp_destroy(tqec_mlp* p) {
   cudaFree(p->count);
   cudaFree(p->syn);
   cudaFree(p->d_err);
+  cudaFree(p->d_bad);
   if (p->h_err) cudaFreeHost(p->h_err);
   if (p->h_loss) cudaFreeHost(p->h_loss);
   if (p->h_count) cudaFreeHost(p->h_count);
@@ -389,6 +392,50 @@ int tqec_mlp_gradients(tqec_mlp* p, const uint8_t* syn, const float* targets, in
   return TQEC_OK;
 }
 
+}  // extern "C"
+
+namespace {
+
+// Forward, backward and one Adam step over rows [0, n) of staged syndromes
+// `ds` with targets in p->tgt; the loss is read back (one synchronisation)
+// only when asked for.
+int train_rows(tqec_mlp* p, const uint8_t* ds, int64_t n, float lr, float* loss_out, cudaStream_t st) {
+  int rc;
+  if ((rc = forward(p, ds, n, st))) return rc;
+  if ((rc = backward(p, n, st))) return rc;
+  p->adam_t += 1;
+  const float b1 = 0.9f, b2 = 0.999f;
+  const float c1 = 1.0f / (1.0f - std::pow(b1, float(p->adam_t)));
+  const float c2 = 1.0f / (1.0f - std::pow(b2, float(p->adam_t)));
+  SQ_CUDA(tqec::adam_update(p->w32, p->g, p->m, p->v, p->w16, (int64_t)p->n_params, lr, b1, b2, 1e-8f, c1, c2, st));
+  if (loss_out) {
+    SQ_CUDA(cudaMemcpyAsync(p->h_loss, p->loss, sizeof(float), cudaMemcpyDeviceToHost, st));
+    SQ_CUDA(cudaStreamSynchronize(st));
+    *loss_out = *p->h_loss / float(n);
+  }
+  return TQEC_OK;
+}
+
+// rows[i] of a resident training set (syndromes `sb` bytes a row, targets
+// `nc` floats a row) into the step buffers; an index outside [0, n_set)
+// reads row 0 and raises *bad
+__global__ void gather_rows_kernel(const uint8_t* syn, int sb, const float* tgt, int nc, int64_t n_set,
+                                   const int32_t* rows, int64_t n, uint8_t* syn_out, float* tgt_out, int* bad) {
+  for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x) {
+    int64_t r = rows[i];
+    if (r < 0 || r >= n_set) {
+      atomicExch(bad, 1);
+      r = 0;
+    }
+    for (int b = 0; b < sb; ++b) syn_out[i * sb + b] = syn[r * sb + b];
+    for (int c = 0; c < nc; ++c) tgt_out[i * nc + c] = tgt[r * nc + c];
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
 int tqec_mlp_train_step(tqec_mlp* p, const uint8_t* syn, const float* targets, int64_t n, float lr, float* loss_out,
                         void* stream) {
   if (!p || !syn || !targets || n <= 0) return sfail(TQEC_ERR_INVALID, "bad argument");
@@ -401,17 +448,32 @@ int tqec_mlp_train_step(tqec_mlp* p, const uint8_t* syn, const float* targets, i
   if ((rc = stage_syn(p, syn, n, st, &ds))) return rc;
   SQ_CUDA(cudaMemcpyAsync(p->tgt, targets, sizeof(float) * n * p->cfg.n_out,
                           dev_ptr(targets) ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, st));
-  if ((rc = forward(p, ds, n, st))) return rc;
-  if ((rc = backward(p, n, st))) return rc;
-  p->adam_t += 1;
-  const float b1 = 0.9f, b2 = 0.999f;
-  const float c1 = 1.0f / (1.0f - std::pow(b1, float(p->adam_t)));
-  const float c2 = 1.0f / (1.0f - std::pow(b2, float(p->adam_t)));
-  SQ_CUDA(tqec::adam_update(p->w32, p->g, p->m, p->v, p->w16, (int64_t)p->n_params, lr, b1, b2, 1e-8f, c1, c2, st));
+  return train_rows(p, ds, n, lr, loss_out, st);
+}
+
+int tqec_mlp_train_step_rows(tqec_mlp* p, const uint8_t* syn, const float* targets, int64_t n_set,
+                             const int32_t* rows, int64_t n, float lr, float* loss_out, void* stream) {
+  if (!p || !syn || !targets || !rows || n <= 0 || n_set <= 0) return sfail(TQEC_ERR_INVALID, "bad argument");
+  if (!dev_ptr(syn) || !dev_ptr(targets) || !dev_ptr(rows))
+    return sfail(TQEC_ERR_INVALID, "the training set and the row indices must be in device memory");
+  std::lock_guard<std::mutex> lk(p->mu);
+  SQ_CUDA(cudaSetDevice(p->cfg.device));
+  cudaStream_t st = stream ? (cudaStream_t)stream : p->stream;
+  int rc = ensure_cap(p, n);
+  if (rc) return rc;
+  const int sb = (p->cfg.n_in + 7) / 8;
+  const int grid = (int)std::min<int64_t>((n + 255) / 256, 4096);
+  gather_rows_kernel<<<grid, 256, 0, st>>>(syn, sb, targets, p->cfg.n_out, n_set, rows, n, p->gathered, p->tgt,
+                                           p->d_bad);
+  SQ_CUDA(cudaGetLastError());
+  if ((rc = train_rows(p, p->gathered, n, lr, loss_out, st))) return rc;
   if (loss_out) {
-    SQ_CUDA(cudaMemcpyAsync(p->h_loss, p->loss, sizeof(float), cudaMemcpyDeviceToHost, st));
-    SQ_CUDA(cudaStreamSynchronize(st));
-    *loss_out = *p->h_loss / float(n);
+    int bad = 0;
+    SQ_CUDA(cudaMemcpy(&bad, p->d_bad, sizeof(int), cudaMemcpyDeviceToHost));
+    if (bad) {
+      cudaMemset(p->d_bad, 0, sizeof(int));
+      return sfail(TQEC_ERR_INVALID, "a row index was outside the training set");
+    }
   }
   return TQEC_OK;
 }

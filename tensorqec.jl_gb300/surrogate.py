@@ -31,6 +31,7 @@ def _lib():
                "tqec_mlp_get_params": [vp, vp, i64], "tqec_mlp_set_params": [vp, vp, i64],
                "tqec_mlp_gradients": [vp, vp, vp, i64, vp, vp],
                "tqec_mlp_train_step": [vp, vp, vp, i64, C.c_float, vp, vp],
+               "tqec_mlp_train_step_rows": [vp, vp, vp, i64, vp, i64, C.c_float, vp, vp],
                "tqec_mlp_infer": [vp, vp, i64, vp, vp, vp],
                "tqec_gated_decode": [vp, vp, C.c_float, vp, i64, vp, vp, vp],
                "tqec_mlp_save": [vp, C.c_char_p], "tqec_mlp_load": [vp, C.c_char_p],
@@ -102,6 +103,17 @@ class Surrogate:
                                                 C.byref(loss), None))
         return loss.value
 
+    def train_step_rows(self, syn_ptr, tgt_ptr, n_set, rows_ptr, n, lr, with_loss=False, stream=None):
+        """One Adam step on rows[0..n) of a device-resident training set
+        (raw device pointers); returns the loss only when asked (that call
+        synchronises)."""
+        loss = C.c_float()
+        native.check(_lib().tqec_mlp_train_step_rows(self._h, C.c_void_p(syn_ptr), C.c_void_p(tgt_ptr), n_set,
+                                                     C.c_void_p(rows_ptr), n, lr,
+                                                     C.byref(loss) if with_loss else None,
+                                                     C.c_void_p(stream) if stream else None))
+        return loss.value if with_loss else None
+
     def infer(self, packed):
         packed = np.ascontiguousarray(packed, dtype=np.uint8)
         n = packed.shape[0]
@@ -143,46 +155,108 @@ def sample_bits(ct, n, rng):
     return np.concatenate([s.sx, s.sz], axis=1)
 
 
+def _draw_labelled(ct, sampler, rng, seed, offset, m, nbytes):
+    """m syndromes (GPU sampler at counter `offset`, or the host sampler) and
+    their exact class probabilities, as host arrays."""
+    sub = 1 << 20
+    packed = np.empty((m, nbytes), dtype=np.uint8)
+    targets = np.empty((m, ct.n_classes), dtype=np.float32)
+    for i in range(0, m, sub):
+        k = min(sub, m - i)
+        if sampler is not None:
+            packed[i:i + k], _ = sampler.sample(seed, k, offset=offset + i)
+        else:
+            packed[i:i + k] = pack_syndromes(sample_bits(ct, k, rng))
+        targets[i:i + k] = soft_labels(ct.program.contract_packed(packed[i:i + k], native.TQEC_F32))
+    return packed, targets
+
+
 def train_surrogate(ct, n_train=1 << 24, batch=16384, epochs=4, lr=3e-3, hidden=512, n_layers=4, seed=1,
-                    rng=None, log=None, gpu_sampler=True):
+                    rng=None, log=None, gpu_sampler=True, chunk=0, device_resident=None):
     """Trains a surrogate for a compiled CSS decoder on n_train sampled
     syndromes labelled by the exact contraction (float32 with its rounding
     bound).  Syndromes come from the GPU sampler (Philox, seeded by `seed`)
-    or, with gpu_sampler=False, from the host sampler.  Returns (surrogate,
-    stats)."""
+    or, with gpu_sampler=False, from the host sampler.  With chunk > 0 the
+    syndromes are drawn and labelled `chunk` at a time and each chunk gets
+    its `epochs` passes before the next is drawn (fresh data in bounded
+    memory); chunk=0 draws them all first.  The learning rate follows one
+    cosine schedule over all steps.
+
+    device_resident (default: when torch sees a GPU): the training set lives
+    in device memory, each epoch's shuffle is a device permutation, and a
+    step gathers its batch on the device without a host round trip (the loss
+    is read back every 200 steps and over the last 50).  Otherwise every step
+    copies its batch from host memory.  Returns (surrogate, stats)."""
     rng = np.random.default_rng(seed) if rng is None else rng
-    t0 = time.time()
-    chunk = 1 << 20
-    packed = np.empty((n_train, (ct.n_syndrome + 7) // 8), dtype=np.uint8)
-    targets = np.empty((n_train, ct.n_classes), dtype=np.float32)
+    chunk = n_train if chunk <= 0 else min(chunk, n_train)
+    n_train -= n_train % batch
+    chunk -= chunk % batch
+    if n_train <= 0 or chunk <= 0:
+        raise ValueError("n_train and chunk must hold at least one batch")
+    torch = None
+    if device_resident is None or device_resident:
+        try:
+            import torch
+            if not torch.cuda.is_available():
+                torch = None
+        except ImportError:
+            torch = None
+        if device_resident and torch is None:
+            raise RuntimeError("device_resident training needs torch with a CUDA device")
+    nbytes = (ct.n_syndrome + 7) // 8
     sampler = native.Sampler(ct.tanner, ct.lx, ct.lz, ct.em, ct.decoder.device) if gpu_sampler else None
+    sur = Surrogate(ct.n_syndrome, ct.n_classes, hidden, n_layers, seed, ct.decoder.device)
+    total_steps = epochs * (n_train // batch)
+    losses = []
+    t_label = t_train = 0.0
+    s = 0
+    gen = None
+    if torch is not None:
+        dev = torch.device("cuda", ct.decoder.device)
+        gen = torch.Generator(device=dev)
+        gen.manual_seed(int(seed) & 0x7FFFFFFFFFFFFFFF)
     try:
-        for i in range(0, n_train, chunk):
-            m = min(chunk, n_train - i)
-            if sampler is not None:
-                packed[i:i + m], _ = sampler.sample(seed, m, offset=i)
-            else:
-                packed[i:i + m] = pack_syndromes(sample_bits(ct, m, rng))
-            targets[i:i + m] = soft_labels(ct.program.contract_packed(packed[i:i + m], native.TQEC_F32))
+        for c0 in range(0, n_train, chunk):
+            m = min(chunk, n_train - c0)
+            t0 = time.time()
+            packed, targets = _draw_labelled(ct, sampler, rng, seed, c0, m, nbytes)
+            if torch is not None:
+                d_syn = torch.from_numpy(packed).to(dev)
+                d_tgt = torch.from_numpy(targets).to(dev)
+                del packed, targets
+            t1 = time.time()
+            t_label += t1 - t0
+            nb = m // batch
+            for _ in range(epochs):
+                if torch is not None:
+                    perm = torch.randperm(m, generator=gen, device=dev, dtype=torch.int64).to(torch.int32)
+                    stream = torch.cuda.current_stream(dev).cuda_stream
+                else:
+                    perm = rng.permutation(m)
+                for j in range(nb):
+                    cur_lr = lr * 0.5 * (1 + np.cos(np.pi * s / total_steps))
+                    want = s % 200 == 0 or s >= total_steps - 50
+                    if torch is not None:
+                        loss = sur.train_step_rows(d_syn.data_ptr(), d_tgt.data_ptr(), m,
+                                                   perm.data_ptr() + 4 * j * batch, batch, cur_lr,
+                                                   with_loss=want, stream=stream)
+                    else:
+                        idx = perm[j * batch:(j + 1) * batch]
+                        loss = sur.train_step(packed[idx], targets[idx], cur_lr)
+                    if want:
+                        losses.append(loss)
+                        if log and s % 200 == 0:
+                            log(f"step {s}/{total_steps} loss {loss:.5f}")
+                    s += 1
+            if torch is not None:
+                torch.cuda.synchronize(dev)
+            t_train += time.time() - t1
     finally:
         if sampler is not None:
             sampler.close()
-    t_label = time.time() - t0
-    sur = Surrogate(ct.n_syndrome, ct.n_classes, hidden, n_layers, seed, ct.decoder.device)
-    steps = epochs * (n_train // batch)
-    losses = []
-    t1 = time.time()
-    for s in range(steps):
-        if s % (n_train // batch) == 0:
-            perm = rng.permutation(n_train)
-        j = s % (n_train // batch)
-        idx = perm[j * batch:(j + 1) * batch]
-        cur_lr = lr * 0.5 * (1 + np.cos(np.pi * s / steps))
-        losses.append(sur.train_step(packed[idx], targets[idx], cur_lr))
-        if log and s % 200 == 0:
-            log(f"step {s}/{steps} loss {losses[-1]:.5f}")
-    stats = {"label_seconds": t_label, "train_seconds": time.time() - t1, "steps": steps, "batch": batch,
-             "n_train": n_train, "final_loss": float(np.mean(losses[-50:])) if losses else None}
+    stats = {"label_seconds": t_label, "train_seconds": t_train, "steps": s, "batch": batch,
+             "n_train": n_train, "epochs": epochs, "chunk": chunk, "device_resident": torch is not None,
+             "final_loss": float(np.mean(losses[-50:])) if losses else None}
     return sur, stats
 
 

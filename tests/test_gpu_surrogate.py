@@ -125,3 +125,35 @@ def test_tensor_core_gemm_matches_simt(pkg):
         assert np.abs(got - ref).max() <= 3e-2 * scale, np.abs(got - ref).max() / scale
         assert (got.argmax(1) == ref.argmax(1)).mean() > 0.99
         sur.close()
+
+
+def test_device_resident_step_equals_host_step(pkg):
+    """A training step on rows gathered from a device-resident set matches
+    the host step on the same batch; an index outside the set is reported
+    (and reads row 0, never outside the buffers)."""
+    torch = pytest.importorskip("torch")
+    from tensorqec_gb300.surrogate import Surrogate
+
+    rng = np.random.default_rng(12)
+    n_set, n_in, n_out, batch = 5000, 48, 4, 1024
+    packed = pkg.pack_syndromes((rng.random((n_set, n_in)) < 0.2).astype(np.uint8))
+    t = rng.random((n_set, n_out)).astype(np.float32)
+    t /= t.sum(axis=1, keepdims=True)
+    idx = rng.permutation(n_set)[:batch].astype(np.int32)
+    a = Surrogate(n_in, n_out, 256, 4, seed=5)
+    b = Surrogate(n_in, n_out, 256, 4, seed=5)
+    la = a.train_step(packed[idx], t[idx], 1e-3)
+    d_syn, d_t, d_idx = (torch.from_numpy(x).cuda() for x in (packed, t, idx))
+    lb = b.train_step_rows(d_syn.data_ptr(), d_t.data_ptr(), n_set, d_idx.data_ptr(), batch, 1e-3, with_loss=True)
+    # weight gradients are summed with atomics, so only the order of float32
+    # additions differs: the loss to float32 rounding, and after one Adam step
+    # (a step of about lr per parameter) at most a sign flip where a gradient
+    # is near zero
+    assert abs(la - lb) <= 1e-5 * abs(la)
+    diff = np.abs(a.params() - b.params())
+    assert diff.max() <= 2.5e-3 and (diff > 1e-6).mean() < 1e-3
+    bad = torch.tensor([0, n_set], dtype=torch.int32, device="cuda")
+    with pytest.raises(pkg.native.TqecError):
+        b.train_step_rows(d_syn.data_ptr(), d_t.data_ptr(), n_set, bad.data_ptr(), 2, 1e-3, with_loss=True)
+    a.close()
+    b.close()
