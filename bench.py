@@ -40,7 +40,8 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--batch", type=int, default=BATCH)
-    ap.add_argument("--cpu-sample", type=int, default=12000)
+    ap.add_argument("--cpu-sample", type=int, default=65536,
+                    help="syndromes the CPU restatement decodes (timed; also the decision-mismatch sample)")
     ap.add_argument("--profile", action="store_true",
                     help="one float32 contraction launch of --batch syndromes (for ncu), no timing")
     ap.add_argument("--no-autotune", action="store_true")
@@ -68,7 +69,7 @@ def parse():
     ap.add_argument("--split-arena", action="store_true",
                     help="--profile: small intermediates in shared memory, large ones in global memory")
     ap.add_argument("--no-surrogate", action="store_true", help="time the batched exact decoder alone")
-    ap.add_argument("--train-n", type=int, default=1 << 25, help="surrogate training syndromes")
+    ap.add_argument("--train-n", type=int, default=1 << 26, help="surrogate training syndromes")
     ap.add_argument("--train-epochs", type=int, default=16, help="surrogate training epochs")
     ap.add_argument("--calib-n", type=int, default=1 << 20, help="surrogate calibration syndromes")
     ap.add_argument("--eval-n", type=int, default=1 << 20, help="fresh syndromes for the evaluation")
@@ -439,6 +440,7 @@ def run_ours(args):
             "speedup_vs_plain_f64_gpu": value / plain_rate,
             "fallback_fraction_last_step": fallback / B,
             "decision_mismatch_vs_f64_oracle": mismatch,
+            "decision_mismatch_sample": int(len(cpu_cls)),
             "recheck_fraction": rechecks / B,
             "surrogate": sur_stats,
             "evaluation": evaluation,

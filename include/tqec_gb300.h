@@ -303,8 +303,10 @@ int tqec_mlp_infer(tqec_mlp* mlp, const uint8_t* syndromes, int64_t n, int32_t* 
  * (tqec_decode_batch).  Writes the number of such rows. */
 int tqec_gated_decode(tqec_mlp* mlp, tqec_program* prog, float threshold, const uint8_t* syndromes,
                       int64_t n, int32_t* class_out, int64_t* n_fallback_out, void* stream);
-/* Hidden layers on the tcgen05 tensor cores (1, the default, where the shape
- * allows: hidden a multiple of 256) or on the SIMT GEMM (0). */
+/* Hidden layers on the tcgen05 tensor cores (where the shape allows: hidden
+ * a multiple of 256) -- 2, the default: a 2-stage TMA ring, two blocks per SM
+ * (one's epilogue overlaps the other's main loop); 1: a 4-stage ring, one
+ * block per SM; both give identical results -- or on the SIMT GEMM (0). */
 int tqec_mlp_set_gemm(tqec_mlp* mlp, int use_tensor_cores);
 /* Raw output-layer logits (n x n_out float32, host or device memory). */
 int tqec_mlp_forward_logits(tqec_mlp* mlp, const uint8_t* syndromes, int64_t n, float* logits_out);

@@ -51,9 +51,10 @@ cudaError_t gate_rows(const float* logits, int ldl, int64_t n, int n_out, float 
 // tcgen05 GEMM (umma_gemm.cu): out = relu(A * B^T + bias) as bf16.
 bool umma_gemm_supported(int M, int N, int K, int lda, int ldb, int ldo, const void* A, const void* B,
                          const void* out);
+// variant 1: 4-stage ring, one block per SM; 2: 2-stage ring, two blocks per SM.
 cudaError_t umma_gemm_bias_relu(int M, int N, int K, const __nv_bfloat16* A, int lda, const __nv_bfloat16* B,
                                 int ldb, const float* bias, __nv_bfloat16* out, int ldo, int* err,
-                                cudaStream_t st);
+                                cudaStream_t st, int variant = 1);
 
 cudaError_t gather_rows(const uint8_t* src, int row_bytes, const int32_t* list, int64_t n, uint8_t* dst,
                         cudaStream_t st);

@@ -77,7 +77,8 @@ struct tqec_mlp {
   uint8_t* gathered = nullptr;
   int32_t* gcls = nullptr;
   int adam_t = 0;
-  int use_tensor_cores = 1;                   // hidden layers on tcgen05 where the shape allows
+  int use_tensor_cores = 2;                   // hidden layers on tcgen05 where the shape allows (2: two
+                                              // blocks per SM, 1: one), 0: SIMT
   int* d_err = nullptr;                       // timeout flag of the tcgen05 kernel
   int* h_err = nullptr;                       // pinned
   int* d_bad = nullptr;                       // a gathered row index was outside the set
@@ -165,7 +166,7 @@ int forward(tqec_mlp* p, const uint8_t* dsyn, int64_t n, cudaStream_t st) {
       if (p->use_tensor_cores &&
           tqec::umma_gemm_supported((int)n, p->dout[l], p->din[l], ldx, p->din[l], p->cfg.hidden, x, W, p->H[l]))
         SQ_CUDA(tqec::umma_gemm_bias_relu((int)n, p->dout[l], p->din[l], x, ldx, W, p->din[l], b, p->H[l],
-                                          p->cfg.hidden, p->d_err, st));
+                                          p->cfg.hidden, p->d_err, st, p->use_tensor_cores));
       else
         SQ_CUDA(tqec::gemm_bf16(true, true, tqec::EPI_BIAS_RELU_BF16, (int)n, p->dout[l], p->din[l], x, ldx, W,
                                 p->din[l], p->H[l], p->cfg.hidden, b, nullptr, 0, 1, st));
@@ -243,7 +244,8 @@ extern "C" {
 int tqec_mlp_set_gemm(tqec_mlp* p, int use_tensor_cores) {
   if (!p) return sfail(TQEC_ERR_INVALID, "NULL argument");
   std::lock_guard<std::mutex> lk(p->mu);
-  p->use_tensor_cores = use_tensor_cores ? 1 : 0;
+  if (use_tensor_cores < 0 || use_tensor_cores > 2) return sfail(TQEC_ERR_INVALID, "GEMM mode must be 0, 1 or 2");
+  p->use_tensor_cores = use_tensor_cores;
   return TQEC_OK;
 }
 

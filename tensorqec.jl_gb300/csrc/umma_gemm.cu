@@ -23,7 +23,7 @@
 namespace tqec {
 namespace {
 
-constexpr int UM = 128, UN = 256, UK = 64, STAGES = 4;
+constexpr int UM = 128, UN = 256, UK = 64;
 constexpr int A_BYTES = UM * UK * 2;  // 16 KB
 constexpr int B_BYTES = UN * UK * 2;  // 32 KB
 constexpr int STAGE_BYTES = A_BYTES + B_BYTES;
@@ -113,7 +113,11 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
   asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
 
-__global__ void __launch_bounds__(UMMA_THREADS, 1)
+// STAGES-deep TMA ring; MINB blocks per SM (4 stages: one 193 KB block per
+// SM; 2 stages: two 97 KB blocks, one's epilogue overlapping the other's
+// main loop)
+template <int STAGES, int MINB>
+__global__ void __launch_bounds__(UMMA_THREADS, MINB)
     umma_gemm_relu_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensorMap map_b,
                           int M, int N, int K, const float* __restrict__ bias, __nv_bfloat16* __restrict__ out,
                           int ldo, int* __restrict__ err) {
@@ -260,17 +264,29 @@ bool umma_gemm_supported(int M, int N, int K, int lda, int ldb, int ldo, const v
          (reinterpret_cast<uintptr_t>(out) % 16) == 0 && encode_fn() != nullptr;
 }
 
-cudaError_t umma_gemm_bias_relu(int M, int N, int K, const __nv_bfloat16* A, int lda, const __nv_bfloat16* B,
-                                int ldb, const float* bias, __nv_bfloat16* out, int ldo, int* err,
-                                cudaStream_t st) {
-  CUtensorMap ma, mb;
-  if (!make_map(&ma, A, M, K, lda, UM) || !make_map(&mb, B, N, K, ldb, UN)) return cudaErrorInvalidValue;
+namespace {
+
+template <int STAGES, int MINB>
+cudaError_t launch_umma(const CUtensorMap& ma, const CUtensorMap& mb, int M, int N, int K, const float* bias,
+                        __nv_bfloat16* out, int ldo, int* err, cudaStream_t st) {
   const size_t smem = size_t(STAGES) * STAGE_BYTES + 1024 + 256;
-  cudaError_t e = cudaFuncSetAttribute(umma_gemm_relu_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+  auto kernel = umma_gemm_relu_kernel<STAGES, MINB>;
+  cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
   if (e != cudaSuccess) return e;
   dim3 grid(N / UN, (M + UM - 1) / UM);
-  umma_gemm_relu_kernel<<<grid, UMMA_THREADS, smem, st>>>(ma, mb, M, N, K, bias, out, ldo, err);
+  kernel<<<grid, UMMA_THREADS, smem, st>>>(ma, mb, M, N, K, bias, out, ldo, err);
   return cudaGetLastError();
+}
+
+}  // namespace
+
+cudaError_t umma_gemm_bias_relu(int M, int N, int K, const __nv_bfloat16* A, int lda, const __nv_bfloat16* B,
+                                int ldb, const float* bias, __nv_bfloat16* out, int ldo, int* err,
+                                cudaStream_t st, int variant) {
+  CUtensorMap ma, mb;
+  if (!make_map(&ma, A, M, K, lda, UM) || !make_map(&mb, B, N, K, ldb, UN)) return cudaErrorInvalidValue;
+  return variant == 2 ? launch_umma<2, 2>(ma, mb, M, N, K, bias, out, ldo, err, st)
+                      : launch_umma<4, 1>(ma, mb, M, N, K, bias, out, ldo, err, st);
 }
 
 }  // namespace tqec

@@ -124,8 +124,10 @@ class Surrogate:
 
     def use_tensor_cores(self, on=True):
         """Hidden layers on the tcgen05 GEMM (where hidden % 256 == 0) or on
-        the SIMT GEMM."""
-        native.check(_lib().tqec_mlp_set_gemm(self._h, 1 if on else 0))
+        the SIMT GEMM.  True (or 2) is the default tcgen05 variant, two blocks
+        per SM with a 2-stage ring; 1 is one block per SM with a 4-stage ring."""
+        mode = 2 if on is True else (0 if on is False else int(on))
+        native.check(_lib().tqec_mlp_set_gemm(self._h, mode))
 
     def logits(self, packed):
         packed = np.ascontiguousarray(packed, dtype=np.uint8)
