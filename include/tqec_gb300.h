@@ -303,10 +303,12 @@ int tqec_mlp_infer(tqec_mlp* mlp, const uint8_t* syndromes, int64_t n, int32_t* 
  * (tqec_decode_batch).  Writes the number of such rows. */
 int tqec_gated_decode(tqec_mlp* mlp, tqec_program* prog, float threshold, const uint8_t* syndromes,
                       int64_t n, int32_t* class_out, int64_t* n_fallback_out, void* stream);
-/* Hidden layers on the tcgen05 tensor cores (where the shape allows: hidden
- * a multiple of 256) -- 2, the default: a 2-stage TMA ring, two blocks per SM
- * (one's epilogue overlaps the other's main loop); 1: a 4-stage ring, one
- * block per SM; both give identical results -- or on the SIMT GEMM (0). */
+/* How the layers run.  0: SIMT GEMMs.  1, 2: tcgen05 GEMMs layer by layer
+ * (hidden a multiple of 256), a 4-stage TMA ring with one block per SM or a
+ * 2-stage ring with two blocks per SM.  3, the default: inference (infer,
+ * gated decode, logits) by one persistent tcgen05 kernel for the whole
+ * forward, activations kept in shared and tensor memory (4 layers, hidden
+ * 512, at most 64 inputs and 16 outputs; otherwise as 2), training as 2. */
 int tqec_mlp_set_gemm(tqec_mlp* mlp, int use_tensor_cores);
 /* Raw output-layer logits (n x n_out float32, host or device memory). */
 int tqec_mlp_forward_logits(tqec_mlp* mlp, const uint8_t* syndromes, int64_t n, float* logits_out);

@@ -58,6 +58,16 @@ cudaError_t umma_gemm_bias_relu(int M, int N, int K, const __nv_bfloat16* A, int
 
 cudaError_t gather_rows(const uint8_t* src, int row_bytes, const int32_t* list, int64_t n, uint8_t* dst,
                         cudaStream_t st);
+
+// The whole forward of a 4-layer surrogate with hidden width 512 (inputs
+// padded to 64, at most 16 outputs) in one persistent tcgen05 kernel
+// (umma_gemm.cu): logits[n][ldl] from packed syndromes.  W[l] are the bf16
+// weight matrices [dout][din] and bias[l] the float32 biases.
+bool mlp_fused_supported(int n_in, int in_pad, int hidden, int n_layers, int n_out, const __nv_bfloat16* const W[4],
+                         const float* const bias[4]);
+cudaError_t mlp_fused_logits(const uint8_t* syn, int64_t n, int sb, int n_in, const __nv_bfloat16* const W[4],
+                             const float* const bias[4], int n_out, float* logits, int ldl, int* err,
+                             cudaStream_t st);
 cudaError_t scatter_classes(const int32_t* src, const int32_t* list, int64_t n, int32_t* dst, cudaStream_t st);
 
 }  // namespace tqec

@@ -77,8 +77,10 @@ struct tqec_mlp {
   uint8_t* gathered = nullptr;
   int32_t* gcls = nullptr;
   int adam_t = 0;
-  int use_tensor_cores = 2;                   // hidden layers on tcgen05 where the shape allows (2: two
-                                              // blocks per SM, 1: one), 0: SIMT
+  // hidden layers: 0 SIMT GEMM; tcgen05 GEMM layer by layer with 1 or 2
+  // blocks per SM; 3 (default) inference by the fused forward kernel where
+  // the shape allows (training keeps mode 2's GEMMs)
+  int use_tensor_cores = 3;
   int* d_err = nullptr;                       // timeout flag of the tcgen05 kernel
   int* h_err = nullptr;                       // pinned
   int* d_bad = nullptr;                       // a gathered row index was outside the set
@@ -166,7 +168,7 @@ int forward(tqec_mlp* p, const uint8_t* dsyn, int64_t n, cudaStream_t st) {
       if (p->use_tensor_cores &&
           tqec::umma_gemm_supported((int)n, p->dout[l], p->din[l], ldx, p->din[l], p->cfg.hidden, x, W, p->H[l]))
         SQ_CUDA(tqec::umma_gemm_bias_relu((int)n, p->dout[l], p->din[l], x, ldx, W, p->din[l], b, p->H[l],
-                                          p->cfg.hidden, p->d_err, st, p->use_tensor_cores));
+                                          p->cfg.hidden, p->d_err, st, p->use_tensor_cores == 1 ? 1 : 2));
       else
         SQ_CUDA(tqec::gemm_bf16(true, true, tqec::EPI_BIAS_RELU_BF16, (int)n, p->dout[l], p->din[l], x, ldx, W,
                                 p->din[l], p->H[l], p->cfg.hidden, b, nullptr, 0, 1, st));
@@ -182,6 +184,25 @@ int forward(tqec_mlp* p, const uint8_t* dsyn, int64_t n, cudaStream_t st) {
     }
   }
   return TQEC_OK;
+}
+
+// Inference forward: the fused kernel (all layers in one persistent launch,
+// activations kept on chip) in mode 3 where the shape allows, else forward().
+int forward_infer(tqec_mlp* p, const uint8_t* dsyn, int64_t n, cudaStream_t st) {
+  if (p->use_tensor_cores == 3) {
+    const __nv_bfloat16* W[4];
+    const float* B[4];
+    for (int l = 0; l < p->L && l < 4; ++l) {
+      W[l] = p->w16 + p->w_off[l];
+      B[l] = p->w32 + p->b_off[l];
+    }
+    if (tqec::mlp_fused_supported(p->cfg.n_in, p->in_pad, p->cfg.hidden, p->L, p->cfg.n_out, W, B)) {
+      SQ_CUDA(tqec::mlp_fused_logits(dsyn, n, (p->cfg.n_in + 7) / 8, p->cfg.n_in, W, B, p->cfg.n_out, p->logits,
+                                     p->out_pad, p->d_err, st));
+      return TQEC_OK;
+    }
+  }
+  return forward(p, dsyn, n, st);
 }
 
 // gradients into p->g for rows [0, n) with float targets already in p->tgt
@@ -244,7 +265,7 @@ extern "C" {
 int tqec_mlp_set_gemm(tqec_mlp* p, int use_tensor_cores) {
   if (!p) return sfail(TQEC_ERR_INVALID, "NULL argument");
   std::lock_guard<std::mutex> lk(p->mu);
-  if (use_tensor_cores < 0 || use_tensor_cores > 2) return sfail(TQEC_ERR_INVALID, "GEMM mode must be 0, 1 or 2");
+  if (use_tensor_cores < 0 || use_tensor_cores > 3) return sfail(TQEC_ERR_INVALID, "GEMM mode must be 0 to 3");
   p->use_tensor_cores = use_tensor_cores;
   return TQEC_OK;
 }
@@ -258,7 +279,7 @@ int tqec_mlp_forward_logits(tqec_mlp* p, const uint8_t* syn, int64_t n, float* l
   if (rc) return rc;
   const uint8_t* ds;
   if ((rc = stage_syn(p, syn, n, st, &ds))) return rc;
-  if ((rc = forward(p, ds, n, st))) return rc;
+  if ((rc = forward_infer(p, ds, n, st))) return rc;
   SQ_CUDA(cudaMemcpy2DAsync(logits_out, sizeof(float) * p->cfg.n_out, p->logits, sizeof(float) * p->out_pad,
                             sizeof(float) * p->cfg.n_out, size_t(n), cudaMemcpyDeviceToHost, st));
   return check_device_error(p, st);
@@ -496,7 +517,7 @@ int tqec_mlp_infer(tqec_mlp* p, const uint8_t* syn, int64_t n, int32_t* class_ou
     const int64_t m = std::min(chunk, n - r0);
     const uint8_t* ds;
     if ((rc = stage_syn(p, syn + r0 * sb, m, st, &ds))) return rc;
-    if ((rc = forward(p, ds, m, st))) return rc;
+    if ((rc = forward_infer(p, ds, m, st))) return rc;
     int32_t* c = host_cls ? p->cls : (class_out ? class_out + r0 : nullptr);
     float* f = host_conf ? p->conf : (conf_out ? conf_out + r0 : nullptr);
     SQ_CUDA(tqec::gate_rows(p->logits, p->out_pad, m, p->cfg.n_out, 0.f, c, f, nullptr, nullptr, st));
@@ -528,7 +549,7 @@ int tqec_gated_decode(tqec_mlp* p, tqec_program* prog, float threshold, const ui
     const int64_t m = std::min(chunk, n - r0);
     const uint8_t* ds;
     if ((rc = stage_syn(p, syn + r0 * sb, m, st, &ds))) return rc;
-    if ((rc = forward(p, ds, m, st))) return rc;
+    if ((rc = forward_infer(p, ds, m, st))) return rc;
     SQ_CUDA(cudaMemsetAsync(p->count, 0, sizeof(int32_t), st));
     SQ_CUDA(tqec::gate_rows(p->logits, p->out_pad, m, p->cfg.n_out, threshold, p->cls, p->conf, p->list, p->count,
                             st));

@@ -15,6 +15,7 @@
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstdint>
 #include <mutex>
 
@@ -255,6 +256,269 @@ bool make_map(CUtensorMap* map, const __nv_bfloat16* base, int rows, int cols, i
             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
+// ---- the whole surrogate forward in one persistent kernel ----------------
+//
+// Hidden width 512, three ReLU layers and a small output layer.  A CTA owns
+// 128-row tiles in turn.  The layer input lives in shared memory as eight
+// 128x64 bf16 k-tiles (128 KB, the 128-byte-swizzled K-major layout the MMA
+// reads); the 512-wide float32 accumulator fills all of tensor memory (two
+// 256-column halves).  Warp 0 streams 256x64 weight tiles through a 3-stage
+// ring with TMA; warp 1 issues the MMAs of a layer once its input is ready
+// and commits the accumulator; warps 4-7 (one TMEM lane quadrant each, one
+// row per thread) write the layer-1 input from the packed syndrome bits,
+// turn each accumulator into the next layer's bf16 input (bias, ReLU), and
+// for the last hidden layer compute the output logits directly from tensor
+// memory.  No activation leaves the SM.  Every wait is bounded.
+constexpr int FM = 128, FH = 512, FNH = 256, FSTAGES = 3;
+constexpr int FA_TILE = FM * UK * 2;           // 16 KB: 128 rows x 64 bf16
+constexpr int FA_BYTES = (FH / UK) * FA_TILE;  // 128 KB: a layer input
+constexpr int FB_STAGE = FNH * UK * 2;         // 32 KB: 256 weight rows x 64 bf16
+constexpr uint32_t FTMEM_COLS = 512;
+constexpr int FTHREADS = 256;
+constexpr int FMAX_OUT = 16;
+constexpr size_t FUSED_SMEM = size_t(FA_BYTES) + size_t(FSTAGES) * FB_STAGE + 256 + 1024;
+
+struct FusedArgs {
+  const uint8_t* syn;
+  int sb, n_in;
+  int64_t n;
+  const float* bias[3];
+  const __nv_bfloat16* w4;  // [n_out][512]
+  const float* b4;
+  int n_out, ldl;
+  float* logits;
+  int* err;
+};
+
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
+}
+
+__device__ __forceinline__ void fence_proxy_async_smem() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+__device__ __forceinline__ uint32_t pack_bf16x2(float a, float b) {
+  __nv_bfloat162 v = __floats2bfloat162_rn(a, b);
+  return *reinterpret_cast<uint32_t*>(&v);
+}
+
+__global__ void __launch_bounds__(FTHREADS, 1)
+    mlp_fused_kernel(const __grid_constant__ CUtensorMap w1, const __grid_constant__ CUtensorMap w2,
+                     const __grid_constant__ CUtensorMap w3, const __grid_constant__ FusedArgs a) {
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  unsigned char* smem = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
+                                                         ~uintptr_t(1023));
+  unsigned char* sA = smem;
+  unsigned char* sB = smem + FA_BYTES;
+  uint64_t* full = reinterpret_cast<uint64_t*>(sB + FSTAGES * FB_STAGE);
+  uint64_t* empty = full + FSTAGES;
+  uint64_t* acc_ready = empty + FSTAGES;
+  uint64_t* a_ready = acc_ready + 1;
+  uint64_t* mma_done = a_ready + 1;
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(mma_done + 1);
+  volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t ntiles = (a.n + FM - 1) / FM;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < FSTAGES; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], 1);
+    }
+    mbar_init(acc_ready, 1);
+    mbar_init(a_ready, 128);  // every epilogue thread
+    mbar_init(mma_done, 1);
+    *abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(tmem_slot)),
+                 "r"(FTMEM_COLS));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = *tmem_slot;
+
+  if (warp == 0 && lane == 0) {
+    // TMA producer: per tile, per layer, per 256-row half of the weights,
+    // per 64-wide k slice
+    uint32_t q = 0;
+    bool ok = true;
+    for (int64_t t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
+      for (int L = 0; L < 3 && ok; ++L) {
+        const CUtensorMap* map = L == 0 ? &w1 : (L == 1 ? &w2 : &w3);
+        const int kbs = L == 0 ? 1 : FH / UK;
+        for (int h = 0; h < 2 && ok; ++h) {
+          for (int kb = 0; kb < kbs; ++kb) {
+            const int s = int(q % FSTAGES);
+            if (q >= uint32_t(FSTAGES) && !mbar_wait(&empty[s], uint32_t((q / FSTAGES - 1) & 1), a.err)) {
+              *abort_flag = 1;
+              ok = false;
+              break;
+            }
+            if (*abort_flag) {
+              ok = false;
+              break;
+            }
+            mbar_arrive_expect_tx(&full[s], FB_STAGE);
+            tma_load_2d(map, &full[s], sB + s * FB_STAGE, kb * UK, h * FNH);
+            ++q;
+          }
+        }
+      }
+    }
+    // the copies still in flight land before the block exits (bounded)
+    for (uint32_t k = q > uint32_t(FSTAGES) ? q - FSTAGES : 0; k < q; ++k)
+      mbar_wait(&full[k % FSTAGES], uint32_t((k / FSTAGES) & 1), a.err);
+  } else if (warp == 1 && lane == 0) {
+    // MMA issuer
+    uint32_t q = 0, c = 0;
+    bool ok = true;
+    for (int64_t t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
+      for (int L = 0; L < 3 && ok; ++L) {
+        if (!mbar_wait(a_ready, c & 1u, a.err) || *abort_flag) {
+          *abort_flag = 1;
+          ok = false;
+          break;
+        }
+        ++c;
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        const int kbs = L == 0 ? 1 : FH / UK;
+        for (int h = 0; h < 2 && ok; ++h) {
+          for (int kb = 0; kb < kbs; ++kb) {
+            const int s = int(q % FSTAGES);
+            if (!mbar_wait(&full[s], uint32_t((q / FSTAGES) & 1), a.err)) {
+              *abort_flag = 1;
+              ok = false;
+              break;
+            }
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            const uint64_t da = sdesc(smem_addr(sA + kb * FA_TILE)), db = sdesc(smem_addr(sB + s * FB_STAGE));
+#pragma unroll
+            for (int kk = 0; kk < UK / 16; ++kk)
+              umma(tmem + uint32_t(h * FNH), da + uint64_t(kk * 2), db + uint64_t(kk * 2), (kb | kk) != 0 ? 1u : 0u);
+            umma_commit(&empty[s]);
+            ++q;
+          }
+        }
+        if (ok) umma_commit(acc_ready);
+      }
+    }
+    // every MMA issued has completed before the tensor memory is freed
+    umma_commit(mma_done);
+    mbar_wait(mma_done, 0u, a.err);
+  } else if (warp >= 4) {
+    // epilogue: TMEM lane quadrant qd, row r of the tile per thread
+    const int qd = warp & 3;
+    const int r = qd * 32 + lane;
+    uint32_t c = 0;
+    bool ok = true;
+    for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+      const int64_t row = t * FM + r;
+      {
+        // layer-1 input: the syndrome bits as bf16 0/1 in k-tile 0
+        uint32_t bytes[8];
+#pragma unroll
+        for (int b = 0; b < 8; ++b) bytes[b] = (row < a.n && b < a.sb) ? uint32_t(a.syn[row * a.sb + b]) : 0u;
+#pragma unroll
+        for (int ch = 0; ch < 8; ++ch) {
+          uint32_t w[4];
+#pragma unroll
+          for (int j = 0; j < 4; ++j) {
+            const int c0 = ch * 8 + 2 * j;
+            const float v0 = c0 < a.n_in ? float((bytes[c0 >> 3] >> (c0 & 7)) & 1u) : 0.f;
+            const float v1 = c0 + 1 < a.n_in ? float((bytes[(c0 + 1) >> 3] >> ((c0 + 1) & 7)) & 1u) : 0.f;
+            w[j] = pack_bf16x2(v0, v1);
+          }
+          *reinterpret_cast<uint4*>(sA + r * 128 + ((ch ^ (r & 7)) << 4)) = make_uint4(w[0], w[1], w[2], w[3]);
+        }
+      }
+      fence_proxy_async_smem();
+      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+      mbar_arrive(a_ready);
+      for (int L = 0; L < 3; ++L) {
+        if (ok && !mbar_wait(acc_ready, c & 1u, a.err)) {
+          *abort_flag = 1;
+          ok = false;
+        }
+        ++c;
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        // tcgen05.ld is warp-collective: decide for the whole warp
+        const bool go = __all_sync(0xffffffffu, ok && *abort_flag == 0);
+        float lg[FMAX_OUT];
+#pragma unroll
+        for (int o = 0; o < FMAX_OUT; ++o) lg[o] = 0.f;
+        if (go) {
+          const float* bias = a.bias[L];
+#pragma unroll 1
+          for (int cc = 0; cc < FH / 32; ++cc) {
+            uint32_t v[32];
+            tmem_ld32(tmem + (uint32_t(qd * 32) << 16) + uint32_t(cc * 32), v);
+            float x[32];
+#pragma unroll
+            for (int j = 0; j < 32; j += 4) {
+              const float4 b = *reinterpret_cast<const float4*>(bias + cc * 32 + j);
+              x[j] = fmaxf(__uint_as_float(v[j]) + b.x, 0.f);
+              x[j + 1] = fmaxf(__uint_as_float(v[j + 1]) + b.y, 0.f);
+              x[j + 2] = fmaxf(__uint_as_float(v[j + 2]) + b.z, 0.f);
+              x[j + 3] = fmaxf(__uint_as_float(v[j + 3]) + b.w, 0.f);
+            }
+            if (L < 2) {
+              // the next layer's input: bf16, k-tile cc/2, 16-byte chunks
+              // (cc%2)*4 .. +3 of row r
+              unsigned char* tile = sA + (cc >> 1) * FA_TILE + r * 128;
+#pragma unroll
+              for (int u = 0; u < 4; ++u) {
+                const int chunk = (cc & 1) * 4 + u;
+                *reinterpret_cast<uint4*>(tile + ((chunk ^ (r & 7)) << 4)) =
+                    make_uint4(pack_bf16x2(x[8 * u], x[8 * u + 1]), pack_bf16x2(x[8 * u + 2], x[8 * u + 3]),
+                               pack_bf16x2(x[8 * u + 4], x[8 * u + 5]), pack_bf16x2(x[8 * u + 6], x[8 * u + 7]));
+              }
+            } else {
+              // output layer on the bf16-rounded activations
+#pragma unroll
+              for (int j = 0; j < 32; ++j) x[j] = __bfloat162float(__float2bfloat16(x[j]));
+              for (int o = 0; o < a.n_out; ++o) {
+                const __nv_bfloat16* wrow = a.w4 + o * FH + cc * 32;
+                float s = 0.f;
+#pragma unroll
+                for (int j = 0; j < 32; j += 8) {
+                  const uint4 wv = *reinterpret_cast<const uint4*>(wrow + j);
+                  const __nv_bfloat162* w2 = reinterpret_cast<const __nv_bfloat162*>(&wv);
+#pragma unroll
+                  for (int u = 0; u < 4; ++u) {
+                    const float2 wf = __bfloat1622float2(w2[u]);
+                    s = fmaf(x[j + 2 * u], wf.x, s);
+                    s = fmaf(x[j + 2 * u + 1], wf.y, s);
+                  }
+                }
+                lg[o] += s;
+              }
+            }
+          }
+        }
+        if (L < 2) {
+          fence_proxy_async_smem();
+          asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+          mbar_arrive(a_ready);
+        } else if (go && row < a.n) {
+          for (int o = 0; o < a.n_out; ++o) a.logits[row * a.ldl + o] = lg[o] + a.b4[o];
+        }
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 0) {
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(FTMEM_COLS));
+  }
+}
+
 }  // namespace
 
 bool umma_gemm_supported(int M, int N, int K, int lda, int ldb, int ldo, const void* A, const void* B,
@@ -287,6 +551,49 @@ cudaError_t umma_gemm_bias_relu(int M, int N, int K, const __nv_bfloat16* A, int
   if (!make_map(&ma, A, M, K, lda, UM) || !make_map(&mb, B, N, K, ldb, UN)) return cudaErrorInvalidValue;
   return variant == 2 ? launch_umma<2, 2>(ma, mb, M, N, K, bias, out, ldo, err, st)
                       : launch_umma<4, 1>(ma, mb, M, N, K, bias, out, ldo, err, st);
+}
+
+bool mlp_fused_supported(int n_in, int in_pad, int hidden, int n_layers, int n_out, const __nv_bfloat16* const W[4],
+                         const float* const bias[4]) {
+  if (n_layers != 4 || hidden != FH || in_pad != UK || n_in <= 0 || n_in > UK || n_out <= 0 || n_out > FMAX_OUT ||
+      encode_fn() == nullptr)
+    return false;
+  for (int l = 0; l < 4; ++l)
+    if ((reinterpret_cast<uintptr_t>(W[l]) % 16) != 0 || (reinterpret_cast<uintptr_t>(bias[l]) % 16) != 0)
+      return false;
+  return true;
+}
+
+cudaError_t mlp_fused_logits(const uint8_t* syn, int64_t n, int sb, int n_in, const __nv_bfloat16* const W[4],
+                             const float* const bias[4], int n_out, float* logits, int ldl, int* err,
+                             cudaStream_t st) {
+  if (n <= 0) return cudaSuccess;
+  if (sb > 8) return cudaErrorInvalidValue;
+  CUtensorMap m1, m2, m3;
+  if (!make_map(&m1, W[0], FH, UK, UK, FNH) || !make_map(&m2, W[1], FH, FH, FH, FNH) ||
+      !make_map(&m3, W[2], FH, FH, FH, FNH))
+    return cudaErrorInvalidValue;
+  FusedArgs a;
+  a.syn = syn;
+  a.sb = sb;
+  a.n_in = n_in;
+  a.n = n;
+  for (int l = 0; l < 3; ++l) a.bias[l] = bias[l];
+  a.w4 = W[3];
+  a.b4 = bias[3];
+  a.n_out = n_out;
+  a.ldl = ldl;
+  a.logits = logits;
+  a.err = err;
+  int dev = 0, sms = 1;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaError_t e = cudaFuncSetAttribute(mlp_fused_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(FUSED_SMEM));
+  if (e != cudaSuccess) return e;
+  const int64_t ntiles = (n + FM - 1) / FM;
+  const int grid = int(std::min<int64_t>(ntiles, sms));
+  mlp_fused_kernel<<<grid, FTHREADS, FUSED_SMEM, st>>>(m1, m2, m3, a);
+  return cudaGetLastError();
 }
 
 }  // namespace tqec

@@ -123,10 +123,11 @@ class Surrogate:
         return cls, conf
 
     def use_tensor_cores(self, on=True):
-        """Hidden layers on the tcgen05 GEMM (where hidden % 256 == 0) or on
-        the SIMT GEMM.  True (or 2) is the default tcgen05 variant, two blocks
-        per SM with a 2-stage ring; 1 is one block per SM with a 4-stage ring."""
-        mode = 2 if on is True else (0 if on is False else int(on))
+        """How the layers run: False (0) SIMT GEMMs; 1 or 2 tcgen05 GEMMs layer
+        by layer (one block per SM with a 4-stage ring, or two with a 2-stage
+        ring); True (3, the default) inference by the fused tcgen05 forward
+        kernel where the shape allows, training as 2."""
+        mode = 3 if on is True else (0 if on is False else int(on))
         native.check(_lib().tqec_mlp_set_gemm(self._h, mode))
 
     def logits(self, packed):

@@ -157,3 +157,29 @@ def test_device_resident_step_equals_host_step(pkg):
         b.train_step_rows(d_syn.data_ptr(), d_t.data_ptr(), n_set, bad.data_ptr(), 2, 1e-3, with_loss=True)
     a.close()
     b.close()
+
+
+@pytest.mark.parametrize("rows", [1000, 65536 + 77])
+def test_fused_forward_matches_layer_by_layer(pkg, rows):
+    """The fused tcgen05 forward (all layers in one persistent kernel, the
+    default for inference) against the layer-by-layer tcgen05 GEMMs: the
+    hidden activations are the same bf16 values, so the logits differ only by
+    the float32 summation order of the output layer (1e-4 relative), and the
+    classes agree wherever the top two logits are not that close."""
+    from tensorqec_gb300.surrogate import Surrogate
+
+    rng = np.random.default_rng(rows)
+    sur = Surrogate(48, 4, 512, 4, seed=9)
+    packed = pkg.pack_syndromes((rng.random((rows, 48)) < 0.15).astype(np.uint8))
+    sur.use_tensor_cores(True)
+    lf = sur.logits(packed)
+    cf, pf = sur.infer(packed)
+    sur.use_tensor_cores(2)
+    ll = sur.logits(packed)
+    cl, pl = sur.infer(packed)
+    assert np.max(np.abs(lf - ll) / (1.0 + np.abs(ll))) <= 1e-4
+    srt = np.sort(ll, axis=1)
+    close = (srt[:, -1] - srt[:, -2]) <= 1e-3
+    assert not ((cf != cl) & ~close).any()
+    assert np.max(np.abs(pf - pl)) <= 1e-4
+    sur.close()
