@@ -49,6 +49,9 @@ def parse():
                     help="W warm-up decodes then one decode of ROWS d=7 syndromes, every one sent to the "
                          "recheck (margin above any float32 result), for ncu; --recheck-f64: float64 recheck")
     ap.add_argument("--recheck-f64", action="store_true")
+    ap.add_argument("--profile-forward", type=int, default=0, metavar="ROWS",
+                    help="W warm-up then one surrogate inference (4x512 MLP, 48 inputs, random weights) of ROWS "
+                         "rows, for ncu")
     ap.add_argument("--precision-sweep", action="store_true",
                     help="float32 vs float64 log-probability error and decision mismatch over d in {5,7} and "
                          "p in {0.02,0.05,0.08,0.11}, one JSON line per (d,p)")
@@ -498,6 +501,35 @@ def run_profile_recheck(args):
     ct.close()
 
 
+def run_profile_forward(args):
+    """The surrogate's inference launch on its own: a 4x512 MLP (48 inputs,
+    4 classes, seeded random weights) on ROWS seeded syndromes."""
+    import ctypes as C
+
+    import torch
+
+    import __graft_entry__ as G
+
+    pkg = G.load_package()
+    from tensorqec_gb300 import surrogate as S
+
+    rows = args.profile_forward
+    sur = S.Surrogate(48, 4, 512, 4, seed=3)
+    rng = np.random.default_rng(SEED)
+    packed = pkg.pack_syndromes((rng.random((rows, 48)) < 0.1).astype(np.uint8))
+    d_syn = torch.from_numpy(packed).cuda()
+    d_cls = torch.empty(rows, dtype=torch.int32, device="cuda")
+    d_conf = torch.empty(rows, dtype=torch.float32, device="cuda")
+    sptr = torch.cuda.current_stream().cuda_stream
+    L = S._lib()
+    for _ in range(args.warmup + 1):
+        pkg.native.check(L.tqec_mlp_infer(sur.handle, C.c_void_p(d_syn.data_ptr()), rows, C.c_void_p(d_cls.data_ptr()),
+                                          C.c_void_p(d_conf.data_ptr()), C.c_void_p(sptr)))
+    torch.cuda.synchronize()
+    print(json.dumps({"profile_case": "surrogate forward", "rows": rows}), flush=True)
+    sur.close()
+
+
 def run_precision_sweep(args):
     """Per (d, p): --batch seeded syndromes contracted in one float32 launch
     (power-of-two renormalised) and in float64; reports the class
@@ -782,6 +814,8 @@ def main():
         run_precision_sweep(args)
     elif args.profile_recheck:
         run_profile_recheck(args)
+    elif args.profile_forward:
+        run_profile_forward(args)
     elif args.profile:
         run_profile(args)
     elif args.impl == "reference":
