@@ -20,6 +20,7 @@ import json
 import os
 import statistics
 import subprocess
+import tempfile
 import sys
 import time
 
@@ -111,7 +112,9 @@ class ClockSampler:
     def __init__(self, gpu_index):
         self.gpu = gpu_index
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_rank{gpu_index}.csv")
+        # the raw samples: TQEC_CLOCKS_CSV if set, else a temporary file
+        self.path = os.environ.get("TQEC_CLOCKS_CSV") or os.path.join(tempfile.gettempdir(),
+                                                                      f"tqec_clocks_rank{gpu_index}_{os.getpid()}.csv")
 
     def start(self):
         try:

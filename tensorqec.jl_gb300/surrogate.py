@@ -4,8 +4,8 @@ A ReLU MLP (float32 master weights, bf16 GEMM operands, float32
 accumulation; trained by the native library's own kernels) maps syndrome
 bits to the logical class.  Its labels are the exact contraction's class
 probabilities.  At decode time the rows whose softmax confidence is below a
-calibrated threshold go to the exact contraction, which is therefore also
-the judge of the surrogate's decisions.
+calibrated threshold go to the exact contraction, which also serves as the
+reference the surrogate's decisions are measured against.
 """
 from __future__ import annotations
 
