@@ -3,9 +3,11 @@
 code-capacity depolarising noise p=0.05 (X, Y, Z each p/3), batches of
 65,536 seeded syndromes.
 
-One step = decoding one batch: the float32 contraction of every syndrome
-plus the float64 recheck of low-margin syndromes (and, when a surrogate
-checkpoint is given, the gated surrogate in front of them).  ``value`` times
+One step = decoding one batch with the gated decoder: the learned surrogate
+(trained and calibrated first, outside the timed region) answers the rows it
+is confident about, the float32 contraction decodes the rest, and the
+double-float recheck re-contracts the rows whose class margin is inside the
+float32 rounding bound (``--no-surrogate``: every row exact).  ``value`` times
 the decode with syndromes already in HBM; ``e2e`` times the same call through
 the C ABI with pinned host buffers, copies included.  ``--impl reference``
 times the CPU restatement of the reference's per-syndrome float64
@@ -63,7 +65,7 @@ def parse():
     ap.add_argument("--mixed-batch", type=int, default=1000)
     ap.add_argument("--circuit", action="store_true",
                     help="circuit-level rotated Z-memory d=5, 5 rounds, p=0.001: DEM from the generator, "
-                         "--circuit-n seeded detector samples, float32 + float64 recheck")
+                         "--circuit-n seeded detector samples, float32 + recheck")
     ap.add_argument("--circuit-n", type=int, default=262144,
                     help="--circuit: detector samples (with --profile: samples in the one profiled launch)")
     ap.add_argument("--no-tensor-cores", action="store_true",
@@ -128,8 +130,12 @@ class ClockSampler:
             os.makedirs(os.path.dirname(self.path), exist_ok=True)
             self.f = open(self.path, "w")
             self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
                                          stdout=self.f, stderr=subprocess.DEVNULL)
+            # the timed regions are short: start them only once sampling runs
+            t0 = time.time()
+            while time.time() - t0 < 10.0 and os.path.getsize(self.path) == 0 and self.proc.poll() is None:
+                time.sleep(0.02)
         except Exception:
             self.proc = None
 
@@ -352,11 +358,10 @@ def run_ours(args):
     torch.cuda.nvtx.range_pop()
     if dist:
         dist.barrier()
-    clk = clocks.stop()
     step_ms = sum(ms) / K
     fallback = gd.last_fallback if gd is not None else B
 
-    # ---- the batched exact decoder alone (float32 + float64 recheck) -------
+    # ---- the batched exact decoder alone (float32 + double-float recheck) -------
     tn_ms = timed(lambda i: ct.program.decode_ptrs(d_syn[W + i].data_ptr(), B, d_cls.data_ptr(), None, None, sptr),
                   range(min(K, 5)))
     tn_rate = B / (statistics.median(tn_ms) / 1e3)
@@ -397,6 +402,9 @@ def run_ours(args):
     torch.cuda.synchronize()
     e2e_ms = timed(lambda i: decode(h_syn[W + i].data_ptr(), h_cls.data_ptr()), range(K))
     e2e_step = sum(e2e_ms) / K
+    # clocks sampled from before the first timed step to after the last one
+    # (device-resident, exact-alone, kernel-alone, surrogate-alone and e2e)
+    clk = clocks.stop()
 
     # ---- plain float64 form: one launch per syndrome (drop-in baseline) ----
     plain = pkg.compile(pkg.TNMMAP(precision="f64", plain=True, device=local, optimizer=d7_order(pkg)), t, em)
@@ -445,8 +453,9 @@ def run_ours(args):
                          # flops per cycle at the sampled SM clock (nominal, not measured)
                          "fp32_simt_peak_tflops": fp32_peak,
                          "frac_of_fp32_simt_peak": achieved_tflops / fp32_peak,
-                         "traffic_note": "dram read+write of the autotuned split-arena shape, per 65,536 "
-                                         "syndromes (ncu, scaled from 16,384)"},
+                         "traffic_note": "dram read+write of the split-arena shape (1 syndrome per 128-thread "
+                                         "block) per 65,536 syndromes (ncu, scaled from 16,384): big-pool "
+                                         "intermediates, not algorithmic bytes (42 B per syndrome)"},
             "surrogate_gemm": mlp_part,
             "cpu_baseline": cpu,
             "clocks": clk,
@@ -545,7 +554,7 @@ def run_precision_sweep(args):
     """Per (d, p): --batch seeded syndromes contracted in one float32 launch
     (power-of-two renormalised) and in float64; reports the class
     log-probability error of float32 against float64, its bound, the decision
-    mismatch before and after the float64 recheck, and float32 syndromes/s."""
+    mismatch before and after the recheck, and float32 syndromes/s."""
     import torch
 
     import __graft_entry__ as G
@@ -589,7 +598,7 @@ def run_precision_sweep(args):
             c64 = np.argmax(l64, axis=1)
             srt = np.sort(l64, axis=1)
             tie = (srt[:, -1] - srt[:, -2]) <= 1e-9
-            gated = ct.program.decode_packed(packed)  # float32 + float64 recheck
+            gated = ct.program.decode_packed(packed)  # float32 + recheck
             line = {"sweep": "precision", "d": d, "p": p, "syndromes": B, "flops_per_syndrome": info["flops_per_syndrome"],
                     "f32_ms": ms["f32"], "f32_syn_per_s": B / (ms["f32"] / 1e3), "f64_ms": ms["f64"],
                     "f64_syn_per_s": B / (ms["f64"] / 1e3),
@@ -688,7 +697,7 @@ def run_mixed(args):
         torch.cuda.synchronize()
         lat = [a.elapsed_time(b) for a, b in ev]
     total_ms = sum(lat)
-    # the same decisions as each program's own decoder (float32 + float64 recheck), outside exact ties
+    # the same decisions as each program's own decoder (float32 + recheck), outside exact ties
     mism = 0
     for prog, h, c in zip(progs, syn_host, d_cls):
         got = c.cpu().numpy()
@@ -757,7 +766,7 @@ def run_circuit_profile(args):
 def run_circuit(args):
     """Circuit-level noise: the Z-memory circuit's detector error model
     decoded by the batched contraction of its factor graph (float32 with a
-    float64 recheck of low-margin samples)."""
+    recheck of low-margin samples)."""
     import torch
 
     t0 = time.time()
@@ -797,7 +806,7 @@ def run_circuit(args):
     z = 1.96
     se = np.sqrt(ler * (1 - ler) / n)
     line = {"config": "circuit", "metric": "detector samples/s, circuit-level rotated Z-memory d=5, 5 rounds, "
-                                           "p=0.001, float32 + float64 recheck",
+                                           "p=0.001, float32 + double-float recheck",
             "samples": n, "ms": ms, "samples_per_s": n / (ms / 1e3),
             "mechanisms": len(dem.error_rates), "detectors": len(dem.detector_list), "observables": k,
             "width": info["width"], "flops_per_sample": info["flops_per_syndrome"],

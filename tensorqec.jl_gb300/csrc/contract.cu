@@ -1049,7 +1049,7 @@ __global__ void __launch_bounds__(sizeof(T) == 8 || TENSOR ? 512 : 1024) tn_cont
 // row) of the current batch are claimed from a device counter; each unit's
 // program descriptor and steps are copied into shared memory, then one group
 // of its rows is contracted.  With `list_mode` every program instead
-// contracts the rows of its own device-side list (the float64 recheck), block
+// contracts the rows of its own device-side list (the recheck), block
 // by block in a grid-stride loop.
 template <typename T, bool NORM>
 __global__ void __launch_bounds__(kMultiThreads) tn_contract_multi_kernel(MultiArgs m) {
