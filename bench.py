@@ -22,7 +22,6 @@ import json
 import os
 import statistics
 import subprocess
-import tempfile
 import sys
 import time
 
@@ -112,58 +111,98 @@ def config(batch):
 
 
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons during the timed region."""
+    """SM clocks and throttle reasons sampled by a background thread while
+    the timed regions run: NVML through ctypes (read-only queries), else
+    one-shot nvidia-smi queries."""
 
-    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
-              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
-              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+    # nvmlClocksEventReasons bits (nvml.h): SwPowerCap, HwSlowdown,
+    # SwThermalSlowdown, HwThermalSlowdown
+    REASONS = {0x4: "sw_power_cap", 0x8: "hw_slowdown", 0x20: "sw_thermal_slowdown", 0x40: "hw_thermal_slowdown"}
+    SMI_FIELDS = ("clocks.sm,clocks.max.sm,clocks_event_reasons.hw_slowdown,"
+                  "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+                  "clocks_event_reasons.sw_power_cap")
 
     def __init__(self, gpu_index):
+        import threading
+
         self.gpu = gpu_index
-        self.proc = None
-        # the raw samples: TQEC_CLOCKS_CSV if set, else a temporary file
-        self.path = os.environ.get("TQEC_CLOCKS_CSV") or os.path.join(tempfile.gettempdir(),
-                                                                      f"tqec_clocks_rank{gpu_index}_{os.getpid()}.csv")
+        self.samples = []  # (sm_mhz, max_mhz, set of reasons)
+        self.stop_event = threading.Event()
+        self.thread = None
+        self.source = None
+
+    def _nvml(self):
+        import ctypes as C
+
+        lib = C.CDLL("libnvidia-ml.so.1")
+        if lib.nvmlInit_v2() != 0:
+            raise RuntimeError("nvmlInit")
+        n = C.c_uint()
+        lib.nvmlDeviceGetCount_v2(C.byref(n))
+        h = C.c_void_p()
+        idx = self.gpu if n.value > self.gpu else 0
+        if lib.nvmlDeviceGetHandleByIndex_v2(C.c_uint(idx), C.byref(h)) != 0:
+            raise RuntimeError("nvmlDeviceGetHandleByIndex")
+
+        def sample():
+            sm, mx, rs = C.c_uint(), C.c_uint(), C.c_ulonglong()
+            if lib.nvmlDeviceGetClockInfo(h, 1, C.byref(sm)) != 0:  # NVML_CLOCK_SM
+                return None
+            lib.nvmlDeviceGetMaxClockInfo(h, 1, C.byref(mx))
+            lib.nvmlDeviceGetCurrentClocksThrottleReasons(h, C.byref(rs))
+            return float(sm.value), float(mx.value), {v for k, v in self.REASONS.items() if rs.value & k}
+
+        return sample
+
+    def _smi(self):
+        def sample():
+            out = subprocess.run(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.SMI_FIELDS}",
+                                  "--format=csv,noheader,nounits"], capture_output=True, text=True, timeout=10)
+            parts = [x.strip() for x in out.stdout.strip().splitlines()[0].split(",")]
+            names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+            return float(parts[0]), float(parts[1]), {n for n, v in zip(names, parts[2:6]) if v.lower() == "active"}
+
+        return sample
 
     def start(self):
-        try:
-            os.makedirs(os.path.dirname(self.path), exist_ok=True)
-            self.f = open(self.path, "w")
-            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}",
-                                          "--format=csv,noheader,nounits", "-lms", "100"],
-                                         stdout=self.f, stderr=subprocess.DEVNULL)
-            # the timed regions are short: start them only once sampling runs
-            t0 = time.time()
-            while time.time() - t0 < 10.0 and os.path.getsize(self.path) == 0 and self.proc.poll() is None:
-                time.sleep(0.02)
-        except Exception:
-            self.proc = None
+        import threading
+
+        sample = None
+        for name, make in (("nvml", self._nvml), ("nvidia-smi", self._smi)):
+            try:
+                sample = make()
+                first = sample()
+                if first is None:
+                    continue
+                self.samples.append(first)
+                self.source = name
+                break
+            except Exception:
+                sample = None
+        if sample is None:
+            return
+
+        def loop():
+            while not self.stop_event.wait(0.05):
+                try:
+                    x = sample()
+                    if x is not None:
+                        self.samples.append(x)
+                except Exception:
+                    pass
+
+        self.thread = threading.Thread(target=loop, daemon=True)
+        self.thread.start()
 
     def stop(self):
-        if not self.proc:
-            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
-        self.proc.terminate()
-        try:
-            self.proc.wait(timeout=5)
-        except Exception:
-            self.proc.kill()
-        self.f.close()
-        sm, smax, reasons = [], [], set()
-        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for line in open(self.path):
-            parts = [x.strip() for x in line.split(",")]
-            if len(parts) < 9:
-                continue
-            try:
-                sm.append(float(parts[1]))
-                smax.append(float(parts[2]))
-            except ValueError:
-                continue
-            for n, v in zip(names, parts[5:9]):
-                if v.lower() == "active":
-                    reasons.add(n)
-        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
-                "reasons": sorted(reasons), "samples": len(sm)}
+        if self.thread is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"], "samples": 0}
+        self.stop_event.set()
+        self.thread.join(timeout=15)
+        sm = [x[0] for x in self.samples]
+        reasons = sorted(set().union(*[x[2] for x in self.samples]))
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(x[1] for x in self.samples),
+                "reasons": reasons, "samples": len(sm), "source": self.source}
 
 
 def read_traffic():
