@@ -349,7 +349,7 @@ def run_ours(args):
         t0 = time.time()
         sur, tstats = train_surrogate(ct, n_train=args.train_n, batch=16384, epochs=args.train_epochs, lr=3e-3, hidden=512,
                                       n_layers=4, seed=SEED + 17 + rank)
-        # calibrated at half the 1e-4 budget so fresh syndromes stay under it
+        # calibrated at half the 1e-4 mismatch limit so fresh syndromes stay under it
         thr, cstats = calibrate(sur, ct, n_val=args.calib_n, target_mismatch=5e-5, seed=SEED + 29 + rank)
         gd = GatedDecoder(ct, sur, thr)
         sur_stats = {"train": tstats, "calibration": cstats, "setup_seconds": time.time() - t0}

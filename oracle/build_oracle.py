@@ -1,5 +1,5 @@
 """Builds oracle/liboracle_contract.so (the float64 CPU contractor used only
-as the tests' checker and the benchmark's CPU baseline).  gcc + OpenMP."""
+as the tests' oracle and the benchmark's CPU baseline).  gcc + OpenMP."""
 import os
 import subprocess
 import sys

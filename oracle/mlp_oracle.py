@@ -1,4 +1,4 @@
-"""Float64 CPU checker for the surrogate MLP's kernels (test infrastructure
+"""Float64 CPU oracle for the surrogate MLP's kernels (test infrastructure
 only).
 
 Mirrors the computation of the surrogate kernels: inputs are syndrome bits,

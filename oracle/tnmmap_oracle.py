@@ -1,6 +1,6 @@
 """CPU oracle for the TNMMAP decoder path (test infrastructure only).
 
-This module is the checker, never the product: only the tests, the smoke
+This module is the oracle, never the product: only the tests, the smoke
 entry point and the CPU-baseline leg of the benchmark may import it.  It is a
 plain numpy restatement of TensorQEC.jl's tensor-network marginal-MAP decoder,
 written line by line from the reference sources (paths below are relative to

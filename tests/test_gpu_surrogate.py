@@ -1,8 +1,8 @@
 """GPU tests of the learned surrogate: gradients against the float64 CPU
-checker, training that reduces the loss, checkpoint round trip, and the
+oracle, training that reduces the loss, checkpoint round trip, and the
 gated decoder's decisions against the exact contraction.
 
-Gradient tolerance: relative L2 error 2e-3 against the checker with bf16
+Gradient tolerance: relative L2 error 2e-3 against the oracle with bf16
 rounding at the kernels' rounding points (float32 accumulation order is the
 only other difference), and 0.2 against the unquantised float64 network
 (the size of bf16 rounding in a small network).
