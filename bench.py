@@ -274,7 +274,10 @@ def run_reference(args):
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "syndromes/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic (seeded depolarizing errors)", "config": dict(config(per), batch=per),
+            "data": "synthetic (seeded depolarizing errors)",
+            # the workload of the GPU arm; each timed step contracts a bounded sample of it
+            "config": dict(config(args.batch), decoder="float64 per-syndrome tree contraction on all host cores",
+                           sample_per_step=per),
             "cpu_baseline": {"value": value, "unit": "syndromes/s", "cores": max_threads(), "kind": "port",
                              "sample": f"{per} syndromes per step, float64 per-syndrome tree contraction "
                                        f"(CPU restatement; Julia/OMEinsum not runnable here)"},
