@@ -42,7 +42,8 @@ def test_stabilizers_and_logicals_match_oracle(pkg, oracle, kind, d):
     assert not ((t.stgx.H.astype(int) @ t.stgz.H.T) % 2).any()
     assert not ((t.stgx.H.astype(int) @ lz.T) % 2).any()
     assert not ((t.stgz.H.astype(int) @ lx.T) % 2).any()
-    assert np.array_equal((lx.astype(int) @ lz.T) % 2 != 0, np.eye(lx.shape[0], dtype=bool)) or lx.shape[0] > 1
+    # row j of lx anticommutes with row j of lz (same_qubit_order, code_distance.jl:84-100)
+    assert ((lx.astype(int) * lz).sum(axis=1) % 2 == 1).all()
 
 
 def test_logical_kat(pkg, kat):
@@ -178,3 +179,36 @@ def test_right_inverse(pkg, oracle, kind, d):
             s = np.zeros(H.shape[0], dtype=np.int64)
             s[np.flatnonzero(Cc[0])[0]] = 1
             assert ((Cc.astype(np.int64) @ s) % 2).any()
+
+
+@pytest.mark.parametrize("m", [3, 4])
+def test_toric_logical_pairing(pkg, oracle, m):
+    """test/codes/code_distance.jl:97-115: on the toric code, X on the
+    support of lx row i anticommutes with lz row i only, and both rows
+    commute with every stabiliser."""
+    t = pkg.tanner_graph(pkg.ToricCode(m, m))
+    lx, lz = pkg.logical_operator(t)
+    assert lx.shape == lz.shape == (2, 2 * m * m)
+    assert np.array_equal((lx.astype(int) @ lz.T) % 2, np.eye(2, dtype=int))
+    assert not ((t.stgz.H.astype(int) @ lx.T) % 2).any()
+    assert not ((t.stgx.H.astype(int) @ lz.T) % 2).any()
+    olx, olz = oracle.logical_operator(oracle.css_tanner(*oracle.toric_code_stabilizers(m, m)))
+    assert np.array_equal(lx, olx) and np.array_equal(lz, olz)
+
+
+def test_bivariate_bicycle_144_12_12(pkg, oracle):
+    """test/codes/codes.jl:160-173: the [[144,12,12]] bivariate bicycle code
+    has 132 independent stabilisers and 12 logical qubits; with 11 of its lz
+    rows added as Z stabilisers one logical pair remains."""
+    code = pkg.BivariateBicycleCode(6, 12, ((3, 0), (0, 1), (0, 2)), ((0, 3), (1, 0), (2, 0)))
+    st = pkg.stabilizers(code)
+    assert len(st) == 132
+    t = pkg.CSSTannerGraph.from_stabilizers(st)
+    lx, lz = pkg.logical_operator(t)
+    assert lx.shape == lz.shape == (12, 144)
+    ost, onq = oracle.bivariate_bicycle_stabilizers(6, 12, ((3, 0), (0, 1), (0, 2)), ((0, 3), (1, 0), (2, 0)))
+    olx, olz = oracle.logical_operator(oracle.css_tanner(ost, onq))
+    assert np.array_equal(lx, olx) and np.array_equal(lz, olz)
+    st2 = list(st) + [pkg.PauliString.of(144, [int(q) + 1 for q in np.flatnonzero(lz[i])], 3) for i in range(11)]
+    lx2, lz2 = pkg.logical_operator(pkg.CSSTannerGraph.from_stabilizers(st2))
+    assert lx2.shape == lz2.shape == (1, 144)
