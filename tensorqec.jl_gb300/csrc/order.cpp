@@ -20,6 +20,10 @@
 
 #include "../../include/tqec_gb300.h"
 
+namespace tqec {
+std::string& last_error_ref();
+}  // namespace tqec
+
 namespace {
 
 struct VC {  // a label and how many leaves of the subtree carry it
@@ -279,7 +283,16 @@ void emit(const Tree& t, int T, const std::vector<int>& leaf_id, int next, int n
 
 extern "C" int tqec_optimize_order(const tqec_network* net, const tqec_order_options* opts, int32_t* steps_out,
                                    double* log2_macs_out, int32_t* width_out) {
-  if (!net || !steps_out || net->n_tensors < 1 || !net->ix_offsets || !net->ix_labels) return TQEC_ERR_INVALID;
+  auto invalid = [](const char* m) {
+    tqec::last_error_ref() = m;
+    return TQEC_ERR_INVALID;
+  };
+  if (!net || !steps_out || net->n_tensors < 1 || !net->ix_offsets || !net->ix_labels)
+    return invalid("NULL argument or empty network");
+  if (net->n_out < 0 || (net->n_out > 0 && !net->out_labels)) return invalid("bad output label list");
+  for (int i = 0; i < net->n_tensors; ++i)
+    if (net->ix_offsets[i] < 0 || net->ix_offsets[i + 1] < net->ix_offsets[i])
+      return invalid("ix_offsets must be non-negative and non-decreasing");
   tqec_order_options o;
   std::memset(&o, 0, sizeof(o));
   o.trials = 32;

@@ -209,6 +209,7 @@ static std::string build_plan_once(const NetworkView& net, int32_t n_steps, cons
     *unsupported = net.n_out > 16;
     return "n_out must be in [0, 16]";
   }
+  if (net.n_out > 0 && !net.out_labels) return "output labels must not be NULL";
   if (net.n_syndrome < 0 || (net.n_syndrome > 0 && !net.syndrome_tensors))
     return "bad syndrome leaf list";
   if (n_steps != T - 1) return "tree must have n_tensors - 1 steps";
