@@ -118,3 +118,44 @@ def test_malformed_inputs_return_status(pkg):
                        timeout=600, env=env, cwd=ROOT)
     assert r.returncode == 0, r.stdout[-2000:] + r.stderr[-4000:]
     assert "cases" in r.stdout
+
+
+NULL_CHILD = textwrap.dedent(r'''
+    import ctypes as C, os, re, sys
+    sys.path.insert(0, ROOT)
+    import __graft_entry__ as G
+    lib = G.load_package().native.lib()
+    text = open(os.path.join(ROOT, "include", "tqec_gb300.h")).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    scalar = {"int32_t": C.c_int32, "uint32_t": C.c_uint32, "int": C.c_int, "int64_t": C.c_int64,
+              "uint64_t": C.c_uint64, "size_t": C.c_size_t, "float": C.c_float, "double": C.c_double}
+    n = 0
+    for name, params in re.findall(r"^int\s+(tqec_\w+)\s*\(([^)]*)\)\s*;", text, re.M | re.S):
+        types = []
+        for p in params.split(","):
+            p = " ".join(p.replace("const", " ").split())
+            if not p or p == "void":
+                continue
+            if "*" in p:
+                types.append(C.c_void_p)
+            else:
+                types.append(scalar[p.rsplit(" ", 1)[0]])
+        f = getattr(lib, name)
+        f.argtypes = types
+        f.restype = C.c_int
+        rc = f(*[t() for t in types])
+        lenient = name.endswith(("_destroy", "_release")) or name == "tqec_last_error"
+        assert rc < 0 or (lenient and rc == 0), (name, rc)
+        n += 1
+    print("entry points", n)
+''')
+
+
+def test_null_arguments_return_status(pkg):
+    """Every int-returning entry point of the header, called with NULL
+    pointers and zero sizes, returns an error status (destroy and release of
+    NULL may succeed) and does not crash."""
+    r = subprocess.run([sys.executable, "-c", f"ROOT = {ROOT!r}\n" + NULL_CHILD], capture_output=True, text=True,
+                       timeout=300, cwd=ROOT)
+    assert r.returncode == 0, r.stdout[-2000:] + r.stderr[-4000:]
+    assert int(r.stdout.split()[-1]) >= 40
