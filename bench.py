@@ -229,17 +229,18 @@ def peaks():
 
 def cpu_baseline(pkg, ct, bits, sample):
     """The oracle's float64 per-syndrome contraction on all host cores."""
-    from oracle.c_oracle import CContractor, max_threads
+    from oracle.c_oracle import CContractor, host_cores
 
     g = ct.graph
     cc = CContractor(g.ixs, [np.asarray(x) for x in g.tensors], g.iy, g.syndrome_positions, ct.steps)
     sub = bits[:sample]
     packed = pkg.pack_syndromes(sub)
-    cc.contract(packed[:64])
+    cores = host_cores()
+    cc.contract(packed[:64], threads=cores)
     t0 = time.perf_counter()
-    marg, cls = cc.contract(packed)
+    marg, cls = cc.contract(packed, threads=cores)
     dt = time.perf_counter() - t0
-    return {"value": len(sub) / dt, "unit": "syndromes/s", "cores": max_threads(), "kind": "port",
+    return {"value": len(sub) / dt, "unit": "syndromes/s", "cores": cores, "kind": "port",
             "sample": f"{len(sub)} syndromes of the same workload, float64 tree contraction per syndrome "
                       f"(CPU restatement of TNMMAP; the reference Julia package is not runnable here)",
             "seconds": dt}, cls
@@ -252,7 +253,7 @@ def run_reference(args):
     if rank != 0:
         return
     pkg = G.load_package()
-    from oracle.c_oracle import CContractor, max_threads
+    from oracle.c_oracle import CContractor, host_cores
 
     t, em, bits = workload(pkg, 0, 1, max(args.cpu_sample, 256))
     lx, lz = pkg.logical_operator(t)
@@ -260,14 +261,15 @@ def run_reference(args):
     steps = pkg.optimize_code(g, d7_order(pkg))
     cc = CContractor(g.ixs, [np.asarray(x) for x in g.tensors], g.iy, g.syndrome_positions, steps)
     per = max(64, args.cpu_sample // max(args.steps, 1))
+    cores = host_cores()
     packed = pkg.pack_syndromes(bits[0])
     for w in range(args.warmup):
-        cc.contract(packed[:min(per, 256)])
+        cc.contract(packed[:min(per, 256)], threads=cores)
     times = []
     for s in range(args.steps):
         lo = (s * per) % max(len(packed) - per, 1)
         t0 = time.perf_counter()
-        cc.contract(packed[lo:lo + per])
+        cc.contract(packed[lo:lo + per], threads=cores)
         times.append(time.perf_counter() - t0)
     total = sum(times)
     value = per * args.steps / total
@@ -278,7 +280,7 @@ def run_reference(args):
             # the workload of the GPU arm; each timed step contracts a bounded sample of it
             "config": dict(config(args.batch), decoder="float64 per-syndrome tree contraction on all host cores",
                            sample_per_step=per),
-            "cpu_baseline": {"value": value, "unit": "syndromes/s", "cores": max_threads(), "kind": "port",
+            "cpu_baseline": {"value": value, "unit": "syndromes/s", "cores": cores, "kind": "port",
                              "sample": f"{per} syndromes per step, float64 per-syndrome tree contraction "
                                        f"(CPU restatement; Julia/OMEinsum not runnable here)"},
             "e2e": {"value": value, "unit": "syndromes/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}

@@ -69,3 +69,12 @@ class CContractor:
 
 def max_threads():
     return lib().oracle_max_threads()
+
+
+def host_cores():
+    """Cores this process may run on.  OMP_NUM_THREADS (which torchrun sets
+    to 1 for every rank) does not limit it."""
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
