@@ -38,7 +38,6 @@ errors at d=3 that is independent of any contraction order.
 """
 from __future__ import annotations
 
-import math
 import re
 from dataclasses import dataclass, field
 
