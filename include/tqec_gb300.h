@@ -182,6 +182,22 @@ int tqec_last_recheck_count(const tqec_program* prog, int64_t* count);
  * precision, timing n_probe synthetic syndromes. */
 int tqec_program_autotune(tqec_program* prog, int64_t n_probe);
 
+/* Program files.  No direct counterpart in the reference (a compiled Julia
+ * decoder is serialised whole); they keep compile's contraction-order search
+ * (optimize_code, tndecoder.jl:140-144) and the autotuning out of a new
+ * process's start-up.  tqec_program_save writes what the program was compiled
+ * from (network, tree, options) and its current launch shapes to `path`
+ * (written to path.tmp, then renamed).  tqec_program_load compiles the stored
+ * network with the stored tree on `device` (< 0: the stored device), fails
+ * with TQEC_ERR_IO when the file cannot be read (or written, on save), with
+ * TQEC_ERR_INVALID on a malformed or corrupted file (checksummed) or when
+ * the network no longer compiles to the same program, and takes the stored
+ * launch shapes when the device has the same SM count and shared-memory limit
+ * (otherwise the shapes creation picks; autotune again).  Files use the
+ * writer's byte order. */
+int tqec_program_save(tqec_program* prog, const char* path);
+int tqec_program_load(const char* path, int32_t device, tqec_program** out);
+
 /* The compiled program without a device, for inspection (the counterpart of
  * OMEinsum.contraction_complexity(ct), tndecoder.jl:273-279).  `steps` holds
  * n_steps records of 64 bytes: int32 a_kind, b_kind, a_ref, b_ref, a_prod,

@@ -73,6 +73,18 @@ struct DevBuf {
   }
 };
 
+// The inputs a program was compiled from, kept for tqec_program_save: the
+// network repacked densely (tensor i's labels and entries start at offsets
+// i, the one-hot syndrome leaves stored as [1, 0], which the planner never
+// reads), the tree and the options.
+struct ProgramInputs {
+  tqec_options opts;
+  int32_t n_tensors = 0;
+  std::vector<int32_t> ix_offsets, ix_labels, out_labels, syndrome_tensors, steps;
+  std::vector<int64_t> data_offsets;
+  std::vector<double> data;
+};
+
 }  // namespace
 
 struct tqec_program {
@@ -106,6 +118,7 @@ struct tqec_program {
   DevBuf syn, cls, logp, err, list, count;
   int32_t* h_count = nullptr;  // pinned
   int64_t last_recheck = 0;
+  ProgramInputs inputs;
   std::mutex mu;
 };
 
@@ -511,6 +524,38 @@ int program_multi_view(tqec_program* p, ProgramMultiView* v) {
 
 }  // namespace tqec
 
+namespace {
+
+// Copies a network and tree that build_plan accepted (so every offset, size
+// and position in them has been checked) into `in`.
+void keep_inputs(const tqec_network& net, const tqec_tree& tree, const tqec_options& o, ProgramInputs* in) {
+  const int T = net.n_tensors;
+  in->opts = o;
+  in->n_tensors = T;
+  std::vector<char> leaf(T, 0);
+  for (int j = 0; j < net.n_syndrome; ++j) leaf[net.syndrome_tensors[j]] = 1;
+  in->ix_offsets.assign(1, 0);
+  in->data_offsets.assign(1, 0);
+  in->ix_labels.clear();
+  in->data.clear();
+  for (int i = 0; i < T; ++i) {
+    in->ix_labels.insert(in->ix_labels.end(), net.ix_labels + net.ix_offsets[i], net.ix_labels + net.ix_offsets[i + 1]);
+    in->ix_offsets.push_back((int32_t)in->ix_labels.size());
+    if (leaf[i]) {
+      in->data.push_back(1.0);
+      in->data.push_back(0.0);
+    } else {
+      in->data.insert(in->data.end(), net.data + net.data_offsets[i], net.data + net.data_offsets[i + 1]);
+    }
+    in->data_offsets.push_back((int64_t)in->data.size());
+  }
+  in->out_labels.assign(net.out_labels, net.out_labels + std::max(net.n_out, 0));
+  in->syndrome_tensors.assign(net.syndrome_tensors, net.syndrome_tensors + std::max(net.n_syndrome, 0));
+  in->steps.assign(tree.steps, tree.steps + 2 * std::max(tree.n_steps, 0));
+}
+
+}  // namespace
+
 extern "C" {
 
 const char* tqec_version(void) { return "tqec-gb300 0.1.0 sm_103a"; }
@@ -549,6 +594,7 @@ int tqec_program_create(const tqec_network* net, const tqec_tree* tree, const tq
     delete p;
     return fail(unsupported ? TQEC_ERR_UNSUPPORTED : TQEC_ERR_INVALID, err);
   }
+  keep_inputs(*net, *tree, o, &p->inputs);
   p->device = o.device;
   p->precision = o.precision;
   p->flags = o.flags;
@@ -930,6 +976,292 @@ int tqec_plan_inspect_flags(const tqec_network* net, const tqec_tree* tree, uint
 
 int tqec_plan_release(void* handle) {
   delete static_cast<tqec::Plan*>(handle);
+  return TQEC_OK;
+}
+
+}  // extern "C"
+
+// ---- program files -------------------------------------------------------
+// A program file holds what a program was compiled from (network, tree,
+// options) and the launch shapes chosen for it (by tqec_program_autotune or
+// at creation), so a process can skip the order search and the autotuning
+// that produced them.  Loading compiles the network again with the stored
+// tree, requires the same program as when it was saved (a fingerprint of the
+// step records and tables) and takes the stored shapes when the device has
+// the same SM count and shared-memory limit and each shape is consistent with
+// the program.  Layout: "TQECPROG", version, byte-order mark, the fields in
+// the order written below (arrays as a uint64 count and the elements), and a
+// 64-bit FNV-1a checksum of everything before it.
+
+namespace {
+
+constexpr char kFileMagic[8] = {'T', 'Q', 'E', 'C', 'P', 'R', 'O', 'G'};
+constexpr uint32_t kFileVersion = 1;
+constexpr uint32_t kByteOrderMark = 0x01020304u;
+constexpr size_t kMaxFileBytes = size_t(1) << 31;
+
+uint64_t fnv1a(const void* data, size_t n, uint64_t h = 0xcbf29ce484222325ull) {
+  const unsigned char* b = static_cast<const unsigned char*>(data);
+  for (size_t i = 0; i < n; ++i) {
+    h ^= b[i];
+    h *= 0x100000001b3ull;
+  }
+  return h;
+}
+
+// Identifies a compiled program: its step records, tables and sizes.
+uint64_t plan_fingerprint(const tqec::Plan& P) {
+  uint64_t h = fnv1a(P.steps.data(), P.steps.size() * sizeof(tqec::StepDesc));
+  h = fnv1a(P.perm.data(), P.perm.size() * sizeof(int32_t), h);
+  h = fnv1a(P.consts.data(), P.consts.size() * sizeof(double), h);
+  h = fnv1a(P.vartab.data(), P.vartab.size() * sizeof(int32_t), h);
+  const int64_t sizes[] = {P.arena_elems, P.arena_small, P.n_classes, P.n_syndrome, P.width, P.map_mode ? 1 : 0};
+  return fnv1a(sizes, sizeof(sizes), h);
+}
+
+struct Writer {
+  std::string buf;
+  template <class T>
+  void put(const T& v) {
+    buf.append(reinterpret_cast<const char*>(&v), sizeof(T));
+  }
+  template <class T>
+  void put_vec(const std::vector<T>& v) {
+    put<uint64_t>(v.size());
+    if (!v.empty()) buf.append(reinterpret_cast<const char*>(v.data()), v.size() * sizeof(T));
+  }
+  void put_shape(const Shape& s) {
+    put<int32_t>(s.G);
+    put<int32_t>(s.threads);
+    put<uint8_t>(s.smem_arena);
+    put<uint8_t>(s.smem_tables);
+    put<uint8_t>(s.split);
+    put<uint8_t>(s.tensor);
+    put<uint64_t>(s.smem);
+    put<int32_t>(s.grid_cap);
+  }
+};
+
+struct Reader {
+  const char* p;
+  size_t left;
+  bool ok = true;
+  template <class T>
+  T get() {
+    T v{};
+    if (!ok || left < sizeof(T)) {
+      ok = false;
+      return v;
+    }
+    std::memcpy(&v, p, sizeof(T));
+    p += sizeof(T);
+    left -= sizeof(T);
+    return v;
+  }
+  template <class T>
+  std::vector<T> get_vec(uint64_t max_count) {
+    const uint64_t n = get<uint64_t>();
+    std::vector<T> v;
+    if (!ok || n > max_count || n > left / sizeof(T)) {
+      ok = false;
+      return v;
+    }
+    v.resize(n);
+    if (n) std::memcpy(v.data(), p, n * sizeof(T));
+    p += n * sizeof(T);
+    left -= n * sizeof(T);
+    return v;
+  }
+  Shape get_shape() {
+    Shape s;
+    s.G = get<int32_t>();
+    s.threads = get<int32_t>();
+    s.smem_arena = get<uint8_t>() != 0;
+    s.smem_tables = get<uint8_t>() != 0;
+    s.split = get<uint8_t>() != 0;
+    s.tensor = get<uint8_t>() != 0;
+    s.smem = (size_t)get<uint64_t>();
+    s.grid_cap = get<int32_t>();
+    return s;
+  }
+};
+
+// True when a stored shape is one this program can launch on its device: the
+// field values are in range and its shared memory, occupancy and grid cap are
+// what the shape choosers would compute for them.
+bool shape_consistent(const tqec_program* p, int prec, const Shape& s) {
+  if (s.G < 1 || s.G > 1024 || (s.G & (s.G - 1))) return false;
+  if (s.tensor && !tensor_program(p, prec)) return false;
+  if (s.threads < (s.tensor ? 128 : 32) || s.threads > tqec::contract_max_threads(prec, s.tensor) ||
+      (s.threads & (s.threads - 1)))
+    return false;
+  if (s.split && (s.smem_arena || p->plan.arena_small <= 0 || p->plan.map_mode)) return false;
+  const int nsteps = (int)p->plan.steps.size();
+  const size_t tb = s.smem_tables ? table_bytes(p, prec) : 0;
+  const size_t want =
+      s.split ? tqec::contract_smem_bytes(prec, nsteps, syn_words(p), s.G, p->plan.arena_small, true, 0, tb, s.tensor)
+              : tqec::contract_smem_bytes(prec, nsteps, syn_words(p), s.G, p->plan.arena_elems, s.smem_arena,
+                                          var_words(p), tb, s.tensor);
+  if (s.smem != want || s.smem > tqec::contract_smem_limit(p->device)) return false;
+  const int occ = tqec::contract_occupancy(prec, s.threads, s.smem, p->plan.map_mode, s.tensor);
+  return occ >= 1 && s.grid_cap >= 1 && int64_t(s.grid_cap) <= int64_t(occ) * p->sm_count;
+}
+
+}  // namespace
+
+extern "C" {
+
+int tqec_program_save(tqec_program* p, const char* path) {
+  if (!p || !path) return fail(TQEC_ERR_INVALID, "NULL argument");
+  std::lock_guard<std::mutex> lk(p->mu);
+  const ProgramInputs& in = p->inputs;
+  Writer w;
+  w.buf.append(kFileMagic, sizeof(kFileMagic));
+  w.put<uint32_t>(kFileVersion);
+  w.put<uint32_t>(kByteOrderMark);
+  w.put<int32_t>(in.opts.precision);
+  w.put<uint32_t>(in.opts.flags);
+  w.put<int32_t>(in.opts.device);
+  w.put<int32_t>(in.opts.group);
+  w.put<int32_t>(in.opts.threads);
+  w.put<double>(in.opts.margin);
+  w.put<int32_t>(in.opts.big_elems);
+  w.put<int32_t>(in.n_tensors);
+  w.put_vec(in.ix_offsets);
+  w.put_vec(in.ix_labels);
+  w.put_vec(in.data_offsets);
+  w.put_vec(in.data);
+  w.put_vec(in.out_labels);
+  w.put_vec(in.syndrome_tensors);
+  w.put_vec(in.steps);
+  w.put<uint64_t>(plan_fingerprint(p->plan));
+  w.put<int32_t>(p->sm_count);
+  w.put<uint64_t>(tqec::contract_smem_limit(p->device));
+  for (int prec = 0; prec < 3; ++prec) {
+    w.put_shape(p->shape[prec]);
+    w.put<int32_t>((int32_t)p->sized[prec].size());
+    for (const auto& [rows, s] : p->sized[prec]) {
+      w.put<int64_t>(rows);
+      w.put_shape(s);
+    }
+  }
+  w.put_shape(p->recheck_shape);
+  w.put<uint64_t>(fnv1a(w.buf.data(), w.buf.size()));
+  const std::string tmp = std::string(path) + ".tmp";
+  FILE* f = std::fopen(tmp.c_str(), "wb");
+  if (!f) return fail(TQEC_ERR_IO, std::string("cannot write ") + tmp);
+  const bool wrote = std::fwrite(w.buf.data(), 1, w.buf.size(), f) == w.buf.size();
+  const bool closed = std::fclose(f) == 0;
+  if (!wrote || !closed || std::rename(tmp.c_str(), path) != 0) {
+    std::remove(tmp.c_str());
+    return fail(TQEC_ERR_IO, std::string("cannot write ") + path);
+  }
+  g_last_error.clear();
+  return TQEC_OK;
+}
+
+int tqec_program_load(const char* path, int32_t device, tqec_program** out) {
+  if (!path || !out) return fail(TQEC_ERR_INVALID, "NULL argument");
+  *out = nullptr;
+  std::string buf;
+  {
+    FILE* f = std::fopen(path, "rb");
+    if (!f) return fail(TQEC_ERR_IO, std::string("cannot open ") + path);
+    char chunk[1 << 16];
+    size_t n;
+    while ((n = std::fread(chunk, 1, sizeof(chunk), f)) > 0 && buf.size() <= kMaxFileBytes) buf.append(chunk, n);
+    std::fclose(f);
+  }
+  const size_t head = sizeof(kFileMagic) + 2 * sizeof(uint32_t);
+  if (buf.size() > kMaxFileBytes || buf.size() < head + sizeof(uint64_t) ||
+      std::memcmp(buf.data(), kFileMagic, sizeof(kFileMagic)) != 0)
+    return fail(TQEC_ERR_INVALID, "not a program file");
+  uint64_t stored_sum;
+  std::memcpy(&stored_sum, buf.data() + buf.size() - sizeof(uint64_t), sizeof(uint64_t));
+  if (fnv1a(buf.data(), buf.size() - sizeof(uint64_t)) != stored_sum)
+    return fail(TQEC_ERR_INVALID, "program file checksum mismatch (truncated or corrupted)");
+  Reader r{buf.data() + sizeof(kFileMagic), buf.size() - sizeof(kFileMagic) - sizeof(uint64_t)};
+  if (r.get<uint32_t>() != kFileVersion) return fail(TQEC_ERR_INVALID, "unsupported program file version");
+  if (r.get<uint32_t>() != kByteOrderMark) return fail(TQEC_ERR_INVALID, "program file written with another byte order");
+  tqec_options o;
+  std::memset(&o, 0, sizeof(o));
+  o.precision = r.get<int32_t>();
+  o.flags = r.get<uint32_t>();
+  o.device = r.get<int32_t>();
+  o.group = r.get<int32_t>();
+  o.threads = r.get<int32_t>();
+  o.margin = r.get<double>();
+  o.big_elems = r.get<int32_t>();
+  const int32_t T = r.get<int32_t>();
+  const uint64_t cap = uint64_t(1) << 28;
+  auto ix_offsets = r.get_vec<int32_t>(cap);
+  auto ix_labels = r.get_vec<int32_t>(cap);
+  auto data_offsets = r.get_vec<int64_t>(cap);
+  auto data = r.get_vec<double>(cap);
+  auto out_labels = r.get_vec<int32_t>(cap);
+  auto syndrome_tensors = r.get_vec<int32_t>(cap);
+  auto steps = r.get_vec<int32_t>(cap);
+  const uint64_t fingerprint = r.get<uint64_t>();
+  const int32_t sm_count = r.get<int32_t>();
+  const uint64_t smem_limit = r.get<uint64_t>();
+  Shape shape[3];
+  std::vector<std::pair<int64_t, Shape>> sized[3];
+  for (int prec = 0; prec < 3 && r.ok; ++prec) {
+    shape[prec] = r.get_shape();
+    const int32_t ns = r.get<int32_t>();
+    if (ns < 0 || ns > 64) r.ok = false;
+    for (int32_t i = 0; i < ns && r.ok; ++i) {
+      const int64_t rows = r.get<int64_t>();
+      sized[prec].push_back({rows, r.get_shape()});
+    }
+  }
+  const Shape recheck = r.get_shape();
+  if (!r.ok || r.left != 0) return fail(TQEC_ERR_INVALID, "malformed program file");
+  // the arrays must describe a network before the planner reads them
+  bool sane = T >= 1 && ix_offsets.size() == size_t(T) + 1 && data_offsets.size() == size_t(T) + 1 &&
+              ix_offsets[0] == 0 && data_offsets[0] == 0 && size_t(ix_offsets[T]) == ix_labels.size() &&
+              uint64_t(data_offsets[T]) == data.size() && out_labels.size() <= (size_t(1) << 20) &&
+              syndrome_tensors.size() <= size_t(T) && steps.size() == 2 * (size_t(T) - 1);
+  for (int32_t i = 0; sane && i < T; ++i)
+    sane = ix_offsets[i + 1] >= ix_offsets[i] && data_offsets[i + 1] >= data_offsets[i];
+  if (!sane) return fail(TQEC_ERR_INVALID, "malformed network in program file");
+  if (device >= 0) o.device = device;
+  tqec_network net{T,
+                   ix_offsets.data(),
+                   ix_labels.data(),
+                   data_offsets.data(),
+                   data.data(),
+                   (int32_t)out_labels.size(),
+                   out_labels.empty() ? nullptr : out_labels.data(),
+                   (int32_t)syndrome_tensors.size(),
+                   syndrome_tensors.empty() ? nullptr : syndrome_tensors.data()};
+  tqec_tree tree{T - 1, steps.empty() ? nullptr : steps.data()};
+  tqec_program* p = nullptr;
+  int rc = tqec_program_create(&net, &tree, &o, &p);
+  if (rc) return rc;
+  if (plan_fingerprint(p->plan) != fingerprint) {
+    tqec_program_destroy(p);
+    return fail(TQEC_ERR_INVALID, "the network compiles to a different program than the one saved");
+  }
+  // the stored shapes, when the device matches and every one is consistent
+  const int rp = p->plan.map_mode ? TQEC_F64 : recheck_precision(p);
+  bool take = sm_count == p->sm_count && smem_limit == uint64_t(tqec::contract_smem_limit(p->device)) &&
+              shape_consistent(p, rp, recheck);
+  for (int prec = 0; take && prec < 3; ++prec) {
+    if (prec == TQEC_F32X2 && p->plan.map_mode) continue;
+    take = shape_consistent(p, prec, shape[prec]);
+    for (const auto& [rows, s] : sized[prec]) take = take && rows > 0 && shape_consistent(p, prec, s);
+  }
+  if (take) {
+    for (int prec = 0; prec < 3; ++prec) {
+      if (prec == TQEC_F32X2 && p->plan.map_mode) continue;
+      p->shape[prec] = shape[prec];
+      p->sized[prec] = sized[prec];
+    }
+    p->recheck_shape = recheck;
+  }
+  g_last_error.clear();
+  *out = p;
   return TQEC_OK;
 }
 

@@ -105,6 +105,8 @@ def lib():
         "tqec_contract_batch": [vp, vp, i64, i32, vp, vp],
         "tqec_last_recheck_count": [vp, vp],
         "tqec_program_autotune": [vp, i64],
+        "tqec_program_save": [vp, C.c_char_p],
+        "tqec_program_load": [C.c_char_p, i32, vp],
         "tqec_plan_inspect": [vp, vp, vp, vp],
         "tqec_multi_create": [vp, i32, vp],
         "tqec_multi_destroy": [vp],
@@ -286,9 +288,32 @@ class Program:
 
     def autotune(self, n_probe=4096):
         check(lib().tqec_program_autotune(self._h, n_probe))
+        self._refresh_info()
+
+    def _refresh_info(self):
         info = ProgramInfo()
         check(lib().tqec_program_info(self._h, C.byref(info)))
         self.info = {f: getattr(info, f) for f, _ in ProgramInfo._fields_}
+
+    def save(self, path):
+        """Writes the network, tree, options and launch shapes to `path`."""
+        check(lib().tqec_program_save(self._h, os.fsencode(path)))
+
+    @classmethod
+    def load(cls, path, device=-1):
+        """A program compiled again from a file of ``save`` on `device`
+        (-1: the device it was saved from), with the saved launch shapes when
+        the device matches."""
+        h = C.c_void_p()
+        check(lib().tqec_program_load(os.fsencode(path), device, C.byref(h)))
+        self = cls.__new__(cls)
+        self._h = h
+        self._refresh_info()
+        # the options follow the 16-byte file header (magic, version, byte-order mark)
+        with open(path, "rb") as f:
+            f.seek(16)
+            self.precision, self.flags = (int(v) for v in np.frombuffer(f.read(8), dtype="<i4"))
+        return self
 
 
 class PatternDecoder:
