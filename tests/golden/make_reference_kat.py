@@ -84,6 +84,42 @@ def main(ref_root=None):
     else:
         with open(OUT) as f:
             dem_text = json.load(f)["dem_small"]["text"]
+    kat["dem_from_circuit"] = {
+        "source": "test/decoding/dem.jl:5-86",
+        "note": "detector_error_model(parse_stim_string(circuit)): mechanism rates (atol 1e-10) and the "
+                "detectors (then logicals, numbered after the detectors) each flips; the reference lists "
+                "them in dictionary order, so they compare as a set",
+        "cases": [
+            {"circuit": "X_ERROR(0.2) 0 1\nDEPOLARIZE1(0.03) 0 1\n\nCX 0 1\n\nM 0 1\nDETECTOR rec[-1]\n"
+                        "DETECTOR rec[-2]\nDETECTOR rec[-1] rec[-2]\nOBSERVABLE_INCLUDE(0) rec[-1] rec[-2]\n",
+             "n_qubits": 2, "error_rates": [0.212, 0.212], "flipped_detectors": [[1, 3, 4], [1, 2]],
+             "source": "test/decoding/dem.jl:5-22"},
+            {"circuit": "DEPOLARIZE1(0.3) 0\nM 0\nDETECTOR rec[-1]\n",
+             "n_qubits": 1, "error_rates": [0.2], "flipped_detectors": [[1]],
+             "source": "test/decoding/dem.jl:24-35"},
+            {"circuit": "H 0\nCX 0 1\nDEPOLARIZE1(0.0297) 0\nH 3\nCX 0 2 1 2 3 0 3 1\nH 3\nM 2 3\n"
+                        "DETECTOR rec[-2]\nDETECTOR rec[-1]\n",
+             "n_qubits": 4, "error_rates": [0.01, 0.01, 0.01], "flipped_detectors": [[1], [1, 2], [2]],
+             "source": "test/decoding/dem.jl:37-53"},
+            {"circuit": "X_ERROR(0.2) 0 1\n\nCX 0 1\n\nM 0 1\nDETECTOR rec[-1] rec[-2]\n\nR 1\n\n"
+                        "X_ERROR(0.2) 0 1\nCX 1 0\n\nM 0 1\nDETECTOR rec[-1] rec[-2]\n",
+             "n_qubits": 2, "error_rates": [0.2, 0.32], "flipped_detectors": [[1], [2]],
+             "source": "test/decoding/dem.jl:56-78"},
+        ],
+    }
+    kat["stim_parse"] = {
+        "source": "test/stim_parser/stim_parser.jl:5-48",
+        "note": "the nested-REPEAT circuit parses (7 qubits); an unknown instruction is an error",
+        "circuit": "CNOT 0 1 2 3 4 5 # A CNOT gate\nCNOT 2 1 4 3 6 5\nMR 1 3 5\n\nDETECTOR rec[-3]\n"
+                   "DETECTOR rec[-2]\nDETECTOR rec[-1]\n\nREPEAT 2 {\n    CNOT 0 1 2 3 4 5 # A CNOT gate\n"
+                   "    CNOT 2 1 4 3 6 5\n    MR 1 3 5\n\n    DETECTOR rec[-3] rec[-6]\n"
+                   "    DETECTOR rec[-2] rec[-5]\n    DETECTOR rec[-1] rec[-4]\n    REPEAT 2 \n    {\n"
+                   "    X 0 1 2 3 4 5 6\n    }\n}\n\nM(0.1) 0 2 4 6\n\nDETECTOR rec[-3] rec[-4] rec[-7]\n"
+                   "DETECTOR rec[-2] rec[-3] rec[-6]\nDETECTOR rec[-1] rec[-2] rec[-5]\n\n"
+                   "OBSERVABLE_INCLUDE(0) rec[-1]\n",
+        "n_qubits": 7,
+        "bad_circuit": "WRONG_INSTRUCTION 1\n",
+    }
     kat["dem_small"] = {
         "source": "test/decoding/test_circuits/dem.dem (read by test/decoding/tndecoder.jl:112-121)",
         "text": dem_text,

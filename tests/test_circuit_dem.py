@@ -16,20 +16,26 @@ import pytest
 
 
 def _components(op):
-    """(probability, {qubit: (x, z)}) of every Pauli component of a channel."""
+    """(probability, {qubit: (x, z)}) of the independent Pauli channels of a
+    noise op: a depolarising channel is the composition of one channel per
+    non-identity Pauli, each of rate q with (1 - 2q)^2 = 1 - 4p/3 on one qubit
+    (dem.jl:44-63) and (1 - 2q)^8 = 1 - 16p/15 on two."""
     paulis = {1: (1, 0), 2: (1, 1), 3: (0, 1)}
     if op.name == "DEP1":
-        return [(op.p / 3, {q: paulis[a]}) for q in op.targets for a in (1, 2, 3)]
+        q1 = 0.5 * (1 - np.sqrt(1 - 4 * op.p / 3))
+        return [(q1, {q: paulis[a]}) for q in op.targets for a in (1, 2, 3)]
     if op.name == "DEP2":
+        q2 = 0.5 * (1 - (1 - 16 * op.p / 15) ** 0.125)
         out = []
         for a, b in zip(op.targets[0::2], op.targets[1::2]):
             for pa in range(4):
                 for pb in range(4):
                     if pa or pb:
-                        out.append((op.p / 15, {q: paulis[x] for q, x in ((a, pa), (b, pb)) if x}))
+                        out.append((q2, {q: paulis[x] for q, x in ((a, pa), (b, pb)) if x}))
         return out
-    if op.name == "XERR":
-        return [(op.p, {q: (1, 0)}) for q in op.targets]
+    if op.name in ("XERR", "YERR", "ZERR"):
+        pa = paulis[{"XERR": 1, "YERR": 2, "ZERR": 3}[op.name]]
+        return [(op.p, {q: pa}) for q in op.targets]
     return []
 
 
@@ -40,24 +46,33 @@ def _signature(circ, start, frame):
     for q, (px, pz) in frame.items():
         x[q] ^= bool(px)
         z[q] ^= bool(pz)
-    m = sum(len(op.targets) for op in circ.ops[:start] if op.name == "M")
+    m = sum(len(op.targets) for op in circ.ops[:start] if op.name in ("M", "MX", "MR"))
     flips = set()
     for op in circ.ops[start:]:
-        if op.name == "R":
+        if op.name in ("R", "RX"):
             x[list(op.targets)] = False
             z[list(op.targets)] = False
         elif op.name == "H":
             t = list(op.targets)
             x[t], z[t] = z[t].copy(), x[t].copy()
+        elif op.name == "S":
+            for q in op.targets:
+                z[q] ^= x[q]
         elif op.name == "CX":
             for c, tg in zip(op.targets[0::2], op.targets[1::2]):
                 x[tg] ^= x[c]
                 z[c] ^= z[tg]
-        elif op.name == "M":
+        elif op.name == "CZ":
+            for a, b in zip(op.targets[0::2], op.targets[1::2]):
+                z[a] ^= x[b]
+                z[b] ^= x[a]
+        elif op.name in ("M", "MX", "MR"):
             for q in op.targets:
-                if x[q]:
+                if (z[q] if op.name == "MX" else x[q]):
                     flips.add(m)
                 m += 1
+                if op.name == "MR":
+                    x[q] = z[q] = False
     return flips
 
 
@@ -68,10 +83,10 @@ def _per_fault_model(circ):
         for pr, frame in _components(op):
             flips = _signature(circ, oi + 1, frame)
             ds = tuple(i + 1 for i, dt in enumerate(circ.detectors) if len(flips & set(dt)) % 2)
-            obs = len(flips & set(circ.observable)) % 2 == 1
+            obs = tuple(n_det + 1 + k for k, o in enumerate(circ.observables) if len(flips & set(o)) % 2)
             if not ds and not obs:
                 continue
-            key = ds + ((n_det + 1,) if obs else ())
+            key = ds + obs
             q = merged.get(key, 0.0)
             merged[key] = q * (1 - pr) + pr * (1 - q)
     return merged
@@ -139,3 +154,92 @@ def test_noiseless_circuit_has_no_mechanisms(pkg):
     assert dm.error_rates == [] and dm.flipped_detectors == []
     with pytest.raises(ValueError):
         pkg.parse_dem_string("")
+
+
+def _kat():
+    import json
+    import os
+
+    with open(os.path.join(os.path.dirname(__file__), "golden", "reference_kat.json")) as f:
+        return json.load(f)
+
+
+@pytest.mark.parametrize("case", range(4))
+def test_reference_dem_known_answers(pkg, case):
+    """test/decoding/dem.jl:5-86: the reference's circuit -> DEM answers
+    (merged X_ERROR and DEPOLARIZE1 rates, resets, propagation through H
+    and CX), through the stim text parser."""
+    from tensorqec_gb300 import circuit
+
+    k = _kat()["dem_from_circuit"]["cases"][case]
+    circ = circuit.parse_stim_string(k["circuit"], k["n_qubits"])
+    assert circ.n_qubits == k["n_qubits"]
+    dm = circuit.detector_error_model(circ)
+    got = {tuple(f): r for f, r in zip(dm.flipped_detectors, dm.error_rates)}
+    want = {tuple(f): r for f, r in zip(k["flipped_detectors"], k["error_rates"])}
+    assert got.keys() == want.keys()
+    for key in want:
+        assert abs(got[key] - want[key]) <= 1e-10, (key, got[key], want[key])
+
+
+def test_reference_stim_parse_known_answers(pkg):
+    """test/stim_parser/stim_parser.jl:5-48: nested REPEAT blocks and a
+    noisy measurement parse; an unknown instruction is an error."""
+    from tensorqec_gb300 import circuit
+
+    k = _kat()["stim_parse"]
+    circ = circuit.parse_stim_string(k["circuit"], k["n_qubits"])
+    assert circ.n_qubits == 7
+    assert circ.n_measurements == 3 + 2 * 3 + 4
+    assert len(circ.detectors) == 3 + 2 * 3 + 3
+    assert circ.observables == [[circ.n_measurements - 1]]
+    # the second round's first detector compares its first MR with the first round's
+    assert circ.detectors[3] == [3, 0]
+    # M(0.1) puts a 0.1 X flip in front of the readout of qubits 0, 2, 4, 6
+    flip = [op for op in circ.ops if op.name == "XERR"]
+    assert len(flip) == 1 and flip[0].targets == (0, 2, 4, 6) and flip[0].p == 0.1
+    with pytest.raises(ValueError):
+        circuit.parse_stim_string(k["bad_circuit"], 5)
+
+
+def test_stim_text_round_trip_of_the_workload_circuit(pkg):
+    """The d=5, 5-round Z-memory circuit written as stim text and read back
+    gives the same detector error model."""
+    from tensorqec_gb300 import circuit
+
+    circ = circuit.memory_z_circuit(5, 5, 0.001)
+    back = circuit.parse_stim_string(circ.to_stim_text())
+    assert back.n_qubits == circ.n_qubits and back.n_measurements == circ.n_measurements
+    assert back.detectors == circ.detectors and back.observables == circ.observables
+    a, b = circuit.detector_error_model(circ), circuit.detector_error_model(back)
+    assert a.flipped_detectors == b.flipped_detectors and a.error_rates == b.error_rates
+
+
+def test_parsed_circuit_with_x_basis_and_cz(pkg):
+    """X-basis reset and measurement, S and CZ: an X-basis Bell-pair check
+    is deterministic, Z errors on the pair flip it, X errors do not, and the
+    per-fault propagation agrees with the bit-packed model."""
+    from tensorqec_gb300 import circuit
+
+    text = """
+    RX 0 1
+    H 1
+    CZ 0 1
+    H 1
+    S 2
+    Z_ERROR(0.05) 0
+    X_ERROR(0.07) 1
+    DEPOLARIZE1(0.03) 0
+    MX 0 1
+    DETECTOR rec[-1] rec[-2]
+    """
+    circ = circuit.parse_stim_string(text)
+    assert circ.n_qubits == 3
+    assert circuit.detectors_deterministic(circ)
+    dm = circuit.detector_error_model(circ)
+    want = _per_fault_model(circ)
+    got = {tuple(f): r for f, r in zip(dm.flipped_detectors, dm.error_rates)}
+    assert got.keys() == want.keys() == {(1,)}
+    q = 0.5 * (1 - np.sqrt(1 - 4 * 0.03 / 3))
+    z = 2 * q * (1 - q)  # the Z and Y components of the depolarising channel
+    assert abs(got[(1,)] - (0.05 * (1 - z) + z * (1 - 0.05))) < 1e-15
