@@ -5,7 +5,8 @@ TNMMAP factor graph and its contraction order are built here; the contraction
 itself runs in ``libtqec_gb300.so`` (hand-written sm_103a CUDA kernels behind
 the C ABI of include/tqec_gb300.h).
 """
-from .circuit import Circuit, detector_error_model, memory_z_circuit, parse_stim_file, parse_stim_string
+from .circuit import (Circuit, detector_error_model, insert_errors, memory_z_circuit, parse_stim_file,
+                      parse_stim_string)
 from .codes import (BivariateBicycleCode, Code422, Code832, Code1573, Color488, Color666, CSSTannerGraph,
                     PauliString, ShorCode, SimpleTannerGraph, SteaneCode, SurfaceCode, ToricCode,
                     remove_linear_dependency, stabilizers, tanner_graph)

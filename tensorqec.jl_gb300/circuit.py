@@ -27,7 +27,7 @@ non-identity two-qubit Pauli anticommutes with 8 of the 15).
 
 ``parse_stim_string`` reads stim's circuit text (in place of
 stim_parser.jl:14-335) for the instructions such circuits use: resets
-R/RX, H, S, CX/CNOT, CZ, Pauli gates, measurements M/MX/MR (optionally
+R/RX, H, S, C_XYZ/C_ZYX, CX/CNOT, CZ, Pauli gates, measurements M/MX/MR (optionally
 noisy, ``M(p)``), X/Y/Z_ERROR, DEPOLARIZE1/2, DETECTOR,
 OBSERVABLE_INCLUDE(k), REPEAT blocks, and the annotations TICK,
 QUBIT_COORDS and SHIFT_COORDS; anything else raises ValueError.
@@ -48,8 +48,9 @@ from .dem import DetectorErrorModel
 
 @dataclass
 class Op:
-    # "R", "RX" (resets), "H", "S", "CX", "CZ", "M", "MX", "MR" (measurements;
-    # MR resets after measuring), "DEP1", "DEP2", "XERR", "YERR", "ZERR"
+    # "R", "RX" (resets), "H", "S", "CXYZ", "CZYX", "CX", "CZ", "X", "Y", "Z" (gates), "M",
+    # "MX", "MR" (measurements; MR resets after measuring), "DEP1", "DEP2",
+    # "XERR", "YERR", "ZERR" (noise)
     name: str
     targets: tuple       # qubit ids (pairs for CX / CZ / DEP2)
     p: float = 0.0
@@ -57,8 +58,10 @@ class Op:
 
 NOISE = ("DEP1", "DEP2", "XERR", "YERR", "ZERR")
 MEASURE = ("M", "MX", "MR")
+PAULI = ("X", "Y", "Z")  # Pauli gates: they move no Pauli frame
 STIM_NAMES = {"R": "R", "RX": "RX", "H": "H", "S": "S", "CX": "CX", "CZ": "CZ", "M": "M", "MX": "MX", "MR": "MR",
-              "DEP1": "DEPOLARIZE1", "DEP2": "DEPOLARIZE2", "XERR": "X_ERROR", "YERR": "Y_ERROR", "ZERR": "Z_ERROR"}
+              "X": "X", "Y": "Y", "Z": "Z", "CXYZ": "C_XYZ", "CZYX": "C_ZYX", "DEP1": "DEPOLARIZE1", "DEP2": "DEPOLARIZE2", "XERR": "X_ERROR",
+              "YERR": "Y_ERROR", "ZERR": "Z_ERROR"}
 
 
 @dataclass
@@ -262,6 +265,11 @@ def detector_error_model(circ: Circuit) -> DetectorErrorModel:
         elif op.name == "S":
             for q in op.targets:
                 Z[q] ^= X[q]
+        elif op.name in ("CXYZ", "CZYX"):
+            # C_XYZ: X -> Y -> Z -> X (x' = x ^ z, z' = x); C_ZYX is its inverse
+            for q in op.targets:
+                x, z = X[q].copy(), Z[q].copy()
+                X[q], Z[q] = (x ^ z, x) if op.name == "CXYZ" else (z, x ^ z)
         elif op.name == "CX":
             t = op.targets
             for i in range(0, len(t), 2):
@@ -364,6 +372,11 @@ def detectors_deterministic(circ: Circuit) -> bool:
             elif op.name == "S":
                 for q in op.targets:
                     z[q] ^= x[q]
+            elif op.name in ("CXYZ", "CZYX"):
+                # backwards each cycles the other way
+                for q in op.targets:
+                    xq, zq = x[q], z[q]
+                    x[q], z[q] = (zq, xq ^ zq) if op.name == "CXYZ" else (xq ^ zq, xq)
             elif op.name in ("CX", "CZ"):
                 t = op.targets
                 for i in range(len(t) - 2, -1, -2):
@@ -385,10 +398,11 @@ def detectors_deterministic(circ: Circuit) -> bool:
 # ---------------------------------------------------------------------------
 
 _GATES = {"R": "R", "RZ": "R", "RX": "RX", "H": "H", "H_XZ": "H", "S": "S", "SQRT_Z": "S", "S_DAG": "S",
-          "SQRT_Z_DAG": "S", "CX": "CX", "CNOT": "CX", "ZCX": "CX", "CZ": "CZ", "ZCZ": "CZ",
+          "SQRT_Z_DAG": "S", "CX": "CX", "CNOT": "CX", "ZCX": "CX", "CZ": "CZ", "ZCZ": "CZ", "X": "X", "Y": "Y",
+          "Z": "Z", "C_XYZ": "CXYZ", "C_ZYX": "CZYX",
           "M": "M", "MZ": "M", "MX": "MX", "MR": "MR", "MRZ": "MR",
           "X_ERROR": "XERR", "Y_ERROR": "YERR", "Z_ERROR": "ZERR", "DEPOLARIZE1": "DEP1", "DEPOLARIZE2": "DEP2"}
-_IGNORED = {"TICK", "QUBIT_COORDS", "SHIFT_COORDS", "I", "X", "Y", "Z"}  # Pauli gates move no frame
+_IGNORED = {"TICK", "QUBIT_COORDS", "SHIFT_COORDS", "I"}
 _LINE = re.compile(r"^([A-Za-z_][A-Za-z0-9_]*)\s*(?:\(([^)]*)\))?\s*(.*)$")
 
 
@@ -486,3 +500,28 @@ def parse_stim_file(path: str, n_qubits: int = None) -> Circuit:
     """parse_stim_file (stim_parser.jl:14-20)."""
     with open(path) as f:
         return parse_stim_string(f.read(), n_qubits)
+
+
+def insert_errors(circ: Circuit, after_clifford_depolarization: float = 0.0, after_reset_flip_probability: float = 0.0,
+                  before_measure_flip_probability: float = 0.0) -> Circuit:
+    """A copy of `circ` with noise added around its operations (in place of
+    insert_errors, dem.jl:166-207): a depolarising channel after every
+    Clifford gate on the gate's qubits (DEPOLARIZE1 after one-qubit gates,
+    DEPOLARIZE2 on each pair of a two-qubit gate), a flip after every reset
+    and a flip of every measurement result before the measurement.  A flip
+    is X for the Z basis (R, M, MR) and Z for the X basis (RX, MX), so it
+    always flips the reset state or the result."""
+    out = Circuit(circ.n_qubits, [], [list(d) for d in circ.detectors], [list(o) for o in circ.observables],
+                  circ.n_measurements)
+    p_gate, p_reset, p_meas = after_clifford_depolarization, after_reset_flip_probability, before_measure_flip_probability
+    for op in circ.ops:
+        if p_meas and op.name in MEASURE:
+            out.ops.append(Op("ZERR" if op.name == "MX" else "XERR", op.targets, p_meas))
+        out.ops.append(op)
+        if p_gate and op.name in ("H", "S", "CXYZ", "CZYX") + PAULI:
+            out.ops.append(Op("DEP1", op.targets, p_gate))
+        elif p_gate and op.name in ("CX", "CZ"):
+            out.ops.append(Op("DEP2", op.targets, p_gate))
+        if p_reset and op.name in ("R", "RX", "MR"):
+            out.ops.append(Op("ZERR" if op.name == "RX" else "XERR", op.targets, p_reset))
+    return out

@@ -58,6 +58,13 @@ def _signature(circ, start, frame):
         elif op.name == "S":
             for q in op.targets:
                 z[q] ^= x[q]
+        elif op.name in ("CXYZ", "CZYX"):
+            # conjugation by C_XYZ sends X to Y, Y to Z, Z to X
+            cyc = {(1, 0): (1, 1), (1, 1): (0, 1), (0, 1): (1, 0), (0, 0): (0, 0)}
+            if op.name == "CZYX":
+                cyc = {v: k for k, v in cyc.items()}
+            for q in op.targets:
+                x[q], z[q] = cyc[(int(x[q]), int(z[q]))]
         elif op.name == "CX":
             for c, tg in zip(op.targets[0::2], op.targets[1::2]):
                 x[tg] ^= x[c]
@@ -243,3 +250,55 @@ def test_parsed_circuit_with_x_basis_and_cz(pkg):
     q = 0.5 * (1 - np.sqrt(1 - 4 * 0.03 / 3))
     z = 2 * q * (1 - q)  # the Z and Y components of the depolarising channel
     assert abs(got[(1,)] - (0.05 * (1 - z) + z * (1 - 0.05))) < 1e-15
+
+
+def test_insert_errors_rebuilds_the_workload_noise(pkg):
+    """insert_errors (dem.jl:166-207) on the noiseless Z-memory circuit with
+    p everywhere gives the noisy circuit's model mechanism for mechanism."""
+    from tensorqec_gb300 import circuit
+
+    for d, rounds, p in ((3, 2, 0.004), (5, 5, 0.001)):
+        clean = circuit.memory_z_circuit(d, rounds, 0.0)
+        noisy = circuit.insert_errors(clean, p, p, p)
+        a = circuit.detector_error_model(circuit.memory_z_circuit(d, rounds, p))
+        b = circuit.detector_error_model(noisy)
+        assert a.flipped_detectors == b.flipped_detectors
+        np.testing.assert_allclose(a.error_rates, b.error_rates, rtol=1e-14)
+
+
+def test_reference_insert_errors_circuit(pkg):
+    """The circuit of test/decoding/dem.jl:88-128 (with MR and C_XYZ): noise
+    lands where insert_errors puts it, the model matches per-fault
+    propagation, and C_XYZ followed by C_ZYX is the identity."""
+    from tensorqec_gb300 import circuit
+
+    text = """
+    H 0 1
+    CX 0 1
+    M 0
+    MR 1
+    DETECTOR rec[-1] rec[-2]
+    R 1
+    CX 1 0
+    M 0 1
+    DETECTOR rec[-1] rec[-2]
+    C_XYZ 1
+    """
+    circ = circuit.parse_stim_string(text, 2)
+    noisy = circuit.insert_errors(circ, after_clifford_depolarization=0.01, after_reset_flip_probability=0.02,
+                                  before_measure_flip_probability=0.03)
+    names = [op.name for op in noisy.ops]
+    assert names == ["H", "DEP1", "CX", "DEP2", "XERR", "M", "XERR", "MR", "XERR", "R", "XERR", "CX", "DEP2",
+                     "XERR", "M", "CXYZ", "DEP1"]
+    dm = circuit.detector_error_model(noisy)
+    got = {tuple(f): r for f, r in zip(dm.flipped_detectors, dm.error_rates)}
+    want = _per_fault_model(noisy)
+    assert got.keys() == want.keys() and got
+    for k in want:
+        assert abs(got[k] - want[k]) <= 1e-15 * want[k]
+    # C_XYZ then C_ZYX leaves every frame as it was
+    twice = circuit.parse_stim_string("RX 0\nR 1\nC_XYZ 0 1\nC_ZYX 0 1\nMX 0\nM 1\nDETECTOR rec[-2]\n"
+                                      "DETECTOR rec[-1]\n")
+    assert circuit.detectors_deterministic(twice)
+    once = circuit.parse_stim_string("RX 0\nC_XYZ 0\nMX 0\nDETECTOR rec[-1]\n")
+    assert not circuit.detectors_deterministic(once)
