@@ -173,12 +173,12 @@ class CompiledTNMMAP:
         return self.program.n_classes
 
     def _bits(self, syndromes):
+        """Syndrome rows from one CSSSyndrome, a batched one (2-D sx, sz), a
+        list of them, or 0/1 rows [sx..., sz...]."""
         if isinstance(syndromes, CSSSyndrome):
-            return syndromes.bits()[None, :]
+            return np.atleast_2d(syndromes.bits())
         if isinstance(syndromes, (list, tuple)) and syndromes and isinstance(syndromes[0], CSSSyndrome):
             return np.stack([s.bits() for s in syndromes])
-        if isinstance(syndromes, CSSSyndrome.__mro__[0]):
-            return syndromes.bits()[None, :]
         b = np.asarray(syndromes, dtype=np.uint8)
         return np.atleast_2d(b) & 1
 
@@ -419,7 +419,7 @@ class CompiledGeneralTNMAP:
     def decode_batch(self, syndromes, return_logp=False):
         """(ex, ez) rows for syndrome rows [sx..., sz...]."""
         if isinstance(syndromes, CSSSyndrome):
-            syndromes = syndromes.bits()[None, :]
+            syndromes = np.atleast_2d(syndromes.bits())
         cfg, logp = self.cd.decode_batch(syndromes, return_logp=True)
         nq = self.css.nq
         out = (cfg[:, :nq], cfg[:, nq:])

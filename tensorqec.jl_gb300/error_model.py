@@ -74,7 +74,9 @@ class CSSSyndrome:
     sz: np.ndarray
 
     def bits(self) -> np.ndarray:
-        return np.concatenate([np.asarray(self.sx, np.uint8), np.asarray(self.sz, np.uint8)]) & 1
+        """[sx..., sz...] (the update_syndrome! order, tndecoder.jl:148-158);
+        a batch of syndromes (2-D sx, sz) gives one row per syndrome."""
+        return np.concatenate([np.asarray(self.sx, np.uint8), np.asarray(self.sz, np.uint8)], axis=-1) & 1
 
     def __eq__(self, other):
         return (np.array_equal(np.asarray(self.sx) & 1, np.asarray(other.sx) & 1)

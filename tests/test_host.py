@@ -212,3 +212,24 @@ def test_bivariate_bicycle_144_12_12(pkg, oracle):
     st2 = list(st) + [pkg.PauliString.of(144, [int(q) + 1 for q in np.flatnonzero(lz[i])], 3) for i in range(11)]
     lx2, lz2 = pkg.logical_operator(pkg.CSSTannerGraph.from_stabilizers(st2))
     assert lx2.shape == lz2.shape == (1, 144)
+
+
+def test_syndrome_rows_from_single_batched_and_listed_syndromes(pkg):
+    """The rows a decoder reads ([sx..., sz...], tndecoder.jl:148-158) from
+    one CSSSyndrome, from the batched one syndrome_extraction returns for a
+    batch of error patterns, and from a list of single ones."""
+    from tensorqec_gb300.decoder import CompiledTNMMAP
+
+    t = pkg.tanner_graph(pkg.SurfaceCode(5, 5))
+    em = pkg.depolarizing(0.1, t.nq)
+    ep = pkg.random_error_pattern(em, np.random.default_rng(3), nsamples=9)
+    syn = pkg.syndrome_extraction(ep, t)
+    want = np.concatenate([syn.sx, syn.sz], axis=1)
+    np.testing.assert_array_equal(syn.bits(), want)
+    rows = CompiledTNMMAP._bits(None, syn)
+    np.testing.assert_array_equal(rows, want)
+    singles = [pkg.CSSSyndrome(syn.sx[i], syn.sz[i]) for i in range(9)]
+    np.testing.assert_array_equal(singles[4].bits(), want[4])
+    np.testing.assert_array_equal(CompiledTNMMAP._bits(None, singles[4]), want[4:5])
+    np.testing.assert_array_equal(CompiledTNMMAP._bits(None, singles), want)
+    np.testing.assert_array_equal(CompiledTNMMAP._bits(None, want), want)
