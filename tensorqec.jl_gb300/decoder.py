@@ -21,6 +21,16 @@ from .error_model import (CSSErrorPattern, CSSSyndrome, DecodingResult, Independ
 from .network import FactorGraph, reduce2general, tnmap_graph, tnmmap_css_graph, tnmmap_dem_graph
 
 
+def simple_rows(syndromes) -> np.ndarray:
+    """0/1 syndrome rows from a SimpleSyndrome (one, or a batch with a 2-D
+    ``s``), a list of them, or rows already."""
+    if isinstance(syndromes, SimpleSyndrome):
+        syndromes = syndromes.s
+    elif isinstance(syndromes, (list, tuple)) and syndromes and isinstance(syndromes[0], SimpleSyndrome):
+        syndromes = np.stack([np.asarray(x.s) for x in syndromes])
+    return np.atleast_2d(np.asarray(syndromes, dtype=np.uint8)) & 1
+
+
 # ---------------------------------------------------------------------------
 # contraction-order optimisers (stand-ins for OMEinsum's CodeOptimizer)
 # ---------------------------------------------------------------------------
@@ -287,7 +297,7 @@ class CompiledDEMTNMMAP:
         return self.program.n_classes
 
     def decode_batch(self, syndromes, return_logp=False):
-        bits = np.atleast_2d(np.asarray(syndromes, dtype=np.uint8)) & 1
+        bits = simple_rows(syndromes)
         packed = pack_syndromes(bits)
         n = packed.shape[0]
         logp = np.empty((n, self.n_classes), dtype=np.float64) if return_logp else None
@@ -295,7 +305,7 @@ class CompiledDEMTNMMAP:
         return (cls, logp) if return_logp else cls
 
     def class_logprobs(self, syndromes, precision=None):
-        packed = pack_syndromes(np.atleast_2d(np.asarray(syndromes, dtype=np.uint8)) & 1)
+        packed = pack_syndromes(simple_rows(syndromes))
         prec = self.decoder._native_precision() if precision is None else \
             {"f64": native.TQEC_F64, "f32": native.TQEC_F32, "f32x2": native.TQEC_F32X2}[precision]
         return self.program.contract_packed(packed, prec)
@@ -375,7 +385,7 @@ class CompiledTNMAP:
     def decode_batch(self, syndromes, return_logp=False):
         """Most probable bit configuration for each syndrome row: an
         (n, nq) 0/1 array (and the natural log of its probability)."""
-        bits = np.atleast_2d(np.asarray(syndromes, dtype=np.uint8)) & 1
+        bits = simple_rows(syndromes)
         cfg, logp = self.program.map_decode_packed(pack_syndromes(bits), self.tanner.nq)
         return (cfg, logp) if return_logp else cfg
 

@@ -233,3 +233,19 @@ def test_syndrome_rows_from_single_batched_and_listed_syndromes(pkg):
     np.testing.assert_array_equal(CompiledTNMMAP._bits(None, singles[4]), want[4:5])
     np.testing.assert_array_equal(CompiledTNMMAP._bits(None, singles), want)
     np.testing.assert_array_equal(CompiledTNMMAP._bits(None, want), want)
+
+
+def test_simple_syndrome_rows(pkg):
+    """DEM and TNMAP decoders read rows from one SimpleSyndrome, a batched
+    one, a list of them, or 0/1 rows."""
+    from tensorqec_gb300.decoder import simple_rows
+
+    t = pkg.tanner_graph(pkg.SurfaceCode(3, 3)).stgz
+    e = pkg.random_error_pattern(pkg.iid_error(0.2, t.nq), np.random.default_rng(5), nsamples=6)
+    syn = pkg.syndrome_extraction(e, t)
+    want = np.asarray(syn.s)
+    assert want.shape == (6, t.ns)
+    np.testing.assert_array_equal(simple_rows(syn), want)
+    np.testing.assert_array_equal(simple_rows([pkg.SimpleSyndrome(r) for r in want]), want)
+    np.testing.assert_array_equal(simple_rows(pkg.SimpleSyndrome(want[2])), want[2:3])
+    np.testing.assert_array_equal(simple_rows(want), want)
