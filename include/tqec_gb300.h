@@ -152,7 +152,10 @@ int tqec_program_info(const tqec_program* prog, tqec_program_info_t* info);
  * error bound.  logp_out and err_bound_out may be NULL.  With TQEC_F32 the
  * syndromes whose class margin is below the bound are contracted again
  * (TQEC_F32X2, or float64 with TQEC_FLAG_RECHECK_F64) before the call
- * returns; their err_bound_out is that arithmetic's bound. */
+ * returns; their err_bound_out is that arithmetic's bound.  A syndrome that
+ * no error produces (an all-zero marginal, where the reference's
+ * error_pattern integer program fails) is reported per row rather than by
+ * failing the batch: class 0 and every log-marginal -inf. */
 int tqec_decode_batch(tqec_program* prog, const uint8_t* syndromes, int64_t n,
                       int32_t* class_out, double* logp_out,
                       float* err_bound_out, void* stream);
