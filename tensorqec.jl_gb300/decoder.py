@@ -18,7 +18,8 @@ from .codes import CSSTannerGraph, SimpleTannerGraph
 from .dem import DetectorErrorModel, dem2tanner, logical_map
 from .error_model import (CSSErrorPattern, CSSSyndrome, DecodingResult, IndependentDepolarizingError,
                           IndependentFlipError, SimpleSyndrome, iid_error, pack_syndromes)
-from .network import FactorGraph, reduce2general, tnmap_graph, tnmmap_css_graph, tnmmap_dem_graph
+from .network import (FactorGraph, choose_slice_labels, reduce2general, slice_graph, tnmap_graph, tnmmap_css_graph,
+                      tnmmap_dem_graph)
 
 
 def simple_rows(syndromes) -> np.ndarray:
@@ -133,7 +134,10 @@ class TNMMAP:
     rounding-error bound, in double-float (pairs of float32, about 48
     significant bits; GB300 runs float64 at 1/64 of the float32 rate) or, with
     ``recheck_f64``, in float64.  ``plain`` launches one syndrome at a time
-    (the drop-in form of the reference's per-syndrome ``decode``)."""
+    (the drop-in form of the reference's per-syndrome ``decode``).
+    ``slices`` > 0 fixes that many inner labels of the tree and contracts the
+    2^slices narrower networks (``SlicedProgram``), for networks too wide to
+    contract whole."""
     optimizer: object = field(default_factory=TreeSA)
     factorize: bool = True
     precision: str = "f32"
@@ -146,6 +150,7 @@ class TNMMAP:
     big_elems: int = 0
     tensor_cores: bool = True
     recheck_f64: bool = False
+    slices: int = 0
 
     def _native_precision(self):
         return {"f64": native.TQEC_F64, "f32": native.TQEC_F32}[self.precision]
@@ -155,6 +160,122 @@ class TNMMAP:
                 (native.TQEC_FLAG_SPLIT_ARENA if self.split_arena else 0) |
                 (0 if self.tensor_cores else native.TQEC_FLAG_NO_TENSOR_CORES) |
                 (native.TQEC_FLAG_RECHECK_F64 if self.recheck_f64 else 0))
+
+    def _program(self, graph, steps):
+        """The GPU program of a compiled network: whole, or sliced."""
+        args = (self._native_precision(), self._flags(), self.device, self.group, self.threads, self.margin,
+                self.big_elems)
+        if self.slices > 0:
+            return SlicedProgram.build(graph, steps, choose_slice_labels(graph, steps, self.slices), *args)
+        return native.Program(graph, steps, *args)
+
+
+class SlicedProgram:
+    """A network contracted in 2^k slices: one program per value of k fixed
+    inner labels (network.slice_graph), whose marginals add up to the
+    network's (the whole contraction of tndecoder.jl:162).  It answers the
+    calls the decoders make on a ``native.Program``.  ``decode_packed``
+    follows tqec_decode_batch: the slices contract without their own
+    recheck, their marginals are summed (log-sum-exp), and with float32 the
+    rows whose log-margin is below twice the largest slice bound (a sum of
+    non-negative terms keeps the largest relative error of its terms) are
+    contracted again in double-float, or float64 with recheck_f64, before
+    the first maximum (Julia's findmax order) is taken."""
+
+    def __init__(self, parts, labels, precision, recheck_precision, recheck=True, margin=-1.0):
+        self.parts = list(parts)
+        self.labels = list(labels)
+        self.precision = precision
+        self.recheck_precision = recheck_precision
+        self.recheck = recheck
+        self.margin = margin
+        self.last_recheck = 0
+        info = dict(self.parts[0].info)
+        for key in ("err_bound_f32", "err_bound_f64", "err_bound_f32x2", "arena_elems", "width"):
+            if key in info:
+                info[key] = max(p.info[key] for p in self.parts)
+        info["flops_per_syndrome"] = sum(p.info["flops_per_syndrome"] for p in self.parts)
+        info["slices"] = len(self.parts)
+        self.info = info
+
+    @classmethod
+    def build(cls, graph, steps, labels, precision, flags, device=0, group=0, threads=0, margin=-1.0, big_elems=0):
+        parts = []
+        try:
+            for v in range(1 << len(labels)):
+                parts.append(native.Program(slice_graph(graph, labels, v), steps, precision,
+                                            flags | native.TQEC_FLAG_NORECHECK, device, group, threads, margin,
+                                            big_elems))
+        except Exception:
+            for p in parts:
+                p.close()
+            raise
+        recheck = precision == native.TQEC_F32 and not flags & native.TQEC_FLAG_NORECHECK
+        rp = native.TQEC_F64 if flags & native.TQEC_FLAG_RECHECK_F64 else native.TQEC_F32X2
+        return cls(parts, labels, precision, rp, recheck, margin)
+
+    @property
+    def n_classes(self):
+        return self.parts[0].n_classes
+
+    @property
+    def syndrome_bytes(self):
+        return self.parts[0].syndrome_bytes
+
+    def contract_packed(self, packed, precision, logp=None):
+        lps = np.stack([p.contract_packed(packed, precision) for p in self.parts])
+        top = lps.max(axis=0)
+        safe = np.where(np.isfinite(top), top, 0.0)
+        with np.errstate(divide="ignore"):
+            out = safe + np.log(np.exp(lps - safe).sum(axis=0))
+        out[~np.isfinite(top)] = -np.inf
+        if logp is not None:
+            logp[...] = out
+            return logp
+        return out
+
+    def _bound(self, precision):
+        key = {native.TQEC_F32: "err_bound_f32", native.TQEC_F64: "err_bound_f64",
+               native.TQEC_F32X2: "err_bound_f32x2"}[precision]
+        return self.info[key]
+
+    def decode_packed(self, packed, classes=None, logp=None, err=None, stream=None):
+        packed = np.ascontiguousarray(packed, dtype=np.uint8)
+        n = packed.shape[0]
+        lp = self.contract_packed(packed, self.precision)
+        bound = np.full(n, self._bound(self.precision))
+        self.last_recheck = 0
+        if self.recheck and n and self.n_classes > 1:
+            thr = self.margin if self.margin >= 0 else 2.0 * self._bound(self.precision)
+            top2 = np.sort(lp, axis=1)[:, -2:]
+            with np.errstate(invalid="ignore"):
+                low = ~(top2[:, 1] - top2[:, 0] >= thr) | (top2[:, 1] == -np.inf)
+            rows = np.flatnonzero(low)
+            if rows.size:
+                lp[rows] = self.contract_packed(packed[rows], self.recheck_precision)
+                bound[rows] = self._bound(self.recheck_precision)
+            self.last_recheck = int(rows.size)
+        cls = np.argmax(lp, axis=1).astype(np.int32)  # first maximum; a row of -inf gives 0
+        if classes is None:
+            classes = cls
+        else:
+            classes[...] = cls
+        if logp is not None:
+            logp[...] = lp
+        if err is not None:
+            err[...] = bound
+        return classes
+
+    def last_recheck_count(self):
+        return self.last_recheck
+
+    def autotune(self, n_probe=4096):
+        for p in self.parts:
+            p.autotune(n_probe)
+
+    def close(self):
+        for p in self.parts:
+            p.close()
 
 
 class CompiledTNMMAP:
@@ -167,9 +288,7 @@ class CompiledTNMMAP:
         self.lx, self.lz = gf2.logical_operator(tanner)
         self.graph = tnmmap_css_graph(tanner, em, self.lx, self.lz)
         self.steps = optimize_code(self.graph, decoder.optimizer)
-        self.program = native.Program(self.graph, self.steps, decoder._native_precision(), decoder._flags(),
-                                      decoder.device, decoder.group, decoder.threads, decoder.margin,
-                                      decoder.big_elems)
+        self.program = decoder._program(self.graph, self.steps)
         self._px = gf2.solve_particular(tanner.stgz.H)   # ex from sz
         self._pz = gf2.solve_particular(tanner.stgx.H)   # ez from sx
         self.k = self.lx.shape[0]
@@ -266,9 +385,7 @@ class CompiledDEMTNMMAP:
         self.graph = tnmmap_dem_graph(self.tanner, self.l2q, dem.error_rates, len(dem.logical_list),
                                       decoder.factorize)
         self.steps = optimize_code(self.graph, decoder.optimizer)
-        self.program = native.Program(self.graph, self.steps, decoder._native_precision(), decoder._flags(),
-                                      decoder.device, decoder.group, decoder.threads, decoder.margin,
-                                      decoder.big_elems)
+        self.program = decoder._program(self.graph, self.steps)
         self._part = gf2.solve_particular(self.tanner.H)
         self._logical_fix = self._logical_corrections()
 

@@ -173,3 +173,87 @@ def reduce2general(tanner, em):
         px, py, pz = float(em.px[i]), float(em.py[i]), float(em.pz[i])
         ts.append(np.array([1 - px - py - pz, px, pz, py], dtype=np.float64))
     return general, ixs, ts
+
+
+# ---------------------------------------------------------------------------
+# sliced contraction: fixing a few inner labels splits one wide contraction
+# into 2^k narrower ones whose marginals add up to the original
+# ---------------------------------------------------------------------------
+
+
+def slice_graph(graph: FactorGraph, labels, value: int) -> FactorGraph:
+    """The network with label ``labels[j]`` fixed to bit j of ``value``:
+    every tensor carrying a fixed label keeps only the entries with that
+    index (the label disappears; a tensor that loses every label becomes a
+    scalar).  Summing the marginals of all 2^k slices gives the marginal of
+    ``graph``.  Output labels and the labels of syndrome leaves cannot be
+    fixed."""
+    fixed = {int(l): (value >> j) & 1 for j, l in enumerate(labels)}
+    synd_labels = {v for p in graph.syndrome_positions for v in graph.ixs[p]}
+    bad = set(fixed) & (set(graph.iy) | synd_labels)
+    if bad:
+        raise ValueError(f"labels {sorted(bad)} are outputs or syndrome labels")
+    ixs, tensors = [], []
+    for ix, t in zip(graph.ixs, graph.tensors):
+        t = np.asarray(t, dtype=np.float64)
+        if not any(v in fixed for v in ix):
+            ixs.append(list(ix))
+            tensors.append(t)
+            continue
+        arr = t.reshape((2,) * len(ix), order="F") if ix else t.reshape(())
+        index = tuple(fixed[v] if v in fixed else slice(None) for v in ix)
+        ixs.append([v for v in ix if v not in fixed])
+        tensors.append(np.ascontiguousarray(arr[index]).ravel(order="F"))
+    return FactorGraph(ixs, tensors, list(graph.iy), list(graph.syndrome_positions), graph.map_mode)
+
+
+def step_label_sets(graph: FactorGraph, steps):
+    """Per tree step: (labels of the step's product, labels of its result).
+    The result keeps a label while a tensor outside the subtree or the
+    output still carries it."""
+    total = {}
+    for ix in graph.ixs:
+        for v in ix:
+            total[v] = total.get(v, 0) + 1
+    for v in graph.iy:
+        total[v] = total.get(v, 0) + 1
+    n = graph.n_tensors
+    count = [dict() for _ in range(n + len(steps))]
+    keep = [set(ix) for ix in graph.ixs] + [set() for _ in steps]
+    for i, ix in enumerate(graph.ixs):
+        for v in ix:
+            count[i][v] = count[i].get(v, 0) + 1
+    out = []
+    for s, (a, b) in enumerate(np.asarray(steps, dtype=np.int64).reshape(-1, 2)):
+        c = dict(count[a])
+        for v, k in count[b].items():
+            c[v] = c.get(v, 0) + k
+        union = keep[a] | keep[b]
+        res = {v for v in union if c[v] < total[v]}
+        count[n + s] = c
+        keep[n + s] = res
+        out.append((union, res))
+    return out
+
+
+def choose_slice_labels(graph: FactorGraph, steps, k: int):
+    """k labels to fix, chosen greedily: each time the label that occurs in
+    the most of the widest step products (outputs and syndrome labels
+    excluded), which narrows the widest steps first."""
+    synd_labels = {v for p in graph.syndrome_positions for v in graph.ixs[p]}
+    banned = set(graph.iy) | synd_labels
+    chosen = []
+    for _ in range(k):
+        g = slice_graph(graph, chosen, 0) if chosen else graph
+        sets = step_label_sets(g, steps)
+        widest = max(len(u) for u, _ in sets)
+        score = {}
+        for u, _ in sets:
+            if len(u) >= widest - 1:
+                for v in u:
+                    if v not in banned and v not in chosen:
+                        score[v] = score.get(v, 0) + (2 if len(u) == widest else 1)
+        if not score:
+            break
+        chosen.append(max(sorted(score), key=lambda v: score[v]))
+    return chosen
