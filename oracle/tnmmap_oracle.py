@@ -556,9 +556,10 @@ def dem2tanner(dem: DEM) -> TannerGraph:
 
 
 def _push_check_node(ixs, tensors, c, node, nvars, factorize):
-    """tndecoder.jl:221-238."""
+    """tndecoder.jl:221-238 (a check over fewer than three bits is one
+    parity tensor: the reference's chain fails on a single-bit check)."""
     L = len(c)
-    if not factorize or L == 2:
+    if not factorize or L <= 2:
         ixs.append(list(c) + [node])
         tensors.append(parity_check_matrix(L))
     else:

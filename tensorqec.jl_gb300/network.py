@@ -93,9 +93,11 @@ def tnmmap_css_graph(tanner, em, lx, lz) -> FactorGraph:
 
 def push_check_node(ixs, tensors, c, node, nvars, factorize):
     """tndecoder.jl:221-238: a parity check over bits c and label `node`,
-    optionally as a chain of rank-3 parity tensors over new labels."""
+    optionally as a chain of rank-3 parity tensors over new labels.  A check
+    over fewer than three bits is one parity tensor either way (the
+    reference's chain reads c[2] and fails on a check over a single bit)."""
     L = len(c)
-    if not factorize or L == 2:
+    if not factorize or L <= 2:
         ixs.append(list(c) + [node])
         tensors.append(parity_tensor(L + 1))
         return nvars

@@ -249,3 +249,30 @@ def test_simple_syndrome_rows(pkg):
     np.testing.assert_array_equal(simple_rows([pkg.SimpleSyndrome(r) for r in want]), want)
     np.testing.assert_array_equal(simple_rows(pkg.SimpleSyndrome(want[2])), want[2:3])
     np.testing.assert_array_equal(simple_rows(want), want)
+
+
+def test_dem_with_single_mechanism_checks(pkg, oracle):
+    """A detector and a logical flipped by one mechanism each: the factorised
+    network keeps them as single parity tensors, and the compiled program
+    reproduces the enumeration over all mechanism subsets."""
+    from plan_emulator import run_plan
+
+    text = "error(0.1) D0 D1\nerror(0.2) D1\nerror(0.05) D0 L0\nerror(0.15) D2 D1 D0\nerror(0.3) D1 D0\n"
+    dem = pkg.parse_dem_string(text)
+    t = pkg.dem2tanner(dem)
+    g = pkg.tnmmap_dem_graph(t, pkg.logical_map(dem), dem.error_rates, 1, True)
+    plan = pkg.native.inspect_plan(g, pkg.optimize_code(g, pkg.TreeSA(trials=2, sweeps=50)))
+    bits = ((np.arange(8)[:, None] >> np.arange(3)[None, :]) & 1).astype(np.uint8)
+    got = run_plan(plan, bits)
+    p = np.array(dem.error_rates)
+    want = np.zeros((8, 2))
+    for m in range(1 << 5):
+        e = (m >> np.arange(5)) & 1
+        prob = np.prod(np.where(e == 1, p, 1 - p))
+        det = sum(((sum(e[j] for j, f in enumerate(dem.flipped_detectors) if d in f) % 2) << (d - 1))
+                  for d in (1, 2, 3))
+        lg = sum(e[j] for j, f in enumerate(dem.flipped_detectors) if 4 in f) % 2
+        want[det, lg] += prob
+    np.testing.assert_allclose(got, want, rtol=1e-12, atol=1e-300)
+    dec = oracle.OracleDEMDecoder(oracle.parse_dem_string(text))
+    np.testing.assert_allclose(dec.marginals(bits), want, rtol=1e-12, atol=1e-300)
