@@ -40,3 +40,16 @@ def gpu_available():
         return torch.cuda.is_available()
     except Exception:
         return False
+
+
+@pytest.fixture
+def emulated(pkg, monkeypatch):
+    """``native.Program`` replaced by the numpy emulator of the compiled
+    program, so the decoder classes run on the CPU (the product itself has
+    no CPU path: this stand-in exists only in the tests)."""
+    import tensorqec_gb300.native as native
+    from plan_emulator import EmulatedProgram
+
+    EmulatedProgram.instances = []
+    monkeypatch.setattr(native, "Program", EmulatedProgram)
+    return EmulatedProgram

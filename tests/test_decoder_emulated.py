@@ -1,0 +1,116 @@
+"""The Python mirror of the reference's decoder API (compile / decode,
+src/decoding/interfaces.jl:74-119, tndecoder.jl) on the CPU: the GPU
+program is replaced by the numpy emulator of the same compiled program
+(the ``emulated`` fixture), so what runs here is the host side a user calls
+— network building, order search, planning, syndrome rows, class choice,
+error patterns, DEM and TNMAP decoding — against the oracle.  The same
+calls on the GPU are covered by the gpu-marked tests.
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+
+def _kat():
+    with open(os.path.join(os.path.dirname(__file__), "golden", "reference_kat.json")) as f:
+        return json.load(f)
+
+
+@pytest.mark.parametrize("precision", ["f64", "f32"])
+def test_css_decode_batch_decode_and_patterns(pkg, oracle, emulated, precision):
+    t = pkg.tanner_graph(pkg.SurfaceCode(5, 5))
+    em = pkg.depolarizing(0.08, t.nq)
+    ct = pkg.compile(pkg.TNMMAP(precision=precision, optimizer=pkg.TreeSA(trials=4, sweeps=200, restarts=1)), t, em)
+    ep = pkg.random_error_pattern(em, np.random.default_rng(8), nsamples=200)
+    syn = pkg.syndrome_extraction(ep, t)
+    want = oracle.OracleDecoder(oracle.css_tanner(*oracle.surface_code_stabilizers(5, 5)), em.px, em.py,
+                                em.pz).marginals(np.concatenate([syn.sx, syn.sz], axis=1))
+    cls, lp = ct.decode_batch(syn, return_logp=True)   # the batched CSSSyndrome itself
+    np.testing.assert_allclose(np.exp(lp), want, rtol=1e-10, atol=1e-12 * want.max())
+    top = want.max(axis=1)
+    assert (want[np.arange(len(cls)), cls] >= top * (1 - 1e-9)).all()
+    lx, lz = pkg.logical_operator(t)
+    for i in range(10):
+        s = pkg.CSSSyndrome(syn.sx[i], syn.sz[i])
+        res = pkg.decode(ct, s)
+        assert res.success_tag and pkg.syndrome_extraction(res.error_pattern, t) == s
+        # the decoded pattern lies in the decoded class: no logical error against
+        # the class representative the decoder reports
+        e = res.error_pattern
+        a = (lx.astype(int) @ e.zerror) % 2
+        b = (lz.astype(int) @ e.xerror) % 2
+        assert int(a[0]) + 2 * int(b[0]) == cls[i]
+
+
+def test_reference_x1_decision_kat_through_the_api(pkg, oracle, emulated):
+    """test/decoding/tndecoder.jl:60-73: X on qubit 1 with px=0.1 decodes to
+    no logical error.  With px=0.26 on qubits 2 and 3 the reference's TNMAP
+    decodes it into a logical error (:75-85, test_map.py); TNMMAP does too,
+    since its marginal sums every error of a class and the class of X2 X3
+    outweighs that of X1 — the decision equals the oracle's argmax."""
+    t = pkg.tanner_graph(pkg.SurfaceCode(3, 3))
+    lx, lz = pkg.logical_operator(t)
+    ex = np.zeros(9, np.uint8)
+    ex[0] = 1
+    truth = pkg.CSSErrorPattern(ex, np.zeros(9, np.uint8))
+    syn = pkg.syndrome_extraction(truth, t)
+    ot = oracle.css_tanner(*oracle.surface_code_stabilizers(3, 3))
+    for p23, logical_error in ((0.1, False), (0.26, True)):
+        px = np.full(9, 0.1)
+        px[1] = px[2] = p23
+        em = pkg.IndependentDepolarizingError(px, np.zeros(9), np.zeros(9))
+        res = pkg.decode(pkg.TNMMAP(precision="f64"), t, syn, em)
+        assert res.success_tag and pkg.syndrome_extraction(res.error_pattern, t) == syn
+        assert bool(pkg.check_logical_error(res.error_pattern, truth, lx, lz)) == logical_error
+        want = oracle.OracleDecoder(ot, px, 0.0, 0.0).marginal(syn.bits())
+        e = res.error_pattern
+        assert int((lz.astype(int) @ e.xerror)[0] % 2) * 2 == int(np.argmax(want))
+
+
+def test_dem_decode_every_syndrome(pkg, oracle, emulated):
+    """The reference's dem.dem (tndecoder.jl:112-121 decodes one sample of
+    it): every detector pattern's class against the oracle, and the error
+    pattern reproduces the detectors with the decoded logical flips."""
+    text = _kat()["dem_small"]["text"]
+    dem = pkg.parse_dem_string(text)
+    ct = pkg.compile(pkg.TNMMAP(precision="f64", optimizer=pkg.TreeSA(trials=4, sweeps=100)), dem)
+    nd = len(dem.detector_list)
+    bits = ((np.arange(1 << nd)[:, None] >> np.arange(nd)[None, :]) & 1).astype(np.uint8)
+    want = oracle.OracleDEMDecoder(oracle.parse_dem_string(text)).marginals(bits)
+    cls = ct.decode_batch([pkg.SimpleSyndrome(b) for b in bits])
+    possible = want.max(axis=1) > 0
+    assert (cls[possible] == np.argmax(want[possible], axis=1)).all()
+    t = pkg.dem2tanner(dem)
+    l2q = pkg.logical_map(dem)
+    for r in np.flatnonzero(possible)[:16]:
+        res = ct.decode(pkg.SimpleSyndrome(bits[r]))
+        assert res.success_tag
+        e = np.asarray(res.error_pattern)
+        np.testing.assert_array_equal(pkg.syndrome_extraction(e, t).s, bits[r])
+        flips = sum((int(e[np.array(l) - 1].sum()) % 2) << i for i, l in enumerate(l2q))
+        assert flips == cls[r]
+
+
+def test_tnmap_css_decode(pkg, oracle, emulated):
+    """compile(TNMAP(), tanner, em) and decode (tndecoder.jl:33-57 through
+    reduce2general): the configuration reproduces the syndrome and is a most
+    probable one."""
+    from tensorqec_gb300 import network
+
+    t = pkg.tanner_graph(pkg.SurfaceCode(3, 3))
+    em = pkg.iid_error(0.05, 0.06, 0.1, t.nq)
+    ct = pkg.compile(pkg.TNMAP(), t, em)
+    ep = pkg.random_error_pattern(em, np.random.default_rng(2), nsamples=12)
+    syn = pkg.syndrome_extraction(ep, t)
+    general, ixs, ts = network.reduce2general(t, em)
+    bits = np.concatenate([syn.sx, syn.sz], axis=1)
+    best = oracle.most_probable_configs(general.H, ixs, ts, bits)
+    for r in range(12):
+        s = pkg.CSSSyndrome(syn.sx[r], syn.sz[r])
+        res = pkg.decode(ct, s)
+        assert pkg.syndrome_extraction(res.error_pattern, t) == s
+        cfg = np.concatenate([res.error_pattern.xerror, res.error_pattern.zerror])[None, :]
+        got = oracle.config_log_probability(ixs, ts, cfg)[0]
+        assert abs(got - best[r][0]) <= 1e-12 * abs(best[r][0])

@@ -16,60 +16,6 @@ import pytest
 
 from plan_emulator import run_plan
 
-U32, U64, UX2 = 2.0 ** -24, 2.0 ** -53, 2.0 ** -43
-
-
-class EmulatedProgram:
-    """The calls the decoders make on ``native.Program``, answered by the
-    numpy emulator of the compiled program (float32 or float64)."""
-
-    instances = []
-
-    def __init__(self, graph, steps, precision=1, flags=0, device=0, group=0, threads=0, margin=-1.0,
-                 big_elems=0):
-        import tensorqec_gb300.native as native
-
-        self.plan = native.inspect_plan(graph, steps)
-        t = self.plan["err_terms"] * 1.01
-        self.info = {"err_bound_f32": U32 * t, "err_bound_f64": U64 * t, "err_bound_f32x2": UX2 * t,
-                     "flops_per_syndrome": self.plan["flops_per_syndrome"], "arena_elems": self.plan["arena_elems"],
-                     "width": self.plan["width"], "n_classes": self.plan["n_classes"],
-                     "syndrome_bytes": (self.plan["n_syndrome"] + 7) // 8}
-        self.precision, self.flags = precision, flags
-        self.calls = []
-        EmulatedProgram.instances.append(self)
-
-    @property
-    def n_classes(self):
-        return self.plan["n_classes"]
-
-    @property
-    def syndrome_bytes(self):
-        return self.info["syndrome_bytes"]
-
-    def contract_packed(self, packed, precision, logp=None):
-        self.calls.append((precision, packed.shape[0]))
-        bits = np.unpackbits(np.atleast_2d(packed), axis=1, count=self.plan["n_syndrome"], bitorder="little")
-        m = run_plan(self.plan, bits, dtype=np.float32 if precision == 1 else np.float64).astype(np.float64)
-        with np.errstate(divide="ignore"):
-            out = np.log(m)
-        if logp is not None:
-            logp[...] = out
-            return logp
-        return out
-
-    def close(self):
-        pass
-
-
-@pytest.fixture
-def emulated(pkg, monkeypatch):
-    import tensorqec_gb300.native as native
-
-    EmulatedProgram.instances = []
-    monkeypatch.setattr(native, "Program", EmulatedProgram)
-    return EmulatedProgram
-
 
 def _surface(pkg, d, p, n, seed):
     t = pkg.tanner_graph(pkg.SurfaceCode(d, d))
