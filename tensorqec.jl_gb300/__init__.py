@@ -11,7 +11,7 @@ from .codes import (BivariateBicycleCode, Code422, Code832, Code1573, Color488, 
                     PauliString, ShorCode, SimpleTannerGraph, SteaneCode, SurfaceCode, ToricCode,
                     remove_linear_dependency, stabilizers, tanner_graph)
 from .decoder import (CompiledDEMTNMMAP, CompiledGeneralTNMAP, CompiledTNMAP, CompiledTNMMAP, GreedyMethod,
-                      NoOptimizer, TNMAP, TNMMAP, TreeSA, compile, decode, optimize_code)
+                      NoOptimizer, TNMAP, TNMMAP, TreeSA, compile, decode, multi_round_qec, optimize_code)
 from .dem import DetectorErrorModel, dem2tanner, logical_map, parse_dem_file, parse_dem_string, sample_dem
 from .error_model import (CSSErrorPattern, CSSSyndrome, DecodingResult, IndependentDepolarizingError,
                           IndependentFlipError, SimpleSyndrome, check_logical_error, depolarizing, iid_error,

@@ -17,7 +17,8 @@ from . import gf2, native
 from .codes import CSSTannerGraph, SimpleTannerGraph
 from .dem import DetectorErrorModel, dem2tanner, logical_map
 from .error_model import (CSSErrorPattern, CSSSyndrome, DecodingResult, IndependentDepolarizingError,
-                          IndependentFlipError, SimpleSyndrome, iid_error, pack_syndromes)
+                          IndependentFlipError, SimpleSyndrome, iid_error, pack_syndromes, random_error_pattern,
+                          syndrome_extraction)
 from .network import (FactorGraph, choose_slice_labels, reduce2general, slice_graph, tnmap_graph, tnmmap_css_graph,
                       tnmmap_dem_graph)
 
@@ -607,5 +608,43 @@ def decode(ct_or_decoder, *args):
     ct = compile(decoder, tanner, em)
     try:
         return ct.decode(syndrome)
+    finally:
+        ct.close()
+
+
+def multi_round_qec(tanner, decoder, em, rounds=10, rng=None, batch=1 << 16):
+    """multi_round_qec(tanner, decoder, em; rounds) (threshold.jl:1-19):
+    samples `rounds` errors, decodes their syndromes and returns the rates
+    of (X-type logical errors, Z-type logical errors, any logical error).
+    Rounds are decoded in batches; a round is a logical error of a type when
+    the decoded class differs from the sampled error's class in that type's
+    bits (the reference's CSS check_logical_error, error_model.jl:161-181:
+    lz . ex for X errors, lx . ez for Z errors).  The reference's loop checks
+    the differences against the stabiliser matrices instead; the logical
+    operators are what its CSS check uses."""
+    rng = np.random.default_rng() if rng is None else rng
+    ct = compile(decoder, tanner, em)
+    try:
+        k = ct.lx.shape[0]
+        lx, lz = ct.lx.astype(np.int64), ct.lz.astype(np.int64)
+        nx = nz = nany = 0
+        done = 0
+        while done < rounds:
+            n = min(batch, rounds - done)
+            ep = random_error_pattern(em, rng, nsamples=n)
+            syn = syndrome_extraction(ep, tanner)
+            cls = np.asarray(ct.decode_batch(syn), dtype=np.int64)
+            a = (np.asarray(ep.zerror, dtype=np.int64) @ lx.T) % 2   # Z-type class bits
+            b = (np.asarray(ep.xerror, dtype=np.int64) @ lz.T) % 2   # X-type class bits
+            w = 1 << np.arange(k)
+            true_a, true_b = a @ w, b @ w
+            dec_a, dec_b = cls & ((1 << k) - 1), cls >> k
+            ex_err = dec_b != true_b
+            ez_err = dec_a != true_a
+            nx += int(ex_err.sum())
+            nz += int(ez_err.sum())
+            nany += int((ex_err | ez_err).sum())
+            done += n
+        return nx / rounds, nz / rounds, nany / rounds
     finally:
         ct.close()

@@ -114,3 +114,32 @@ def test_tnmap_css_decode(pkg, oracle, emulated):
         cfg = np.concatenate([res.error_pattern.xerror, res.error_pattern.zerror])[None, :]
         got = oracle.config_log_probability(ixs, ts, cfg)[0]
         assert abs(got - best[r][0]) <= 1e-12 * abs(best[r][0])
+
+
+def test_multi_round_qec(pkg, oracle, emulated):
+    """multi_round_qec (threshold.jl:1-19) over batches: the X, Z and total
+    logical error rates equal those of the oracle's argmax decisions on the
+    same sampled errors (same seed)."""
+    t = pkg.tanner_graph(pkg.SurfaceCode(3, 3))
+    em = pkg.depolarizing(0.1, t.nq)
+    dec = pkg.TNMMAP(precision="f64", optimizer=pkg.TreeSA(trials=2, sweeps=50, restarts=1))
+    rates = pkg.multi_round_qec(t, dec, em, rounds=500, rng=np.random.default_rng(4), batch=128)
+    rng = np.random.default_rng(4)
+    ot = oracle.css_tanner(*oracle.surface_code_stabilizers(3, 3))
+    od = oracle.OracleDecoder(ot, em.px, em.py, em.pz)
+    nx = nz = nany = ties = 0
+    for n in (128, 128, 128, 116):
+        ep = pkg.random_error_pattern(em, rng, nsamples=n)
+        s = pkg.syndrome_extraction(ep, t)
+        mar = od.marginals(np.concatenate([s.sx, s.sz], axis=1))
+        cls = np.argmax(mar, axis=1)
+        srt = np.sort(mar, axis=1)
+        ties += int((srt[:, -1] - srt[:, -2] <= 1e-9 * srt[:, -1]).sum())
+        a = (ep.zerror.astype(int) @ od.lx.T.astype(int))[:, 0] % 2
+        b = (ep.xerror.astype(int) @ od.lz.T.astype(int))[:, 0] % 2
+        xe, ze = (cls >> 1) != b, (cls & 1) != a
+        nx, nz, nany = nx + xe.sum(), nz + ze.sum(), nany + (xe | ze).sum()
+    # rows whose top two classes tie may resolve either way
+    for got, want in zip(rates, (nx, nz, nany)):
+        assert abs(got * 500 - want) <= ties
+    assert 0 < rates[2] < 0.5 and ties < 100
