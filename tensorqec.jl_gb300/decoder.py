@@ -612,38 +612,53 @@ def decode(ct_or_decoder, *args):
         ct.close()
 
 
-def multi_round_qec(tanner, decoder, em, rounds=10, rng=None, batch=1 << 16):
-    """multi_round_qec(tanner, decoder, em; rounds) (threshold.jl:1-19):
-    samples `rounds` errors, decodes their syndromes and returns the rates
-    of (X-type logical errors, Z-type logical errors, any logical error).
-    Rounds are decoded in batches; a round is a logical error of a type when
-    the decoded class differs from the sampled error's class in that type's
-    bits (the reference's CSS check_logical_error, error_model.jl:161-181:
-    lz . ex for X errors, lx . ez for Z errors).  The reference's loop checks
-    the differences against the stabiliser matrices instead; the logical
-    operators are what its CSS check uses."""
+def multi_round_qec(tanner, decoder, em, tanner_check=None, rounds=10, rng=None, batch=1 << 16, prior=None):
+    """multi_round_qec (threshold.jl:1-33): samples `rounds` errors from
+    `em`, decodes their syndromes (in batches) and returns logical error
+    rates.  Like the reference, the decoder is compiled with the default
+    noise of ``compile(decoder, tanner)`` (interfaces.jl:74-76) unless
+    `prior` gives another error model.
+
+    CSS code: returns the rates of (X-type, Z-type, any) logical errors; a
+    round counts for a type when the decoded class differs from the sampled
+    error's class in that type's bits (lz . ex for X errors, lx . ez for Z
+    errors, the CSS check_logical_error of error_model.jl:161-181; the
+    reference's loop compares against the stabiliser matrices instead).
+    Classical code (threshold.jl:21-33, a SimpleTannerGraph decoded by
+    TNMAP): returns the rate of rounds whose decoded bits differ from the
+    sampled ones by a vector with odd overlap with a row of
+    ``tanner_check.H``."""
     rng = np.random.default_rng() if rng is None else rng
-    ct = compile(decoder, tanner, em)
+    ct = compile(decoder, tanner, prior)
     try:
+        if isinstance(tanner, SimpleTannerGraph):
+            if tanner_check is None:
+                raise TypeError("a classical code needs tanner_check, the checks of a logical error")
+            Hc = np.asarray(tanner_check.H, dtype=np.int64)
+            bad = done = 0
+            while done < rounds:
+                n = min(batch, rounds - done)
+                ex = random_error_pattern(em, rng, nsamples=n)
+                syn = syndrome_extraction(ex, tanner)
+                cfg = np.asarray(ct.decode_batch(syn), dtype=np.int64)
+                bad += int((((ex.astype(np.int64) - cfg) % 2) @ Hc.T % 2).any(axis=1).sum())
+                done += n
+            return bad / rounds
         k = ct.lx.shape[0]
         lx, lz = ct.lx.astype(np.int64), ct.lz.astype(np.int64)
-        nx = nz = nany = 0
-        done = 0
+        w = 1 << np.arange(k)
+        nx = nz = nany = done = 0
         while done < rounds:
             n = min(batch, rounds - done)
             ep = random_error_pattern(em, rng, nsamples=n)
-            syn = syndrome_extraction(ep, tanner)
-            cls = np.asarray(ct.decode_batch(syn), dtype=np.int64)
-            a = (np.asarray(ep.zerror, dtype=np.int64) @ lx.T) % 2   # Z-type class bits
-            b = (np.asarray(ep.xerror, dtype=np.int64) @ lz.T) % 2   # X-type class bits
-            w = 1 << np.arange(k)
-            true_a, true_b = a @ w, b @ w
-            dec_a, dec_b = cls & ((1 << k) - 1), cls >> k
-            ex_err = dec_b != true_b
-            ez_err = dec_a != true_a
-            nx += int(ex_err.sum())
-            nz += int(ez_err.sum())
-            nany += int((ex_err | ez_err).sum())
+            cls = np.asarray(ct.decode_batch(syndrome_extraction(ep, tanner)), dtype=np.int64)
+            true_a = ((np.asarray(ep.zerror, dtype=np.int64) @ lx.T) % 2) @ w   # Z-type class bits
+            true_b = ((np.asarray(ep.xerror, dtype=np.int64) @ lz.T) % 2) @ w   # X-type class bits
+            x_err = (cls >> k) != true_b
+            z_err = (cls & ((1 << k) - 1)) != true_a
+            nx += int(x_err.sum())
+            nz += int(z_err.sum())
+            nany += int((x_err | z_err).sum())
             done += n
         return nx / rounds, nz / rounds, nany / rounds
     finally:

@@ -123,7 +123,7 @@ def test_multi_round_qec(pkg, oracle, emulated):
     t = pkg.tanner_graph(pkg.SurfaceCode(3, 3))
     em = pkg.depolarizing(0.1, t.nq)
     dec = pkg.TNMMAP(precision="f64", optimizer=pkg.TreeSA(trials=2, sweeps=50, restarts=1))
-    rates = pkg.multi_round_qec(t, dec, em, rounds=500, rng=np.random.default_rng(4), batch=128)
+    rates = pkg.multi_round_qec(t, dec, em, rounds=500, rng=np.random.default_rng(4), batch=128, prior=em)
     rng = np.random.default_rng(4)
     ot = oracle.css_tanner(*oracle.surface_code_stabilizers(3, 3))
     od = oracle.OracleDecoder(ot, em.px, em.py, em.pz)
@@ -143,3 +143,31 @@ def test_multi_round_qec(pkg, oracle, emulated):
     for got, want in zip(rates, (nx, nz, nany)):
         assert abs(got * 500 - want) <= ties
     assert 0 < rates[2] < 0.5 and ties < 100
+
+
+def test_multi_round_qec_classical(pkg, oracle, emulated):
+    """The classical overload (threshold.jl:21-33): TNMAP on the Z checks of
+    the d=3 surface code, bit flips at 0.1, logical errors read off the
+    Z logical; with the reference's default decoding prior (0.05)."""
+    from tensorqec_gb300 import network
+
+    t = pkg.tanner_graph(pkg.SurfaceCode(3, 3))
+    lx, lz = pkg.logical_operator(t)
+    check = pkg.SimpleTannerGraph(9, [[int(q) + 1 for q in np.flatnonzero(lz[0])]])
+    em = pkg.iid_error(0.1, 9)
+    rate = pkg.multi_round_qec(t.stgz, pkg.TNMAP(), em, check, rounds=300, rng=np.random.default_rng(6), batch=100)
+    rng = np.random.default_rng(6)
+    ex = np.concatenate([pkg.random_error_pattern(em, rng, nsamples=100) for _ in range(3)])
+    syn = (ex.astype(int) @ t.stgz.H.T.astype(int)) % 2
+    ixs = [[i + 1] for i in range(9)]
+    ts = [np.array([0.95, 0.05]) for _ in range(9)]
+    best = oracle.most_probable_configs(t.stgz.H, ixs, ts, syn)
+    # most probable configurations are the minimum-weight ones; count rounds
+    # where every one of them is a logical error, and where any is
+    always = maybe = 0
+    for r in range(300):
+        errs = [int(((ex[r] + np.asarray(c)) % 2) @ lz[0] % 2) for c in best[r][1]]
+        always += all(errs)
+        maybe += any(errs)
+    assert always <= rate * 300 <= maybe
+    assert 0 < rate < 0.5
