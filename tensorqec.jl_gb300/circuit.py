@@ -318,7 +318,9 @@ def detector_error_model(circ: Circuit) -> DetectorErrorModel:
         q = merged.get(key, 0.0)
         merged[key] = q * (1 - pr) + pr * (1 - q)
     rates, flipped = [], []
-    for key, pr in sorted(merged.items()):
+    # mechanisms ordered by their detectors, then by their observables
+    for key, pr in sorted(merged.items(), key=lambda kv: (tuple(v for v in kv[0] if v <= n_det),
+                                                          tuple(v for v in kv[0] if v > n_det))):
         rates.append(pr)
         flipped.append(list(key))
     return DetectorErrorModel(rates, flipped, list(range(1, n_det + 1)),

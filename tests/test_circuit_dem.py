@@ -302,3 +302,17 @@ def test_reference_insert_errors_circuit(pkg):
     assert circuit.detectors_deterministic(twice)
     once = circuit.parse_stim_string("RX 0\nC_XYZ 0\nMX 0\nDETECTOR rec[-1]\n")
     assert not circuit.detectors_deterministic(once)
+
+
+def test_mechanism_order(pkg):
+    """Mechanisms are listed by their detectors, then by their observables,
+    so a model's factor graph (and the contraction order searched for it)
+    does not move when rates change."""
+    from tensorqec_gb300 import circuit
+
+    dm = circuit.detector_error_model(circuit.memory_z_circuit(5, 5, 0.001))
+    n_det = len(dm.detector_list)
+    keys = [(tuple(v for v in f if v <= n_det), tuple(v for v in f if v > n_det)) for f in dm.flipped_detectors]
+    assert keys == sorted(keys) and len(set(keys)) == len(keys)
+    other = circuit.detector_error_model(circuit.memory_z_circuit(5, 5, 0.003))
+    assert other.flipped_detectors == dm.flipped_detectors
