@@ -9,8 +9,7 @@
  * compile(::TNMMAP, ...) builds it (tndecoder.jl:97-139 restricted to one
  * error type): bits 1..3, checks (1,2) and (2,3) with syndrome labels 4 and
  * 5, a logical parity over bit 1 with output label 6, priors [1-p, p] per
- * bit, one-hot syndrome leaves.  The marginal it computes is checked by the
- * Python test through the same calls. */
+ * bit, one-hot syndrome leaves. */
 #include <stdio.h>
 #include <string.h>
 
