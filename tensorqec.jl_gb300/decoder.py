@@ -274,6 +274,10 @@ class SlicedProgram:
         for p in self.parts:
             p.autotune(n_probe)
 
+    def save(self, path):
+        """Each slice is its own program: ``parts[i].save`` keeps slice i."""
+        raise TypeError("a sliced program is saved slice by slice: SlicedProgram.parts[i].save(path)")
+
     def close(self):
         for p in self.parts:
             p.close()
