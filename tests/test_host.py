@@ -276,3 +276,50 @@ def test_dem_with_single_mechanism_checks(pkg, oracle):
     np.testing.assert_allclose(got, want, rtol=1e-12, atol=1e-300)
     dec = oracle.OracleDEMDecoder(oracle.parse_dem_string(text))
     np.testing.assert_allclose(dec.marginals(bits), want, rtol=1e-12, atol=1e-300)
+
+
+def _code_distance(t, lx, lz):
+    """code_distance(::CSSTannerGraph) (code_distance.jl:256-298) by
+    enumeration: the least weight of an X-type vector with even overlap with
+    every Z check and odd overlap with some row of lz, and the same for Z."""
+    from tensorqec_gb300 import gf2
+
+    best = []
+    for H, L in ((t.stgz.H, lz), (t.stgx.H, lx)):
+        ns = gf2.null_space(np.asarray(H, dtype=np.uint8)).astype(np.int64)
+        k = ns.shape[0]
+        assert k <= 16
+        combos = ((np.arange(1 << k)[:, None] >> np.arange(k)) & 1) @ ns % 2
+        odd = ((combos @ np.asarray(L, dtype=np.int64).T) % 2).any(axis=1)
+        best.append(int(combos[odd].sum(axis=1).min()))
+    return min(best)
+
+
+@pytest.mark.parametrize("name,make,n_stab,distance", [
+    ("steane", lambda p: p.SteaneCode(), 6, 3), ("shor", lambda p: p.ShorCode(), 8, 3),
+    ("1573", lambda p: p.Code1573(), 8, 3), ("832", lambda p: p.Code832(), 5, 2),
+    ("422", lambda p: p.Code422(), 2, 2), ("surface3", lambda p: p.SurfaceCode(3, 3), 8, 3),
+    ("color488_5", lambda p: p.Color488(5), 16, 5), ("color666_5", lambda p: p.Color666(5), 18, 5)])
+def test_reference_code_known_answers(pkg, name, make, n_stab, distance):
+    """test/codes/codes.jl:42-187: code distances (the reference solves an
+    integer program; here the kernel of the check matrix is enumerated) and
+    stabiliser counts (n - k; the reference asserts them for the colour
+    codes)."""
+    code = make(pkg)
+    st = pkg.stabilizers(code)
+    assert len(st) == n_stab
+    t = pkg.tanner_graph(code)
+    lx, lz = pkg.logical_operator(t)
+    assert _code_distance(t, lx, lz) == distance
+    if name == "422":  # codes.jl:127-133: XXXX then ZZZZ
+        assert [s.ops for s in st] == [(1, 1, 1, 1), (3, 3, 3, 3)]
+
+
+def test_bivariate_bicycle_98_6_12_stabilizer_count(pkg):
+    """test/codes/codes.jl:154-158."""
+    code = pkg.BivariateBicycleCode(7, 7, ((1, 0), (0, 3), (0, 4)), ((0, 1), (3, 0), (4, 0)))
+    st = pkg.stabilizers(code)
+    assert len(st) == 92
+    t = pkg.CSSTannerGraph.from_stabilizers(st)
+    lx, lz = pkg.logical_operator(t)
+    assert lx.shape == lz.shape == (6, 98)
