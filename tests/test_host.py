@@ -323,3 +323,21 @@ def test_bivariate_bicycle_98_6_12_stabilizer_count(pkg):
     t = pkg.CSSTannerGraph.from_stabilizers(st)
     lx, lz = pkg.logical_operator(t)
     assert lx.shape == lz.shape == (6, 98)
+
+
+def test_reference_error_model_known_answers(pkg):
+    """test/decoding/error_model.jl:5-40: flip rates of a depolarising
+    sample (X part px + py, Z part pz + py) and check_logical_error on the
+    d=3 surface code's logical operators."""
+    em = pkg.iid_error(0.05, 0.06, 0.1, 100000)
+    ep = pkg.random_error_pattern(em, np.random.default_rng(0))
+    assert abs(ep.xerror.mean() - 0.11) < 0.05 and abs(ep.zerror.mean() - 0.16) < 0.05
+    flips = pkg.random_error_pattern(pkg.iid_error(0.1, 10), np.random.default_rng(1))
+    assert flips.shape == (10,) and set(np.unique(flips)) <= {0, 1}
+    t = pkg.tanner_graph(pkg.SurfaceCode(3, 3))
+    lx, lz = pkg.logical_operator(t)
+    zero = np.zeros(9, np.uint8)
+    assert pkg.check_logical_error(zero, np.array([1, 1, 1, 0, 0, 0, 0, 0, 0], np.uint8), lz)
+    assert not pkg.check_logical_error(zero, np.array([1, 1, 0, 1, 1, 0, 0, 0, 0], np.uint8), lz)
+    css = pkg.CSSErrorPattern(zero, zero)
+    assert not pkg.check_logical_error(css, pkg.CSSErrorPattern(zero.copy(), zero.copy()), lx, lz)
