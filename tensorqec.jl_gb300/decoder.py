@@ -628,6 +628,8 @@ def multi_round_qec(tanner, decoder, em, tanner_check=None, rounds=10, rng=None,
     error's class in that type's bits (lz . ex for X errors, lx . ez for Z
     errors, the CSS check_logical_error of error_model.jl:161-181; the
     reference's loop compares against the stabiliser matrices instead).
+    TNMMAP decoders are judged by their classes, TNMAP decoders by the
+    difference of their decoded error from the sampled one.
     Classical code (threshold.jl:21-33, a SimpleTannerGraph decoded by
     TNMAP): returns the rate of rounds whose decoded bits differ from the
     sampled ones by a vector with odd overlap with a row of
@@ -648,18 +650,23 @@ def multi_round_qec(tanner, decoder, em, tanner_check=None, rounds=10, rng=None,
                 bad += int((((ex.astype(np.int64) - cfg) % 2) @ Hc.T % 2).any(axis=1).sum())
                 done += n
             return bad / rounds
-        k = ct.lx.shape[0]
-        lx, lz = ct.lx.astype(np.int64), ct.lz.astype(np.int64)
+        lx, lz = (m.astype(np.int64) for m in gf2.logical_operator(tanner))
+        k = lx.shape[0]
         w = 1 << np.arange(k)
         nx = nz = nany = done = 0
         while done < rounds:
             n = min(batch, rounds - done)
             ep = random_error_pattern(em, rng, nsamples=n)
-            cls = np.asarray(ct.decode_batch(syndrome_extraction(ep, tanner)), dtype=np.int64)
-            true_a = ((np.asarray(ep.zerror, dtype=np.int64) @ lx.T) % 2) @ w   # Z-type class bits
-            true_b = ((np.asarray(ep.xerror, dtype=np.int64) @ lz.T) % 2) @ w   # X-type class bits
-            x_err = (cls >> k) != true_b
-            z_err = (cls & ((1 << k) - 1)) != true_a
+            ex = np.asarray(ep.xerror, dtype=np.int64)
+            ez = np.asarray(ep.zerror, dtype=np.int64)
+            out = ct.decode_batch(syndrome_extraction(ep, tanner))
+            if isinstance(out, tuple):  # TNMAP: decoded (ex, ez) rows
+                x_err = (((ex ^ np.asarray(out[0], dtype=np.int64)) @ lz.T) % 2).any(axis=1)
+                z_err = (((ez ^ np.asarray(out[1], dtype=np.int64)) @ lx.T) % 2).any(axis=1)
+            else:  # TNMMAP: decoded classes
+                cls = np.asarray(out, dtype=np.int64)
+                x_err = (cls >> k) != ((ex @ lz.T) % 2) @ w     # X-type class bits
+                z_err = (cls & ((1 << k) - 1)) != ((ez @ lx.T) % 2) @ w   # Z-type class bits
             nx += int(x_err.sum())
             nz += int(z_err.sum())
             nany += int((x_err | z_err).sum())

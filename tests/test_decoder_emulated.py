@@ -171,3 +171,19 @@ def test_multi_round_qec_classical(pkg, oracle, emulated):
         maybe += any(errs)
     assert always <= rate * 300 <= maybe
     assert 0 < rate < 0.5
+
+
+def test_reference_threshold_calls(pkg, emulated):
+    """test/decoding/threshold.jl:5-12 with TNMAP in place of the integer
+    program decoder: the classical form (Z checks decoded, X checks as the
+    logical test) returns one rate, the CSS form three."""
+    t = pkg.tanner_graph(pkg.SurfaceCode(3, 3))
+    r = pkg.multi_round_qec(t.stgz, pkg.TNMAP(), pkg.iid_error(0.05, 9), t.stgx, rng=np.random.default_rng(123))
+    assert isinstance(r, float) and 0 <= r <= 1
+    r3 = pkg.multi_round_qec(t, pkg.TNMAP(), pkg.iid_error(0.05, 0.05, 0.05, 9), rounds=200,
+                             rng=np.random.default_rng(123))
+    assert isinstance(r3, tuple) and len(r3) == 3 and all(isinstance(x, float) for x in r3)
+    assert max(r3[0], r3[1]) <= r3[2] <= r3[0] + r3[1] and r3[2] < 0.5
+    r3m = pkg.multi_round_qec(t, pkg.TNMMAP(precision="f64"), pkg.iid_error(0.05, 0.05, 0.05, 9), rounds=200,
+                              rng=np.random.default_rng(123))
+    assert max(r3m[0], r3m[1]) <= r3m[2] <= r3m[0] + r3m[1]
