@@ -187,3 +187,23 @@ def test_reference_threshold_calls(pkg, emulated):
     r3m = pkg.multi_round_qec(t, pkg.TNMMAP(precision="f64"), pkg.iid_error(0.05, 0.05, 0.05, 9), rounds=200,
                               rng=np.random.default_rng(123))
     assert max(r3m[0], r3m[1]) <= r3m[2] <= r3m[0] + r3m[1]
+
+
+def test_reference_interface_calls(pkg, emulated):
+    """test/decoding/interfaces.jl:5-30 with TNMAP: decode(decoder, tanner,
+    syndrome) on a classical problem and compile(decoder, tanner) with the
+    default noise then decode on a CSS one both give a DecodingResult whose
+    pattern reproduces the syndrome."""
+    t = pkg.tanner_graph(pkg.SurfaceCode(3, 3))
+    e = np.array([0, 0, 0, 1, 0, 0, 0, 0, 0], np.uint8)
+    syn = pkg.syndrome_extraction(e, t.stgz)
+    res = pkg.decode(pkg.TNMAP(), t.stgz, syn)
+    assert isinstance(res, pkg.DecodingResult)
+    np.testing.assert_array_equal(pkg.syndrome_extraction(res.error_pattern, t.stgz).s, syn.s)
+    em = pkg.iid_error(0.05, 0.06, 0.1, 9)
+    ep = pkg.random_error_pattern(em, np.random.default_rng(123))
+    s = pkg.syndrome_extraction(ep, t)
+    for dec in (pkg.TNMAP(), pkg.TNMMAP(precision="f64")):
+        ct = pkg.compile(dec, t)
+        r = pkg.decode(ct, s)
+        assert isinstance(r, pkg.DecodingResult) and pkg.syndrome_extraction(r.error_pattern, t) == s
