@@ -42,6 +42,10 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--batch", type=int, default=BATCH)
+    ap.add_argument("--ref-sample", type=int, default=0,
+                    help="--impl reference: syndromes contracted per timed step (0: the whole batch)")
+    ap.add_argument("--write-order", action="store_true",
+                    help="run the longer d=7 order search and write the committed tree file")
     ap.add_argument("--cpu-sample", type=int, default=65536,
                     help="syndromes the CPU restatement decodes (timed; also the decision-mismatch sample)")
     ap.add_argument("--profile", action="store_true",
@@ -81,11 +85,68 @@ def parse():
     return ap.parse_args()
 
 
+# The d=7 workload's contraction tree, shared by every arm (batched, plain
+# float64, the CPU baseline and the reference arm): found once by a longer
+# order search than the default (TreeSA(trials=128, sweeps=8000, restarts=8,
+# seed=2): 1.23e6 flops per syndrome in 42 runtime steps against 1.41e6 in
+# 49) and committed, so that every machine contracts the same tree.
+ORDER_PATH = os.path.join(ROOT, "tensorqec.jl_gb300", "orders", "surface_d7.tree")
+CIRCUIT_ORDER_PATH = os.path.join(ROOT, "tensorqec.jl_gb300", "orders", "circuit_d5_r5.tree")
+
+
+def _circuit_search(pkg):
+    """The order search of the circuit-level workload (width target 20)."""
+    return pkg.TreeSA(trials=32, sweeps=2000, target_width=20, width_penalty=2.0, seed=1, restarts=4)
+
+
+def read_order(path=ORDER_PATH):
+    """The committed tree as an (n_tensors - 1, 2) int32 array (plain text:
+    '#' comments, then one 'a b' pair of node ids per step)."""
+    rows = [ln.split() for ln in open(path) if ln.strip() and not ln.startswith("#")]
+    return np.array([[int(a), int(b)] for a, b in rows], dtype=np.int32).reshape(-1, 2)
+
+
 def d7_order(pkg):
-    """The contraction-order search of the d=7 workload, shared by every arm
-    (batched, plain float64, CPU): a longer search than the default finds
-    1.23e6 flops per syndrome in 42 runtime steps against 1.41e6 in 49."""
-    return pkg.TreeSA(trials=128, sweeps=8000, restarts=8, seed=2)
+    """The optimizer every d=7 arm compiles with: the committed tree."""
+    return pkg.FixedOrder(read_order())
+
+
+def write_order():
+    """Runs the longer order search and writes the committed tree file."""
+    import __graft_entry__ as G
+
+    pkg = G.load_package()
+    t = pkg.tanner_graph(pkg.SurfaceCode(D, D))
+    em = pkg.depolarizing(P, t.nq)
+    lx, lz = pkg.logical_operator(t)
+    g = pkg.tnmmap_css_graph(t, em, lx, lz)
+    steps = pkg.optimize_code(g, pkg.TreeSA(trials=128, sweeps=8000, restarts=8, seed=2))
+    info = pkg.native.inspect_plan(g, steps)
+    os.makedirs(os.path.dirname(ORDER_PATH), exist_ok=True)
+    pkg.save_order(ORDER_PATH, steps,
+                   f"Contraction tree of the TNMMAP factor graph of SurfaceCode({D},{D}) (tnmmap_css_graph node ids;\n"
+                   f"the tree does not depend on p).  Found by TreeSA(trials=128, sweeps=8000, restarts=8, seed=2).\n"
+                   f"Compiled program: {info['flops_per_syndrome']:.0f} flops per syndrome, width {info['width']},\n"
+                   f"{len(info['steps'])} runtime steps.  Regenerate with: python bench.py --write-order")
+    print(json.dumps({"order": os.path.relpath(ORDER_PATH, ROOT), "flops_per_syndrome": info["flops_per_syndrome"],
+                      "width": info["width"], "runtime_steps": len(info["steps"])}))
+    # the circuit-level workload's tree (its order search takes about half a minute)
+    from tensorqec_gb300 import circuit as cz
+
+    dem = cz.detector_error_model(cz.memory_z_circuit(5, 5, 0.001))
+    g = pkg.tnmmap_dem_graph(pkg.dem2tanner(dem), pkg.logical_map(dem), dem.error_rates, len(dem.logical_list), True)
+    steps = pkg.optimize_code(g, _circuit_search(pkg))
+    info = pkg.native.inspect_plan(g, steps)
+    pkg.save_order(CIRCUIT_ORDER_PATH, steps,
+                   "Contraction tree of the factorised TNMMAP factor graph of the detector error model of the\n"
+                   "rotated Z-memory circuit d=5, 5 rounds, p=0.001 (circuit.memory_z_circuit; tnmmap_dem_graph\n"
+                   "node ids).  Found by TreeSA(trials=32, sweeps=2000, target_width=20, width_penalty=2.0, seed=1,\n"
+                   "restarts=4).\n"
+                   f"Compiled program: {info['flops_per_syndrome']:.0f} flops per sample, width {info['width']}, "
+                   f"{len(info['steps'])} runtime steps.\nRegenerate with: python bench.py --write-order")
+    print(json.dumps({"order": os.path.relpath(CIRCUIT_ORDER_PATH, ROOT),
+                      "flops_per_syndrome": info["flops_per_syndrome"], "width": info["width"],
+                      "runtime_steps": len(info["steps"])}))
 
 
 def workload(pkg, rank, nbatches, batch):
@@ -247,42 +308,54 @@ def cpu_baseline(pkg, ct, bits, sample):
 
 
 def run_reference(args):
-    import __graft_entry__ as G
-
+    """The reference's CPU path: per-syndrome float64 contraction of the
+    TNMMAP network along the committed tree, on every host core, over the
+    same seeded 65,536-syndrome batches as the GPU arm.  Built from the
+    oracle's restatement alone (network, sampler, C contractor): nothing of
+    the product library is imported or loaded here."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    pkg = G.load_package()
+    from oracle import tnmmap_oracle as O
     from oracle.c_oracle import CContractor, host_cores
 
-    t, em, bits = workload(pkg, 0, 1, max(args.cpu_sample, 256))
-    lx, lz = pkg.logical_operator(t)
-    g = pkg.tnmmap_css_graph(t, em, lx, lz)
-    steps = pkg.optimize_code(g, d7_order(pkg))
-    cc = CContractor(g.ixs, [np.asarray(x) for x in g.tensors], g.iy, g.syndrome_positions, steps)
-    per = max(64, args.cpu_sample // max(args.steps, 1))
+    stabs, nq = O.surface_code_stabilizers(D, D)
+    ot = O.css_tanner(stabs, nq)
+    p3 = P / 3.0
+    net = O.tnmmap_network(ot, p3, p3, p3)
+    cc = CContractor(net.ixs, net.tensors, net.iy, net.syndrome_positions, read_order())
     cores = host_cores()
-    packed = pkg.pack_syndromes(bits[0])
-    for w in range(args.warmup):
-        cc.contract(packed[:min(per, 256)], threads=cores)
+    B = args.batch
+    per = args.ref_sample if args.ref_sample > 0 else B
+    # the GPU arm's batches: the host stream of rank 0, one batch per step
+    rng = np.random.default_rng(SEED)
+
+    def batch():
+        pq = np.full(nq, p3)
+        ex, ez = O.sample_depolarizing(rng, pq, pq, pq, B)
+        sx, sz = O.syndrome_extraction(ex, ez, ot)
+        return np.packbits(np.concatenate([sx, sz], axis=1), axis=1, bitorder="little")
+
+    for _ in range(args.warmup):
+        cc.contract(batch()[:256], threads=cores)  # untimed: a short sample of each warm-up batch
     times = []
-    for s in range(args.steps):
-        lo = (s * per) % max(len(packed) - per, 1)
+    for _ in range(args.steps):
+        packed = batch()[:per]
         t0 = time.perf_counter()
-        cc.contract(packed[lo:lo + per], threads=cores)
+        cc.contract(packed, threads=cores)
         times.append(time.perf_counter() - t0)
     total = sum(times)
     value = per * args.steps / total
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "syndromes/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic (seeded depolarizing errors)",
-            # the workload of the GPU arm; each timed step contracts a bounded sample of it
-            "config": dict(config(args.batch), decoder="float64 per-syndrome tree contraction on all host cores",
-                           sample_per_step=per),
+            "data": "synthetic (seeded depolarizing errors, numpy PCG64, the GPU arm's batches)",
+            "config": dict(config(B), decoder="float64 per-syndrome tree contraction on all host cores",
+                           syndromes_per_step=per),
             "cpu_baseline": {"value": value, "unit": "syndromes/s", "cores": cores, "kind": "port",
-                             "sample": f"{per} syndromes per step, float64 per-syndrome tree contraction "
-                                       f"(CPU restatement; Julia/OMEinsum not runnable here)"},
+                             "sample": f"{per} syndromes per step (the whole batch), float64 per-syndrome tree "
+                                       f"contraction along the committed d={D} tree (CPU restatement of TNMMAP; "
+                                       f"Julia/OMEinsum not runnable here)"},
             "e2e": {"value": value, "unit": "syndromes/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -404,6 +477,7 @@ def run_ours(args):
         dist.barrier()
     step_ms = sum(ms) / K
     fallback = gd.last_fallback if gd is not None else B
+    step_rechecks = ct.program.last_recheck_count()  # of the last timed step's exact rows
 
     # ---- the batched exact decoder alone (float32 + double-float recheck) -------
     tn_ms = timed(lambda i: ct.program.decode_ptrs(d_syn[W + i].data_ptr(), B, d_cls.data_ptr(), None, None, sptr),
@@ -411,7 +485,7 @@ def run_ours(args):
     tn_rate = B / (statistics.median(tn_ms) / 1e3)
     rechecks = ct.program.last_recheck_count()
 
-    # ---- roofline: the float32 contraction kernel alone --------------------
+    # ---- the float32 contraction kernel alone, on the full batch -----------
     d_lp = torch.empty((B, info["n_classes"]), dtype=torch.float64, device="cuda")
     kms = timed(lambda i: ct.program.contract_ptrs(d_syn[W + i].data_ptr(), B, pkg.native.TQEC_F32,
                                                    d_lp.data_ptr(), sptr), range(min(K, 5)))
@@ -419,6 +493,23 @@ def run_ours(args):
     flops = info["flops_per_syndrome"]
     achieved_tflops = flops * B / (kernel_ms / 1e3) / 1e12
     bf16_peak, hbm_peak, peak_kind = peaks()
+
+    # ---- the contraction launches of the gated step, each alone on the same
+    # row counts as the last timed step: float32 over its exact rows, the
+    # recheck arithmetic over its rechecked rows (CUDA events, L2 flushed)
+    step_parts = []
+    if gd is not None and fallback > 0:
+        fms = timed(lambda i: ct.program.contract_ptrs(d_syn[W + i].data_ptr(), fallback, pkg.native.TQEC_F32,
+                                                       d_lp.data_ptr(), sptr), range(min(K, 5)))
+        step_parts.append(("tn_contract_kernel<float> over the rows the gate rejects", fallback,
+                           statistics.median(fms)))
+    if step_rechecks > 0:
+        rp = info["recheck_precision"]
+        rname = "tn_contract_kernel<dfloat>" if rp == pkg.native.TQEC_F32X2 else "tn_contract_kernel<double>"
+        rms = timed(lambda i: ct.program.contract_ptrs(d_syn[W + i].data_ptr(), step_rechecks, rp,
+                                                       d_lp.data_ptr(), sptr), range(min(K, 5)))
+        step_parts.append((f"{rname}, the recheck of the rows inside the float32 bound", step_rechecks,
+                           statistics.median(rms)))
 
     # the surrogate's forward pass alone (tensor-core GEMMs)
     mlp_part = None
@@ -452,12 +543,18 @@ def run_ours(args):
 
     # ---- plain float64 form: one launch per syndrome (drop-in baseline) ----
     plain = pkg.compile(pkg.TNMMAP(precision="f64", plain=True, device=local, optimizer=d7_order(pkg)), t, em)
-    m = 128
-    plain.program.decode_ptrs(d_syn[0].data_ptr(), 8, d_cls.data_ptr(), None, None, sptr)
+    m = 1024
+    for _ in range(3):
+        plain.program.decode_ptrs(d_syn[0].data_ptr(), 8, d_cls.data_ptr(), None, None, sptr)
     torch.cuda.synchronize()
-    pms = timed(lambda i: plain.program.decode_ptrs(d_syn[0].data_ptr(), m, d_cls.data_ptr(), None, None, sptr),
-                range(1))
-    plain_rate = m / (pms[0] / 1e3)
+    pms = timed(lambda i: plain.program.decode_ptrs(d_syn[0].data_ptr() + i * m * packed[0].shape[1], m,
+                                                    d_cls.data_ptr(), None, None, sptr), range(3))
+    plain_rate = m / (statistics.median(pms) / 1e3)
+    # one decode call of one syndrome, as the drop-in caller makes it (CUDA events around the call)
+    one = timed(lambda i: plain.program.decode_ptrs(d_syn[1].data_ptr() + i * packed[1].shape[1], 1,
+                                                    d_cls.data_ptr(), None, None, sptr), range(200))
+    plain_latency_us = {"p50": 1e3 * float(np.percentile(one, 50)), "p99": 1e3 * float(np.percentile(one, 99)),
+                        "calls": len(one)}
     plain.close()
 
     # max over ranks (replicas: the slowest rank sets the step)
@@ -476,6 +573,28 @@ def run_ours(args):
         sm_count = torch.cuda.get_device_properties(local).multi_processor_count
         fp32_peak = sm_count * 128 * 2 * (clk.get("sm_mhz") or 2070.0) * 1e6 / 1e12
         evaluation = surrogate_eval(pkg, ct, gd, args.eval_n, SEED + 41) if gd is not None else None
+        # every kernel of the step with its own roofline: flops = rows x the plain tree's flops per row
+        # (the same figure for every precision), peak = the measured bf16 tensor rate (the float32
+        # pipes' nominal rate beside it); bound = the pipe the kernel runs on
+        kernels = []
+        for name, rows, kms_ in step_parts:
+            ach = flops * rows / (kms_ / 1e3) / 1e12
+            kernels.append({"kernel": name, "bound": "fp32_simt", "rows": int(rows), "ms": kms_,
+                            "flops_per_row": flops, "achieved": ach, "unit": "TFLOP/s", "peak": bf16_peak,
+                            "frac": ach / bf16_peak, "fp32_simt_peak_tflops": fp32_peak,
+                            "frac_of_fp32_simt_peak": ach / fp32_peak})
+        if mlp_part is not None:
+            kernels.append({"kernel": mlp_part["kernel"], "bound": "tensor", "rows": B, "ms": mlp_part["forward_ms"],
+                            "flops_per_row": mlp_part["flops_per_syndrome"], "achieved": mlp_part["achieved_tflops"],
+                            "unit": "TFLOP/s", "peak": bf16_peak, "frac": mlp_part["frac"]})
+        if kernels:
+            top = max(kernels, key=lambda k: k["ms"])
+            dominant = dict(top, traffic=None,
+                            note=f"the longest kernel of the timed step ({top['ms']:.3f} of {step_ms:.3f} ms), timed "
+                                 f"alone on the same rows; peak = measured bf16 tensor rate ({peak_kind})")
+        else:
+            dominant = {"kernel": "tn_contract_kernel<float>", "bound": "fp32_simt", "achieved": achieved_tflops,
+                        "peak": bf16_peak, "unit": "TFLOP/s", "frac": achieved_tflops / bf16_peak, "traffic": traffic}
         # launches per step: gated = fused surrogate forward, gate, gather, float32 contraction,
         # recheck contraction, scatter; exact alone = the two contractions
         per_step = 6 if gd is not None else 2
@@ -488,24 +607,24 @@ def run_ours(args):
                            else "batched TN f32 with double-float recheck"),
             "e2e": {"value": e2e_value, "unit": "syndromes/s", "h2d_bytes_per_step": int(packed[0].nbytes),
                     "d2h_bytes_per_step": int(B * 4)},
-            "roofline": {"bound": "tensor", "achieved": achieved_tflops, "peak": bf16_peak, "unit": "TFLOP/s",
-                         "frac": achieved_tflops / bf16_peak, "traffic": traffic,
-                         "kernel": "tn_contract_kernel<float> (SIMT float32; peak is the measured bf16 "
-                                   f"tensor rate, {peak_kind})",
-                         "flops_per_syndrome": flops, "kernel_ms": kernel_ms,
-                         # the float32 FMA pipes this kernel actually runs on: 152 SMs x 128 lanes x 2
-                         # flops per cycle at the sampled SM clock (nominal, not measured)
-                         "fp32_simt_peak_tflops": fp32_peak,
-                         "frac_of_fp32_simt_peak": achieved_tflops / fp32_peak,
-                         "traffic_note": "dram read+write of the split-arena shape (1 syndrome per 128-thread "
-                                         "block) per 65,536 syndromes (ncu, scaled from 16,384): big-pool "
-                                         "intermediates, not algorithmic bytes (42 B per syndrome)"},
+            "roofline": dominant,
+            "step_kernels": kernels,
+            "roofline_full_batch": {
+                "bound": "fp32_simt", "achieved": achieved_tflops, "peak": bf16_peak, "unit": "TFLOP/s",
+                "frac": achieved_tflops / bf16_peak, "traffic": traffic,
+                "kernel": f"tn_contract_kernel<float> over all {B} rows (the batched exact decoder's float32 "
+                          "launch, timed alone outside the gated step)",
+                "flops_per_syndrome": flops, "rows": B, "kernel_ms": kernel_ms,
+                "fp32_simt_peak_tflops": fp32_peak, "frac_of_fp32_simt_peak": achieved_tflops / fp32_peak,
+                "traffic_note": "dram read+write of one full-batch launch (ncu, scaled from 16,384 rows): "
+                                "big-pool intermediates, not algorithmic bytes (42 B per syndrome)"},
             "surrogate_gemm": mlp_part,
             "cpu_baseline": cpu,
             "clocks": clk,
             "gpu_launches": per_step * K,
             "batched_tn_syn_per_s": tn_rate,
             "plain_f64_gpu_syn_per_s": plain_rate,
+            "plain_f64_gpu_latency_us": plain_latency_us,
             "speedup_vs_plain_f64_gpu": value / plain_rate,
             "fallback_fraction_last_step": fallback / B,
             "decision_mismatch_vs_f64_oracle": mismatch,
@@ -780,7 +899,7 @@ def circuit_program(args):
     d, rounds, p = 5, 5, 0.001
     circ = cz.memory_z_circuit(d, rounds, p)
     dem = cz.detector_error_model(circ)
-    opt = dec.TreeSA(trials=32, sweeps=2000, target_width=20, width_penalty=2.0, seed=1, restarts=4)
+    opt = dec.FixedOrder(read_order(CIRCUIT_ORDER_PATH))
     ct = pkg.compile(pkg.TNMMAP(optimizer=opt, precision="f32", tensor_cores=not args.no_tensor_cores), dem)
     return pkg, dem, ct
 
@@ -868,7 +987,9 @@ def run_circuit(args):
 
 def main():
     args = parse()
-    if args.circuit and args.profile:
+    if args.write_order:
+        write_order()
+    elif args.circuit and args.profile:
         run_circuit_profile(args)
     elif args.circuit:
         run_circuit(args)

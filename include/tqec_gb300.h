@@ -365,14 +365,18 @@ int tqec_monte_carlo(tqec_sampler* s, tqec_program* prog, tqec_mlp* mlp, float t
  * real-time decoding loop that must not stall or fail on an allocation, or a
  * process whose device memory is already reserved in full by another
  * allocator.  Same results as tqec_decode_batch with TQEC_F64, whatever the
- * program's own precision.  All pointers must be device memory (host
- * pointers are rejected, since staging them would allocate); logp_out may be
+ * program's own precision; a TQEC_FLAG_MAP program is rejected with
+ * TQEC_ERR_INVALID, as tqec_decode_batch rejects it.  All pointers must be
+ * device memory of the program's device (host pointers and other GPUs'
+ * buffers are rejected, since staging them would allocate); logp_out may be
  * NULL.  The only scratch is a 32 MiB array inside the library, which every
  * GPU that loads the library holds until the process exits; a program whose
  * float64 working set exceeds it (tqec_program_info: arena_elems * 8 bytes per
  * syndrome) is rejected with TQEC_ERR_UNSUPPORTED.  The first call on a device
- * looks up that array's device address on the current device and caches it;
- * make that first call before any stream capture.  All calls share the one
+ * looks up that array's device address on the current device and caches it
+ * for the life of the process; make that first call before any stream
+ * capture, and do not call this entry point on a device after a
+ * cudaDeviceReset of it (the cached address belonged to the old context).  All calls share the one
  * array: calls whose kernels overlap on the GPU (concurrent streams, other
  * threads) race on it and must be serialised by the caller.  Every scratch
  * element a call reads it has written first, so nothing needs clearing.  With

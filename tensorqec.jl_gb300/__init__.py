@@ -10,8 +10,9 @@ from .circuit import (Circuit, detector_error_model, insert_errors, memory_z_cir
 from .codes import (BivariateBicycleCode, Code422, Code832, Code1573, Color488, Color666, CSSTannerGraph,
                     PauliString, ShorCode, SimpleTannerGraph, SteaneCode, SurfaceCode, ToricCode,
                     remove_linear_dependency, stabilizers, tanner_graph)
-from .decoder import (CompiledDEMTNMMAP, CompiledGeneralTNMAP, CompiledTNMAP, CompiledTNMMAP, GreedyMethod,
-                      NoOptimizer, TNMAP, TNMMAP, TreeSA, compile, decode, multi_round_qec, optimize_code)
+from .decoder import (CompiledDEMTNMMAP, CompiledGeneralTNMAP, CompiledTNMAP, CompiledTNMMAP, FixedOrder,
+                      GreedyMethod, NoOptimizer, TNMAP, TNMMAP, TreeSA, compile, decode, load_order,
+                      multi_round_qec, optimize_code, save_order)
 from .dem import DetectorErrorModel, dem2tanner, logical_map, parse_dem_file, parse_dem_string, sample_dem
 from .error_model import (CSSErrorPattern, CSSSyndrome, DecodingResult, IndependentDepolarizingError,
                           IndependentFlipError, SimpleSyndrome, check_logical_error, depolarizing, iid_error,

@@ -43,7 +43,9 @@ int nfail(int code, const std::string& m) {
 }
 
 // Device address of the scratch array on `device`, which must be current.
-// Resolved once per device and cached.
+// Resolved once per device and cached for the life of the process: a
+// cudaDeviceReset by the caller destroys the context the address belongs to,
+// so this entry point must not be called on that device after such a reset.
 int scratch_address(int device, void** out) {
   if (device < 0 || device >= kMaxDevices) return nfail(TQEC_ERR_INVALID, "device ordinal out of range");
   std::lock_guard<std::mutex> lk(g_setup_mu);
@@ -58,13 +60,16 @@ int scratch_address(int device, void** out) {
   return TQEC_OK;
 }
 
-bool on_device(const void* p) {
+// True when p is device (or managed) memory of `device`: a buffer on another
+// GPU would be dereferenced directly by the kernel, which faults without peer
+// access, so it is rejected like a host pointer.
+bool on_device(const void* p, int device) {
   cudaPointerAttributes at;
   if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
     cudaGetLastError();
     return false;
   }
-  return at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged;
+  return (at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged) && at.device == device;
 }
 
 }  // namespace
@@ -76,14 +81,20 @@ extern "C" int tqec_decode_batch_noalloc(tqec_program* prog, const uint8_t* synd
   tqec::ProgramF64View v;
   int rc = tqec::program_f64_view(prog, &v);
   if (rc) return nfail(rc, "bad program");
+  // a most-probable-configuration program returns assignments, not classes
+  // (tqec_map_decode_batch); tqec_decode_batch rejects it the same way
+  if (v.args.map_mode)
+    return nfail(TQEC_ERR_INVALID, "a TQEC_FLAG_MAP program decodes with tqec_map_decode_batch");
   std::lock_guard<std::mutex> lk(*v.mu);
   cudaError_t e = cudaSetDevice(v.device);
   if (e != cudaSuccess) return nfail(TQEC_ERR_CUDA, std::string("cudaSetDevice: ") + cudaGetErrorString(e));
   void* scratch = nullptr;
   if ((rc = scratch_address(v.device, &scratch))) return rc;
   if (n == 0) return TQEC_OK;
-  if (!on_device(syndromes) || !on_device(class_out) || (logp_out && !on_device(logp_out)))
-    return nfail(TQEC_ERR_INVALID, "tqec_decode_batch_noalloc takes device pointers only");
+  if (!on_device(syndromes, v.device) || !on_device(class_out, v.device) ||
+      (logp_out && !on_device(logp_out, v.device)))
+    return nfail(TQEC_ERR_INVALID,
+                 "tqec_decode_batch_noalloc takes device pointers only, on the program's device");
   const size_t per_syndrome = size_t(v.args.arena_elems) * sizeof(double);
   if (per_syndrome > kNoallocScratchBytes)
     return nfail(TQEC_ERR_UNSUPPORTED,
@@ -95,8 +106,8 @@ extern "C" int tqec_decode_batch_noalloc(tqec_program* prog, const uint8_t* synd
   int lg = 0;
   while ((1 << lg) < G) ++lg;
   const size_t smem = tqec::contract_smem_bytes(TQEC_F64, v.args.n_steps, v.args.syn_words, G, v.args.arena_elems,
-                                                false);
-  const int occ = tqec::contract_occupancy(TQEC_F64, v.threads, smem);
+                                                false, v.args.var_words);
+  const int occ = tqec::contract_occupancy(TQEC_F64, v.threads, smem, v.args.map_mode != 0);
   if (occ < 1) return nfail(TQEC_ERR_UNSUPPORTED, "launch shape cannot be resident on this device");
   const int64_t by_scratch = int64_t(kNoallocScratchBytes / (size_t(G) * per_syndrome));
   const int64_t by_rows = (n + G - 1) / G;

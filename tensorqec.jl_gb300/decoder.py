@@ -62,12 +62,42 @@ class NoOptimizer:
     """tndecoder.jl:64: contract the tensors left to right."""
 
 
+@dataclass
+class FixedOrder:
+    """A contraction tree found earlier (OMEinsum accepts an already
+    optimised code the same way): an (n_tensors - 1, 2) array of node ids in
+    the tqec_tree convention, e.g. read by ``load_order``."""
+    steps: np.ndarray
+
+
+def save_order(path, steps, comment=""):
+    """Writes a contraction tree as text: '#' comment lines, then one
+    'a b' pair of node ids per binary step."""
+    steps = np.asarray(steps, dtype=np.int64).reshape(-1, 2)
+    with open(path, "w") as f:
+        for line in comment.splitlines():
+            f.write(f"# {line}\n")
+        for a, b in steps:
+            f.write(f"{a} {b}\n")
+
+
+def load_order(path) -> np.ndarray:
+    """Reads a tree written by ``save_order``."""
+    rows = [ln.split() for ln in open(path) if ln.strip() and not ln.startswith("#")]
+    return np.array([[int(a), int(b)] for a, b in rows], dtype=np.int32).reshape(-1, 2)
+
+
 def optimize_code(graph: FactorGraph, optimizer) -> np.ndarray:
     """Returns the tree as an (n_tensors - 1, 2) array of node ids."""
     if graph.map_mode:
         # the root of a most-probable-configuration contraction is a scalar
         return optimize_code(FactorGraph(graph.ixs, graph.tensors, [], graph.syndrome_positions), optimizer)
     n = graph.n_tensors
+    if isinstance(optimizer, FixedOrder):
+        steps = np.ascontiguousarray(optimizer.steps, dtype=np.int32).reshape(-1, 2)
+        if steps.shape[0] != max(n - 1, 0):
+            raise ValueError(f"the fixed order has {steps.shape[0]} steps; the network needs {max(n - 1, 0)}")
+        return steps
     if isinstance(optimizer, NoOptimizer) or n == 1:
         steps = np.zeros((max(n - 1, 0), 2), dtype=np.int32)
         acc = 0

@@ -158,9 +158,10 @@ def sample_bits(ct, n, rng):
     return np.concatenate([s.sx, s.sz], axis=1)
 
 
-def _draw_labelled(ct, sampler, rng, seed, offset, m, nbytes):
+def _draw_labelled(ct, sampler, rng, seed, offset, m, nbytes, label_precision=native.TQEC_F32):
     """m syndromes (GPU sampler at counter `offset`, or the host sampler) and
-    their exact class probabilities, as host arrays."""
+    their exact class probabilities (contracted in `label_precision`), as
+    host arrays."""
     sub = 1 << 20
     packed = np.empty((m, nbytes), dtype=np.uint8)
     targets = np.empty((m, ct.n_classes), dtype=np.float32)
@@ -170,15 +171,18 @@ def _draw_labelled(ct, sampler, rng, seed, offset, m, nbytes):
             packed[i:i + k], _ = sampler.sample(seed, k, offset=offset + i)
         else:
             packed[i:i + k] = pack_syndromes(sample_bits(ct, k, rng))
-        targets[i:i + k] = soft_labels(ct.program.contract_packed(packed[i:i + k], native.TQEC_F32))
+        targets[i:i + k] = soft_labels(ct.program.contract_packed(packed[i:i + k], label_precision))
     return packed, targets
 
 
 def train_surrogate(ct, n_train=1 << 24, batch=16384, epochs=4, lr=3e-3, hidden=512, n_layers=4, seed=1,
-                    rng=None, log=None, gpu_sampler=True, chunk=0, device_resident=None):
+                    rng=None, log=None, gpu_sampler=True, chunk=0, device_resident=None, label_precision="f32"):
     """Trains a surrogate for a compiled CSS decoder on n_train sampled
-    syndromes labelled by the exact contraction (float32 with its rounding
-    bound).  Syndromes come from the GPU sampler (Philox, seeded by `seed`)
+    syndromes labelled by the exact contraction's class probabilities:
+    label_precision "f32" (the renormalised float32 contraction, every class
+    probability within the program's rounding bound of float64: 4.8e-5
+    relative at d=7) or "f64" (the float64 contraction, about 4x slower to
+    label).  Syndromes come from the GPU sampler (Philox, seeded by `seed`)
     or, with gpu_sampler=False, from the host sampler.  With chunk > 0 the
     syndromes are drawn and labelled `chunk` at a time and each chunk gets
     its `epochs` passes before the next is drawn (fresh data in bounded
@@ -222,7 +226,8 @@ def train_surrogate(ct, n_train=1 << 24, batch=16384, epochs=4, lr=3e-3, hidden=
         for c0 in range(0, n_train, chunk):
             m = min(chunk, n_train - c0)
             t0 = time.time()
-            packed, targets = _draw_labelled(ct, sampler, rng, seed, c0, m, nbytes)
+            packed, targets = _draw_labelled(ct, sampler, rng, seed, c0, m, nbytes,
+                                             {"f32": native.TQEC_F32, "f64": native.TQEC_F64}[label_precision])
             if torch is not None:
                 d_syn = torch.from_numpy(packed).to(dev)
                 d_tgt = torch.from_numpy(targets).to(dev)
@@ -258,6 +263,7 @@ def train_surrogate(ct, n_train=1 << 24, batch=16384, epochs=4, lr=3e-3, hidden=
         if sampler is not None:
             sampler.close()
     stats = {"label_seconds": t_label, "train_seconds": t_train, "steps": s, "batch": batch,
+             "label_precision": label_precision,
              "n_train": n_train, "epochs": epochs, "chunk": chunk, "device_resident": torch is not None,
              "final_loss": float(np.mean(losses[-50:])) if losses else None}
     return sur, stats

@@ -13,9 +13,20 @@ from conftest import gpu_available
 pytestmark = [pytest.mark.gpu, pytest.mark.skipif(not gpu_available(), reason="needs a CUDA GPU")]
 
 
+def _specs(pkg):
+    return [(pkg.SurfaceCode(3, 3), 0.08, 500), (pkg.SurfaceCode(5, 5), 0.05, 700), (pkg.Color488(5), 0.06, 300),
+            (pkg.ToricCode(4, 4), 0.04, 200), (pkg.SurfaceCode(7, 7), 0.05, 150)]
+
+
+def _oracle_stabilizers(oracle, i):
+    """The oracle's stabilisers of _specs(pkg)[i]."""
+    return [lambda: oracle.surface_code_stabilizers(3, 3), lambda: oracle.surface_code_stabilizers(5, 5),
+            lambda: oracle.color_code_stabilizers("488", 5), lambda: oracle.toric_code_stabilizers(4, 4),
+            lambda: oracle.surface_code_stabilizers(7, 7)][i]()
+
+
 def _setup(pkg):
-    specs = [(pkg.SurfaceCode(3, 3), 0.08, 500), (pkg.SurfaceCode(5, 5), 0.05, 700), (pkg.Color488(5), 0.06, 300),
-             (pkg.ToricCode(4, 4), 0.04, 200), (pkg.SurfaceCode(7, 7), 0.05, 150)]
+    specs = _specs(pkg)
     progs = []
     for i, (code, p, n) in enumerate(specs):
         t = pkg.tanner_graph(code)
@@ -96,3 +107,36 @@ def test_multi_programs_must_agree_on_recheck(pkg):
     md.close()
     a.close()
     b.close()
+
+
+def test_multi_program_launch_vs_oracle(pkg, oracle):
+    """The persistent multi-program launch (float32 + one recheck launch for
+    every program) decides each row like the oracle's float64 contraction of
+    that row's own code, outside exact ties (tests/parity.py)."""
+    import torch
+    from oracle.c_oracle import CContractor, host_cores
+    from parity import assert_decisions
+
+    progs = _setup(pkg)
+    md = pkg.native.MultiDecoder([ct.program for ct, _ in progs])
+    syn = [torch.from_numpy(pkg.pack_syndromes(b)).cuda() for _, b in progs]
+    cls = [torch.full((b.shape[0],), -1, dtype=torch.int32, device="cuda") for _, b in progs]
+    n = np.array([b.shape[0] for _, b in progs])
+    ends = np.stack([n // 2, n])
+    md.set_work(ends, [x.data_ptr() for x in syn], [x.data_ptr() for x in cls])
+    stream = torch.cuda.current_stream()
+    md.reset(stream.cuda_stream)
+    for _ in range(ends.shape[0]):
+        md.launch(stream.cuda_stream)
+    torch.cuda.synchronize()
+    for i, ((ct, bits), c) in enumerate(zip(progs, cls)):
+        st, nq = _oracle_stabilizers(oracle, i)
+        em = ct.em
+        net = oracle.tnmmap_network(oracle.css_tanner(st, nq), em.px, em.py, em.pz)
+        assert ct.graph.ixs == net.ixs
+        cc = CContractor(net.ixs, [np.asarray(t) for t in net.tensors], net.iy, net.syndrome_positions, ct.steps)
+        want, _ = cc.contract(pkg.pack_syndromes(bits), threads=host_cores())
+        assert_decisions(c.cpu().numpy(), want)
+    md.close()
+    for ct, _ in progs:
+        ct.close()

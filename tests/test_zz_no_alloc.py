@@ -74,6 +74,14 @@ def test_noalloc_rejects_host_pointers_and_oversized_programs(pkg):
     assert rc == pkg.native.TqecError(-1, "").code
     assert "device pointers" in pkg.native.last_error()
     ct.close()
+    # a most-probable-configuration (TNMAP) program is refused before any launch
+    mp = pkg.compile(pkg.TNMAP(), t, pkg.depolarizing(0.05, t.nq))
+    d_syn = torch.zeros((4, mp.program.syndrome_bytes), dtype=torch.uint8, device="cuda")
+    d_cls = torch.zeros(4, dtype=torch.int32, device="cuda")
+    rc = noalloc(mp.program._h, C.c_void_p(d_syn.data_ptr()), 4, C.c_void_p(d_cls.data_ptr()), None, None)
+    assert rc == -1
+    assert "tqec_map_decode_batch" in pkg.native.last_error()
+    mp.close()
     # toric 5x5: a float64 working set far above the 32 MiB scratch
     tb = pkg.tanner_graph(pkg.ToricCode(5, 5))
     big = pkg.compile(pkg.TNMMAP(precision="f64", optimizer=pkg.TreeSA(restarts=1, sweeps=300)), tb,
