@@ -130,7 +130,9 @@ typedef struct {
   int32_t tensor_steps;      /* GEMM-shaped steps (tcgen05 tf32 in float32 launches) */
   int32_t tensor_f32;        /* 1: the float32 shape runs them on the tensor cores */
   int32_t recheck_precision; /* TQEC_F32X2 or TQEC_F64: arithmetic of the recheck */
-  int32_t reserved_;
+  int32_t cluster_blocks;    /* blocks of the thread-block cluster that contracts one
+                                syndrome in single-syndrome launches (the recheck; all
+                                launches of a TQEC_FLAG_PLAIN program); 0: one block */
   double err_bound_f32x2;    /* relative error bound of a TQEC_F32X2 marginal */
 } tqec_program_info_t;
 
@@ -160,6 +162,21 @@ int tqec_decode_batch(tqec_program* prog, const uint8_t* syndromes, int64_t n,
                       int32_t* class_out, double* logp_out,
                       float* err_bound_out, void* stream);
 
+/* decode over the rows rows[0 .. *n_rows) of a syndrome array, with the row
+ * list and its length in device memory (no reference counterpart: it lets a
+ * filter that runs on the device, such as the surrogate's confidence gate,
+ * hand its rejected rows to the contraction without a host round trip).
+ * class_out[rows[r]] receives row rows[r]'s class, with the float32 recheck
+ * as in tqec_decode_batch; other entries are untouched.  Device pointers
+ * only; n_max bounds *n_rows; n_hint (the expected row count, e.g. the
+ * previous call's) picks the tuned launch shape.  Stream-ordered: returns
+ * without waiting and performs no host synchronisation (stream == NULL: the
+ * program's own stream).  Not for TQEC_FLAG_PLAIN or TQEC_FLAG_MAP
+ * programs. */
+int tqec_decode_rows(tqec_program* prog, const uint8_t* syndromes,
+                     const int32_t* rows, const int32_t* n_rows, int64_t n_max,
+                     int64_t n_hint, int32_t* class_out, void* stream);
+
 /* The contraction alone in a chosen precision, without argmax or recheck:
  * writes n x n_classes natural-log marginals (the reference's
  * `ct.code(ct.tensors...)`, tndecoder.jl:162, in log form). */
@@ -178,7 +195,9 @@ int tqec_map_decode_batch(tqec_program* prog, const uint8_t* syndromes, int64_t 
                           uint8_t* assignment_out, double* logp_out, void* stream);
 
 /* Count of syndromes the last TQEC_F32 decode call sent to the
- * recheck (a measure of how often the rounding bound was not enough). */
+ * recheck (a measure of how often the rounding bound was not enough).  After
+ * a call that returned before its work ended (a stream given, device
+ * outputs), synchronise that stream before asking. */
 int tqec_last_recheck_count(const tqec_program* prog, int64_t* count);
 
 /* Tries the launch shapes that fit and keeps the fastest for each
@@ -322,6 +341,12 @@ int tqec_mlp_infer(tqec_mlp* mlp, const uint8_t* syndromes, int64_t n, int32_t* 
  * (tqec_decode_batch).  Writes the number of such rows. */
 int tqec_gated_decode(tqec_mlp* mlp, tqec_program* prog, float threshold, const uint8_t* syndromes,
                       int64_t n, int32_t* class_out, int64_t* n_fallback_out, void* stream);
+
+/* Rows the last tqec_gated_decode call sent to the exact contraction (the
+ * gate's rejections).  A call given a stream and device buffers with
+ * n_fallback_out == NULL returns without a host synchronisation; synchronise
+ * its stream before asking. */
+int tqec_gated_last_fallback(tqec_mlp* mlp, int64_t* n_fallback);
 /* How the layers run.  0: SIMT GEMMs.  1, 2: tcgen05 GEMMs layer by layer
  * (hidden a multiple of 256), a 4-stage TMA ring with one block per SM or a
  * 2-stage ring with two blocks per SM.  3, the default: inference (infer,

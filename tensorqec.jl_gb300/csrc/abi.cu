@@ -87,6 +87,17 @@ struct ProgramInputs {
 
 }  // namespace
 
+// The cluster form of a precision: `size` blocks of `threads` threads per
+// syndrome, `cap` clusters resident at once, the tables staged in each
+// block's shared memory when `tables`.
+struct ClusterShape {
+  int size = 0;
+  int threads = 0;
+  int cap = 0;
+  size_t smem = 0;
+  bool tables = false;
+};
+
 struct tqec_program {
   tqec::Plan plan;
   int device = 0;
@@ -114,10 +125,16 @@ struct tqec_program {
   // latency matters, so one syndrome per block with the most threads and the
   // tables staged
   Shape recheck_shape;
-  DevBuf arena[3];
+  // single-syndrome launches (the plain form, the recheck) as one syndrome
+  // per thread-block cluster, per precision (size 0: one block per syndrome)
+  ClusterShape cluster[3];
+  DevBuf arena[3], carena[3];
   DevBuf syn, cls, logp, err, list, count;
   int32_t* h_count = nullptr;  // pinned
   int64_t last_recheck = 0;
+  // the last call's count is still being copied to h_count on its stream
+  // (a call on a caller's stream with device outputs returns before it ends)
+  bool recheck_async = false;
   ProgramInputs inputs;
   std::mutex mu;
 };
@@ -333,6 +350,44 @@ int launch_rows(tqec_program* p, int precision, tqec::KArgs a, int64_t n_rows_ma
   return TQEC_OK;
 }
 
+// The cluster form of `precision` with csize blocks of `threads` threads
+// (the tables staged when they fit); false if it cannot launch here.
+bool choose_cluster(tqec_program* p, int precision, int csize, int threads, ClusterShape* out) {
+  if (p->plan.map_mode || (precision != TQEC_F64 && precision != TQEC_F32X2) || csize < 2) return false;
+  const size_t limit = tqec::contract_smem_limit(p->device);
+  const int nsteps = (int)p->plan.steps.size();
+  ClusterShape c;
+  c.size = csize;
+  c.threads = threads;
+  const size_t tb = table_bytes(p, precision);
+  c.smem = tqec::contract_smem_bytes(precision, nsteps, syn_words(p), 1, p->plan.arena_elems, false, 0, tb);
+  c.tables = c.smem <= limit;
+  if (!c.tables) c.smem = tqec::contract_smem_bytes(precision, nsteps, syn_words(p), 1, p->plan.arena_elems, false);
+  if (c.smem > limit) return false;
+  c.cap = tqec::contract_cluster_capacity(precision, csize, threads, c.smem);
+  if (c.cap < 1) return false;
+  *out = c;
+  return true;
+}
+
+// One syndrome per cluster over up to n_rows_max rows (a.list / a.n), at
+// most one wave of resident clusters striding over the rows.
+int launch_cluster_rows(tqec_program* p, int precision, tqec::KArgs a, int64_t n_rows_max, cudaStream_t st) {
+  const ClusterShape& c = p->cluster[precision];
+  const int clusters = (int)std::max<int64_t>(1, std::min<int64_t>(n_rows_max, c.cap));
+  const size_t esz = precision == TQEC_F32 ? 4 : 8;
+  TQ_CUDA(p->carena[precision].ensure(size_t(clusters) * size_t(p->plan.arena_elems) * esz));
+  a.G = 1;
+  a.lg = 0;
+  a.tables_smem = c.tables ? 1 : 0;
+  a.perm16 = c.tables ? p->d_perm16 : nullptr;
+  a.arena_global = p->carena[precision].p;
+  a.arena_small = 0;
+  a.tc = 0;
+  TQ_CUDA(tqec::contract_cluster_launch(precision, a, clusters, c.size, c.threads, c.smem, st));
+  return TQEC_OK;
+}
+
 // Runs the plain form: one launch (one block, one syndrome) per row.
 // After a synchronisation: a tensor-core wait that gave up makes the call fail
 // (its results are not valid); the flag is cleared for the next call.
@@ -348,6 +403,8 @@ int check_tensor_error(tqec_program* p) {
 }
 
 int launch_plain(tqec_program* p, int precision, tqec::KArgs a, int64_t n, cudaStream_t st) {
+  // the cluster form: one launch, each syndrome on its own cluster
+  if (p->cluster[precision].size > 0) return launch_cluster_rows(p, precision, a, n, st);
   Shape s = p->shape[precision];
   const size_t limit = tqec::contract_smem_limit(p->device);
   const int nsteps = (int)p->plan.steps.size();
@@ -379,6 +436,30 @@ int launch_plain(tqec_program* p, int precision, tqec::KArgs a, int64_t n, cudaS
     TQ_CUDA(tqec::contract_launch(precision, a, 1, one.threads, one.smem, st));
   }
   return TQEC_OK;
+}
+
+// The re-contraction of the rows a float32 launch listed (b.list,
+// b.list_count on the device; at most n_max of them).
+// Programs at least this wide (log2 of the largest intermediate) run their
+// single-syndrome launches on clusters by default.
+constexpr int kClusterMinWidth = 12;
+
+void default_clusters(tqec_program* p) {
+  for (auto& c : p->cluster) c = ClusterShape{};
+  if (p->plan.map_mode || p->plan.width < kClusterMinWidth) return;
+  const bool plain = (p->flags & TQEC_FLAG_PLAIN) != 0;
+  for (int prec : {recheck_precision(p), plain ? p->precision : -1}) {
+    if (prec < 0) continue;
+    ClusterShape c;
+    if (choose_cluster(p, prec, 8, 512, &c)) p->cluster[prec] = c;
+  }
+  cudaGetLastError();
+}
+
+int launch_recheck(tqec_program* p, const tqec::KArgs& b, int64_t n_max, cudaStream_t st) {
+  const int rp = recheck_precision(p);
+  if (p->cluster[rp].size > 0) return launch_cluster_rows(p, rp, b, n_max, st);
+  return launch_rows(p, rp, b, n_max, st, &p->recheck_shape);
 }
 
 struct Staged {
@@ -461,15 +542,14 @@ int decode_locked(tqec_program* p, const uint8_t* syn, int64_t n, int32_t* cls, 
     rc = plain ? launch_plain(p, precision, a, n, st) : launch_rows(p, precision, a, n, st);
     if (rc) return rc;
     if (recheck && precision == TQEC_F32) {
-      const int rp = recheck_precision(p);
-      tqec::KArgs b = base_args(p, rp);
+      tqec::KArgs b = base_args(p, recheck_precision(p));
       b.syn = s.d_syn;
       b.list = (const int32_t*)p->list.p;
       b.list_count = (const int32_t*)p->count.p;
       b.class_out = a.class_out;
       b.logp_out = s.d_logp;
       b.err_out = s.d_err;
-      rc = launch_rows(p, rp, b, n, st, &p->recheck_shape);
+      rc = launch_recheck(p, b, n, st);
       if (rc) return rc;
       TQ_CUDA(cudaMemcpyAsync(p->h_count, p->count.p, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
     }
@@ -685,6 +765,9 @@ int tqec_program_create(const tqec_network* net, const tqec_tree* tree, const tq
       return bail(rc, m);
     }
   }
+  // wide programs take their single-syndrome launches (the recheck; the
+  // plain form) on 8-block clusters until tqec_program_autotune measures
+  default_clusters(p);
   g_last_error.clear();
   *out = p;
   return TQEC_OK;
@@ -742,6 +825,7 @@ int tqec_program_info(const tqec_program* p, tqec_program_info_t* info) {
   info->split_f32 = p->shape[TQEC_F32].split ? 1 : 0;
   info->split_f64 = p->shape[TQEC_F64].split ? 1 : 0;
   info->recheck_precision = P.map_mode ? TQEC_F64 : recheck_precision(p);
+  info->cluster_blocks = p->cluster[(p->flags & TQEC_FLAG_PLAIN) ? p->precision : info->recheck_precision].size;
   info->err_bound_f32x2 = err_bound(p, TQEC_F32X2);
   return TQEC_OK;
 }
@@ -761,8 +845,59 @@ int tqec_decode_batch(tqec_program* p, const uint8_t* syndromes, int64_t n, int3
       (err_bound_out && !is_device_ptr(err_bound_out))) {
     TQ_CUDA(cudaStreamSynchronize(st));
     p->last_recheck = recheck ? *p->h_count : 0;
+    p->recheck_async = false;
     return check_tensor_error(p);
   }
+  p->last_recheck = 0;
+  p->recheck_async = recheck && n > 0;
+  return TQEC_OK;
+}
+
+int tqec_decode_rows(tqec_program* p, const uint8_t* syndromes, const int32_t* rows, const int32_t* n_rows,
+                     int64_t n_max, int64_t n_hint, int32_t* class_out, void* stream) {
+  if (!p || n_max < 0 || (n_max > 0 && (!syndromes || !rows || !n_rows || !class_out)))
+    return fail(TQEC_ERR_INVALID, "bad argument");
+  if (p->plan.map_mode) return fail(TQEC_ERR_INVALID, "a TQEC_FLAG_MAP program decodes with tqec_map_decode_batch");
+  if (n_max > INT32_MAX) return fail(TQEC_ERR_INVALID, "n_max above 2^31 rows");
+  if ((p->flags & TQEC_FLAG_PLAIN) != 0) return fail(TQEC_ERR_UNSUPPORTED, "the plain form decodes with tqec_decode_batch");
+  std::lock_guard<std::mutex> lk(p->mu);
+  TQ_CUDA(cudaSetDevice(p->device));
+  if (n_max == 0) return TQEC_OK;
+  if (!is_device_ptr(syndromes) || !is_device_ptr(rows) || !is_device_ptr(n_rows) || !is_device_ptr(class_out))
+    return fail(TQEC_ERR_INVALID, "tqec_decode_rows takes device pointers only");
+  cudaStream_t st = stream ? (cudaStream_t)stream : p->stream;
+  const bool recheck = p->precision == TQEC_F32 && !(p->flags & TQEC_FLAG_NORECHECK);
+  tqec::KArgs a = base_args(p, p->precision);
+  a.syn = syndromes;
+  a.n = n_max;
+  a.list = rows;
+  a.list_count = n_rows;
+  a.class_out = class_out;
+  if (recheck) {
+    TQ_CUDA(p->list.ensure(sizeof(int32_t) * n_max));
+    TQ_CUDA(p->count.ensure(sizeof(int32_t)));
+    TQ_CUDA(cudaMemsetAsync(p->count.p, 0, sizeof(int32_t), st));
+    a.recheck_margin = p->margin >= 0.0 ? p->margin : 2.0 * err_bound(p, TQEC_F32);
+    a.recheck_list = (int32_t*)p->list.p;
+    a.recheck_count = (int32_t*)p->count.p;
+  }
+  // the shape tuned for about n_hint rows; the grid is at most one wave of
+  // resident blocks, whose blocks stride over however many rows there are
+  const Shape& s = pick_shape(p, p->precision, std::max<int64_t>(1, std::min(n_hint, n_max)));
+  int rc = launch_rows(p, p->precision, a, n_max, st, &s);
+  if (rc) return rc;
+  if (recheck) {
+    tqec::KArgs b = base_args(p, recheck_precision(p));
+    b.syn = syndromes;
+    b.list = (const int32_t*)p->list.p;
+    b.list_count = (const int32_t*)p->count.p;
+    b.n = n_max;
+    b.class_out = class_out;
+    if ((rc = launch_recheck(p, b, n_max, st))) return rc;
+    TQ_CUDA(cudaMemcpyAsync(p->h_count, p->count.p, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+  }
+  p->last_recheck = 0;
+  p->recheck_async = recheck;
   return TQEC_OK;
 }
 
@@ -821,7 +956,9 @@ int tqec_map_decode_batch(tqec_program* p, const uint8_t* syndromes, int64_t n, 
 
 int tqec_last_recheck_count(const tqec_program* p, int64_t* count) {
   if (!p || !count) return fail(TQEC_ERR_INVALID, "NULL argument");
-  *count = p->last_recheck;
+  // after an asynchronous call the count is in the pinned word once the
+  // caller's stream has passed the call (the caller synchronises first)
+  *count = p->recheck_async ? int64_t(*p->h_count) : p->last_recheck;
   return TQEC_OK;
 }
 
@@ -887,6 +1024,59 @@ bool tune_shape(tqec_program* p, int prec, int64_t n, cudaEvent_t e0, cudaEvent_
 
 }  // namespace
 
+namespace {
+
+// Single-syndrome launches of one precision: the block form (the recheck
+// shape, or one launch per row in the plain form) against clusters of 2-16
+// blocks of 256 or 512 threads, timed on 1 and on 8 rows (the sum decides).
+bool tune_cluster(tqec_program* p, int prec, bool plain, cudaEvent_t e0, cudaEvent_t e1) {
+  std::vector<ClusterShape> cands(1);  // the block form
+  for (int cs : {2, 4, 8, 16})
+    for (int th : {256, 512}) {
+      ClusterShape c;
+      if (choose_cluster(p, prec, cs, th, &c)) cands.push_back(c);
+    }
+  cudaGetLastError();
+  ClusterShape best;
+  float best_ms = 1e30f;
+  for (const ClusterShape& c : cands) {
+    p->cluster[prec] = c;
+    float total = 0.f;
+    bool ok = true;
+    for (int64_t rows : {int64_t(1), int64_t(8)}) {
+      tqec::KArgs a = base_args(p, prec);
+      a.syn = (const uint8_t*)p->syn.p;
+      a.n = rows;
+      a.logp_out = (double*)p->logp.p;
+      auto run = [&]() {
+        if (plain) return launch_plain(p, prec, a, rows, p->stream);
+        if (c.size > 0) return launch_cluster_rows(p, prec, a, rows, p->stream);
+        return launch_rows(p, prec, a, rows, p->stream, &p->recheck_shape);
+      };
+      if (run() != TQEC_OK) {  // warm-up
+        ok = false;
+        break;
+      }
+      cudaEventRecord(e0, p->stream);
+      for (int r = 0; r < 3; ++r) run();
+      cudaEventRecord(e1, p->stream);
+      if (cudaEventSynchronize(e1) != cudaSuccess) return false;
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, e0, e1);
+      total += ms;
+    }
+    if (ok && total < best_ms) {
+      best_ms = total;
+      best = c;
+    }
+    cudaGetLastError();
+  }
+  p->cluster[prec] = best;
+  return true;
+}
+
+}  // namespace
+
 int tqec_program_autotune(tqec_program* p, int64_t n_probe) {
   if (!p || n_probe <= 0) return fail(TQEC_ERR_INVALID, "bad argument");
   std::lock_guard<std::mutex> lk(p->mu);
@@ -919,6 +1109,12 @@ int tqec_program_autotune(tqec_program* p, int64_t n_probe) {
     if (!ok) break;
     p->shape[prec] = big;
     p->sized[prec] = sized;
+  }
+  // single-syndrome launches: the recheck's arithmetic, and the plain form
+  if (ok && !p->plan.map_mode) {
+    const bool plain = (p->flags & TQEC_FLAG_PLAIN) != 0;
+    ok = tune_cluster(p, recheck_precision(p), false, e0, e1);
+    if (ok && plain && p->precision != TQEC_F32) ok = tune_cluster(p, p->precision, true, e0, e1);
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);

@@ -164,9 +164,60 @@ __device__ __forceinline__ void flush_max(bool had_items, uint32_t bits, uint32_
   if ((threadIdx.x & 31) == 0) atomicMax(slot, bits);
 }
 
+// A team is the threads that contract one syndrome group together: the
+// block, or in the cluster kernel every block of a thread-block cluster
+// (threads numbered rank by rank).  Team sizes are powers of two.
+__device__ __forceinline__ uint32_t cluster_rank() {
+  uint32_t r;
+  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+  return r;
+}
+__device__ __forceinline__ uint32_t cluster_blocks() {
+  uint32_t r;
+  asm volatile("mov.u32 %0, %%cluster_nctarank;" : "=r"(r));
+  return r;
+}
+__device__ __forceinline__ uint32_t cluster_id() {
+  uint32_t r;
+  asm volatile("mov.u32 %0, %%clusterid.x;" : "=r"(r));
+  return r;
+}
+__device__ __forceinline__ uint32_t cluster_count() {
+  uint32_t r;
+  asm volatile("mov.u32 %0, %%nclusterid.x;" : "=r"(r));
+  return r;
+}
+// The address of `p`'s counterpart in the shared memory of cluster block
+// `rank` (a generic address: ordinary loads, stores and atomics reach it).
+template <typename P>
+__device__ __forceinline__ P* cluster_map(P* p, uint32_t rank) {
+  uint64_t out;
+  asm volatile("mapa.u64 %0, %1, %2;" : "=l"(out) : "l"(reinterpret_cast<uint64_t>(p)), "r"(rank));
+  return reinterpret_cast<P*>(out);
+}
+template <bool CL>
+__device__ __forceinline__ int team_tid() {
+  return CL ? int(cluster_rank() * blockDim.x + threadIdx.x) : int(threadIdx.x);
+}
+template <bool CL>
+__device__ __forceinline__ int team_size() {
+  return CL ? int(cluster_blocks() * blockDim.x) : int(blockDim.x);
+}
+// Team barrier: for a cluster, arrive with release and wait with acquire
+// semantics at cluster scope, which orders every block's arena writes
+// (global memory) before the other blocks' reads of them.
+template <bool CL>
+__device__ __forceinline__ void team_sync() {
+  if (CL) {
+    asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+  } else {
+    __syncthreads();
+  }
+}
+
 // Thread t's position in a step whose items start item_base threads into the
-// block (block sizes are powers of two; item_base is a multiple of 32).
-__device__ __forceinline__ int rotated(int t, int item_base) { return (t - item_base) & int(blockDim.x - 1); }
+// team (team sizes n are powers of two; item_base is a multiple of 32).
+__device__ __forceinline__ int rotated(int t, int item_base, int n) { return (t - item_base) & (n - 1); }
 
 // The normalisers of a step's arena operands (1 for constant operands).
 template <typename T, bool NORM>
@@ -194,7 +245,7 @@ __device__ __forceinline__ void segment_max(bool valid, uint32_t bits, int lw_it
 // One output per work item.  G1: the step runs for one syndrome (the
 // block's only one, or one of its G in turn), so its bases and normalisers
 // are step invariants.
-template <typename T, bool NORM, bool MAXP, bool G1>
+template <typename T, bool NORM, bool MAXP, bool G1, bool CL>
 __device__ void run_step(const KArgs& a, const StepDesc& dref, int st, int item_base, uint32_t* s_max,
                          const StepPtrs<T>* ptrs, const PermTab& ptab) {
   // a register copy: arena stores (same shared array) cannot alias it
@@ -208,7 +259,8 @@ __device__ void run_step(const KArgs& a, const StepDesc& dref, int st, int item_
   const int K = 1 << d.lk;
   const bool bT = (d.flags & kStepTensor) != 0;
   const int kstride = bT ? 1 : (1 << d.lfb);
-  const int i0 = rotated(int(threadIdx.x), item_base);
+  const int nthr = team_size<CL>();
+  const int i0 = rotated(team_tid<CL>(), item_base, nthr);
   StepPtrs<T> p1{};
   T fa1 = T(1), fb1 = T(1);
   if (G1) {
@@ -216,7 +268,7 @@ __device__ void run_step(const KArgs& a, const StepDesc& dref, int st, int item_
     step_norms<T, NORM>(d, s_max, &fa1, &fb1);
   }
   uint32_t run_bits = 0u;
-  for (int i = i0; i < (G1 ? total : total_r); i += blockDim.x) {
+  for (int i = i0; i < (G1 ? total : total_r); i += nthr) {
     const bool valid = G1 || i < total;
     const int g = G1 ? 0 : (valid ? (i >> lw) : 0);
     const int e = i & mw;
@@ -305,7 +357,7 @@ __device__ __forceinline__ void store4<dfloat>(dfloat* p, const dfloat v[4]) {
 // so the vector accesses are aligned.  Permuted outputs are written in a
 // lane-rotated order where the planner found that it spreads the stores of
 // one warp instruction over more shared-memory banks.
-template <typename T, int VW, bool NORM, bool MAXP, bool G1>
+template <typename T, int VW, bool NORM, bool MAXP, bool G1, bool CL>
 __device__ void run_step_vec(const KArgs& a, const StepDesc& dref, int st, int item_base, uint32_t* s_max,
                              const StepPtrs<T>* ptrs, const PermTab& ptab) {
   constexpr int LV = VW == 8 ? 3 : 2;
@@ -322,7 +374,8 @@ __device__ void run_step_vec(const KArgs& a, const StepDesc& dref, int st, int i
   const bool permuted = d.perm_off >= 0;
   const int cb0 = lw < 8 ? lw : 8;
   const int rot = threadIdx.x & (VW - 1);
-  const int i0 = rotated(int(threadIdx.x), item_base);
+  const int nthr = team_size<CL>();
+  const int i0 = rotated(team_tid<CL>(), item_base, nthr);
   StepPtrs<T> p1{};
   T fa1 = T(1), fb1 = T(1);
   if (G1) {
@@ -330,7 +383,7 @@ __device__ void run_step_vec(const KArgs& a, const StepDesc& dref, int st, int i
     step_norms<T, NORM>(d, s_max, &fa1, &fb1);
   }
   uint32_t run_bits = 0u;
-  for (int i = i0; i < (G1 ? total : total_r); i += blockDim.x) {
+  for (int i = i0; i < (G1 ? total : total_r); i += nthr) {
     const bool valid = G1 || i < total;
     const int g = G1 ? 0 : (valid ? (i >> lwv) : 0);
     const int e0 = (i & mwv) << LV;
@@ -431,7 +484,7 @@ __device__ void run_step_vec(const KArgs& a, const StepDesc& dref, int st, int i
 // A step with few outputs and a long k range: TPO (a power of two, at most
 // 32) consecutive lanes share one output, each summing every TPO-th k, and
 // combine their partial sums with shuffles (maxima in max-product mode).
-template <typename T, bool NORM, bool MAXP, bool G1>
+template <typename T, bool NORM, bool MAXP, bool G1, bool CL>
 __device__ void run_step_splitk(const KArgs& a, const StepDesc& dref, int st, int item_base, int lt,
                                 uint32_t* s_max, const StepPtrs<T>* ptrs, const PermTab& ptab) {
   const StepDesc d = dref;
@@ -444,10 +497,11 @@ __device__ void run_step_splitk(const KArgs& a, const StepDesc& dref, int st, in
   const int mfa = (1 << d.lfa) - 1;
   const int mw = (1 << lw) - 1;
   const int K = 1 << d.lk;
-  const int vt0 = rotated(int(threadIdx.x), item_base);
+  const int nthr = team_size<CL>();
+  const int vt0 = rotated(team_tid<CL>(), item_base, nthr);
   uint32_t run_bits = 0u;
   // whole warps iterate together (the shuffles below need every lane)
-  for (int vt = vt0; vt < total_r; vt += blockDim.x) {
+  for (int vt = vt0; vt < total_r; vt += nthr) {
     const bool valid = vt < total;
     const int item = vt >> lt, sub = vt & (tpo - 1);
     const int g = G1 ? 0 : (valid ? (item >> lw) : 0);
@@ -597,10 +651,10 @@ struct StepShape {
 };
 
 template <typename T>
-__device__ __forceinline__ StepShape step_shape(int lh, int lfa, int lfb, int lk, int lg, int flags, bool tensor) {
+__device__ __forceinline__ StepShape step_shape(int lh, int lfa, int lfb, int lk, int lg, int flags, bool tensor,
+                                                int64_t bd) {
   const int lw = lh + lfa + lfb;
   const int64_t outs = int64_t(1) << (lw + lg);
-  const int64_t bd = blockDim.x;
   StepShape sh;
   sh.lt = 0;
   const bool bT = (flags & kStepTensor) != 0;
@@ -765,11 +819,11 @@ __device__ void run_step_tc(const KArgs& a, const StepDesc& dref, int st, uint32
 // The planner hands the kernel arena and constant operands only (parity
 // operands become syndrome-selected tables), so each step shape has one code
 // path: the kernel stays small enough for the instruction caches.
-template <typename T, bool NORM, bool MAXP, bool G1, bool TENSOR>
+template <typename T, bool NORM, bool MAXP, bool G1, bool TENSOR, bool CL>
 __device__ __forceinline__ void dispatch_step(const KArgs& a, const StepDesc& d, const StepShape& sh, int st,
                                               int item_base, uint32_t* s_max, const StepPtrs<T>* ptrs,
                                               const PermTab& ptab, TcState* ts, unsigned char* tbuf) {
-  if constexpr (TENSOR && std::is_same<T, float>::value && NORM && !MAXP && G1) {
+  if constexpr (TENSOR && !CL && std::is_same<T, float>::value && NORM && !MAXP && G1) {
     if (sh.kind == SK_TENSOR) {
       run_step_tc<T, NORM>(a, d, st, s_max, ptrs, ptab, ts, tbuf);
       return;
@@ -777,16 +831,16 @@ __device__ __forceinline__ void dispatch_step(const KArgs& a, const StepDesc& d,
   }
   switch (sh.kind) {
     case SK_SPLITK:
-      run_step_splitk<T, NORM, MAXP, G1>(a, d, st, item_base, sh.lt, s_max, ptrs, ptab);
+      run_step_splitk<T, NORM, MAXP, G1, CL>(a, d, st, item_base, sh.lt, s_max, ptrs, ptab);
       break;
     case SK_VEC8:
-      run_step_vec<T, 8, NORM, MAXP, G1>(a, d, st, item_base, s_max, ptrs, ptab);
+      run_step_vec<T, 8, NORM, MAXP, G1, CL>(a, d, st, item_base, s_max, ptrs, ptab);
       break;
     case SK_VEC4:
-      run_step_vec<T, 4, NORM, MAXP, G1>(a, d, st, item_base, s_max, ptrs, ptab);
+      run_step_vec<T, 4, NORM, MAXP, G1, CL>(a, d, st, item_base, s_max, ptrs, ptab);
       break;
     default:
-      run_step<T, NORM, MAXP, G1>(a, d, st, item_base, s_max, ptrs, ptab);
+      run_step<T, NORM, MAXP, G1, CL>(a, d, st, item_base, s_max, ptrs, ptab);
   }
 }
 
@@ -845,14 +899,14 @@ __device__ __forceinline__ void copy16(void* dst, const void* src, size_t bytes)
 // fills the block for one syndrome alone, in a block of several), and how
 // many items (threads' worth) it takes, which also rotates the next member of
 // its barrier group.  One thread per step; the caller synchronises.
-template <typename T, bool tensor_ok>
+template <typename T, bool tensor_ok, bool CL>
 __device__ __forceinline__ void fill_step_plan(const KArgs& a, const StepDesc* steps, int2* plan) {
-  const int bd = int(blockDim.x);
+  const int bd = team_size<CL>();
   for (int st = threadIdx.x; st < a.n_steps; st += blockDim.x) {
     const StepDesc& d = steps[st];
     const bool tensor = tensor_ok && a.tc != 0;
-    const StepShape sh = step_shape<T>(d.lh, d.lfa, d.lfb, d.lk, a.lg, d.flags, tensor);
-    const StepShape sh1 = a.G > 1 ? step_shape<T>(d.lh, d.lfa, d.lfb, d.lk, 0, d.flags, tensor) : sh;
+    const StepShape sh = step_shape<T>(d.lh, d.lfa, d.lfb, d.lk, a.lg, d.flags, tensor, bd);
+    const StepShape sh1 = a.G > 1 ? step_shape<T>(d.lh, d.lfa, d.lfb, d.lk, 0, d.flags, tensor, bd) : sh;
     const bool per_syndrome = a.G > 1 && sh1.total_r >= bd;
     const StepShape& use = per_syndrome ? sh1 : sh;
     plan[st] = make_int2(use.kind | (use.lt << 8) | (int(per_syndrome) << 16), per_syndrome ? bd : sh.total_r);
@@ -862,7 +916,7 @@ __device__ __forceinline__ void fill_step_plan(const KArgs& a, const StepDesc* s
 // One group of up to G syndromes (rows base .. base+G-1 below nrows) through
 // the whole program: load the syndrome words, run every step, back-track
 // (MAP), then the epilogue.  Ends with a block barrier.
-template <typename T, bool NORM, bool MAXP, bool TENSOR>
+template <typename T, bool NORM, bool MAXP, bool TENSOR, bool CL>
 __device__ void contract_group(const KArgs& a, int64_t base, int64_t nrows, const BlockSmem& sm,
                                const Arena<T>& arena,
                                const T* consts, const PermTab& ptab) {
@@ -884,9 +938,11 @@ __device__ void contract_group(const KArgs& a, int64_t base, int64_t nrows, cons
     }
     s_syn[i] = word;
   }
-  if (NORM)
+  // the step maxima (in a cluster: the first block's, which every block
+  // updates and reads) start at zero before any block's step runs
+  if (NORM && (!CL || cluster_rank() == 0))
     for (int i = threadIdx.x; i < a.G * a.n_steps; i += blockDim.x) s_max[i] = 0u;
-  __syncthreads();
+  team_sync<CL>();
   fill_step_ptrs<T>(a, s_steps, s_syn, arena, consts, s_ptrs);
   __syncthreads();
   int item_base = 0;
@@ -901,21 +957,22 @@ __device__ void contract_group(const KArgs& a, int64_t base, int64_t nrows, cons
     const int items = pl.y;
     // first virtual thread of this warp (steps of a barrier group start on
     // different warps); a warp past the step's items goes to the barrier
-    const int vt_warp = rotated(int(threadIdx.x & ~31u), item_base);
+    const int vt_warp = rotated(team_tid<CL>() & ~31, item_base, team_size<CL>());
     if (vt_warp < items) {
       if (a.G == 1) {
-        dispatch_step<T, NORM, MAXP, true, TENSOR>(a, d, sh, st, item_base, s_max, s_ptrs, ptab, sm.tc, sm.tbuf);
+        dispatch_step<T, NORM, MAXP, true, TENSOR, CL>(a, d, sh, st, item_base, s_max, s_ptrs, ptab, sm.tc, sm.tbuf);
       } else if (per_syndrome) {
         // the block's syndromes one after another with hoisted invariants
         for (int g = 0; g < a.G; ++g)
-          dispatch_step<T, NORM, MAXP, true, TENSOR>(a, d, sh, st, item_base, s_max + g * a.n_steps,
-                                                     s_ptrs + g * a.n_steps, ptab, sm.tc, sm.tbuf);
+          dispatch_step<T, NORM, MAXP, true, TENSOR, CL>(a, d, sh, st, item_base, s_max + g * a.n_steps,
+                                                         s_ptrs + g * a.n_steps, ptab, sm.tc, sm.tbuf);
       } else {
-        dispatch_step<T, NORM, MAXP, false, TENSOR>(a, d, sh, st, item_base, s_max, s_ptrs, ptab, sm.tc, sm.tbuf);
+        dispatch_step<T, NORM, MAXP, false, TENSOR, CL>(a, d, sh, st, item_base, s_max, s_ptrs, ptab, sm.tc,
+                                                        sm.tbuf);
       }
     }
     if (d.flags & kStepSync) {
-      __syncthreads();
+      team_sync<CL>();
       item_base = 0;
     } else {
       item_base += items;
@@ -926,7 +983,7 @@ __device__ void contract_group(const KArgs& a, int64_t base, int64_t nrows, cons
     __syncthreads();
   }
   // epilogue: log-marginals, first argmax (Julia findmax order), recheck flag
-  for (int g = threadIdx.x; g < a.G; g += blockDim.x) {
+  for (int g = team_tid<CL>(); g < a.G; g += team_size<CL>()) {
     const int64_t r = base + g;
     if (r >= nrows) continue;
     const int64_t row = a.list ? int64_t(a.list[r]) : r + a.row_offset;
@@ -964,7 +1021,7 @@ __device__ void contract_group(const KArgs& a, int64_t base, int64_t nrows, cons
       }
     }
   }
-  __syncthreads();
+  team_sync<CL>();
 }
 
 // Stages the program's tables (if requested) after the fixed layout; returns
@@ -1015,7 +1072,7 @@ __global__ void __launch_bounds__(sizeof(T) == 8 || TENSOR ? 512 : 1024) tn_cont
   copy16(sm.steps, a.steps, size_t(a.n_steps) * sizeof(StepDesc));
   __syncthreads();
   constexpr bool kTensor = TENSOR && std::is_same<T, float>::value && NORM && !MAXP;
-  fill_step_plan<T, kTensor>(a, sm.steps, sm.plan);
+  fill_step_plan<T, kTensor, false>(a, sm.steps, sm.plan);
   const bool tensor = kTensor && a.tc;
   if (tensor) {
     if (threadIdx.x == 0) {
@@ -1031,7 +1088,7 @@ __global__ void __launch_bounds__(sizeof(T) == 8 || TENSOR ? 512 : 1024) tn_cont
   }
   const int64_t nrows = a.list ? int64_t(*a.list_count) : a.n;
   for (int64_t base = int64_t(blockIdx.x) * a.G; base < nrows; base += int64_t(gridDim.x) * a.G)
-    contract_group<T, NORM, MAXP, TENSOR>(a, base, nrows, sm, arena, consts, ptab);
+    contract_group<T, NORM, MAXP, TENSOR, false>(a, base, nrows, sm, arena, consts, ptab);
   if (tensor) {
     tc::fence_before();
     __syncthreads();
@@ -1043,6 +1100,39 @@ __global__ void __launch_bounds__(sizeof(T) == 8 || TENSOR ? 512 : 1024) tn_cont
       tc::dealloc(sm.tc->tmem, tc::kCols);
     }
   }
+}
+
+// One syndrome per thread-block cluster: the latency form for a few rows
+// (the plain float64 decode of single syndromes, the recheck of the rows
+// inside the float32 bound).  Every block of the cluster copies the step
+// records, plans and tables into its own shared memory; the cluster's
+// threads share each step's work items (rank-major numbering), the arena is
+// the cluster's slice of global memory, and the per-step maxima live in the
+// first block's shared memory, which the others update and read through
+// distributed shared memory.  Steps of a barrier group are separated by
+// cluster barriers (release/acquire at cluster scope).  Rows are taken
+// cluster by cluster in a grid-stride loop.
+template <typename T, bool NORM>
+__global__ void __launch_bounds__(512) tn_contract_cluster_kernel(KArgs a) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  BlockSmem sm = carve_smem<NORM, false>(a, smem);
+  size_t off = sm.tail;
+  const T* consts;
+  PermTab ptab;
+  stage_tables<T>(a, smem, &off, &consts, &ptab);
+  copy16(sm.steps, a.steps, size_t(a.n_steps) * sizeof(StepDesc));
+  __syncthreads();
+  fill_step_plan<T, false, true>(a, sm.steps, sm.plan);
+  if (NORM) sm.max = cluster_map(sm.max, 0);
+  const int64_t nrows = a.list ? int64_t(*a.list_count) : a.n;
+  const int64_t cid = cluster_id(), ncl = cluster_count();
+  T* slice = reinterpret_cast<T*>(a.arena_global) + cid * int64_t(a.G) * a.arena_elems;
+  const Arena<T> arena{slice, slice, INT32_MAX, int32_t(a.arena_elems), int32_t(a.arena_elems)};
+  for (int64_t base = cid * a.G; base < nrows; base += ncl * a.G)
+    contract_group<T, NORM, false, false, true>(a, base, nrows, sm, arena, consts, ptab);
+  // the first block's shared memory stays until no block of the cluster
+  // can still reach it
+  team_sync<true>();
 }
 
 // Several programs in one persistent launch.  Work units (program, first
@@ -1070,12 +1160,12 @@ __global__ void __launch_bounds__(kMultiThreads) tn_contract_multi_kernel(MultiA
     if (first) {
       copy16(sm.steps, a.steps, size_t(a.n_steps) * sizeof(StepDesc));
       __syncthreads();
-      fill_step_plan<T, false>(a, sm.steps, sm.plan);
+      fill_step_plan<T, false, false>(a, sm.steps, sm.plan);
       __syncthreads();
     }
     T* abase = a.arena_global ? gslice : reinterpret_cast<T*>(smem + sm.tail);
     const Arena<T> arena{abase, abase, INT32_MAX, int32_t(a.arena_elems), int32_t(a.arena_elems)};
-    contract_group<T, NORM, false, false>(a, base, nrows, sm, arena, reinterpret_cast<const T*>(a.consts),
+    contract_group<T, NORM, false, false, false>(a, base, nrows, sm, arena, reinterpret_cast<const T*>(a.consts),
                                           PermTab{a.perm, false});
   };
   if (m.list_mode) {
@@ -1088,7 +1178,7 @@ __global__ void __launch_bounds__(kMultiThreads) tn_contract_multi_kernel(MultiA
       const BlockSmem sm = carve_smem<NORM, false>(s_ka, smem);
       copy16(sm.steps, s_ka.steps, size_t(s_ka.n_steps) * sizeof(StepDesc));
       __syncthreads();
-      fill_step_plan<T, false>(s_ka, sm.steps, sm.plan);
+      fill_step_plan<T, false, false>(s_ka, sm.steps, sm.plan);
       __syncthreads();
       for (int64_t base = int64_t(blockIdx.x) * s_ka.G; base < nrows; base += int64_t(gridDim.x) * s_ka.G)
         run_unit(prog, base, nrows, false);
@@ -1191,6 +1281,74 @@ cudaError_t contract_launch(int precision, const KArgs& a, int grid, int threads
   }
   return a.map_mode ? launch_with(tn_contract_kernel<double, false, true, false>, a, grid, threads, smem, stream)
                     : launch_with(tn_contract_kernel<double, false, false, false>, a, grid, threads, smem, stream);
+}
+
+template <typename K>
+cudaError_t cluster_config(K kernel, int csize, int threads, size_t smem) {
+  cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+  if (e == cudaSuccess && csize > 8) e = cudaFuncSetAttribute(kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+  return e;
+}
+
+template <typename K>
+int cluster_capacity_of(K kernel, int csize, int threads, size_t smem) {
+  if (cluster_config(kernel, csize, threads, smem) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(csize);
+  cfg.blockDim = dim3(threads);
+  cfg.dynamicSmemBytes = smem;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = csize;
+  at[0].val.clusterDim.y = 1;
+  at[0].val.clusterDim.z = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  int n = 0;
+  if (cudaOccupancyMaxActiveClusters(&n, kernel, &cfg) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  return n;
+}
+
+template <typename K>
+cudaError_t cluster_launch_with(K kernel, const KArgs& a, int clusters, int csize, int threads, size_t smem,
+                                cudaStream_t stream) {
+  cudaError_t e = cluster_config(kernel, csize, threads, smem);
+  if (e != cudaSuccess) return e;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(unsigned(clusters) * unsigned(csize));
+  cfg.blockDim = dim3(threads);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = stream;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = csize;
+  at[0].val.clusterDim.y = 1;
+  at[0].val.clusterDim.z = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kernel, a);
+}
+
+int contract_cluster_capacity(int precision, int csize, int threads, size_t smem) {
+  if (precision == 2) return cluster_capacity_of(tn_contract_cluster_kernel<dfloat, true>, csize, threads, smem);
+  if (precision == 0) return cluster_capacity_of(tn_contract_cluster_kernel<double, false>, csize, threads, smem);
+  return 0;
+}
+
+cudaError_t contract_cluster_launch(int precision, const KArgs& a, int clusters, int csize, int threads, size_t smem,
+                                    cudaStream_t stream) {
+  if (a.map_mode || a.G != 1) return cudaErrorInvalidValue;
+  if (precision == 2)
+    return cluster_launch_with(tn_contract_cluster_kernel<dfloat, true>, a, clusters, csize, threads, smem, stream);
+  if (precision == 0)
+    return cluster_launch_with(tn_contract_cluster_kernel<double, false>, a, clusters, csize, threads, smem, stream);
+  return cudaErrorInvalidValue;
 }
 
 // Sets the shared-memory limit (outside any stream capture) and returns the

@@ -117,6 +117,14 @@ int contract_occupancy(int precision, int threads, size_t smem, bool map_mode = 
 cudaError_t contract_launch(int precision, const KArgs& a, int grid, int threads, size_t smem,
                             cudaStream_t stream);
 
+// The cluster form (one syndrome per thread-block cluster of csize blocks,
+// G = 1, arena in global memory: a.arena_global holds clusters * arena_elems
+// elements): float64 (precision 0) and double-float (precision 2).  Returns
+// the clusters that can be resident at once (0: the shape cannot launch).
+int contract_cluster_capacity(int precision, int csize, int threads, size_t smem);
+cudaError_t contract_cluster_launch(int precision, const KArgs& a, int clusters, int csize, int threads, size_t smem,
+                                    cudaStream_t stream);
+
 // The multi-program kernel (float32 normalised, or float64), and the
 // per-batch advance (batch + 1, unit counter and recheck counts to zero).
 cudaError_t contract_multi_launch(int precision, const MultiArgs& m, int grid, int threads, size_t smem,

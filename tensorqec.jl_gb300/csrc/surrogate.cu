@@ -73,6 +73,9 @@ struct tqec_mlp {
   size_t syn_cap = 0;
   float* tgt = nullptr;
   int32_t *cls = nullptr, *list = nullptr, *count = nullptr, *h_count = nullptr;
+  int32_t* h_counts = nullptr;                // pinned: rows each chunk of the last gated decode sent on
+  int64_t h_counts_cap = 0, last_chunks = 0;
+  int64_t fallback_hint = 0;                  // rows per chunk the gate sent on, when last read
   float* conf = nullptr;
   uint8_t* gathered = nullptr;
   int32_t* gcls = nullptr;
@@ -362,6 +365,7 @@ int tqec_mlp_destroy(tqec_mlp* p) {
   if (p->h_err) cudaFreeHost(p->h_err);
   if (p->h_loss) cudaFreeHost(p->h_loss);
   if (p->h_count) cudaFreeHost(p->h_count);
+  if (p->h_counts) cudaFreeHost(p->h_counts);
   if (p->stream) cudaStreamDestroy(p->stream);
   delete p;
   return TQEC_OK;
@@ -544,31 +548,55 @@ int tqec_gated_decode(tqec_mlp* p, tqec_program* prog, float threshold, const ui
   if ((rc = ensure_cap(p, std::min(n, chunk)))) return rc;
   const int sb = (p->cfg.n_in + 7) / 8;
   const bool host_cls = !dev_ptr(class_out);
-  int64_t total_fb = 0;
-  for (int64_t r0 = 0; r0 < n; r0 += chunk) {
+  const int64_t n_chunks = (n + chunk - 1) / chunk;
+  if (n_chunks > p->h_counts_cap) {
+    if (p->h_counts) cudaFreeHost(p->h_counts);
+    p->h_counts = nullptr;
+    p->h_counts_cap = 0;
+    SQ_CUDA(cudaMallocHost(&p->h_counts, sizeof(int32_t) * n_chunks));
+    p->h_counts_cap = n_chunks;
+  }
+  // per chunk, all stream-ordered: the forward pass and the gate write the
+  // surrogate's class of every row and list the rows below the threshold;
+  // the exact contraction then overwrites the classes of the listed rows
+  // (tqec_decode_rows, no host round trip), and the chunk's list length is
+  // copied to a pinned word for tqec_gated_last_fallback
+  for (int64_t c = 0; c < n_chunks; ++c) {
+    const int64_t r0 = c * chunk;
     const int64_t m = std::min(chunk, n - r0);
     const uint8_t* ds;
     if ((rc = stage_syn(p, syn + r0 * sb, m, st, &ds))) return rc;
     if ((rc = forward_infer(p, ds, m, st))) return rc;
+    int32_t* cls = host_cls ? p->cls : class_out + r0;
     SQ_CUDA(cudaMemsetAsync(p->count, 0, sizeof(int32_t), st));
-    SQ_CUDA(tqec::gate_rows(p->logits, p->out_pad, m, p->cfg.n_out, threshold, p->cls, p->conf, p->list, p->count,
-                            st));
-    SQ_CUDA(cudaMemcpyAsync(p->h_count, p->count, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
-    SQ_CUDA(cudaStreamSynchronize(st));
-    const int64_t nf = *p->h_count;
-    total_fb += nf;
-    if (nf > 0) {
-      SQ_CUDA(tqec::gather_rows(ds, sb, p->list, nf, p->gathered, st));
-      rc = tqec_decode_batch(prog, p->gathered, nf, p->gcls, nullptr, nullptr, st);
-      if (rc) return rc;
-      SQ_CUDA(tqec::scatter_classes(p->gcls, p->list, nf, p->cls, st));
+    SQ_CUDA(tqec::gate_rows(p->logits, p->out_pad, m, p->cfg.n_out, threshold, cls, p->conf, p->list, p->count, st));
+    rc = tqec_decode_rows(prog, ds, p->list, p->count, m, p->fallback_hint > 0 ? p->fallback_hint : m / 16, cls, st);
+    if (rc) return rc;
+    SQ_CUDA(cudaMemcpyAsync(p->h_counts + c, p->count, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+    if (host_cls) {
+      SQ_CUDA(cudaMemcpyAsync(class_out + r0, p->cls, sizeof(int32_t) * m, cudaMemcpyDeviceToHost, st));
+      SQ_CUDA(cudaStreamSynchronize(st));  // p->cls is reused by the next chunk
     }
-    SQ_CUDA(cudaMemcpyAsync(class_out + r0, p->cls, sizeof(int32_t) * m,
-                            host_cls ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice, st));
-    if (host_cls) SQ_CUDA(cudaStreamSynchronize(st));
   }
-  if (n_fallback_out) *n_fallback_out = total_fb;
+  p->last_chunks = n_chunks;
+  if (n_fallback_out || !stream) {
+    SQ_CUDA(cudaStreamSynchronize(st));
+    int64_t total = 0;
+    for (int64_t c = 0; c < n_chunks; ++c) total += p->h_counts[c];
+    if (n_chunks > 0) p->fallback_hint = std::max<int64_t>(1, total / n_chunks);
+    if (n_fallback_out) *n_fallback_out = total;
+  }
   if (!stream) return check_device_error(p, st);
+  return TQEC_OK;
+}
+
+int tqec_gated_last_fallback(tqec_mlp* p, int64_t* n_fallback) {
+  if (!p || !n_fallback) return sfail(TQEC_ERR_INVALID, "NULL argument");
+  std::lock_guard<std::mutex> lk(p->mu);
+  int64_t total = 0;
+  for (int64_t c = 0; c < p->last_chunks; ++c) total += p->h_counts[c];
+  if (p->last_chunks > 0) p->fallback_hint = std::max<int64_t>(1, total / p->last_chunks);
+  *n_fallback = total;
   return TQEC_OK;
 }
 

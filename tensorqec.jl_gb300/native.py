@@ -60,7 +60,7 @@ class ProgramInfo(C.Structure):
                 ("resident_f32", C.c_int32), ("resident_f64", C.c_int32), ("tables_smem_f32", C.c_int32),
                 ("tables_smem_f64", C.c_int32), ("arena_small", C.c_int64), ("split_f32", C.c_int32),
                 ("split_f64", C.c_int32), ("tensor_steps", C.c_int32), ("tensor_f32", C.c_int32),
-                ("recheck_precision", C.c_int32), ("reserved_", C.c_int32), ("err_bound_f32x2", C.c_double)]
+                ("recheck_precision", C.c_int32), ("cluster_blocks", C.c_int32), ("err_bound_f32x2", C.c_double)]
 
 
 class PlanView(C.Structure):

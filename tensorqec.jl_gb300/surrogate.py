@@ -34,6 +34,7 @@ def _lib():
                "tqec_mlp_train_step_rows": [vp, vp, vp, i64, vp, i64, C.c_float, vp, vp],
                "tqec_mlp_infer": [vp, vp, i64, vp, vp, vp],
                "tqec_gated_decode": [vp, vp, C.c_float, vp, i64, vp, vp, vp],
+               "tqec_gated_last_fallback": [vp, vp],
                "tqec_mlp_save": [vp, C.c_char_p], "tqec_mlp_load": [vp, C.c_char_p],
                "tqec_mlp_set_gemm": [vp, C.c_int], "tqec_mlp_forward_logits": [vp, vp, i64, vp]}
         for name, args in sig.items():
@@ -316,11 +317,26 @@ class GatedDecoder:
         self.last_fallback = nf.value
         return classes
 
-    def decode_ptrs(self, syn_ptr, n, cls_ptr, stream=None):
+    def decode_ptrs(self, syn_ptr, n, cls_ptr, stream=None, wait=True):
+        """Device (or host) buffers.  wait=False with a stream: the call
+        returns without a host synchronisation; after synchronising the
+        stream, ``fallback_count()`` gives the rows sent to the contraction."""
         nf = C.c_int64()
+        sync = wait or not stream
         native.check(_lib().tqec_gated_decode(self.sur.handle, self.ct.program._h, self.threshold,
-                                              C.c_void_p(syn_ptr), n, C.c_void_p(cls_ptr), C.byref(nf),
+                                              C.c_void_p(syn_ptr), n, C.c_void_p(cls_ptr),
+                                              C.byref(nf) if sync else None,
                                               C.c_void_p(stream) if stream else None))
+        if sync:
+            self.last_fallback = nf.value
+            return nf.value
+        return None
+
+    def fallback_count(self):
+        """Rows the last decode sent to the exact contraction (synchronise
+        the stream of an asynchronous decode first)."""
+        nf = C.c_int64()
+        native.check(_lib().tqec_gated_last_fallback(self.sur.handle, C.byref(nf)))
         self.last_fallback = nf.value
         return nf.value
 

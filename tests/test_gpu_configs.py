@@ -91,6 +91,31 @@ def test_config1_d3_thousand_errors_float64(pkg, oracle):
         ct.close()
 
 
+@pytest.mark.parametrize("tune", [False, True])
+def test_plain_float64_d7_on_clusters_vs_oracle(pkg, oracle, tune):
+    """The plain form at d=7: each syndrome contracted in float64 by one
+    thread-block cluster (a wide program's default; the autotuner may keep it
+    or pick the one-block form), one row per decode call and a batch of
+    rows: classes equal to the oracle's outside ties, every class
+    log-probability within 1e-10 relative."""
+    t, em, bits, net = _surface(pkg, oracle, 7, 0.08, 96, 0x7E5A0017)
+    ct = pkg.compile(pkg.TNMMAP(precision="f64", plain=True, optimizer=pkg.FixedOrder(
+        pkg.load_order(os.path.join(ROOT, "tensorqec.jl_gb300", "orders", "surface_d7.tree")))), t, em)
+    if tune:
+        ct.program.autotune(1024)
+    else:
+        assert ct.program.info["cluster_blocks"] == 8
+    want, _ = _oracle_marginals(pkg, oracle, ct, net, bits)
+    cls, logp = ct.decode_batch(bits, return_logp=True)
+    assert_decisions(cls, want)
+    assert_class_logprobs(logp, want, 1e-10)
+    for r in range(0, 96, 19):  # single-syndrome calls, as the drop-in decode makes them
+        c1, l1 = ct.decode_batch(bits[r:r + 1], return_logp=True)
+        assert c1[0] == cls[r]
+        assert_class_logprobs(l1, want[r:r + 1], 1e-10)
+    ct.close()
+
+
 @pytest.mark.parametrize("d", [5, 7])
 @pytest.mark.parametrize("p", [0.02, 0.05, 0.08, 0.11])
 def test_config2_p_sweep_vs_oracle(pkg, oracle, d, p):

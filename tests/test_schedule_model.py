@@ -1,6 +1,6 @@
 """A CPU model of how the contraction kernel spreads a step over a block.
 
-It restates the kernel's step-shape choice (several lanes per output, eight
+It restates the kernels' step-shape choice (several lanes per output, eight
 or four outputs per work item, or one), its per-warp entry test, the
 rotation of barrier-group members over the block and the per-syndrome loop
 of multi-syndrome blocks (csrc/contract.cu: step_shape, the step loop of
@@ -66,8 +66,10 @@ def check_program(plan, is_float):
     bad = []
     for G in (1, 2, 4, 8):
         lg = G.bit_length() - 1
-        for bd in (128, 256, 512, 1024):
-            if not is_float and bd > 512:
+        # blocks, and for one syndrome the teams of 2-16-block clusters of
+        # 256 or 512 threads (the cluster kernel numbers them rank-major)
+        for bd in (128, 256, 512, 1024) + ((2048, 4096, 8192) if G == 1 else ()):
+            if not is_float and 512 < bd <= 1024:
                 continue
             item_base = 0
             for st, d in enumerate(plan["steps"]):
