@@ -200,6 +200,14 @@ int tqec_map_decode_batch(tqec_program* prog, const uint8_t* syndromes, int64_t 
  * outputs), synchronise that stream before asking. */
 int tqec_last_recheck_count(const tqec_program* prog, int64_t* count);
 
+/* The form of single-syndrome launches in `precision` (TQEC_F64: the plain
+ * form's; TQEC_F32X2 or TQEC_F64: the recheck's): blocks = 0 gives each
+ * syndrome one block, blocks = 2, 4, 8 or 16 a thread-block cluster of that
+ * many blocks of `threads` threads that share each step's work.  Wide
+ * programs start with 8 blocks of 512 threads; tqec_program_autotune
+ * measures the forms.  No reference counterpart (a latency setting). */
+int tqec_program_set_cluster(tqec_program* prog, int32_t precision, int32_t blocks, int32_t threads);
+
 /* Tries the launch shapes that fit and keeps the fastest for each
  * precision, timing n_probe synthetic syndromes. */
 int tqec_program_autotune(tqec_program* prog, int64_t n_probe);

@@ -1077,6 +1077,28 @@ bool tune_cluster(tqec_program* p, int prec, bool plain, cudaEvent_t e0, cudaEve
 
 }  // namespace
 
+int tqec_program_set_cluster(tqec_program* p, int32_t precision, int32_t blocks, int32_t threads) {
+  if (!p) return fail(TQEC_ERR_INVALID, "NULL program");
+  if (precision != TQEC_F64 && precision != TQEC_F32X2)
+    return fail(TQEC_ERR_INVALID, "clusters serve TQEC_F64 and TQEC_F32X2 launches");
+  std::lock_guard<std::mutex> lk(p->mu);
+  TQ_CUDA(cudaSetDevice(p->device));
+  if (blocks == 0) {
+    p->cluster[precision] = ClusterShape{};
+    return TQEC_OK;
+  }
+  if (blocks < 2 || blocks > 16 || (blocks & (blocks - 1)) || threads < 32 || threads > 512 ||
+      (threads & (threads - 1)))
+    return fail(TQEC_ERR_INVALID, "blocks must be 0 or 2, 4, 8, 16; threads a power of two from 32 to 512");
+  ClusterShape c;
+  if (!choose_cluster(p, precision, blocks, threads, &c)) {
+    cudaGetLastError();
+    return fail(TQEC_ERR_UNSUPPORTED, "this cluster shape cannot launch for this program on this device");
+  }
+  p->cluster[precision] = c;
+  return TQEC_OK;
+}
+
 int tqec_program_autotune(tqec_program* p, int64_t n_probe) {
   if (!p || n_probe <= 0) return fail(TQEC_ERR_INVALID, "bad argument");
   std::lock_guard<std::mutex> lk(p->mu);
