@@ -441,7 +441,9 @@ int launch_plain(tqec_program* p, int precision, tqec::KArgs a, int64_t n, cudaS
 // The re-contraction of the rows a float32 launch listed (b.list,
 // b.list_count on the device; at most n_max of them).
 // Programs at least this wide (log2 of the largest intermediate) run their
-// single-syndrome launches on clusters by default.
+// single-syndrome launches on clusters by default: 16 blocks of 128 threads
+// (at surface d=7 the fastest single-row form in float64 and double-float,
+// about half the one-block latency), else 8 of 256.
 constexpr int kClusterMinWidth = 12;
 
 void default_clusters(tqec_program* p) {
@@ -451,7 +453,7 @@ void default_clusters(tqec_program* p) {
   for (int prec : {recheck_precision(p), plain ? p->precision : -1}) {
     if (prec < 0) continue;
     ClusterShape c;
-    if (choose_cluster(p, prec, 8, 512, &c)) p->cluster[prec] = c;
+    if (choose_cluster(p, prec, 16, 128, &c) || choose_cluster(p, prec, 8, 256, &c)) p->cluster[prec] = c;
   }
   cudaGetLastError();
 }
@@ -1028,11 +1030,13 @@ namespace {
 
 // Single-syndrome launches of one precision: the block form (the recheck
 // shape, or one launch per row in the plain form) against clusters of 2-16
-// blocks of 256 or 512 threads, timed on 1 and on 8 rows (the sum decides).
+// blocks of 128, 256 or 512 threads, timed on one row (the plain form: the
+// drop-in decodes one syndrome a call) or on one and on four rows (the
+// recheck: a few rows a batch; the sum decides).
 bool tune_cluster(tqec_program* p, int prec, bool plain, cudaEvent_t e0, cudaEvent_t e1) {
   std::vector<ClusterShape> cands(1);  // the block form
   for (int cs : {2, 4, 8, 16})
-    for (int th : {256, 512}) {
+    for (int th : {128, 256, 512}) {
       ClusterShape c;
       if (choose_cluster(p, prec, cs, th, &c)) cands.push_back(c);
     }
@@ -1043,7 +1047,8 @@ bool tune_cluster(tqec_program* p, int prec, bool plain, cudaEvent_t e0, cudaEve
     p->cluster[prec] = c;
     float total = 0.f;
     bool ok = true;
-    for (int64_t rows : {int64_t(1), int64_t(8)}) {
+    for (int64_t rows : {int64_t(1), int64_t(plain ? 0 : 4)}) {
+      if (rows == 0) continue;
       tqec::KArgs a = base_args(p, prec);
       a.syn = (const uint8_t*)p->syn.p;
       a.n = rows;

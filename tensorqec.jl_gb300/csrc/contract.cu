@@ -423,6 +423,34 @@ __device__ void run_step_vec(const KArgs& a, const StepDesc& dref, int st, int i
       };
       if (K == 1) {
         body(0);
+      } else if (K >= 4) {
+        // four k at a time with every load issued before the multiply-adds
+        // (A as one 16-byte vector: rows are K >= 4 elements and operand
+        // bases are 4-aligned), so a step whose operands come from L2 waits
+        // once per four k instead of once per two
+        for (int k = 0; k < K; k += 4) {
+          T a4[4], b4[4][VW];
+          load4<T>(pa + k, a4);
+#pragma unroll
+          for (int c = 0; c < 4; ++c) {
+            load4<T>(pb + (k + c) * bstride, b4[c]);
+            if (VW == 8) load4<T>(pb + (k + c) * bstride + 4, b4[c] + 4);
+          }
+#pragma unroll
+          for (int c = 0; c < 4; ++c) {
+            T av = a4[c];
+            if (NORM) av = scale(scale(av, fa_s), fb_s);
+#pragma unroll
+            for (int j = 0; j < VW; ++j) {
+              if constexpr (MAXP) {
+                const T v = av * b4[c][j];
+                acc[j] = v > acc[j] ? v : acc[j];
+              } else {
+                acc[j] = fma(av, b4[c][j], acc[j]);
+              }
+            }
+          }
+        }
       } else {
         for (int k = 0; k < K; k += 2) {
           body(k);
@@ -833,8 +861,8 @@ __device__ __forceinline__ void dispatch_step(const KArgs& a, const StepDesc& d,
     case SK_SPLITK:
       run_step_splitk<T, NORM, MAXP, G1, CL>(a, d, st, item_base, sh.lt, s_max, ptrs, ptab);
       break;
-    case SK_VEC8:
-      run_step_vec<T, 8, NORM, MAXP, G1, CL>(a, d, st, item_base, s_max, ptrs, ptab);
+    case SK_VEC8:  // float32 only (step_shape)
+      if constexpr (sizeof(T) == 4) run_step_vec<T, 8, NORM, MAXP, G1, CL>(a, d, st, item_base, s_max, ptrs, ptab);
       break;
     case SK_VEC4:
       run_step_vec<T, 4, NORM, MAXP, G1, CL>(a, d, st, item_base, s_max, ptrs, ptab);

@@ -104,7 +104,7 @@ def test_plain_float64_d7_on_clusters_vs_oracle(pkg, oracle, tune):
     if tune:
         ct.program.autotune(1024)
     else:
-        assert ct.program.info["cluster_blocks"] == 8
+        assert ct.program.info["cluster_blocks"] in (8, 16)
     want, _ = _oracle_marginals(pkg, oracle, ct, net, bits)
     cls, logp = ct.decode_batch(bits, return_logp=True)
     assert_decisions(cls, want)

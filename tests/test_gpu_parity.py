@@ -342,7 +342,7 @@ def test_recheck_every_row(pkg, recheck_f64):
     info = ct.program.info
     want_prec = pkg.native.TQEC_F64 if recheck_f64 else pkg.native.TQEC_F32X2
     assert info["recheck_precision"] == want_prec
-    assert info["cluster_blocks"] == 8  # d=7 is wide: each recheck row on an 8-block cluster
+    assert info["cluster_blocks"] in (8, 16)  # d=7 is wide: each recheck row on a cluster
     packed = pkg.pack_syndromes(bits)
     logp = np.empty((len(bits), ct.n_classes))
     err = np.empty(len(bits), dtype=np.float32)
