@@ -78,6 +78,9 @@ def parse():
     ap.add_argument("--split-arena", action="store_true",
                     help="--profile: small intermediates in shared memory, large ones in global memory")
     ap.add_argument("--no-surrogate", action="store_true", help="time the batched exact decoder alone")
+    ap.add_argument("--surrogate-cache", default="",
+                    help="checkpoint file: load the trained surrogate from it when it exists (skipping training "
+                         "and calibration), else train and write it (profiling runs reuse one training)")
     ap.add_argument("--train-n", type=int, default=1 << 26, help="surrogate training syndromes")
     ap.add_argument("--train-epochs", type=int, default=16, help="surrogate training epochs")
     ap.add_argument("--calib-n", type=int, default=1 << 20, help="surrogate calibration syndromes")
@@ -425,12 +428,25 @@ def run_ours(args):
     sur_stats = None
     if not args.no_surrogate:
         t0 = time.time()
-        sur, tstats = train_surrogate(ct, n_train=args.train_n, batch=16384, epochs=args.train_epochs, lr=3e-3, hidden=512,
-                                      n_layers=4, seed=SEED + 17 + rank)
-        # calibrated at half the 1e-4 mismatch limit so fresh syndromes stay under it
-        thr, cstats = calibrate(sur, ct, n_val=args.calib_n, target_mismatch=5e-5, seed=SEED + 29 + rank)
+        cache = args.surrogate_cache
+        if cache and os.path.exists(cache) and os.path.exists(cache + ".json"):
+            from tensorqec_gb300.surrogate import Surrogate
+
+            sur = Surrogate(ct.n_syndrome, ct.n_classes, 512, 4, seed=SEED + 17 + rank, device=local)
+            sur.load(cache)
+            meta = json.load(open(cache + ".json"))
+            thr = meta["threshold"]
+            sur_stats = dict(meta["stats"], loaded_from_cache=True)
+        else:
+            sur, tstats = train_surrogate(ct, n_train=args.train_n, batch=16384, epochs=args.train_epochs, lr=3e-3,
+                                          hidden=512, n_layers=4, seed=SEED + 17 + rank)
+            # calibrated at half the 1e-4 mismatch limit so fresh syndromes stay under it
+            thr, cstats = calibrate(sur, ct, n_val=args.calib_n, target_mismatch=5e-5, seed=SEED + 29 + rank)
+            sur_stats = {"train": tstats, "calibration": cstats, "setup_seconds": time.time() - t0}
+            if cache:
+                sur.save(cache)
+                json.dump({"threshold": thr, "stats": sur_stats}, open(cache + ".json", "w"))
         gd = GatedDecoder(ct, sur, thr)
-        sur_stats = {"train": tstats, "calibration": cstats, "setup_seconds": time.time() - t0}
 
     def decode(syn_ptr, cls_ptr):
         if gd is not None:

@@ -541,7 +541,11 @@ int decode_locked(tqec_program* p, const uint8_t* syn, int64_t n, int32_t* cls, 
         a.class_out = (int32_t*)p->cls.p;
       }
     }
-    rc = plain ? launch_plain(p, precision, a, n, st) : launch_rows(p, precision, a, n, st);
+    // a batch no larger than one wave of clusters takes the cluster form
+    // of its precision (float64, double-float) where the program has one
+    const bool few = precision != TQEC_F32 && p->cluster[precision].size > 0 && n <= p->cluster[precision].cap;
+    rc = plain ? launch_plain(p, precision, a, n, st)
+               : few ? launch_cluster_rows(p, precision, a, n, st) : launch_rows(p, precision, a, n, st);
     if (rc) return rc;
     if (recheck && precision == TQEC_F32) {
       tqec::KArgs b = base_args(p, recheck_precision(p));
