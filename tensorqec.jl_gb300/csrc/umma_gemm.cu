@@ -264,17 +264,22 @@ bool make_map(CUtensorMap* map, const __nv_bfloat16* base, int rows, int cols, i
 // reads); the 512-wide float32 accumulator fills all of tensor memory (two
 // 256-column halves).  Warp 0 streams 256x64 weight tiles through a 3-stage
 // ring with TMA; warp 1 issues the MMAs of a layer once its input is ready
-// and commits the accumulator; warps 4-7 (one TMEM lane quadrant each, one
-// row per thread) write the layer-1 input from the packed syndrome bits,
-// turn each accumulator into the next layer's bf16 input (bias, ReLU), and
-// for the last hidden layer compute the output logits directly from tensor
-// memory.  No activation leaves the SM.  Every wait is bounded.
+// and commits the accumulator; two groups of four epilogue warps (4-7 and
+// 8-11: one TMEM lane quadrant per warp, one row per thread, the group's
+// half of the 512 columns) write the layer-1 input from the packed syndrome
+// bits, turn each accumulator into the next layer's bf16 input (bias, ReLU),
+// and for the last hidden layer compute the output logits directly from
+// tensor memory (the two halves' partial sums meet in shared memory).  No
+// activation leaves the SM.  Every mbarrier wait is bounded; the epilogue
+// groups' named barrier sits outside every conditional, so both groups
+// always reach it.
 constexpr int FM = 128, FH = 512, FNH = 256, FSTAGES = 3;
 constexpr int FA_TILE = FM * UK * 2;           // 16 KB: 128 rows x 64 bf16
 constexpr int FA_BYTES = (FH / UK) * FA_TILE;  // 128 KB: a layer input
 constexpr int FB_STAGE = FNH * UK * 2;         // 32 KB: 256 weight rows x 64 bf16
 constexpr uint32_t FTMEM_COLS = 512;
-constexpr int FTHREADS = 256;
+constexpr int FTHREADS = 384;
+constexpr int FEPI = 256;  // epilogue threads (warps 4-11)
 constexpr int FMAX_OUT = 16;
 constexpr size_t FUSED_SMEM = size_t(FA_BYTES) + size_t(FSTAGES) * FB_STAGE + 256 + 1024;
 
@@ -328,7 +333,7 @@ __global__ void __launch_bounds__(FTHREADS, 1)
       mbar_init(&empty[s], 1);
     }
     mbar_init(acc_ready, 1);
-    mbar_init(a_ready, 128);  // every epilogue thread
+    mbar_init(a_ready, FEPI);  // every epilogue thread
     mbar_init(mma_done, 1);
     *abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -412,9 +417,12 @@ __global__ void __launch_bounds__(FTHREADS, 1)
     umma_commit(mma_done);
     mbar_wait(mma_done, 0u, a.err);
   } else if (warp >= 4) {
-    // epilogue: TMEM lane quadrant qd, row r of the tile per thread
+    // epilogue: TMEM lane quadrant qd, row r of the tile per thread; group
+    // `half` owns columns [256 half, 256 half + 256) of every accumulator
     const int qd = warp & 3;
+    const int half = (warp - 4) >> 2;
     const int r = qd * 32 + lane;
+    float* partial = reinterpret_cast<float*>(sA);  // [128][FMAX_OUT], last layer only
     uint32_t c = 0;
     bool ok = true;
     for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
@@ -425,7 +433,7 @@ __global__ void __launch_bounds__(FTHREADS, 1)
 #pragma unroll
         for (int b = 0; b < 8; ++b) bytes[b] = (row < a.n && b < a.sb) ? uint32_t(a.syn[row * a.sb + b]) : 0u;
 #pragma unroll
-        for (int ch = 0; ch < 8; ++ch) {
+        for (int ch = 4 * half; ch < 4 * half + 4; ++ch) {
           uint32_t w[4];
 #pragma unroll
           for (int j = 0; j < 4; ++j) {
@@ -455,7 +463,7 @@ __global__ void __launch_bounds__(FTHREADS, 1)
         if (go) {
           const float* bias = a.bias[L];
 #pragma unroll 1
-          for (int cc = 0; cc < FH / 32; ++cc) {
+          for (int cc = half * (FH / 64); cc < (half + 1) * (FH / 64); ++cc) {
             uint32_t v[32];
             tmem_ld32(tmem + (uint32_t(qd * 32) << 16) + uint32_t(cc * 32), v);
             float x[32];
@@ -505,8 +513,16 @@ __global__ void __launch_bounds__(FTHREADS, 1)
           fence_proxy_async_smem();
           asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
           mbar_arrive(a_ready);
-        } else if (go && row < a.n) {
-          for (int o = 0; o < a.n_out; ++o) a.logits[row * a.ldl + o] = lg[o] + a.b4[o];
+        } else {
+          // the last layer's input has been read by every MMA (acc_ready), so
+          // its shared memory holds the second group's partial sums
+          if (half == 1)
+            for (int o = 0; o < a.n_out; ++o) partial[r * FMAX_OUT + o] = lg[o];
+          asm volatile("bar.sync 1, %0;" ::"n"(FEPI) : "memory");
+          if (half == 0 && go && row < a.n)
+            for (int o = 0; o < a.n_out; ++o) a.logits[row * a.ldl + o] = lg[o] + partial[r * FMAX_OUT + o] + a.b4[o];
+          // the next tile's layer-1 input overwrites that memory only after
+          asm volatile("bar.sync 1, %0;" ::"n"(FEPI) : "memory");
         }
       }
     }
