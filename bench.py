@@ -66,6 +66,10 @@ def parse():
                          "p ~ U[0.01, 0.1], 100,000 syndromes in batches of --mixed-batch, one persistent launch "
                          "per batch replayed from a CUDA graph; p50/p99 batch latency")
     ap.add_argument("--mixed-batch", type=int, default=1000)
+    ap.add_argument("--latency", action="store_true",
+                    help="single-syndrome latency of the d=7 plain float64 decode and of the float32 decode whose "
+                         "row is always rechecked, for each single-syndrome launch form (one block, clusters of "
+                         "2-16 blocks), then the autotuned form; one JSON line per form")
     ap.add_argument("--circuit", action="store_true",
                     help="circuit-level rotated Z-memory d=5, 5 rounds, p=0.001: DEM from the generator, "
                          "--circuit-n seeded detector samples, float32 + recheck")
@@ -904,6 +908,56 @@ def run_mixed(args):
         p_.close()
 
 
+def run_latency(args):
+    """One decode call of one syndrome at a time (CUDA events around each
+    call, median of 40): the plain float64 form, and a float32 program whose
+    margin sends its row to the double-float recheck."""
+    import torch
+
+    import __graft_entry__ as G
+
+    pkg = G.load_package()
+    N = pkg.native
+    t, em, bits = workload(pkg, 0, 1, 256)
+    packed = pkg.pack_syndromes(bits[0])
+    d_syn = torch.from_numpy(packed).cuda()
+    d_cls = torch.empty(256, dtype=torch.int32, device="cuda")
+    st = torch.cuda.current_stream()
+
+    def lat(prog, reps=40):
+        out = []
+        for i in range(reps):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(st)
+            prog.decode_ptrs(d_syn.data_ptr() + (i % 200) * packed.shape[1], 1, d_cls.data_ptr(), None, None,
+                             st.cuda_stream)
+            b.record(st)
+            torch.cuda.synchronize()
+            out.append(a.elapsed_time(b) * 1e3)
+        return statistics.median(out)
+
+    plain = pkg.compile(pkg.TNMMAP(precision="f64", plain=True, optimizer=d7_order(pkg)), t, em)
+    rech = pkg.compile(pkg.TNMMAP(precision="f32", margin=1e30, optimizer=d7_order(pkg)), t, em)
+    for blocks in (0, 2, 4, 8, 16):
+        for th in ((128, 256, 512) if blocks else (0,)):
+            row = {"latency": "single syndrome", "cluster_blocks": blocks, "threads": th or "block form"}
+            for name, prog, prec in (("plain_f64_us", plain.program, N.TQEC_F64),
+                                     ("f32_then_recheck_us", rech.program, N.TQEC_F32X2)):
+                try:
+                    prog.set_cluster(prec, blocks, th or 512)
+                    lat(prog, 5)
+                    row[name] = lat(prog)
+                except N.TqecError as e:
+                    row[name] = f"not launchable: {e}"
+            print(json.dumps(row), flush=True)
+    for name, ct in (("plain_f64", plain), ("f32_then_recheck", rech)):
+        ct.program.autotune(1024)
+        print(json.dumps({"latency": "single syndrome, autotuned", "program": name,
+                          "cluster_blocks": ct.program.info["cluster_blocks"], "us": lat(ct.program)}), flush=True)
+    plain.close()
+    rech.close()
+
+
 def circuit_program(args):
     """The Z-memory circuit (d=5, 5 rounds, p=0.001), its detector error
     model and the compiled float32 program of its factor graph."""
@@ -1012,6 +1066,8 @@ def main():
         run_circuit(args)
     elif args.mixed:
         run_mixed(args)
+    elif args.latency:
+        run_latency(args)
     elif args.precision_sweep:
         run_precision_sweep(args)
     elif args.profile_recheck:

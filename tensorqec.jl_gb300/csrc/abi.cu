@@ -96,6 +96,7 @@ struct ClusterShape {
   int cap = 0;
   size_t smem = 0;
   bool tables = false;
+  bool split = false;  // the small pool in the first block's shared memory
 };
 
 struct tqec_program {
@@ -360,10 +361,23 @@ bool choose_cluster(tqec_program* p, int precision, int csize, int threads, Clus
   c.size = csize;
   c.threads = threads;
   const size_t tb = table_bytes(p, precision);
-  c.smem = tqec::contract_smem_bytes(precision, nsteps, syn_words(p), 1, p->plan.arena_elems, false, 0, tb);
-  c.tables = c.smem <= limit;
-  if (!c.tables) c.smem = tqec::contract_smem_bytes(precision, nsteps, syn_words(p), 1, p->plan.arena_elems, false);
-  if (c.smem > limit) return false;
+  // the small pool in shared memory when the program has one and it fits
+  // with the tables, else beside global tables, else everything global
+  const int sw = syn_words(p);
+  const int64_t small = p->plan.arena_small;
+  bool found = false;
+  for (int split : {1, 0})
+    for (int tables : {1, 0}) {
+      if (found || (split && small <= 0)) continue;
+      const size_t b = tqec::contract_smem_bytes(precision, nsteps, sw, 1, split ? small : p->plan.arena_elems,
+                                                 split != 0, 0, tables ? tb : 0);
+      if (b > limit) continue;
+      c.smem = b;
+      c.tables = tables != 0;
+      c.split = split != 0;
+      found = true;
+    }
+  if (!found) return false;
   c.cap = tqec::contract_cluster_capacity(precision, csize, threads, c.smem);
   if (c.cap < 1) return false;
   *out = c;
@@ -376,13 +390,14 @@ int launch_cluster_rows(tqec_program* p, int precision, tqec::KArgs a, int64_t n
   const ClusterShape& c = p->cluster[precision];
   const int clusters = (int)std::max<int64_t>(1, std::min<int64_t>(n_rows_max, c.cap));
   const size_t esz = precision == TQEC_F32 ? 4 : 8;
-  TQ_CUDA(p->carena[precision].ensure(size_t(clusters) * size_t(p->plan.arena_elems) * esz));
+  const int64_t per = c.split ? p->plan.arena_elems - p->plan.arena_small : p->plan.arena_elems;
+  TQ_CUDA(p->carena[precision].ensure(size_t(clusters) * size_t(std::max<int64_t>(per, 1)) * esz));
   a.G = 1;
   a.lg = 0;
   a.tables_smem = c.tables ? 1 : 0;
   a.perm16 = c.tables ? p->d_perm16 : nullptr;
   a.arena_global = p->carena[precision].p;
-  a.arena_small = 0;
+  a.arena_small = c.split ? p->plan.arena_small : 0;
   a.tc = 0;
   TQ_CUDA(tqec::contract_cluster_launch(precision, a, clusters, c.size, c.threads, c.smem, st));
   return TQEC_OK;

@@ -1154,8 +1154,19 @@ __global__ void __launch_bounds__(512) tn_contract_cluster_kernel(KArgs a) {
   if (NORM) sm.max = cluster_map(sm.max, 0);
   const int64_t nrows = a.list ? int64_t(*a.list_count) : a.n;
   const int64_t cid = cluster_id(), ncl = cluster_count();
-  T* slice = reinterpret_cast<T*>(a.arena_global) + cid * int64_t(a.G) * a.arena_elems;
-  const Arena<T> arena{slice, slice, INT32_MAX, int32_t(a.arena_elems), int32_t(a.arena_elems)};
+  Arena<T> arena;
+  if (a.arena_small > 0) {
+    // the small tensors in the first block's shared memory (reached by every
+    // block through distributed shared memory), the large ones in the
+    // cluster's slice of global memory
+    const int64_t big = a.arena_elems - a.arena_small;
+    T* slice = reinterpret_cast<T*>(a.arena_global) + cid * big;
+    T* small = cluster_map(reinterpret_cast<T*>(smem + off), 0);
+    arena = Arena<T>{small, slice - a.arena_small, int32_t(a.arena_small), int32_t(a.arena_small), int32_t(big)};
+  } else {
+    T* slice = reinterpret_cast<T*>(a.arena_global) + cid * int64_t(a.G) * a.arena_elems;
+    arena = Arena<T>{slice, slice, INT32_MAX, int32_t(a.arena_elems), int32_t(a.arena_elems)};
+  }
   for (int64_t base = cid * a.G; base < nrows; base += ncl * a.G)
     contract_group<T, NORM, false, false, true>(a, base, nrows, sm, arena, consts, ptab);
   // the first block's shared memory stays until no block of the cluster

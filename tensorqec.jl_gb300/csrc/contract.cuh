@@ -118,8 +118,10 @@ cudaError_t contract_launch(int precision, const KArgs& a, int grid, int threads
                             cudaStream_t stream);
 
 // The cluster form (one syndrome per thread-block cluster of csize blocks,
-// G = 1, arena in global memory: a.arena_global holds clusters * arena_elems
-// elements): float64 (precision 0) and double-float (precision 2).  Returns
+// G = 1; arena in global memory, a.arena_global holding clusters *
+// arena_elems elements, or with a.arena_small > 0 the small pool in the first
+// block's shared memory and clusters * (arena_elems - arena_small) elements
+// in a.arena_global): float64 (precision 0) and double-float (precision 2).  Returns
 // the clusters that can be resident at once (0: the shape cannot launch).
 int contract_cluster_capacity(int precision, int csize, int threads, size_t smem);
 cudaError_t contract_cluster_launch(int precision, const KArgs& a, int clusters, int csize, int threads, size_t smem,
