@@ -359,7 +359,7 @@ __device__ __forceinline__ void store4<dfloat>(dfloat* p, const dfloat v[4]) {
 // one warp instruction over more shared-memory banks.
 template <typename T, int VW, bool NORM, bool MAXP, bool G1, bool CL>
 __device__ void run_step_vec(const KArgs& a, const StepDesc& dref, int st, int item_base, uint32_t* s_max,
-                             const StepPtrs<T>* ptrs, const PermTab& ptab) {
+                             const StepPtrs<T>* ptrs, const PermTab& ptab, bool contiguous) {
   constexpr int LV = VW == 8 ? 3 : 2;
   const StepDesc d = dref;
   const int lw = d.lh + d.lfa + d.lfb;
@@ -457,8 +457,11 @@ __device__ void run_step_vec(const KArgs& a, const StepDesc& dref, int st, int i
           body(k + 1);
         }
       }
-      if (!permuted) {
-        T* out = p.out + e0;
+      if (!permuted || contiguous) {
+        // the permutation keeps the low log2(VW) index bits in place (or
+        // there is none): the VW outputs are VW consecutive elements at the
+        // image of the first, a multiple of VW
+        T* out = p.out + (permuted ? perm_addr(ptab, d.perm_off, e0, lw) : e0);
         store4<T>(out, acc);
         if (VW == 8) store4<T>(out + 4, acc + 4);
       } else {
@@ -676,6 +679,7 @@ struct StepShape {
   int kind;
   int lt;       // SK_SPLITK: log2 of the lanes per output
   int total_r;  // work items (threads for SK_SPLITK), a multiple of 32
+  bool contiguous;  // SK_VEC8 / SK_VEC4: the output permutation keeps the item's low bits in place
 };
 
 template <typename T>
@@ -685,6 +689,7 @@ __device__ __forceinline__ StepShape step_shape(int lh, int lfa, int lfb, int lk
   const int64_t outs = int64_t(1) << (lw + lg);
   StepShape sh;
   sh.lt = 0;
+  sh.contiguous = false;
   const bool bT = (flags & kStepTensor) != 0;
   if (bT && tensor) {  // the tensor cores, the whole block per syndrome
     sh.kind = SK_TENSOR;
@@ -862,10 +867,11 @@ __device__ __forceinline__ void dispatch_step(const KArgs& a, const StepDesc& d,
       run_step_splitk<T, NORM, MAXP, G1, CL>(a, d, st, item_base, sh.lt, s_max, ptrs, ptab);
       break;
     case SK_VEC8:  // float32 only (step_shape)
-      if constexpr (sizeof(T) == 4) run_step_vec<T, 8, NORM, MAXP, G1, CL>(a, d, st, item_base, s_max, ptrs, ptab);
+      if constexpr (sizeof(T) == 4)
+        run_step_vec<T, 8, NORM, MAXP, G1, CL>(a, d, st, item_base, s_max, ptrs, ptab, sh.contiguous);
       break;
     case SK_VEC4:
-      run_step_vec<T, 4, NORM, MAXP, G1, CL>(a, d, st, item_base, s_max, ptrs, ptab);
+      run_step_vec<T, 4, NORM, MAXP, G1, CL>(a, d, st, item_base, s_max, ptrs, ptab, sh.contiguous);
       break;
     default:
       run_step<T, NORM, MAXP, G1, CL>(a, d, st, item_base, s_max, ptrs, ptab);
@@ -877,7 +883,7 @@ __device__ __forceinline__ void dispatch_step(const KArgs& a, const StepDesc& d,
 // staged tables (if any) and the arena (if in shared memory).
 struct BlockSmem {
   StepDesc* steps;
-  int2* plan;  // per step: x = kind | lt << 8 | per-syndrome << 16, y = items (see fill_step_plan)
+  int2* plan;  // per step: x = kind | lt << 8 | per-syndrome << 16 | contiguous << 17, y = items (fill_step_plan)
   void* ptrs;  // per syndrome and step: StepPtrs (operand and output bases)
   uint32_t* syn;
   uint32_t* max;
@@ -937,7 +943,19 @@ __device__ __forceinline__ void fill_step_plan(const KArgs& a, const StepDesc* s
     const StepShape sh1 = a.G > 1 ? step_shape<T>(d.lh, d.lfa, d.lfb, d.lk, 0, d.flags, tensor, bd) : sh;
     const bool per_syndrome = a.G > 1 && sh1.total_r >= bd;
     const StepShape& use = per_syndrome ? sh1 : sh;
-    plan[st] = make_int2(use.kind | (use.lt << 8) | (int(per_syndrome) << 16), per_syndrome ? bd : sh.total_r);
+    // does the output permutation map index bits 0 .. log2(VW)-1 to
+    // themselves?  (it moves whole bits, so checking each bit suffices)
+    int contiguous = 0;
+    if ((use.kind == SK_VEC8 || use.kind == SK_VEC4) && d.perm_off >= 0) {
+      const PermTab gp{a.perm, false};
+      const int lw = d.lh + d.lfa + d.lfb;
+      const int lv = use.kind == SK_VEC8 ? 3 : 2;
+      contiguous = 1;
+      for (int b = 0; b < lv; ++b)
+        if (perm_addr(gp, d.perm_off, 1 << b, lw) != (1 << b)) contiguous = 0;
+    }
+    plan[st] = make_int2(use.kind | (use.lt << 8) | (int(per_syndrome) << 16) | (contiguous << 17),
+                         per_syndrome ? bd : sh.total_r);
   }
 }
 
@@ -980,6 +998,7 @@ __device__ void contract_group(const KArgs& a, int64_t base, int64_t nrows, cons
     StepShape sh;
     sh.kind = pl.x & 0xff;
     sh.lt = (pl.x >> 8) & 0xff;
+    sh.contiguous = ((pl.x >> 17) & 1) != 0;
     sh.total_r = pl.y;
     const bool per_syndrome = (pl.x >> 16) & 1;
     const int items = pl.y;
