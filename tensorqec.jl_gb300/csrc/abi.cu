@@ -620,6 +620,23 @@ int program_multi_view(tqec_program* p, ProgramMultiView* v) {
   v->map_mode = p->plan.map_mode;
   v->flops_per_syndrome = 2.0 * p->plan.macs_runtime;
   v->recheck_margin = p->margin >= 0.0 ? p->margin : 2.0 * err_bound(p, TQEC_F32);
+  const ClusterShape& c = p->cluster[v->recheck_precision];
+  v->cluster_blocks = c.size;
+  if (c.size > 0) {
+    v->cluster_threads = c.threads;
+    v->cluster_cap = c.cap;
+    v->cluster_smem = c.smem;
+    v->cluster_arena_elems = c.split ? p->plan.arena_elems - p->plan.arena_small : p->plan.arena_elems;
+    KArgs a = base_args(p, v->recheck_precision);
+    a.G = 1;
+    a.lg = 0;
+    a.tables_smem = c.tables ? 1 : 0;
+    a.perm16 = c.tables ? p->d_perm16 : nullptr;
+    a.arena_global = nullptr;
+    a.arena_small = c.split ? p->plan.arena_small : 0;
+    a.tc = 0;
+    v->args_cluster = a;
+  }
   return TQEC_OK;
 }
 

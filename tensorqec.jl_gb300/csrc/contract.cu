@@ -242,20 +242,6 @@ __device__ __forceinline__ void segment_max(bool valid, uint32_t bits, int lw_it
   if (valid && (threadIdx.x & (seg - 1)) == 0) atomicMax(slot, bits);
 }
 
-// Operand addressing.  A is [h][fa][k], or [h][k][fa] (kStepAFaMajor); B is
-// [h][k][fb], or [h][fb][k] (kStepTensor, kStepBKMajor).  a_base / b_base
-// give the element for k = 0, a_kstride / b_kstride the step between k.
-__device__ __forceinline__ bool a_fa_major(const StepDesc& d) { return (d.flags & kStepAFaMajor) != 0; }
-__device__ __forceinline__ bool b_k_major(const StepDesc& d) { return (d.flags & (kStepTensor | kStepBKMajor)) != 0; }
-__device__ __forceinline__ int a_base(const StepDesc& d, int h, int fa) {
-  return a_fa_major(d) ? ((h << (d.lk + d.lfa)) | fa) : (((h << d.lfa) | fa) << d.lk);
-}
-__device__ __forceinline__ int a_kstride(const StepDesc& d) { return a_fa_major(d) ? (1 << d.lfa) : 1; }
-__device__ __forceinline__ int b_base(const StepDesc& d, int h, int fb) {
-  return b_k_major(d) ? (((h << d.lfb) | fb) << d.lk) : ((h << (d.lk + d.lfb)) | fb);
-}
-__device__ __forceinline__ int b_kstride(const StepDesc& d) { return b_k_major(d) ? 1 : (1 << d.lfb); }
-
 // One output per work item.  G1: the step runs for one syndrome (the
 // block's only one, or one of its G in turn), so its bases and normalisers
 // are step invariants.
@@ -271,8 +257,8 @@ __device__ void run_step(const KArgs& a, const StepDesc& dref, int st, int item_
   const int mfa = (1 << d.lfa) - 1;
   const int mw = (1 << lw) - 1;
   const int K = 1 << d.lk;
-  const int kstride = b_kstride(d);
-  const int astride = a_kstride(d);
+  const bool bT = (d.flags & kStepTensor) != 0;
+  const int kstride = bT ? 1 : (1 << d.lfb);
   const int nthr = team_size<CL>();
   const int i0 = rotated(team_tid<CL>(), item_base, nthr);
   StepPtrs<T> p1{};
@@ -297,10 +283,11 @@ __device__ void run_step(const KArgs& a, const StepDesc& dref, int st, int item_
       const int fb = e & mfb;
       const int fa = (e >> d.lfb) & mfa;
       const int h = e >> (d.lfb + d.lfa);
-      const T* pa = p.a + a_base(d, h, fa);
-      const T* pb = p.b + b_base(d, h, fb);
+      const T* pa = p.a + (((h << d.lfa) | fa) << d.lk);
+      // B is [h][k][fb], or [h][fb][k] for a GEMM-shaped step
+      const T* pb = p.b + (bT ? (((h << d.lfb) | fb) << d.lk) : ((h << (d.lk + d.lfb)) | fb));
       for (int k = 0; k < K; ++k) {
-        T a0 = pa[k * astride];
+        T a0 = pa[k];
         // both normalisers on the A value (exact powers of two): the output
         // needs no scaling of its own
         if (NORM) a0 = scale(scale(a0, fa_s), fb_s);
@@ -370,7 +357,7 @@ __device__ __forceinline__ void store4<dfloat>(dfloat* p, const dfloat v[4]) {
 // so the vector accesses are aligned.  Permuted outputs are written in a
 // lane-rotated order where the planner found that it spreads the stores of
 // one warp instruction over more shared-memory banks.
-template <typename T, int VW, bool NORM, bool MAXP, bool G1, bool CL, bool BKM>
+template <typename T, int VW, bool NORM, bool MAXP, bool G1, bool CL>
 __device__ void run_step_vec(const KArgs& a, const StepDesc& dref, int st, int item_base, uint32_t* s_max,
                              const StepPtrs<T>* ptrs, const PermTab& ptab, bool contiguous) {
   constexpr int LV = VW == 8 ? 3 : 2;
@@ -413,27 +400,17 @@ __device__ void run_step_vec(const KArgs& a, const StepDesc& dref, int st, int i
       const int fb0 = e0 & mfb;
       const int fa = (e0 >> d.lfb) & mfa;
       const int h = e0 >> (d.lfb + d.lfa);
-      // A [h][fa][k] or [h][k][fa]; B [h][k][fb] (the item's VW values at
-      // one k are consecutive) or [h][fb][k] (each fb's k run is)
-      const bool afm = a_fa_major(d);
-      constexpr bool bkm = BKM;  // dispatched on kStepBKMajor
-      const int astride = a_kstride(d);
-      const T* pa = p.a + a_base(d, h, fa);
-      const T* pb = p.b + b_base(d, h, fb0);
+      const T* pa = p.a + (((h << d.lfa) | fa) << d.lk);
+      const T* pb = p.b + ((h << (d.lk + d.lfb)) | fb0);
       auto body = [&](int k) {
-        T av = pa[k * astride];
+        T av = pa[k];
         // both normalisers on the shared A value (exact powers of two), so
         // the VW outputs need no scaling of their own
         if (NORM) av = scale(scale(av, fa_s), fb_s);
         T bv[VW];
-        if constexpr (bkm) {
-#pragma unroll
-          for (int j = 0; j < VW; ++j) bv[j] = pb[j * K + k];
-        } else {
-          const T* q = pb + k * bstride;
-          load4<T>(q, bv);
-          if (VW == 8) load4<T>(q + 4, bv + 4);
-        }
+        const T* q = pb + k * bstride;
+        load4<T>(q, bv);
+        if (VW == 8) load4<T>(q + 4, bv + 4);
 #pragma unroll
         for (int j = 0; j < VW; ++j) {
           if constexpr (MAXP) {
@@ -453,27 +430,11 @@ __device__ void run_step_vec(const KArgs& a, const StepDesc& dref, int st, int i
         // once per four k instead of once per two
         for (int k = 0; k < K; k += 4) {
           T a4[4], b4[4][VW];
-          if (afm) {
+          load4<T>(pa + k, a4);
 #pragma unroll
-            for (int c = 0; c < 4; ++c) a4[c] = pa[(k + c) * astride];
-          } else {
-            load4<T>(pa + k, a4);
-          }
-          if constexpr (bkm) {
-            // K-major B: one 16-byte vector of four k per fb (K >= 4)
-#pragma unroll
-            for (int j = 0; j < VW; ++j) {
-              T t[4];
-              load4<T>(pb + j * K + k, t);
-#pragma unroll
-              for (int c = 0; c < 4; ++c) b4[c][j] = t[c];
-            }
-          } else {
-#pragma unroll
-            for (int c = 0; c < 4; ++c) {
-              load4<T>(pb + (k + c) * bstride, b4[c]);
-              if (VW == 8) load4<T>(pb + (k + c) * bstride + 4, b4[c] + 4);
-            }
+          for (int c = 0; c < 4; ++c) {
+            load4<T>(pb + (k + c) * bstride, b4[c]);
+            if (VW == 8) load4<T>(pb + (k + c) * bstride + 4, b4[c] + 4);
           }
 #pragma unroll
           for (int c = 0; c < 4; ++c) {
@@ -585,11 +546,12 @@ __device__ void run_step_splitk(const KArgs& a, const StepDesc& dref, int st, in
       const int fb = e & mfb;
       const int fa = (e >> d.lfb) & mfa;
       const int h = e >> (d.lfb + d.lfa);
-      const T* pa = p.a + a_base(d, h, fa);
-      const T* pb = p.b + b_base(d, h, fb);
-      const int kstride = b_kstride(d), astride = a_kstride(d);
+      const T* pa = p.a + (((h << d.lfa) | fa) << d.lk);
+      const bool bT = (d.flags & kStepTensor) != 0;
+      const T* pb = p.b + (bT ? (((h << d.lfb) | fb) << d.lk) : ((h << (d.lk + d.lfb)) | fb));
+      const int kstride = bT ? 1 : (1 << d.lfb);
       for (int k = sub; k < K; k += tpo) {
-        const T av = scale(pa[k * astride], fa_s);
+        const T av = scale(pa[k], fa_s);
         const T bv = pb[k * kstride];
         if constexpr (MAXP) {
           const T v = av * bv;
@@ -905,18 +867,11 @@ __device__ __forceinline__ void dispatch_step(const KArgs& a, const StepDesc& d,
       run_step_splitk<T, NORM, MAXP, G1, CL>(a, d, st, item_base, sh.lt, s_max, ptrs, ptab);
       break;
     case SK_VEC8:  // float32 only (step_shape)
-      if constexpr (sizeof(T) == 4) {
-        if (d.flags & kStepBKMajor)
-          run_step_vec<T, 8, NORM, MAXP, G1, CL, true>(a, d, st, item_base, s_max, ptrs, ptab, sh.contiguous);
-        else
-          run_step_vec<T, 8, NORM, MAXP, G1, CL, false>(a, d, st, item_base, s_max, ptrs, ptab, sh.contiguous);
-      }
+      if constexpr (sizeof(T) == 4)
+        run_step_vec<T, 8, NORM, MAXP, G1, CL>(a, d, st, item_base, s_max, ptrs, ptab, sh.contiguous);
       break;
     case SK_VEC4:
-      if (d.flags & kStepBKMajor)
-        run_step_vec<T, 4, NORM, MAXP, G1, CL, true>(a, d, st, item_base, s_max, ptrs, ptab, sh.contiguous);
-      else
-        run_step_vec<T, 4, NORM, MAXP, G1, CL, false>(a, d, st, item_base, s_max, ptrs, ptab, sh.contiguous);
+      run_step_vec<T, 4, NORM, MAXP, G1, CL>(a, d, st, item_base, s_max, ptrs, ptab, sh.contiguous);
       break;
     default:
       run_step<T, NORM, MAXP, G1, CL>(a, d, st, item_base, s_max, ptrs, ptab);
@@ -1207,6 +1162,9 @@ __global__ void __launch_bounds__(sizeof(T) == 8 || TENSOR ? 512 : 1024) tn_cont
 template <typename T, bool NORM>
 __global__ void __launch_bounds__(512) tn_contract_cluster_kernel(KArgs a) {
   extern __shared__ __align__(16) unsigned char smem[];
+  // a cluster without rows (the same answer for all its blocks) leaves at
+  // once: it reaches no cluster barrier and no other block's memory
+  if (int64_t(cluster_id()) * a.G >= (a.list ? int64_t(*a.list_count) : a.n)) return;
   BlockSmem sm = carve_smem<NORM, false>(a, smem);
   size_t off = sm.tail;
   const T* consts;
@@ -1420,9 +1378,11 @@ int cluster_capacity_of(K kernel, int csize, int threads, size_t smem) {
 
 template <typename K>
 cudaError_t cluster_launch_with(K kernel, const KArgs& a, int clusters, int csize, int threads, size_t smem,
-                                cudaStream_t stream) {
-  cudaError_t e = cluster_config(kernel, csize, threads, smem);
-  if (e != cudaSuccess) return e;
+                                cudaStream_t stream, bool configure) {
+  if (configure) {
+    cudaError_t e = cluster_config(kernel, csize, threads, smem);
+    if (e != cudaSuccess) return e;
+  }
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(unsigned(clusters) * unsigned(csize));
   cfg.blockDim = dim3(threads);
@@ -1445,12 +1405,20 @@ int contract_cluster_capacity(int precision, int csize, int threads, size_t smem
 }
 
 cudaError_t contract_cluster_launch(int precision, const KArgs& a, int clusters, int csize, int threads, size_t smem,
-                                    cudaStream_t stream) {
+                                    cudaStream_t stream, bool configure) {
   if (a.map_mode || a.G != 1) return cudaErrorInvalidValue;
   if (precision == 2)
-    return cluster_launch_with(tn_contract_cluster_kernel<dfloat, true>, a, clusters, csize, threads, smem, stream);
+    return cluster_launch_with(tn_contract_cluster_kernel<dfloat, true>, a, clusters, csize, threads, smem, stream,
+                               configure);
   if (precision == 0)
-    return cluster_launch_with(tn_contract_cluster_kernel<double, false>, a, clusters, csize, threads, smem, stream);
+    return cluster_launch_with(tn_contract_cluster_kernel<double, false>, a, clusters, csize, threads, smem, stream,
+                               configure);
+  return cudaErrorInvalidValue;
+}
+
+cudaError_t contract_cluster_configure(int precision, int csize, int threads, size_t smem) {
+  if (precision == 2) return cluster_config(tn_contract_cluster_kernel<dfloat, true>, csize, threads, smem);
+  if (precision == 0) return cluster_config(tn_contract_cluster_kernel<double, false>, csize, threads, smem);
   return cudaErrorInvalidValue;
 }
 

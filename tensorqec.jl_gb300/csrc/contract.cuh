@@ -123,9 +123,13 @@ cudaError_t contract_launch(int precision, const KArgs& a, int grid, int threads
 // block's shared memory and clusters * (arena_elems - arena_small) elements
 // in a.arena_global): float64 (precision 0) and double-float (precision 2).  Returns
 // the clusters that can be resident at once (0: the shape cannot launch).
+// `configure` sets the kernel's shared-memory and cluster-size attributes
+// first; a launch being captured into a CUDA graph passes false after an
+// earlier contract_cluster_configure of the same shape.
 int contract_cluster_capacity(int precision, int csize, int threads, size_t smem);
 cudaError_t contract_cluster_launch(int precision, const KArgs& a, int clusters, int csize, int threads, size_t smem,
-                                    cudaStream_t stream);
+                                    cudaStream_t stream, bool configure = true);
+cudaError_t contract_cluster_configure(int precision, int csize, int threads, size_t smem);
 
 // The multi-program kernel (float32 normalised, or float64), and the
 // per-batch advance (batch + 1, unit counter and recheck counts to zero).

@@ -9,7 +9,11 @@
 //      units of the current batch from a device counter, largest programs
 //      first, and flag rows whose class margin is inside the float32 bound;
 //   2. the recheck kernel (double-float, or float64 when every program asks
-//      for it) over every program's flagged rows;
+//      for it) over every program's flagged rows -- except the rows of wide
+//      programs (those with a cluster form for their recheck), which one
+//      launch per such program re-contracts with one thread-block cluster
+//      per row: a large code's recheck row no longer holds one block for the
+//      whole batch;
 //   3. an advance kernel: next batch, counters back to zero.
 #include <algorithm>
 #include <cstring>
@@ -112,6 +116,13 @@ struct tqec_multi {
   int rprec = 2;       // arithmetic of the recheck launch (TQEC_F32X2 or TQEC_F64)
   DevArray units, unit_offsets, batch_rows, state, counts;
   std::vector<DevArray> lists;
+  // wide programs' recheck on clusters: per program its arena (cap clusters)
+  // and the launch description, and a zero word the list kernel reads as
+  // those programs' count
+  std::vector<DevArray> carena;
+  std::vector<tqec::KArgs> kcl;
+  std::vector<int> ccl;  // clusters per launch (0: the program rechecks in the list kernel)
+  DevArray zero;
   int32_t n_batches = 0;
   bool ready = false;
   std::mutex mu;
@@ -166,8 +177,25 @@ int tqec_multi_create(tqec_program* const* progs, int32_t n_progs, tqec_multi** 
     return bail(TQEC_ERR_OOM, "float32 arenas");
   if (m->arena_block_r && m->arena_r.zeros(size_t(m->grid_r) * m->arena_block_r * 8) != cudaSuccess)
     return bail(TQEC_ERR_OOM, "recheck arenas");
-  if (m->state.zeros(2 * sizeof(int32_t)) != cudaSuccess || m->counts.zeros(sizeof(int32_t) * m->n) != cudaSuccess)
+  if (m->state.zeros(2 * sizeof(int32_t)) != cudaSuccess || m->counts.zeros(sizeof(int32_t) * m->n) != cudaSuccess ||
+      m->zero.zeros(sizeof(int32_t)) != cudaSuccess)
     return bail(TQEC_ERR_OOM, "counters");
+  m->carena.resize(m->n);
+  m->kcl.resize(m->n);
+  m->ccl.assign(m->n, 0);
+  for (int i = 0; i < m->n; ++i) {
+    const auto& v = m->views[i];
+    if (v.cluster_blocks <= 0) continue;
+    // kernel attributes now: the launches may later be captured into a graph
+    if (tqec::contract_cluster_configure(m->rprec, v.cluster_blocks, v.cluster_threads, v.cluster_smem) != cudaSuccess) {
+      cudaGetLastError();
+      continue;
+    }
+    if (m->carena[i].zeros(size_t(v.cluster_cap) * size_t(std::max<int64_t>(v.cluster_arena_elems, 1)) * 8) !=
+        cudaSuccess)
+      return bail(TQEC_ERR_OOM, "cluster recheck arenas");
+    m->ccl[i] = v.cluster_cap;
+  }
   *out = m;
   return TQEC_OK;
 }
@@ -177,9 +205,10 @@ int tqec_multi_destroy(tqec_multi* m) {
   cudaSetDevice(m->device);
   cudaDeviceSynchronize();
   for (DevArray* a : {&m->arena32, &m->arena_r, &m->k32, &m->k_r, &m->units, &m->unit_offsets, &m->batch_rows,
-                      &m->state, &m->counts})
+                      &m->state, &m->counts, &m->zero})
     a->release();
   for (auto& l : m->lists) l.release();
+  for (auto& c : m->carena) c.release();
   delete m;
   return TQEC_OK;
 }
@@ -248,6 +277,25 @@ int tqec_multi_set_work(tqec_multi* m, int32_t n_batches, const int64_t* batch_e
         a.recheck_list = nullptr;
         a.recheck_count = nullptr;
         a_r[i] = a;
+        if (m->ccl[i] > 0) {
+          // this program's rows go to its cluster launch; the list kernel
+          // sees none
+          a_r[i].list_count = static_cast<const int32_t*>(m->zero.p);
+          tqec::KArgs c = m->views[i].args_cluster;
+          c.syn = syndromes[i];
+          c.class_out = class_out[i];
+          c.logp_out = nullptr;
+          c.err_out = nullptr;
+          c.row_offset = 0;
+          c.list = list;
+          c.list_count = count;
+          c.n = std::max<int64_t>(max_rows[i], 1);
+          c.recheck_margin = -1.0;
+          c.recheck_list = nullptr;
+          c.recheck_count = nullptr;
+          c.arena_global = m->carena[i].p;
+          m->kcl[i] = c;
+        }
       }
     }
   }
@@ -299,6 +347,13 @@ int tqec_multi_launch(tqec_multi* m, void* stream) {
   a.arena_global = m->arena_r.p;
   a.arena_per_block = m->arena_block_r;
   MQ_CUDA(tqec::contract_multi_launch(m->rprec, a, m->grid_r, tqec::kMultiThreads, m->smem_r, st));
+  for (int i = 0; i < m->n; ++i) {
+    if (m->ccl[i] <= 0) continue;
+    const auto& v = m->views[i];
+    const int clusters = int(std::min<int64_t>(m->kcl[i].n, m->ccl[i]));
+    MQ_CUDA(tqec::contract_cluster_launch(m->rprec, m->kcl[i], clusters, v.cluster_blocks, v.cluster_threads,
+                                          v.cluster_smem, st, false));
+  }
   MQ_CUDA(tqec::contract_multi_advance(batch, next, static_cast<int32_t*>(m->counts.p), m->n, st));
   return TQEC_OK;
 }

@@ -478,8 +478,6 @@ static std::string build_plan_once(const NetworkView& net, int32_t n_steps, cons
     int a = -1, b = -1;             // operand node ids
     std::vector<int> out_layout;    // required layout of the output
     bool tensor = false;            // GEMM-shaped (B read K-major)
-    bool a_fmaj = false;            // A read [h][k][fa]
-    bool b_kmaj = false;            // B read [h][fb][k] on the SIMT path
   };
   std::vector<StepLayout> lay(R);
   // Group orders are assigned bottom-up: a step orders each of its index
@@ -540,33 +538,11 @@ static std::string build_plan_once(const NetworkView& net, int32_t n_steps, cons
     order_by(L.Fb, L.b);
     order_by(L.Fa, L.a);
     order_by(L.H, L.b);
-    // An operand's producer writes its output in natural order (its lowest
-    // label in the lowest bits, adjacent threads differing there); it stores
-    // contiguous runs when that label leads the layout this step reads.  The
-    // default layouts lead with k (A) and fb (B); where the producer's lowest
-    // label is instead one of A's fa, A is read [h][k][fa], and where it is
-    // one of B's k (at least four of them, for 16-byte loads along k), B is
-    // read [h][fb][k].
-    auto lowest = [&](int node) {
-      auto it = nat.find(node);
-      return it == nat.end() || it->second.empty() ? -1 : it->second[0];
-    };
-    const int a_low = lowest(L.a), b_low = lowest(L.b);
-    if (lim.producer_layouts && !map_mode && !L.tensor) {
-      L.a_fmaj = a_low >= 0 && in(L.Fa, a_low) && !L.K.empty();
-      L.b_kmaj = b_low >= 0 && in(L.K, b_low) && L.K.size() >= 2;
-    }
-    // contracted labels follow the natural order of the operand whose
-    // producer they lead (both: the larger one), else of the larger
-    // intermediate operand
+    // contracted labels follow the larger intermediate operand's natural order
     {
       const bool ra = nat.count(L.a) > 0, rb = nat.count(L.b) > 0;
       int pick = L.b;
       if (ra && (!rb || nodes[L.a].vars.size() > nodes[L.b].vars.size())) pick = L.a;
-      const bool a_wants = !L.tensor && !L.a_fmaj && a_low >= 0 && in(L.K, a_low);
-      const bool b_wants = L.b_kmaj;
-      if (a_wants && !b_wants) pick = L.a;
-      if (b_wants && !a_wants) pick = L.b;
       order_by(L.K, pick);
     }
     std::vector<int> nn;
@@ -590,15 +566,10 @@ static std::string build_plan_once(const NetworkView& net, int32_t n_steps, cons
     const int id = order[r];
     StepLayout& L = lay[r];
     std::vector<int> la, lb;
-    if (L.a_fmaj) {  // [h][k][fa]
-      la.insert(la.end(), L.Fa.begin(), L.Fa.end());
-      la.insert(la.end(), L.K.begin(), L.K.end());
-    } else {
-      la.insert(la.end(), L.K.begin(), L.K.end());
-      la.insert(la.end(), L.Fa.begin(), L.Fa.end());
-    }
+    la.insert(la.end(), L.K.begin(), L.K.end());
+    la.insert(la.end(), L.Fa.begin(), L.Fa.end());
     la.insert(la.end(), L.H.begin(), L.H.end());
-    if (L.tensor || L.b_kmaj) {  // [h][fb][k]: K-major like A
+    if (L.tensor) {  // [h][fb][k]: K-major like A
       lb.insert(lb.end(), L.K.begin(), L.K.end());
       lb.insert(lb.end(), L.Fb.begin(), L.Fb.end());
     } else {
@@ -741,8 +712,7 @@ static std::string build_plan_once(const NetworkView& net, int32_t n_steps, cons
     d.lfb = (int)L.Fb.size();
     d.lk = (int)L.K.size();
     d.out_off = (int32_t)off;
-    d.flags = (group_end[r] ? kStepSync : 0) | (L.tensor ? kStepTensor : 0) | (L.b_kmaj ? kStepBKMajor : 0) |
-              (L.a_fmaj ? kStepAFaMajor : 0);
+    d.flags = (group_end[r] ? kStepSync : 0) | (L.tensor ? kStepTensor : 0);
     if (L.tensor) P.tensor_steps++;
     d.var_off = map_mode ? d_var_off : 0;
     for (int side = 0; side < 2; ++side) {

@@ -6,9 +6,7 @@
 // where h are labels shared by both operands and still needed later, k are
 // labels shared and summed here, fa / fb are labels of only one operand.
 // Operand layouts are chosen top-down so that every operand is stored in
-// exactly the order its consumer reads ([h][fa][k] for A, [h][k][fb] for B,
-// or [h][k][fa] / [h][fb][k] where that keeps the operand's producer's
-// lowest output labels lowest, so the producer stores contiguous runs);
+// exactly the order its consumer reads ([h][fa][k] for A, [h][k][fb] for B);
 // a step writes its output through a bit-permutation table into the layout
 // its own consumer wants.  Leaves that do not depend on the syndrome are
 // folded on the host; leaves that depend on a few syndrome bits are kept as
@@ -37,10 +35,6 @@ constexpr int32_t kStepRotate4 = 2;  // permuted stores of 4-output items are la
 constexpr int32_t kStepRotate8 = 4;  // the same for 8-output items
 constexpr int32_t kStepTensor = 8;   // GEMM-shaped step: B stored [h][fb][k] (K-major);
                                      // float32 blocks may run it on the tensor cores
-constexpr int32_t kStepBKMajor = 16; // B stored [h][fb][k] (K-major) for the SIMT paths: its
-                                     // producer's lowest output labels are this step's k
-constexpr int32_t kStepAFaMajor = 32;  // A stored [h][k][fa]: its producer's lowest output
-                                       // labels are this step's fa
 
 struct StepDesc {
   int32_t a_kind, b_kind;
@@ -103,9 +97,6 @@ struct PlanLimits {
   bool map_mode = false;      // max-product contraction + back-tracking (TNMAP)
   int64_t big_elems = 1024;   // intermediates above this size go to the big pool
   bool tensor_steps = true;   // mark GEMM-shaped steps (kStepTensor)
-  // lay an operand out [h][k][fa] (A) or [h][fb][k] (B) when its producer's
-  // lowest output label is in that leading group (kStepAFaMajor, kStepBKMajor)
-  bool producer_layouts = true;
   // ... when they hold at least this share of the program's multiply-adds
   double tensor_min_share = 0.25;
 };

@@ -36,6 +36,14 @@ struct ProgramMultiView {
   bool map_mode;
   double flops_per_syndrome;
   double recheck_margin;  // float32 log-margin below which a row is re-contracted
+  // the recheck's cluster form (cluster_blocks 0: none): args_cluster is the
+  // recheck launch description for it (tables and small pool as the shape
+  // places them; no buffers), cluster_arena_elems the global arena elements
+  // one cluster needs
+  int cluster_blocks = 0, cluster_threads = 0, cluster_cap = 0;
+  size_t cluster_smem = 0;
+  int64_t cluster_arena_elems = 0;
+  KArgs args_cluster;
 };
 
 int program_multi_view(tqec_program* p, ProgramMultiView* v);

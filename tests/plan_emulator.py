@@ -52,12 +52,8 @@ def run_plan(plan, bits, dtype=np.float64, return_arena=False):
         fa = (e >> lfb) & ((1 << lfa) - 1)
         h = e >> (lfb + lfa)
         k = np.arange(1 << lk, dtype=np.int64)
-        flags = int(d["flags"])
-        if flags & 32:  # A stored [h][k][fa]
-            aidx = ((h << (lk + lfa)) | fa)[:, None] + (k[None, :] << lfa)
-        else:
-            aidx = (((h << lfa) | fa) << lk)[:, None] + k[None, :]
-        if flags & (8 | 16):  # B stored [h][fb][k] (GEMM-shaped step, or a K-major SIMT layout)
+        aidx = (((h << lfa) | fa) << lk)[:, None] + k[None, :]
+        if int(d["flags"]) & 8:  # GEMM-shaped step: B stored [h][fb][k]
             bidx = (((h << lfb) | fb) << lk)[:, None] + k[None, :]
         else:
             bidx = ((h << (lk + lfb)) | fb)[:, None] + (k[None, :] << lfb)
