@@ -16,6 +16,8 @@
 // two is exact, so the only rounding is that of the products and sums.  The
 // exponents are summed into the final log-probability.
 #include <cstdio>
+#include <map>
+#include <mutex>
 #include <type_traits>
 
 #include "contract.cuh"
@@ -1299,10 +1301,30 @@ size_t contract_smem_limit(int device) {
   return size_t(v);
 }
 
+// Raises a kernel's dynamic shared-memory limit to at least smem. The limit
+// only ever grows (to the largest any program or program set asked for), so a
+// launch prepared earlier -- one captured in a CUDA graph among them -- stays
+// valid after another program's set-up. The kernels of one family share a
+// function type, so the limit is kept per kernel address.
+template <typename K>
+cudaError_t grow_smem_limit(K kernel, size_t smem) {
+  static std::mutex mu;
+  static std::map<const void*, size_t> granted;
+  std::lock_guard<std::mutex> lk(mu);
+  size_t& g = granted[reinterpret_cast<const void*>(kernel)];
+  if (smem <= g) return cudaSuccess;
+  cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+  if (e == cudaSuccess) g = smem;
+  return e;
+}
+
 template <typename K>
 int occupancy_of(K kernel, int threads, size_t smem) {
   int blocks = 0;
-  cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+  if (grow_smem_limit(kernel, smem) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, kernel, threads, smem) != cudaSuccess) {
     cudaGetLastError();
     return 0;
@@ -1323,7 +1345,7 @@ int contract_occupancy(int precision, int threads, size_t smem, bool map_mode, b
 
 template <typename K>
 cudaError_t launch_with(K kernel, const KArgs& a, int grid, int threads, size_t smem, cudaStream_t stream) {
-  cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+  cudaError_t e = grow_smem_limit(kernel, smem);
   if (e != cudaSuccess) return e;
   kernel<<<grid, threads, smem, stream>>>(a);
   return cudaGetLastError();
@@ -1346,7 +1368,7 @@ cudaError_t contract_launch(int precision, const KArgs& a, int grid, int threads
 
 template <typename K>
 cudaError_t cluster_config(K kernel, int csize, int threads, size_t smem) {
-  cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+  cudaError_t e = grow_smem_limit(kernel, smem);
   if (e == cudaSuccess && csize > 8) e = cudaFuncSetAttribute(kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
   return e;
 }

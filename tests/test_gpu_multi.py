@@ -140,3 +140,52 @@ def test_multi_program_launch_vs_oracle(pkg, oracle):
     md.close()
     for ct, _ in progs:
         ct.close()
+
+
+@pytest.mark.parametrize("order", [(7, 9), (9, 7)])
+def test_multi_wide_programs_with_different_cluster_forms(pkg, order):
+    """Two wide programs (surface d=7 and d=9) recheck on thread-block
+    clusters whose shared-memory sizes differ; whichever is set up last, both
+    cluster launches run, directly and from a captured graph, and decide
+    like their single-program decoders."""
+    import torch
+
+    progs = []
+    for i, d in enumerate(order):
+        t = pkg.tanner_graph(pkg.SurfaceCode(d, d))
+        em = pkg.depolarizing(0.06, t.nq)
+        ct = pkg.compile(pkg.TNMMAP(precision="f32"), t, em)
+        ep = pkg.random_error_pattern(em, np.random.default_rng(90 + d), nsamples=120)
+        s = pkg.syndrome_extraction(ep, t)
+        progs.append((ct, np.concatenate([s.sx, s.sz], axis=1)))
+    assert all(ct.program.info["cluster_blocks"] in (8, 16) for ct, _ in progs)
+    md = pkg.native.MultiDecoder([ct.program for ct, _ in progs])
+    syn = [torch.from_numpy(pkg.pack_syndromes(b)).cuda() for _, b in progs]
+    cls = [torch.full((b.shape[0],), -1, dtype=torch.int32, device="cuda") for _, b in progs]
+    n = np.array([b.shape[0] for _, b in progs])
+    ends = np.stack([n // 3, n])
+    md.set_work(ends, [x.data_ptr() for x in syn], [x.data_ptr() for x in cls])
+    stream = torch.cuda.current_stream()
+    md.reset(stream.cuda_stream)
+    for _ in range(ends.shape[0]):
+        md.launch(stream.cuda_stream)
+    torch.cuda.synchronize()
+    _check(pkg, progs, [c.cpu().numpy() for c in cls])
+
+    for c in cls:
+        c.fill_(-1)
+    side = torch.cuda.Stream()
+    side.wait_stream(stream)
+    with torch.cuda.stream(side):
+        md.reset(side.cuda_stream)
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g, stream=side):
+            md.launch(side.cuda_stream)
+        md.reset(side.cuda_stream)
+        for _ in range(ends.shape[0]):
+            g.replay()
+    torch.cuda.synchronize()
+    _check(pkg, progs, [c.cpu().numpy() for c in cls])
+    md.close()
+    for ct, _ in progs:
+        ct.close()
