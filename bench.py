@@ -940,16 +940,19 @@ def run_latency(args):
     rech = pkg.compile(pkg.TNMMAP(precision="f32", margin=1e30, optimizer=d7_order(pkg)), t, em)
     for blocks in (0, 2, 4, 8, 16):
         for th in ((128, 256, 512) if blocks else (0,)):
-            row = {"latency": "single syndrome", "cluster_blocks": blocks, "threads": th or "block form"}
-            for name, prog, prec in (("plain_f64_us", plain.program, N.TQEC_F64),
-                                     ("f32_then_recheck_us", rech.program, N.TQEC_F32X2)):
-                try:
-                    prog.set_cluster(prec, blocks, th or 512)
-                    lat(prog, 5)
-                    row[name] = lat(prog)
-                except N.TqecError as e:
-                    row[name] = f"not launchable: {e}"
-            print(json.dumps(row), flush=True)
+            for small in ((1, 0) if blocks else (-1,)):
+                row = {"latency": "single syndrome", "cluster_blocks": blocks, "threads": th or "block form"}
+                if blocks:
+                    row["small_tensors"] = "first block's shared memory" if small else "global memory"
+                for name, prog, prec in (("plain_f64_us", plain.program, N.TQEC_F64),
+                                         ("f32_then_recheck_us", rech.program, N.TQEC_F32X2)):
+                    try:
+                        prog.set_cluster(prec, blocks, th or 512, small)
+                        lat(prog, 5)
+                        row[name] = lat(prog)
+                    except N.TqecError as e:
+                        row[name] = f"not launchable: {e}"
+                print(json.dumps(row), flush=True)
     for name, ct in (("plain_f64", plain), ("f32_then_recheck", rech)):
         ct.program.autotune(1024)
         print(json.dumps({"latency": "single syndrome, autotuned", "program": name,

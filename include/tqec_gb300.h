@@ -203,11 +203,15 @@ int tqec_last_recheck_count(const tqec_program* prog, int64_t* count);
 /* The form of single-syndrome launches in `precision` (TQEC_F64: the plain
  * form's; TQEC_F32X2 or TQEC_F64: the recheck's): blocks = 0 gives each
  * syndrome one block, blocks = 2, 4, 8 or 16 a thread-block cluster of that
- * many blocks of `threads` threads that share each step's work.  Wide
- * programs start with 16 blocks of 128 threads (8 of 256 where 16-block
- * clusters cannot launch); tqec_program_autotune measures the forms.  No
- * reference counterpart (a latency setting). */
-int tqec_program_set_cluster(tqec_program* prog, int32_t precision, int32_t blocks, int32_t threads);
+ * many blocks of `threads` threads that share each step's work.
+ * small_in_smem = 1 keeps the small intermediates in the first block's
+ * shared memory (the others reach them through distributed shared memory),
+ * 0 keeps every intermediate in global memory, -1 takes the first where it
+ * fits.  Wide programs start with 16 blocks of 128 threads (8 of 256 where
+ * 16-block clusters cannot launch); tqec_program_autotune measures the forms
+ * and placements.  No reference counterpart (a latency setting). */
+int tqec_program_set_cluster(tqec_program* prog, int32_t precision, int32_t blocks, int32_t threads,
+                             int32_t small_in_smem);
 
 /* Tries the launch shapes that fit and keeps the fastest for each
  * precision, timing n_probe synthetic syndromes. */

@@ -110,7 +110,8 @@ struct tqec_program {
   tqec::StepDesc* d_steps = nullptr;
   int32_t* d_perm = nullptr;
   uint16_t* d_perm16 = nullptr;  // the same tables as uint16 (programs of width <= 16)
-  int32_t* d_tc_err = nullptr;   // set by a tensor-core wait that gave up
+  int32_t* h_wait_err = nullptr;  // pinned, mapped: set by a bounded device wait that gave up
+  int32_t* d_tc_err = nullptr;    // its device address
   int64_t n_perm_padded = 0;     // entries, a multiple of 8
   int32_t* d_vartab = nullptr;   // MAP mode tables
   int32_t* d_report = nullptr;
@@ -353,7 +354,12 @@ int launch_rows(tqec_program* p, int precision, tqec::KArgs a, int64_t n_rows_ma
 
 // The cluster form of `precision` with csize blocks of `threads` threads
 // (the tables staged when they fit); false if it cannot launch here.
-bool choose_cluster(tqec_program* p, int precision, int csize, int threads, ClusterShape* out) {
+// small_in_smem: 1 the small tensors in the first block's shared memory
+// (read by the other blocks through distributed shared memory), 0 every
+// intermediate in the cluster's slice of global memory, -1 the first when it
+// fits.
+bool choose_cluster(tqec_program* p, int precision, int csize, int threads, ClusterShape* out,
+                    int small_in_smem = -1) {
   if (p->plan.map_mode || (precision != TQEC_F64 && precision != TQEC_F32X2) || csize < 2) return false;
   const size_t limit = tqec::contract_smem_limit(p->device);
   const int nsteps = (int)p->plan.steps.size();
@@ -368,7 +374,7 @@ bool choose_cluster(tqec_program* p, int precision, int csize, int threads, Clus
   bool found = false;
   for (int split : {1, 0})
     for (int tables : {1, 0}) {
-      if (found || (split && small <= 0)) continue;
+      if (found || (split && small <= 0) || (small_in_smem >= 0 && split != small_in_smem)) continue;
       const size_t b = tqec::contract_smem_bytes(precision, nsteps, sw, 1, split ? small : p->plan.arena_elems,
                                                  split != 0, 0, tables ? tb : 0);
       if (b > limit) continue;
@@ -403,20 +409,23 @@ int launch_cluster_rows(tqec_program* p, int precision, tqec::KArgs a, int64_t n
   return TQEC_OK;
 }
 
-// Runs the plain form: one launch (one block, one syndrome) per row.
-// After a synchronisation: a tensor-core wait that gave up makes the call fail
-// (its results are not valid); the flag is cleared for the next call.
+// After a synchronisation: a bounded device wait that gave up (a tensor-core
+// step waiting for its MMAs, or a block waiting for its table copies) makes
+// the call fail (its results are not valid); the flag, in pinned host memory
+// the device writes through its mapping, is cleared for the next call.
 int check_tensor_error(tqec_program* p) {
-  if (p->plan.tensor_steps == 0 || !p->d_tc_err) return TQEC_OK;
-  int32_t e = 0;
-  TQ_CUDA(cudaMemcpy(&e, p->d_tc_err, sizeof(e), cudaMemcpyDeviceToHost));
+  if (!p->h_wait_err) return TQEC_OK;
+  const int32_t e = *static_cast<volatile int32_t*>(p->h_wait_err);
   if (e) {
-    TQ_CUDA(cudaMemset(p->d_tc_err, 0, sizeof(e)));
-    return fail(TQEC_ERR_TIMEOUT, "a tensor-core step timed out waiting for its MMAs");
+    *static_cast<volatile int32_t*>(p->h_wait_err) = 0;
+    return fail(TQEC_ERR_TIMEOUT, e == 2 ? "a block timed out waiting for its table copies"
+                                         : "a tensor-core step timed out waiting for its MMAs");
   }
   return TQEC_OK;
 }
 
+// Runs the plain form: one launch (one block, one syndrome) per row, or the
+// cluster form.
 int launch_plain(tqec_program* p, int precision, tqec::KArgs a, int64_t n, cudaStream_t st) {
   // the cluster form: one launch, each syndrome on its own cluster
   if (p->cluster[precision].size > 0) return launch_cluster_rows(p, precision, a, n, st);
@@ -775,8 +784,11 @@ int tqec_program_create(const tqec_network* net, const tqec_tree* tree, const tq
     if (!P.fixed.empty()) cudaMemcpy(p->d_fixed, P.fixed.data(), P.fixed.size(), cudaMemcpyHostToDevice);
   }
   if ((e = cudaMallocHost(&p->h_count, sizeof(int32_t))) != cudaSuccess) return bail(TQEC_ERR_OOM, "pinned count");
-  if ((e = cudaMalloc(&p->d_tc_err, sizeof(int32_t))) != cudaSuccess) return bail(TQEC_ERR_OOM, "error flag");
-  cudaMemset(p->d_tc_err, 0, sizeof(int32_t));
+  if ((e = cudaHostAlloc(&p->h_wait_err, sizeof(int32_t), cudaHostAllocMapped)) != cudaSuccess)
+    return bail(TQEC_ERR_OOM, "error flag");
+  *p->h_wait_err = 0;
+  if ((e = cudaHostGetDevicePointer(&p->d_tc_err, p->h_wait_err, 0)) != cudaSuccess)
+    return bail(TQEC_ERR_CUDA, "error flag mapping");
   *p->h_count = 0;
   if ((e = cudaGetLastError()) != cudaSuccess) return bail(TQEC_ERR_CUDA, cudaGetErrorString(e));
   int rc;
@@ -818,7 +830,7 @@ int tqec_program_destroy(tqec_program* p) {
   cudaFree(p->d_steps);
   cudaFree(p->d_perm);
   cudaFree(p->d_perm16);
-  cudaFree(p->d_tc_err);
+  if (p->h_wait_err) cudaFreeHost(p->h_wait_err);
   cudaFree(p->d_c64);
   cudaFree(p->d_c32);
   cudaFree(p->d_cx2);
@@ -1072,10 +1084,11 @@ namespace {
 bool tune_cluster(tqec_program* p, int prec, bool plain, cudaEvent_t e0, cudaEvent_t e1) {
   std::vector<ClusterShape> cands(1);  // the block form
   for (int cs : {2, 4, 8, 16})
-    for (int th : {128, 256, 512}) {
-      ClusterShape c;
-      if (choose_cluster(p, prec, cs, th, &c)) cands.push_back(c);
-    }
+    for (int th : {128, 256, 512})
+      for (int split : {1, 0}) {
+        ClusterShape c;
+        if (choose_cluster(p, prec, cs, th, &c, split)) cands.push_back(c);
+      }
   cudaGetLastError();
   ClusterShape best;
   float best_ms = 1e30f;
@@ -1118,7 +1131,8 @@ bool tune_cluster(tqec_program* p, int prec, bool plain, cudaEvent_t e0, cudaEve
 
 }  // namespace
 
-int tqec_program_set_cluster(tqec_program* p, int32_t precision, int32_t blocks, int32_t threads) {
+int tqec_program_set_cluster(tqec_program* p, int32_t precision, int32_t blocks, int32_t threads,
+                             int32_t small_in_smem) {
   if (!p) return fail(TQEC_ERR_INVALID, "NULL program");
   if (precision != TQEC_F64 && precision != TQEC_F32X2)
     return fail(TQEC_ERR_INVALID, "clusters serve TQEC_F64 and TQEC_F32X2 launches");
@@ -1129,10 +1143,11 @@ int tqec_program_set_cluster(tqec_program* p, int32_t precision, int32_t blocks,
     return TQEC_OK;
   }
   if (blocks < 2 || blocks > 16 || (blocks & (blocks - 1)) || threads < 32 || threads > 512 ||
-      (threads & (threads - 1)))
-    return fail(TQEC_ERR_INVALID, "blocks must be 0 or 2, 4, 8, 16; threads a power of two from 32 to 512");
+      (threads & (threads - 1)) || small_in_smem < -1 || small_in_smem > 1)
+    return fail(TQEC_ERR_INVALID,
+                "blocks must be 0 or 2, 4, 8, 16; threads a power of two from 32 to 512; small_in_smem -1, 0 or 1");
   ClusterShape c;
-  if (!choose_cluster(p, precision, blocks, threads, &c)) {
+  if (!choose_cluster(p, precision, blocks, threads, &c, small_in_smem)) {
     cudaGetLastError();
     return fail(TQEC_ERR_UNSUPPORTED, "this cluster shape cannot launch for this program on this device");
   }

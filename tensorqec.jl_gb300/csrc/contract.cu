@@ -582,6 +582,108 @@ __device__ void run_step_splitk(const KArgs& a, const StepDesc& dref, int st, in
   if (NORM && G1) flush_max(vt0 < total, run_bits, &s_max[st]);
 }
 
+// A step of four-output items (as SK_VEC4) with fewer items than the team
+// has threads: TPO = 2^lt consecutive lanes share an item, lane `sub` sums
+// the k run [sub*K/TPO, (sub+1)*K/TPO) (at least four k, loaded before the
+// multiply-adds), and the partial sums meet by shuffles.  Used where one
+// syndrome has a whole block or cluster to itself, so a step's chain of
+// dependent operand loads is shortened by the lanes that would otherwise idle.
+template <typename T, bool NORM, bool MAXP, bool G1, bool CL>
+__device__ void run_step_vsplit(const KArgs& a, const StepDesc& dref, int st, int item_base, int lt,
+                                uint32_t* s_max, const StepPtrs<T>* ptrs, const PermTab& ptab, bool contiguous) {
+  const StepDesc d = dref;
+  const int tpo = 1 << lt;
+  const int lw = d.lh + d.lfa + d.lfb;
+  const int lwv = lw - 2;
+  const int items = 1 << (lwv + (G1 ? 0 : a.lg));
+  const int total = items << lt;
+  const int total_r = (total + 31) & ~31;
+  const int mfb = (1 << d.lfb) - 1;
+  const int mfa = (1 << d.lfa) - 1;
+  const int mwv = (1 << lwv) - 1;
+  const int kc = (1 << d.lk) >> lt;  // k per lane, a multiple of 4
+  const int bstride = 1 << d.lfb;
+  const bool permuted = d.perm_off >= 0;
+  const int cb0 = lw < 8 ? lw : 8;
+  const int nthr = team_size<CL>();
+  const int vt0 = rotated(team_tid<CL>(), item_base, nthr);
+  uint32_t run_bits = 0u;
+  // whole warps iterate together (the shuffles below need every lane)
+  for (int vt = vt0; vt < total_r; vt += nthr) {
+    const bool valid = vt < total;
+    const int item = vt >> lt, sub = vt & (tpo - 1);
+    const int g = G1 ? 0 : (valid ? (item >> lwv) : 0);
+    const int e0 = (item & mwv) << 2;
+    T acc[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) acc[j] = T(0);
+    StepPtrs<T> p{};
+    if (valid) {
+      p = ptrs[g * a.n_steps + st];
+      T fa_s = T(1), fb_s = T(1);
+      step_norms<T, NORM>(d, s_max + g * a.n_steps, &fa_s, &fb_s);
+      const int fb0 = e0 & mfb;
+      const int fa = (e0 >> d.lfb) & mfa;
+      const int h = e0 >> (d.lfb + d.lfa);
+      const T* pa = p.a + (((h << d.lfa) | fa) << d.lk) + sub * kc;
+      const T* pb = p.b + ((h << (d.lk + d.lfb)) | fb0) + sub * kc * bstride;
+      for (int k = 0; k < kc; k += 4) {
+        T a4[4], b4[4][4];
+        load4<T>(pa + k, a4);
+#pragma unroll
+        for (int c = 0; c < 4; ++c) load4<T>(pb + (k + c) * bstride, b4[c]);
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+          T av = a4[c];
+          if (NORM) av = scale(scale(av, fa_s), fb_s);
+#pragma unroll
+          for (int j = 0; j < 4; ++j) {
+            if constexpr (MAXP) {
+              const T v = av * b4[c][j];
+              acc[j] = v > acc[j] ? v : acc[j];
+            } else {
+              acc[j] = fma(av, b4[c][j], acc[j]);
+            }
+          }
+        }
+      }
+    }
+    for (int o = 1; o < tpo; o <<= 1) {
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const T other = __shfl_xor_sync(0xffffffffu, acc[j], o);
+        if constexpr (MAXP) acc[j] = other > acc[j] ? other : acc[j];
+        else acc[j] = acc[j] + other;
+      }
+    }
+    const bool writer = valid && sub == 0;
+    if (writer) {
+      if (!permuted || contiguous) {
+        store4<T>(p.out + (permuted ? perm_addr(ptab, d.perm_off, e0, lw) : e0), acc);
+      } else {
+        int los[4];
+        ptab.vec<4>(d.perm_off + (e0 & ((1 << cb0) - 1)), los);
+        int hi = 0;
+        int tab = d.perm_off + (1 << cb0);
+        for (int sh = 8; sh < lw; sh += 8) {
+          const int cb = lw - sh < 8 ? lw - sh : 8;
+          hi |= ptab.at(tab + ((e0 >> sh) & ((1 << cb) - 1)));
+          tab += 1 << cb;
+        }
+#pragma unroll
+        for (int j = 0; j < 4; ++j) p.out[los[j] | hi] = acc[j];
+      }
+    }
+    if (NORM && writer) {
+      const float m = fmaxf(fmaxf(float(acc[0]), float(acc[1])), fmaxf(float(acc[2]), float(acc[3])));
+      const uint32_t bits = __float_as_uint(m);
+      if (G1) run_bits = bits > run_bits ? bits : run_bits;
+      else atomicMax(&s_max[g * a.n_steps + st], bits);
+    }
+  }
+  if (NORM && G1) flush_max(vt0 < total, run_bits, &s_max[st]);
+}
+
 // Most probable configuration: after the max-product pass every runtime
 // step's output is still in the arena.  Walking the steps from the root
 // down, the values of a step's output labels are known (set by its
@@ -676,17 +778,17 @@ __device__ void backtrack(const KArgs& a, const StepDesc* s_steps, const uint32_
 // How a step is executed and how many work items it has (rounded up to a
 // warp): several lanes per output for few outputs over a long k range,
 // eight or four outputs per item along fb, else one output per item.
-enum StepKind { SK_SPLITK, SK_VEC8, SK_VEC4, SK_SCALAR, SK_TENSOR };
+enum StepKind { SK_SPLITK, SK_VEC8, SK_VEC4, SK_SCALAR, SK_TENSOR, SK_VSPLIT };
 struct StepShape {
   int kind;
-  int lt;       // SK_SPLITK: log2 of the lanes per output
+  int lt;       // SK_SPLITK / SK_VSPLIT: log2 of the lanes per output / per four outputs
   int total_r;  // work items (threads for SK_SPLITK), a multiple of 32
   bool contiguous;  // SK_VEC8 / SK_VEC4: the output permutation keeps the item's low bits in place
 };
 
 template <typename T>
 __device__ __forceinline__ StepShape step_shape(int lh, int lfa, int lfb, int lk, int lg, int flags, bool tensor,
-                                                int64_t bd) {
+                                                int64_t bd, bool vsplit = false) {
   const int lw = lh + lfa + lfb;
   const int64_t outs = int64_t(1) << (lw + lg);
   StepShape sh;
@@ -711,8 +813,14 @@ __device__ __forceinline__ StepShape step_shape(int lh, int lfa, int lfb, int lk
     sh.kind = SK_VEC8;
     total = outs >> 3;
   } else if (lfb >= 2) {
-    sh.kind = SK_VEC4;
-    total = outs >> 2;
+    // four outputs per item; where that leaves threads idle (and vsplit is
+    // allowed), 2-8 lanes share an item, each taking a run of >= 4 k
+    int vl = 0;
+    if (vsplit)
+      while (vl < 3 && ((outs >> 2) << (vl + 1)) <= bd && lk - (vl + 1) >= 2) ++vl;
+    sh.kind = vl ? SK_VSPLIT : SK_VEC4;
+    total = (outs >> 2) << vl;
+    lt = vl;
   } else {
     sh.kind = SK_SCALAR;
     total = outs;
@@ -807,7 +915,7 @@ __device__ void run_step_tc(const KArgs& a, const StepDesc& dref, int st, uint32
           phase ^= 1u;
           if (!ok) {
             ts->abort = 1;
-            atomicExch(a.tc_err, 1);
+            *static_cast<volatile int32_t*>(a.tc_err) = 1;
           }
           __syncthreads();
         }
@@ -854,7 +962,7 @@ __device__ void run_step_tc(const KArgs& a, const StepDesc& dref, int st, uint32
 // The planner hands the kernel arena and constant operands only (parity
 // operands become syndrome-selected tables), so each step shape has one code
 // path: the kernel stays small enough for the instruction caches.
-template <typename T, bool NORM, bool MAXP, bool G1, bool TENSOR, bool CL>
+template <typename T, bool NORM, bool MAXP, bool G1, bool TENSOR, bool CL, bool VS = false>
 __device__ __forceinline__ void dispatch_step(const KArgs& a, const StepDesc& d, const StepShape& sh, int st,
                                               int item_base, uint32_t* s_max, const StepPtrs<T>* ptrs,
                                               const PermTab& ptab, TcState* ts, unsigned char* tbuf) {
@@ -867,6 +975,10 @@ __device__ __forceinline__ void dispatch_step(const KArgs& a, const StepDesc& d,
   switch (sh.kind) {
     case SK_SPLITK:
       run_step_splitk<T, NORM, MAXP, G1, CL>(a, d, st, item_base, sh.lt, s_max, ptrs, ptab);
+      break;
+    case SK_VSPLIT:  // planned only where VS (the cluster kernel)
+      if constexpr (VS) run_step_vsplit<T, NORM, MAXP, G1, CL>(a, d, st, item_base, sh.lt, s_max, ptrs, ptab,
+                                                               sh.contiguous);
       break;
     case SK_VEC8:  // float32 only (step_shape)
       if constexpr (sizeof(T) == 4)
@@ -885,7 +997,8 @@ __device__ __forceinline__ void dispatch_step(const KArgs& a, const StepDesc& d,
 // staged tables (if any) and the arena (if in shared memory).
 struct BlockSmem {
   StepDesc* steps;
-  int2* plan;  // per step: x = kind | lt << 8 | per-syndrome << 16 | contiguous << 17, y = items (fill_step_plan)
+  int2* plan;  // per step: x = kind | lt << 8 | per-syndrome << 16 | contiguous << 17 | solo << 18 |
+               // block barrier << 19, y = items (fill_step_plan)
   void* ptrs;  // per syndrome and step: StepPtrs (operand and output bases)
   uint32_t* syn;
   uint32_t* max;
@@ -934,30 +1047,81 @@ __device__ __forceinline__ void copy16(void* dst, const void* src, size_t bytes)
 // and lanes per output), whether it runs syndrome by syndrome (a step that
 // fills the block for one syndrome alone, in a block of several), and how
 // many items (threads' worth) it takes, which also rotates the next member of
-// its barrier group.  One thread per step; the caller synchronises.
+// its barrier group.  `ptab` is read for the output permutations (staged in
+// shared memory where the launch staged its tables).  In a cluster, a first
+// pass writes every step's cluster-wide and block-sized plans to `scratch`
+// (2 x n_steps int2) and a second picks, per barrier group, whether it runs
+// on the first block alone; the block barrier between the passes is inside.
+// Otherwise one thread per step; the caller synchronises.
 template <typename T, bool tensor_ok, bool CL>
-__device__ __forceinline__ void fill_step_plan(const KArgs& a, const StepDesc* steps, int2* plan) {
-  const int bd = team_size<CL>();
-  for (int st = threadIdx.x; st < a.n_steps; st += blockDim.x) {
-    const StepDesc& d = steps[st];
-    const bool tensor = tensor_ok && a.tc != 0;
-    const StepShape sh = step_shape<T>(d.lh, d.lfa, d.lfb, d.lk, a.lg, d.flags, tensor, bd);
-    const StepShape sh1 = a.G > 1 ? step_shape<T>(d.lh, d.lfa, d.lfb, d.lk, 0, d.flags, tensor, bd) : sh;
+__device__ __forceinline__ void fill_step_plan(const KArgs& a, const StepDesc* steps, int2* plan,
+                                               const PermTab& ptab, int2* scratch = nullptr) {
+  const bool tensor = tensor_ok && a.tc != 0;
+  // the plan of step d for a team of bd threads
+  auto plan_of = [&](const StepDesc& d, int bd, bool vsplit) {
+    const StepShape sh = step_shape<T>(d.lh, d.lfa, d.lfb, d.lk, a.lg, d.flags, tensor, bd, vsplit);
+    const StepShape sh1 =
+        a.G > 1 ? step_shape<T>(d.lh, d.lfa, d.lfb, d.lk, 0, d.flags, tensor, bd, vsplit) : sh;
     const bool per_syndrome = a.G > 1 && sh1.total_r >= bd;
     const StepShape& use = per_syndrome ? sh1 : sh;
     // does the output permutation map index bits 0 .. log2(VW)-1 to
     // themselves?  (it moves whole bits, so checking each bit suffices)
     int contiguous = 0;
-    if ((use.kind == SK_VEC8 || use.kind == SK_VEC4) && d.perm_off >= 0) {
-      const PermTab gp{a.perm, false};
+    if ((use.kind == SK_VEC8 || use.kind == SK_VEC4 || use.kind == SK_VSPLIT) && d.perm_off >= 0) {
       const int lw = d.lh + d.lfa + d.lfb;
       const int lv = use.kind == SK_VEC8 ? 3 : 2;
       contiguous = 1;
       for (int b = 0; b < lv; ++b)
-        if (perm_addr(gp, d.perm_off, 1 << b, lw) != (1 << b)) contiguous = 0;
+        if (perm_addr(ptab, d.perm_off, 1 << b, lw) != (1 << b)) contiguous = 0;
     }
-    plan[st] = make_int2(use.kind | (use.lt << 8) | (int(per_syndrome) << 16) | (contiguous << 17),
-                         per_syndrome ? bd : sh.total_r);
+    return make_int2(use.kind | (use.lt << 8) | (int(per_syndrome) << 16) | (contiguous << 17),
+                     per_syndrome ? bd : sh.total_r);
+  };
+  if (!CL) {
+    for (int st = threadIdx.x; st < a.n_steps; st += blockDim.x) plan[st] = plan_of(steps[st], blockDim.x, false);
+    return;
+  }
+  int2* team_plan = scratch;
+  int2* block_plan = scratch + a.n_steps;
+  for (int st = threadIdx.x; st < a.n_steps; st += blockDim.x) {
+    team_plan[st] = plan_of(steps[st], team_size<CL>(), true);
+    block_plan[st] = plan_of(steps[st], blockDim.x, true);
+  }
+  __syncthreads();
+  // k summed by one lane of a step planned as pl
+  auto k_per_lane = [](const StepDesc& d, int2 pl) {
+    const int kind = pl.x & 0xff, lt = (pl.x >> 8) & 0xff;
+    return (kind == SK_SPLITK || kind == SK_VSPLIT) ? (1 << d.lk) >> lt : (1 << d.lk);
+  };
+  // a barrier group (steps s0..s1) whose items all fit the first block runs
+  // there alone (block-sized plans), unless that would lengthen a lane's run
+  // of k beyond max(8, its run on the whole cluster)
+  auto solo_group = [&](int s0, int s1) {
+    int items = 0;
+    for (int s = s0; s <= s1; ++s) {
+      const int kb = k_per_lane(steps[s], block_plan[s]), kt = k_per_lane(steps[s], team_plan[s]);
+      if (kb > (kt > 8 ? kt : 8)) return false;
+      items += block_plan[s].y;
+    }
+    return items <= int(blockDim.x);
+  };
+  auto group_end = [&](int s) {
+    while (s + 1 < a.n_steps && !(steps[s].flags & kStepSync)) ++s;
+    return s;
+  };
+  for (int st = threadIdx.x; st < a.n_steps; st += blockDim.x) {
+    int g0 = st;
+    while (g0 > 0 && !(steps[g0 - 1].flags & kStepSync)) --g0;
+    const int g1 = group_end(st);
+    const bool solo = solo_group(g0, g1);
+    int2 pl = solo ? block_plan[st] : team_plan[st];
+    if (solo) {
+      pl.x |= 1 << 18;
+      // the group's end needs only a block barrier when the next group (or,
+      // after the last, the epilogue) also runs on the first block alone
+      if (st == g1 && (g1 + 1 == a.n_steps || solo_group(g1 + 1, group_end(g1 + 1)))) pl.x |= 1 << 19;
+    }
+    plan[st] = pl;
   }
 }
 
@@ -1004,12 +1168,31 @@ __device__ void contract_group(const KArgs& a, int64_t base, int64_t nrows, cons
     sh.total_r = pl.y;
     const bool per_syndrome = (pl.x >> 16) & 1;
     const int items = pl.y;
+    if (CL && ((pl.x >> 18) & 1)) {
+      // a small group on the cluster's first block alone, planned for the
+      // block (the other blocks go on to the next cluster barrier)
+      if (cluster_rank() == 0 && rotated(threadIdx.x & ~31, item_base, blockDim.x) < items)
+        dispatch_step<T, NORM, MAXP, true, TENSOR, false, true>(a, d, sh, st, item_base, s_max, s_ptrs, ptab, sm.tc,
+                                                                sm.tbuf);
+      if (d.flags & kStepSync) {
+        if ((pl.x >> 19) & 1) {
+          if (cluster_rank() == 0) __syncthreads();
+        } else {
+          team_sync<CL>();
+        }
+        item_base = 0;
+      } else {
+        item_base += items;
+      }
+      continue;
+    }
     // first virtual thread of this warp (steps of a barrier group start on
     // different warps); a warp past the step's items goes to the barrier
     const int vt_warp = rotated(team_tid<CL>() & ~31, item_base, team_size<CL>());
     if (vt_warp < items) {
       if (a.G == 1) {
-        dispatch_step<T, NORM, MAXP, true, TENSOR, CL>(a, d, sh, st, item_base, s_max, s_ptrs, ptab, sm.tc, sm.tbuf);
+        dispatch_step<T, NORM, MAXP, true, TENSOR, CL, CL>(a, d, sh, st, item_base, s_max, s_ptrs, ptab, sm.tc,
+                                                           sm.tbuf);
       } else if (per_syndrome) {
         // the block's syndromes one after another with hoisted invariants
         for (int g = 0; g < a.G; ++g)
@@ -1032,6 +1215,67 @@ __device__ void contract_group(const KArgs& a, int64_t base, int64_t nrows, cons
     __syncthreads();
   }
   // epilogue: log-marginals, first argmax (Julia findmax order), recheck flag
+  if (a.G == 1) {
+    // one syndrome: the team's first warp, a lane per class (and per step
+    // for the normalisers' exponents)
+    if (team_tid<CL>() < 32 && base < nrows) {
+      const int lane = threadIdx.x & 31;
+      const int64_t row = a.list ? int64_t(a.list[base]) : base + a.row_offset;
+      const T* rv = s_ptrs[a.n_steps - 1].out;
+      double lsc = 0.0;
+      if (NORM) {
+        int e_sum = 0;
+        for (int st = lane; st < a.n_steps - 1; st += 32) {
+          int ee;
+          norm_factor(s_max[st], &ee);
+          e_sum += ee;
+        }
+        for (int o = 16; o > 0; o >>= 1) e_sum += __shfl_xor_sync(0xffffffffu, e_sum, o);
+        lsc = double(e_sum) * 0.69314718055994530942;
+      }
+      // per lane: the best and second-best of its classes (lane, lane + 32,
+      // ...) in class order; a lane without classes holds index INT_MAX
+      double lb = -INFINITY, ls = -INFINITY;
+      int li = lane < a.n_classes ? lane : INT_MAX;
+      for (int c = lane; c < a.n_classes; c += 32) {
+        const double v = double(rv[c]);
+        const double lp = v > 0.0 ? log(v) + lsc : -INFINITY;
+        if (a.logp_out) a.logp_out[row * a.n_classes + c] = lp;
+        if (lp > lb) {
+          ls = lb;
+          lb = lp;
+          li = c;
+        } else if (lp > ls) {
+          ls = lp;
+        }
+      }
+      // the first maximum over the lanes (equal values: the lower class)
+      double best = lb;
+      int bc = li;
+      for (int o = 16; o > 0; o >>= 1) {
+        const double ob = __shfl_xor_sync(0xffffffffu, best, o);
+        const int oi = __shfl_xor_sync(0xffffffffu, bc, o);
+        if (ob > best || (ob == best && oi < bc)) {
+          best = ob;
+          bc = oi;
+        }
+      }
+      // the largest value of every other class
+      double second = li == bc ? ls : lb;
+      for (int o = 16; o > 0; o >>= 1) second = fmax(second, __shfl_xor_sync(0xffffffffu, second, o));
+      if (lane == 0) {
+        if (a.class_out) a.class_out[row] = bc;
+        if (a.err_out) a.err_out[row] = a.err_bound;
+        if (a.recheck_margin >= 0.0) {
+          const double margin = best - second;
+          if (!(margin >= a.recheck_margin) || best == -INFINITY) {
+            const int slot = atomicAdd(a.recheck_count, 1);
+            a.recheck_list[slot] = int32_t(row);
+          }
+        }
+      }
+    }
+  } else
   for (int g = team_tid<CL>(); g < a.G; g += team_size<CL>()) {
     const int64_t r = base + g;
     if (r >= nrows) continue;
@@ -1082,12 +1326,46 @@ __device__ __forceinline__ void stage_tables(const KArgs& a, unsigned char* smem
   *ptab = PermTab{a.perm, false};
   if (!a.tables_smem) return;
   T* s_consts = reinterpret_cast<T*>(smem + *off);
-  *off += (size_t(a.n_consts) * sizeof(T) + 15) & ~size_t(15);
+  const size_t const_bytes = size_t(a.n_consts) * sizeof(T);
+  *off += (const_bytes + 15) & ~size_t(15);
   void* s_perm = smem + *off;
   const size_t perm_bytes = size_t(a.n_perm) * (a.perm16 ? 2 : 4);
   *off += (perm_bytes + 15) & ~size_t(15);
-  copy16(s_consts, a.consts, size_t(a.n_consts) * sizeof(T));
-  copy16(s_perm, a.perm16 ? static_cast<const void*>(a.perm16) : static_cast<const void*>(a.perm), perm_bytes);
+  const void* perm_src = a.perm16 ? static_cast<const void*>(a.perm16) : static_cast<const void*>(a.perm);
+  // the 16-byte multiples by bulk asynchronous copies (one instruction each,
+  // issued by thread 0, completing on one mbarrier) instead of a load and a
+  // store per thread and 16 bytes; the few bytes past them by plain loads
+  __shared__ uint64_t s_bar;
+  const uint32_t m0 = uint32_t(const_bytes & ~size_t(15)), m1 = uint32_t(perm_bytes & ~size_t(15));
+  if (threadIdx.x == 0) {
+    tc::mbar_init(&s_bar, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;\n\tfence.proxy.async.shared::cta;" ::: "memory");
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(tc::smem_u32(&s_bar)),
+                 "r"(m0 + m1)
+                 : "memory");
+    if (m0)
+      asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                       tc::smem_u32(s_consts)),
+                   "l"(a.consts), "r"(m0), "r"(tc::smem_u32(&s_bar))
+                   : "memory");
+    if (m1)
+      asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                       tc::smem_u32(s_perm)),
+                   "l"(perm_src), "r"(m1), "r"(tc::smem_u32(&s_bar))
+                   : "memory");
+  }
+  for (int i = threadIdx.x; i < int(const_bytes - m0); i += blockDim.x)
+    reinterpret_cast<unsigned char*>(s_consts)[m0 + i] = static_cast<const unsigned char*>(a.consts)[m0 + i];
+  for (int i = threadIdx.x; i < int(perm_bytes - m1); i += blockDim.x)
+    static_cast<unsigned char*>(s_perm)[m1 + i] = static_cast<const unsigned char*>(perm_src)[m1 + i];
+  if (!tc::mbar_wait(&s_bar, 0)) {
+    // the copies never completed (not expected): the results are flagged as
+    // invalid; the block still runs to its end, so no barrier waits for it
+    if (a.tc_err) *static_cast<volatile int32_t*>(a.tc_err) = 2;
+  }
   *consts = s_consts;
   *ptab = PermTab{s_perm, a.perm16 != nullptr};
 }
@@ -1121,7 +1399,7 @@ __global__ void __launch_bounds__(sizeof(T) == 8 || TENSOR ? 512 : 1024) tn_cont
   copy16(sm.steps, a.steps, size_t(a.n_steps) * sizeof(StepDesc));
   __syncthreads();
   constexpr bool kTensor = TENSOR && std::is_same<T, float>::value && NORM && !MAXP;
-  fill_step_plan<T, kTensor, false>(a, sm.steps, sm.plan);
+  fill_step_plan<T, kTensor, false>(a, sm.steps, sm.plan, ptab);
   const bool tensor = kTensor && a.tc;
   if (tensor) {
     if (threadIdx.x == 0) {
@@ -1174,7 +1452,7 @@ __global__ void __launch_bounds__(512) tn_contract_cluster_kernel(KArgs a) {
   stage_tables<T>(a, smem, &off, &consts, &ptab);
   copy16(sm.steps, a.steps, size_t(a.n_steps) * sizeof(StepDesc));
   __syncthreads();
-  fill_step_plan<T, false, true>(a, sm.steps, sm.plan);
+  fill_step_plan<T, false, true>(a, sm.steps, sm.plan, ptab, static_cast<int2*>(sm.ptrs));
   if (NORM) sm.max = cluster_map(sm.max, 0);
   const int64_t nrows = a.list ? int64_t(*a.list_count) : a.n;
   const int64_t cid = cluster_id(), ncl = cluster_count();
@@ -1223,7 +1501,7 @@ __global__ void __launch_bounds__(kMultiThreads) tn_contract_multi_kernel(MultiA
     if (first) {
       copy16(sm.steps, a.steps, size_t(a.n_steps) * sizeof(StepDesc));
       __syncthreads();
-      fill_step_plan<T, false, false>(a, sm.steps, sm.plan);
+      fill_step_plan<T, false, false>(a, sm.steps, sm.plan, PermTab{a.perm, false});
       __syncthreads();
     }
     T* abase = a.arena_global ? gslice : reinterpret_cast<T*>(smem + sm.tail);
@@ -1241,7 +1519,7 @@ __global__ void __launch_bounds__(kMultiThreads) tn_contract_multi_kernel(MultiA
       const BlockSmem sm = carve_smem<NORM, false>(s_ka, smem);
       copy16(sm.steps, s_ka.steps, size_t(s_ka.n_steps) * sizeof(StepDesc));
       __syncthreads();
-      fill_step_plan<T, false, false>(s_ka, sm.steps, sm.plan);
+      fill_step_plan<T, false, false>(s_ka, sm.steps, sm.plan, PermTab{s_ka.perm, false});
       __syncthreads();
       for (int64_t base = int64_t(blockIdx.x) * s_ka.G; base < nrows; base += int64_t(gridDim.x) * s_ka.G)
         run_unit(prog, base, nrows, false);
@@ -1369,7 +1647,16 @@ cudaError_t contract_launch(int precision, const KArgs& a, int grid, int threads
 template <typename K>
 cudaError_t cluster_config(K kernel, int csize, int threads, size_t smem) {
   cudaError_t e = grow_smem_limit(kernel, smem);
-  if (e == cudaSuccess && csize > 8) e = cudaFuncSetAttribute(kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+  if (e != cudaSuccess || csize <= 8) return e;
+  // clusters above the portable 8 blocks: allowed once per kernel
+  static std::mutex mu;
+  static std::map<const void*, bool> allowed;
+  std::lock_guard<std::mutex> lk(mu);
+  bool& ok = allowed[reinterpret_cast<const void*>(kernel)];
+  if (!ok) {
+    e = cudaFuncSetAttribute(kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+    ok = e == cudaSuccess;
+  }
   return e;
 }
 

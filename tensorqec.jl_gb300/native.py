@@ -105,7 +105,7 @@ def lib():
         "tqec_contract_batch": [vp, vp, i64, i32, vp, vp],
         "tqec_last_recheck_count": [vp, vp],
         "tqec_program_autotune": [vp, i64],
-        "tqec_program_set_cluster": [vp, i32, i32, i32],
+        "tqec_program_set_cluster": [vp, i32, i32, i32, i32],
         "tqec_program_save": [vp, C.c_char_p],
         "tqec_program_load": [C.c_char_p, i32, vp],
         "tqec_plan_inspect": [vp, vp, vp, vp],
@@ -287,10 +287,12 @@ class Program:
         check(lib().tqec_last_recheck_count(self._h, C.byref(c)))
         return c.value
 
-    def set_cluster(self, precision, blocks, threads=512):
+    def set_cluster(self, precision, blocks, threads=512, small_in_smem=-1):
         """Single-syndrome launches of `precision` on clusters of `blocks`
-        blocks (0: one block per syndrome)."""
-        check(lib().tqec_program_set_cluster(self._h, precision, blocks, threads))
+        blocks (0: one block per syndrome); small_in_smem 1 / 0 / -1: the
+        small intermediates in the first block's shared memory / all in
+        global memory / the first where it fits."""
+        check(lib().tqec_program_set_cluster(self._h, precision, blocks, threads, small_in_smem))
         self._refresh_info()
 
     def autotune(self, n_probe=4096):

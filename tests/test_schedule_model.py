@@ -4,15 +4,17 @@ It restates the kernels' step-shape choice (several lanes per output, eight
 or four outputs per work item, or one), its per-warp entry test, the
 rotation of barrier-group members over the block and the per-syndrome loop
 of multi-syndrome blocks (csrc/contract.cu: step_shape, the step loop of
-tn_contract_kernel, run_step*, run_step_splitk), and checks on real programs
-that every output of every syndrome of every step is written exactly once for
-each launch shape the autotuner may pick.
+tn_contract_kernel, run_step*, run_step_splitk, run_step_vsplit), and the
+cluster form's plans (fill_step_plan: lanes sharing four-output items, small
+barrier groups on the first block alone), and checks on real programs that
+every output of every syndrome of every step is written exactly once for each
+launch shape the autotuner may pick.
 """
 import numpy as np
 import pytest
 
 
-def step_shape(lh, lfa, lfb, lk, lg, bd, is_float, flags=0):
+def step_shape(lh, lfa, lfb, lk, lg, bd, is_float, flags=0, vsplit=False):
     """SIMT shapes (a tensor-core step covers its outputs tile by tile)."""
     lw = lh + lfa + lfb
     outs = 1 << (lw + lg)
@@ -26,7 +28,10 @@ def step_shape(lh, lfa, lfb, lk, lg, bd, is_float, flags=0):
     elif is_float and lfb >= 3 and (outs >> 3) >= bd:
         kind, total = "vec8", outs >> 3
     elif lfb >= 2:
-        kind, total = "vec4", outs >> 2
+        vl = 0
+        while vsplit and vl < 3 and ((outs >> 2) << (vl + 1)) <= bd and lk - (vl + 1) >= 2:
+            vl += 1
+        kind, total, lt = ("vsplit" if vl else "vec4"), (outs >> 2) << vl, vl
     else:
         kind, total = "scalar", outs
     return kind, lt, (total + 31) & ~31
@@ -49,6 +54,15 @@ def _run(kind, lt, lw, lg, one, bd, item_base, enter, cover, gbase):
                     item = x >> lt
                     g = 0 if one else item >> lw
                     cover[gbase + g, item & ((1 << lw) - 1)] += 1
+        return
+    if kind == "vsplit":  # one syndrome: 2^lt lanes per four outputs
+        total = (1 << (lw - 2)) << lt
+        tr = (total + 31) & ~31
+        for v in vt:
+            for x in range(v, tr, bd):
+                if x < total and (x & ((1 << lt) - 1)) == 0:
+                    e0 = (x >> lt) << 2
+                    cover[gbase, e0:e0 + 4] += 1
         return
     lv = {"vec8": 3, "vec4": 2, "scalar": 0}[kind]
     lwv = lw - lv
@@ -94,6 +108,49 @@ def check_program(plan, is_float):
     return bad
 
 
+def check_cluster_program(plan, is_float, blocks, threads):
+    """The cluster form (one syndrome per cluster of `blocks` blocks): every
+    output written once, and a group planned for the first block alone keeps
+    all its items on that block's threads."""
+    steps = plan["steps"]
+    n = len(steps)
+    sync = [bool(int(d["flags"]) & 1) for d in steps]
+    team = blocks * threads
+
+    def shape(d, bd):
+        return step_shape(int(d["lh"]), int(d["lfa"]), int(d["lfb"]), int(d["lk"]), 0, bd, is_float,
+                          int(d["flags"]), vsplit=True)
+
+    groups, s0 = [], 0
+    for st in range(n):
+        if sync[st] or st == n - 1:
+            groups.append((s0, st))
+            s0 = st + 1
+    def k_per_lane(d, sh):
+        kind, lt, _ = sh
+        return (1 << int(d["lk"])) >> lt if kind in ("splitk", "vsplit") else 1 << int(d["lk"])
+
+    bad = []
+    for s0, s1 in groups:
+        solo = (sum(shape(steps[s], threads)[2] for s in range(s0, s1 + 1)) <= threads and
+                all(k_per_lane(steps[s], shape(steps[s], threads)) <=
+                    max(8, k_per_lane(steps[s], shape(steps[s], team))) for s in range(s0, s1 + 1)))
+        bd = threads if solo else team
+        item_base = 0
+        for st in range(s0, s1 + 1):
+            d = steps[st]
+            lw = int(d["lh"]) + int(d["lfa"]) + int(d["lfb"])
+            kind, lt, tr = shape(d, bd)
+            cover = np.zeros((1, 1 << lw), dtype=np.int64)
+            _run(kind, lt, lw, 0, True, bd, item_base, tr, cover, 0)
+            if not (cover == 1).all():
+                bad.append((blocks, threads, st, kind, solo, int(cover.min()), int(cover.max())))
+            item_base += tr
+        if solo and item_base > threads:
+            bad.append((blocks, threads, s0, "solo group exceeds the first block", item_base))
+    return bad
+
+
 @pytest.mark.parametrize("code", ["surface5", "color488_5", "surface7"])
 def test_every_output_written_once(pkg, code):
     from tensorqec_gb300 import decoder, gf2, network, native
@@ -107,3 +164,22 @@ def test_every_output_written_once(pkg, code):
     plan = native.inspect_plan(graph, steps)
     for is_float in (True, False):
         assert check_program(plan, is_float) == []
+
+
+@pytest.mark.parametrize("code", ["surface7", "color488_5"])
+def test_cluster_plans_write_every_output_once(pkg, code):
+    from tensorqec_gb300 import decoder, gf2, network, native
+    c = {"color488_5": lambda: pkg.Color488(5), "surface7": lambda: pkg.SurfaceCode(7, 7)}[code]()
+    t = pkg.tanner_graph(c)
+    em = pkg.depolarizing(0.05, t.nq)
+    lx, lz = gf2.logical_operator(t)
+    graph = network.tnmmap_css_graph(t, em, lx, lz)
+    steps = decoder.optimize_code(graph, decoder.TreeSA(restarts=1))
+    plan = native.inspect_plan(graph, steps)
+    kinds = set()
+    for blocks, threads in ((2, 128), (4, 256), (8, 256), (16, 128), (16, 256), (8, 512)):
+        assert check_cluster_program(plan, False, blocks, threads) == []
+        for d in plan["steps"]:
+            kinds.add(step_shape(int(d["lh"]), int(d["lfa"]), int(d["lfb"]), int(d["lk"]), 0, blocks * threads,
+                                 False, int(d["flags"]), vsplit=True)[0])
+    assert "vsplit" in kinds
