@@ -70,6 +70,10 @@ extern "C" {
 #define TQEC_FLAG_NO_TENSOR_CORES 16u
 /* TQEC_F32: recheck low margins in float64 instead of TQEC_F32X2 */
 #define TQEC_FLAG_RECHECK_F64 32u
+/* launch shape: in blocks of one syndrome, 2-8 lanes share each four-output
+ * work item of a step that would leave threads idle, each summing a run of
+ * the contracted range (tqec_program_autotune also tries this) */
+#define TQEC_FLAG_SHARED_ITEMS 64u
 
 /* The factor graph, as built by compile(::TNMMAP, ...) (tndecoder.jl:97-146
  * for CSS codes, :186-219 for detector error models). */
@@ -134,6 +138,8 @@ typedef struct {
                                 syndrome in single-syndrome launches (the recheck; all
                                 launches of a TQEC_FLAG_PLAIN program); 0: one block */
   double err_bound_f32x2;    /* relative error bound of a TQEC_F32X2 marginal */
+  int32_t shared_items_f32, shared_items_f64; /* 1: lanes share the work items of steps
+                                                 that leave threads idle (TQEC_FLAG_SHARED_ITEMS) */
 } tqec_program_info_t;
 
 typedef struct tqec_program tqec_program;

@@ -50,6 +50,7 @@ struct Shape {
   bool smem_tables = false;  // constants and permutation tables staged in shared memory
   bool split = false;        // small-tensor pool in shared memory, big-tensor pool in global memory
   bool tensor = false;       // GEMM-shaped steps on the tensor cores (float32 programs that have them)
+  bool vsplit = false;       // lanes may share the four-output items of steps that leave threads idle
   size_t smem = 0;
   int grid_cap = 1;  // blocks resident on the whole device
 };
@@ -347,6 +348,7 @@ int launch_rows(tqec_program* p, int precision, tqec::KArgs a, int64_t n_rows_ma
   a.arena_global = s.smem_arena ? nullptr : p->arena[precision].p;
   a.arena_small = s.split ? p->plan.arena_small : 0;
   a.tc = s.tensor ? 1 : 0;
+  a.vsplit = s.vsplit ? 1 : 0;
   a.tc_err = p->d_tc_err;
   TQ_CUDA(tqec::contract_launch(precision, a, grid, s.threads, s.smem, st));
   return TQEC_OK;
@@ -798,12 +800,12 @@ int tqec_program_create(const tqec_network* net, const tqec_tree* tree, const tq
     if ((o.flags & TQEC_FLAG_SPLIT_ARENA) && p->plan.arena_small > 0 &&
         choose_split_shape(p, prec, std::max(1, o.group), o.threads > 0 ? o.threads : 256, 0, &sp) == TQEC_OK) {
       p->shape[prec] = sp;
-      continue;
-    }
-    if ((rc = choose_shape(p, prec, o.group, o.threads, -1, &p->shape[prec])) != TQEC_OK) {
+    } else if ((rc = choose_shape(p, prec, o.group, o.threads, -1, &p->shape[prec])) != TQEC_OK) {
       std::string m = g_last_error;
       return bail(rc, m);
     }
+    Shape& sh = p->shape[prec];
+    sh.vsplit = (o.flags & TQEC_FLAG_SHARED_ITEMS) && sh.G == 1 && !sh.tensor && !P.map_mode;
   }
   // the recheck keeps the small intermediates and the tables in shared
   // memory when the program has both pools and they fit
@@ -876,6 +878,8 @@ int tqec_program_info(const tqec_program* p, tqec_program_info_t* info) {
   info->split_f64 = p->shape[TQEC_F64].split ? 1 : 0;
   info->recheck_precision = P.map_mode ? TQEC_F64 : recheck_precision(p);
   info->cluster_blocks = p->cluster[(p->flags & TQEC_FLAG_PLAIN) ? p->precision : info->recheck_precision].size;
+  info->shared_items_f32 = p->shape[TQEC_F32].vsplit ? 1 : 0;
+  info->shared_items_f64 = p->shape[TQEC_F64].vsplit ? 1 : 0;
   info->err_bound_f32x2 = err_bound(p, TQEC_F32X2);
   return TQEC_OK;
 }
@@ -1031,6 +1035,10 @@ bool tune_shape(tqec_program* p, int prec, int64_t n, cudaEvent_t e0, cudaEvent_
           // programs with GEMM-shaped steps also try them on the SIMT path
           for (int tensor : {1, 0}) {
           if (!tensor && !tensor_program(p, prec)) continue;
+          // one syndrome per block: also with lanes sharing the items of
+          // steps that would leave threads idle
+          for (int vs : {0, 1}) {
+          if (vs && (G > 1 || tensor || p->plan.map_mode)) continue;
           Shape s;
           if (split) {
             if (choose_split_shape(p, prec, G, th, tables, &s, tensor) != TQEC_OK) continue;
@@ -1038,6 +1046,7 @@ bool tune_shape(tqec_program* p, int prec, int64_t n, cudaEvent_t e0, cudaEvent_
             continue;
           }
           if (tables && !s.smem_tables) continue;
+          s.vsplit = vs != 0;
           if (resident) {
             if (s.smem_arena || tables || resident * p->sm_count >= s.grid_cap) continue;
             s.grid_cap = resident * p->sm_count;
@@ -1061,6 +1070,7 @@ bool tune_shape(tqec_program* p, int prec, int64_t n, cudaEvent_t e0, cudaEvent_
           if (ms < best_ms) {
             best_ms = ms;
             best = s;
+          }
           }
           }
          }
@@ -1310,7 +1320,7 @@ struct Writer {
     put<uint8_t>(s.smem_arena);
     put<uint8_t>(s.smem_tables);
     put<uint8_t>(s.split);
-    put<uint8_t>(s.tensor);
+    put<uint8_t>(uint8_t(s.tensor ? 1 : 0) | uint8_t(s.vsplit ? 2 : 0));
     put<uint64_t>(s.smem);
     put<int32_t>(s.grid_cap);
   }
@@ -1353,7 +1363,9 @@ struct Reader {
     s.smem_arena = get<uint8_t>() != 0;
     s.smem_tables = get<uint8_t>() != 0;
     s.split = get<uint8_t>() != 0;
-    s.tensor = get<uint8_t>() != 0;
+    const uint8_t flags = get<uint8_t>();
+    s.tensor = (flags & 1) != 0;
+    s.vsplit = (flags & 2) != 0;
     s.smem = (size_t)get<uint64_t>();
     s.grid_cap = get<int32_t>();
     return s;
@@ -1366,6 +1378,7 @@ struct Reader {
 bool shape_consistent(const tqec_program* p, int prec, const Shape& s) {
   if (s.G < 1 || s.G > 1024 || (s.G & (s.G - 1))) return false;
   if (s.tensor && !tensor_program(p, prec)) return false;
+  if (s.vsplit && s.G != 1) return false;
   if (s.threads < (s.tensor ? 128 : 32) || s.threads > tqec::contract_max_threads(prec, s.tensor) ||
       (s.threads & (s.threads - 1)))
     return false;

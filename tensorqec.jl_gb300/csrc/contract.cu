@@ -976,7 +976,7 @@ __device__ __forceinline__ void dispatch_step(const KArgs& a, const StepDesc& d,
     case SK_SPLITK:
       run_step_splitk<T, NORM, MAXP, G1, CL>(a, d, st, item_base, sh.lt, s_max, ptrs, ptab);
       break;
-    case SK_VSPLIT:  // planned only where VS (the cluster kernel)
+    case SK_VSPLIT:  // planned where the launch allows it (KArgs::vsplit, the cluster kernel)
       if constexpr (VS) run_step_vsplit<T, NORM, MAXP, G1, CL>(a, d, st, item_base, sh.lt, s_max, ptrs, ptab,
                                                                sh.contiguous);
       break;
@@ -1053,7 +1053,7 @@ __device__ __forceinline__ void copy16(void* dst, const void* src, size_t bytes)
 // (2 x n_steps int2) and a second picks, per barrier group, whether it runs
 // on the first block alone; the block barrier between the passes is inside.
 // Otherwise one thread per step; the caller synchronises.
-template <typename T, bool tensor_ok, bool CL>
+template <typename T, bool tensor_ok, bool CL, bool VS = false>
 __device__ __forceinline__ void fill_step_plan(const KArgs& a, const StepDesc* steps, int2* plan,
                                                const PermTab& ptab, int2* scratch = nullptr) {
   const bool tensor = tensor_ok && a.tc != 0;
@@ -1078,7 +1078,8 @@ __device__ __forceinline__ void fill_step_plan(const KArgs& a, const StepDesc* s
                      per_syndrome ? bd : sh.total_r);
   };
   if (!CL) {
-    for (int st = threadIdx.x; st < a.n_steps; st += blockDim.x) plan[st] = plan_of(steps[st], blockDim.x, false);
+    for (int st = threadIdx.x; st < a.n_steps; st += blockDim.x)
+      plan[st] = plan_of(steps[st], blockDim.x, VS && a.vsplit != 0);  // only kernels with the body
     return;
   }
   int2* team_plan = scratch;
@@ -1128,7 +1129,7 @@ __device__ __forceinline__ void fill_step_plan(const KArgs& a, const StepDesc* s
 // One group of up to G syndromes (rows base .. base+G-1 below nrows) through
 // the whole program: load the syndrome words, run every step, back-track
 // (MAP), then the epilogue.  Ends with a block barrier.
-template <typename T, bool NORM, bool MAXP, bool TENSOR, bool CL>
+template <typename T, bool NORM, bool MAXP, bool TENSOR, bool CL, bool VS>
 __device__ void contract_group(const KArgs& a, int64_t base, int64_t nrows, const BlockSmem& sm,
                                const Arena<T>& arena,
                                const T* consts, const PermTab& ptab) {
@@ -1191,16 +1192,16 @@ __device__ void contract_group(const KArgs& a, int64_t base, int64_t nrows, cons
     const int vt_warp = rotated(team_tid<CL>() & ~31, item_base, team_size<CL>());
     if (vt_warp < items) {
       if (a.G == 1) {
-        dispatch_step<T, NORM, MAXP, true, TENSOR, CL, CL>(a, d, sh, st, item_base, s_max, s_ptrs, ptab, sm.tc,
+        dispatch_step<T, NORM, MAXP, true, TENSOR, CL, VS>(a, d, sh, st, item_base, s_max, s_ptrs, ptab, sm.tc,
                                                            sm.tbuf);
       } else if (per_syndrome) {
         // the block's syndromes one after another with hoisted invariants
         for (int g = 0; g < a.G; ++g)
-          dispatch_step<T, NORM, MAXP, true, TENSOR, CL>(a, d, sh, st, item_base, s_max + g * a.n_steps,
-                                                         s_ptrs + g * a.n_steps, ptab, sm.tc, sm.tbuf);
+          dispatch_step<T, NORM, MAXP, true, TENSOR, CL, VS>(a, d, sh, st, item_base, s_max + g * a.n_steps,
+                                                             s_ptrs + g * a.n_steps, ptab, sm.tc, sm.tbuf);
       } else {
-        dispatch_step<T, NORM, MAXP, false, TENSOR, CL>(a, d, sh, st, item_base, s_max, s_ptrs, ptab, sm.tc,
-                                                        sm.tbuf);
+        dispatch_step<T, NORM, MAXP, false, TENSOR, CL, VS>(a, d, sh, st, item_base, s_max, s_ptrs, ptab, sm.tc,
+                                                            sm.tbuf);
       }
     }
     if (d.flags & kStepSync) {
@@ -1387,7 +1388,10 @@ __device__ __forceinline__ Arena<T> block_arena(const KArgs& a, unsigned char* s
 
 // float64 blocks, and blocks running tensor-core steps, are capped at 512
 // threads, which leaves them 128 registers
-template <typename T, bool NORM, bool MAXP, bool TENSOR>
+// VS: the kernel has the SK_VSPLIT step body (launches with KArgs::vsplit
+// plan it); the float32 kernel without it is kept for launches that do not,
+// its 64 registers a thread being the tighter budget.
+template <typename T, bool NORM, bool MAXP, bool TENSOR, bool VS = (sizeof(T) == 8)>
 __global__ void __launch_bounds__(sizeof(T) == 8 || TENSOR ? 512 : 1024) tn_contract_kernel(KArgs a) {
   extern __shared__ __align__(16) unsigned char smem[];
   const BlockSmem sm = carve_smem<NORM, MAXP>(a, smem);
@@ -1399,7 +1403,7 @@ __global__ void __launch_bounds__(sizeof(T) == 8 || TENSOR ? 512 : 1024) tn_cont
   copy16(sm.steps, a.steps, size_t(a.n_steps) * sizeof(StepDesc));
   __syncthreads();
   constexpr bool kTensor = TENSOR && std::is_same<T, float>::value && NORM && !MAXP;
-  fill_step_plan<T, kTensor, false>(a, sm.steps, sm.plan, ptab);
+  fill_step_plan<T, kTensor, false, VS>(a, sm.steps, sm.plan, ptab);
   const bool tensor = kTensor && a.tc;
   if (tensor) {
     if (threadIdx.x == 0) {
@@ -1415,7 +1419,7 @@ __global__ void __launch_bounds__(sizeof(T) == 8 || TENSOR ? 512 : 1024) tn_cont
   }
   const int64_t nrows = a.list ? int64_t(*a.list_count) : a.n;
   for (int64_t base = int64_t(blockIdx.x) * a.G; base < nrows; base += int64_t(gridDim.x) * a.G)
-    contract_group<T, NORM, MAXP, TENSOR, false>(a, base, nrows, sm, arena, consts, ptab);
+    contract_group<T, NORM, MAXP, TENSOR, false, VS>(a, base, nrows, sm, arena, consts, ptab);
   if (tensor) {
     tc::fence_before();
     __syncthreads();
@@ -1470,7 +1474,7 @@ __global__ void __launch_bounds__(512) tn_contract_cluster_kernel(KArgs a) {
     arena = Arena<T>{slice, slice, INT32_MAX, int32_t(a.arena_elems), int32_t(a.arena_elems)};
   }
   for (int64_t base = cid * a.G; base < nrows; base += ncl * a.G)
-    contract_group<T, NORM, false, false, true>(a, base, nrows, sm, arena, consts, ptab);
+    contract_group<T, NORM, false, false, true, true>(a, base, nrows, sm, arena, consts, ptab);
   // the first block's shared memory stays until no block of the cluster
   // can still reach it
   team_sync<true>();
@@ -1506,7 +1510,7 @@ __global__ void __launch_bounds__(kMultiThreads) tn_contract_multi_kernel(MultiA
     }
     T* abase = a.arena_global ? gslice : reinterpret_cast<T*>(smem + sm.tail);
     const Arena<T> arena{abase, abase, INT32_MAX, int32_t(a.arena_elems), int32_t(a.arena_elems)};
-    contract_group<T, NORM, false, false, false>(a, base, nrows, sm, arena, reinterpret_cast<const T*>(a.consts),
+    contract_group<T, NORM, false, false, false, false>(a, base, nrows, sm, arena, reinterpret_cast<const T*>(a.consts),
                                           PermTab{a.perm, false});
   };
   if (m.list_mode) {
@@ -1614,7 +1618,7 @@ int contract_occupancy(int precision, int threads, size_t smem, bool map_mode, b
   if (precision == 1) {
     if (map_mode) return occupancy_of(tn_contract_kernel<float, true, true, false>, threads, smem);
     return tensor ? occupancy_of(tn_contract_kernel<float, true, false, true>, threads, smem)
-                  : occupancy_of(tn_contract_kernel<float, true, false, false>, threads, smem);
+                  : occupancy_of(tn_contract_kernel<float, true, false, false>, threads, smem);  // same registers with VS
   }
   if (precision == 2) return map_mode ? 0 : occupancy_of(tn_contract_kernel<dfloat, true, false, false>, threads, smem);
   return map_mode ? occupancy_of(tn_contract_kernel<double, false, true, false>, threads, smem)
@@ -1633,8 +1637,9 @@ cudaError_t contract_launch(int precision, const KArgs& a, int grid, int threads
                             cudaStream_t stream) {
   if (precision == 1) {
     if (a.map_mode) return launch_with(tn_contract_kernel<float, true, true, false>, a, grid, threads, smem, stream);
-    return a.tc ? launch_with(tn_contract_kernel<float, true, false, true>, a, grid, threads, smem, stream)
-                : launch_with(tn_contract_kernel<float, true, false, false>, a, grid, threads, smem, stream);
+    if (a.tc) return launch_with(tn_contract_kernel<float, true, false, true>, a, grid, threads, smem, stream);
+    return a.vsplit ? launch_with(tn_contract_kernel<float, true, false, false, true>, a, grid, threads, smem, stream)
+                    : launch_with(tn_contract_kernel<float, true, false, false>, a, grid, threads, smem, stream);
   }
   if (precision == 2) {
     if (a.map_mode) return cudaErrorInvalidValue;  // max-product runs in float32 or float64

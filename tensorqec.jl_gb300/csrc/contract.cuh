@@ -58,7 +58,7 @@ struct KArgs {
   // kStepTensor steps on tcgen05 (float32 only); tc_err is set when a wait
   // for the tensor cores gave up
   int32_t tc;
-  int32_t tc_pad;
+  int32_t vsplit;  // block launches: lanes may share four-output items (SK_VSPLIT)
   int32_t* tc_err;
 };
 static_assert(sizeof(KArgs) % 16 == 0, "KArgs is copied in 16-byte units");

@@ -168,7 +168,8 @@ class TNMMAP:
     (the drop-in form of the reference's per-syndrome ``decode``).
     ``slices`` > 0 fixes that many inner labels of the tree and contracts the
     2^slices narrower networks (``SlicedProgram``), for networks too wide to
-    contract whole."""
+    contract whole.  ``shared_items``: in blocks of one syndrome, lanes share
+    the work items of steps that would leave threads idle."""
     optimizer: object = field(default_factory=TreeSA)
     factorize: bool = True
     precision: str = "f32"
@@ -182,6 +183,7 @@ class TNMMAP:
     tensor_cores: bool = True
     recheck_f64: bool = False
     slices: int = 0
+    shared_items: bool = False
 
     def _native_precision(self):
         return {"f64": native.TQEC_F64, "f32": native.TQEC_F32}[self.precision]
@@ -190,7 +192,8 @@ class TNMMAP:
         return ((native.TQEC_FLAG_PLAIN if self.plain else 0) |
                 (native.TQEC_FLAG_SPLIT_ARENA if self.split_arena else 0) |
                 (0 if self.tensor_cores else native.TQEC_FLAG_NO_TENSOR_CORES) |
-                (native.TQEC_FLAG_RECHECK_F64 if self.recheck_f64 else 0))
+                (native.TQEC_FLAG_RECHECK_F64 if self.recheck_f64 else 0) |
+                (native.TQEC_FLAG_SHARED_ITEMS if self.shared_items else 0))
 
     def _program(self, graph, steps):
         """The GPU program of a compiled network: whole, or sliced."""

@@ -23,6 +23,7 @@ TQEC_FLAG_MAP = 4
 TQEC_FLAG_SPLIT_ARENA = 8
 TQEC_FLAG_NO_TENSOR_CORES = 16
 TQEC_FLAG_RECHECK_F64 = 32
+TQEC_FLAG_SHARED_ITEMS = 64
 
 ERRORS = {-1: "invalid argument", -2: "CUDA error", -3: "out of device memory",
           -4: "unsupported network", -5: "timeout", -6: "I/O error"}
@@ -60,7 +61,8 @@ class ProgramInfo(C.Structure):
                 ("resident_f32", C.c_int32), ("resident_f64", C.c_int32), ("tables_smem_f32", C.c_int32),
                 ("tables_smem_f64", C.c_int32), ("arena_small", C.c_int64), ("split_f32", C.c_int32),
                 ("split_f64", C.c_int32), ("tensor_steps", C.c_int32), ("tensor_f32", C.c_int32),
-                ("recheck_precision", C.c_int32), ("cluster_blocks", C.c_int32), ("err_bound_f32x2", C.c_double)]
+                ("recheck_precision", C.c_int32), ("cluster_blocks", C.c_int32), ("err_bound_f32x2", C.c_double),
+                ("shared_items_f32", C.c_int32), ("shared_items_f64", C.c_int32)]
 
 
 class PlanView(C.Structure):

@@ -252,13 +252,40 @@ def test_split_arena_shapes_vs_plain_f64(pkg, group, threads):
         info = ct.program.info
         assert info["arena_small"] > 0 and info[f"split_{precision}"] == 1
         lp = ct.class_logprobs(bits)
-        tol = 1e-10 if precision == "f64" else 2 * info["err_bound_f32"]
-        top = np.max(want, axis=1, keepdims=True)
-        assert np.max(np.abs(np.exp(lp - top) - np.exp(want - top))) <= tol
-        cls = ct.decode_batch(bits)
-        srt = np.sort(want, axis=1)
-        tie = (srt[:, -1] - srt[:, -2]) <= 1e-9
-        assert not ((cls != np.argmax(want, axis=1)) & ~tie).any()
+        if precision == "f64":
+            assert_class_logprobs(lp, np.exp(want))
+        else:
+            assert_class_logprobs_within(lp, np.exp(want), 2 * info["err_bound_f32"])
+        assert_decisions(ct.decode_batch(bits), np.exp(want))
+        ct.close()
+
+
+@pytest.mark.parametrize("threads", [128, 256, 512])
+def test_shared_item_shapes_vs_plain_f64(pkg, threads):
+    """One-syndrome blocks whose lanes share the four-output items of steps
+    that would leave threads idle (each lane a run of the contracted range,
+    partial sums combined by shuffles): float64 and double-float per class
+    within 1e-10 of the plain float64 contraction, float32 within its bound,
+    the same decisions."""
+    t = pkg.tanner_graph(pkg.SurfaceCode(7, 7))
+    em = pkg.depolarizing(0.06, t.nq)
+    ep = pkg.random_error_pattern(em, np.random.default_rng(78), nsamples=300)
+    s = pkg.syndrome_extraction(ep, t)
+    bits = np.concatenate([s.sx, s.sz], axis=1)
+    ref = pkg.compile(pkg.TNMMAP(precision="f64", plain=True), t, em)
+    want = np.exp(ref.class_logprobs(bits))
+    ref.close()
+    for precision in ("f64", "f32"):
+        ct = pkg.compile(pkg.TNMMAP(precision=precision, group=1, threads=threads, shared_items=True), t, em)
+        info = ct.program.info
+        assert info[f"shared_items_{precision}"] == 1
+        lp = ct.class_logprobs(bits)
+        if precision == "f64":
+            assert_class_logprobs(lp, want)
+        else:
+            assert_class_logprobs_within(lp, want, 2 * info["err_bound_f32"])
+            assert_class_logprobs(ct.class_logprobs(bits, precision="f32x2"), want)
+        assert_decisions(ct.decode_batch(bits), want)
         ct.close()
 
 

@@ -76,9 +76,9 @@ def _run(kind, lt, lw, lg, one, bd, item_base, enter, cover, gbase):
                 cover[gbase + g, e0:e0 + (1 << lv)] += 1
 
 
-def check_program(plan, is_float):
+def check_program(plan, is_float, vsplit=False):
     bad = []
-    for G in (1, 2, 4, 8):
+    for G in ((1,) if vsplit else (1, 2, 4, 8)):
         lg = G.bit_length() - 1
         # blocks, and for one syndrome the teams of 2-16-block clusters of
         # 256 or 512 threads (the cluster kernel numbers them rank-major)
@@ -90,8 +90,8 @@ def check_program(plan, is_float):
                 lh, lfa, lfb, lk = int(d["lh"]), int(d["lfa"]), int(d["lfb"]), int(d["lk"])
                 lw = lh + lfa + lfb
                 fl = int(d["flags"])
-                kind, lt, tr = step_shape(lh, lfa, lfb, lk, lg, bd, is_float, fl)
-                k1, lt1, tr1 = step_shape(lh, lfa, lfb, lk, 0, bd, is_float, fl)
+                kind, lt, tr = step_shape(lh, lfa, lfb, lk, lg, bd, is_float, fl, vsplit)
+                k1, lt1, tr1 = step_shape(lh, lfa, lfb, lk, 0, bd, is_float, fl, vsplit)
                 per_syndrome = G > 1 and tr1 >= bd
                 enter = bd if per_syndrome else tr
                 cover = np.zeros((G, 1 << lw), dtype=np.int64)
@@ -164,6 +164,8 @@ def test_every_output_written_once(pkg, code):
     plan = native.inspect_plan(graph, steps)
     for is_float in (True, False):
         assert check_program(plan, is_float) == []
+        # one syndrome per block with lanes sharing four-output items
+        assert check_program(plan, is_float, vsplit=True) == []
 
 
 @pytest.mark.parametrize("code", ["surface7", "color488_5"])
