@@ -73,8 +73,13 @@ def parse():
     ap.add_argument("--circuit", action="store_true",
                     help="circuit-level rotated Z-memory d=5, 5 rounds, p=0.001: DEM from the generator, "
                          "--circuit-n seeded detector samples, float32 + recheck")
-    ap.add_argument("--circuit-n", type=int, default=262144,
-                    help="--circuit: detector samples (with --profile: samples in the one profiled launch)")
+    ap.add_argument("--circuit-n", type=int, default=0,
+                    help="--circuit: detector samples (0: 262,144 at 5 rounds, 512 otherwise; with --profile: "
+                         "samples in the one profiled launch)")
+    ap.add_argument("--rounds", type=int, default=5, choices=(5, 7),
+                    help="--circuit: measurement rounds (7: a width-25 tree, orders/circuit_d5_r7.tree)")
+    ap.add_argument("--slices", type=int, default=0,
+                    help="--circuit: fix this many inner labels and contract 2^slices programs (TNMMAP(slices=k))")
     ap.add_argument("--no-tensor-cores", action="store_true",
                     help="--circuit: run the GEMM-shaped steps on the SIMT path instead of tcgen05")
     ap.add_argument("--group", type=int, default=0, help="--profile: syndromes per block (0: default shape)")
@@ -99,6 +104,11 @@ def parse():
 # 49) and committed, so that every machine contracts the same tree.
 ORDER_PATH = os.path.join(ROOT, "tensorqec.jl_gb300", "orders", "surface_d7.tree")
 CIRCUIT_ORDER_PATH = os.path.join(ROOT, "tensorqec.jl_gb300", "orders", "circuit_d5_r5.tree")
+
+
+def circuit_order_path(rounds):
+    """The committed tree of the d=5 Z-memory circuit with `rounds` rounds."""
+    return os.path.join(ROOT, "tensorqec.jl_gb300", "orders", f"circuit_d5_r{rounds}.tree")
 
 
 def _circuit_search(pkg):
@@ -137,23 +147,25 @@ def write_order():
                    f"{len(info['steps'])} runtime steps.  Regenerate with: python bench.py --write-order")
     print(json.dumps({"order": os.path.relpath(ORDER_PATH, ROOT), "flops_per_syndrome": info["flops_per_syndrome"],
                       "width": info["width"], "runtime_steps": len(info["steps"])}))
-    # the circuit-level workload's tree (its order search takes about half a minute)
+    # the circuit-level workloads' trees (each search takes under a minute)
     from tensorqec_gb300 import circuit as cz
 
-    dem = cz.detector_error_model(cz.memory_z_circuit(5, 5, 0.001))
-    g = pkg.tnmmap_dem_graph(pkg.dem2tanner(dem), pkg.logical_map(dem), dem.error_rates, len(dem.logical_list), True)
-    steps = pkg.optimize_code(g, _circuit_search(pkg))
-    info = pkg.native.inspect_plan(g, steps)
-    pkg.save_order(CIRCUIT_ORDER_PATH, steps,
-                   "Contraction tree of the factorised TNMMAP factor graph of the detector error model of the\n"
-                   "rotated Z-memory circuit d=5, 5 rounds, p=0.001 (circuit.memory_z_circuit; tnmmap_dem_graph\n"
-                   "node ids).  Found by TreeSA(trials=32, sweeps=2000, target_width=20, width_penalty=2.0, seed=1,\n"
-                   "restarts=4).\n"
-                   f"Compiled program: {info['flops_per_syndrome']:.0f} flops per sample, width {info['width']}, "
-                   f"{len(info['steps'])} runtime steps.\nRegenerate with: python bench.py --write-order")
-    print(json.dumps({"order": os.path.relpath(CIRCUIT_ORDER_PATH, ROOT),
-                      "flops_per_syndrome": info["flops_per_syndrome"], "width": info["width"],
-                      "runtime_steps": len(info["steps"])}))
+    for rounds in (5, 7):
+        dem = cz.detector_error_model(cz.memory_z_circuit(5, rounds, 0.001))
+        g = pkg.tnmmap_dem_graph(pkg.dem2tanner(dem), pkg.logical_map(dem), dem.error_rates, len(dem.logical_list),
+                                 True)
+        steps = pkg.optimize_code(g, _circuit_search(pkg))
+        info = pkg.native.inspect_plan(g, steps)
+        path = circuit_order_path(rounds)
+        pkg.save_order(path, steps,
+                       "Contraction tree of the factorised TNMMAP factor graph of the detector error model of the\n"
+                       f"rotated Z-memory circuit d=5, {rounds} rounds, p=0.001 (circuit.memory_z_circuit;\n"
+                       "tnmmap_dem_graph node ids).  Found by TreeSA(trials=32, sweeps=2000, target_width=20,\n"
+                       "width_penalty=2.0, seed=1, restarts=4).\n"
+                       f"Compiled program: {info['flops_per_syndrome']:.0f} flops per sample, width {info['width']}, "
+                       f"{len(info['steps'])} runtime steps.\nRegenerate with: python bench.py --write-order")
+        print(json.dumps({"order": os.path.relpath(path, ROOT), "flops_per_syndrome": info["flops_per_syndrome"],
+                          "width": info["width"], "runtime_steps": len(info["steps"])}))
 
 
 def workload(pkg, rank, nbatches, batch):
@@ -970,11 +982,12 @@ def circuit_program(args):
     from tensorqec_gb300 import circuit as cz
     from tensorqec_gb300 import decoder as dec
 
-    d, rounds, p = 5, 5, 0.001
+    d, rounds, p = 5, getattr(args, "rounds", 5), 0.001
     circ = cz.memory_z_circuit(d, rounds, p)
     dem = cz.detector_error_model(circ)
-    opt = dec.FixedOrder(read_order(CIRCUIT_ORDER_PATH))
-    ct = pkg.compile(pkg.TNMMAP(optimizer=opt, precision="f32", tensor_cores=not args.no_tensor_cores), dem)
+    opt = dec.FixedOrder(read_order(circuit_order_path(rounds)))
+    ct = pkg.compile(pkg.TNMMAP(optimizer=opt, precision="f32", tensor_cores=not args.no_tensor_cores,
+                                slices=getattr(args, "slices", 0)), dem)
     return pkg, dem, ct
 
 
@@ -987,7 +1000,7 @@ def run_circuit_profile(args):
     pkg, dem, ct = circuit_program(args)
     from tensorqec_gb300.dem import sample_dem
 
-    n = args.circuit_n
+    n = args.circuit_n or 262144
     _, det, _ = sample_dem(dem, n, np.random.default_rng(SEED + 3))
     d_syn = torch.from_numpy(pkg.pack_syndromes(det)).cuda()
     d_lp = torch.empty((n, ct.n_classes), dtype=torch.float64, device="cuda")
@@ -1010,11 +1023,14 @@ def run_circuit(args):
     pkg, dem, ct = circuit_program(args)
     from tensorqec_gb300.dem import sample_dem
 
+    wide = args.rounds != 5 or args.slices > 0
+    if wide:
+        return run_circuit_wide(args, pkg, dem, ct, t0)
     ct.program.autotune(256)
     info = ct.program.info
     compile_s = time.time() - t0
     rng = np.random.default_rng(SEED + 3)
-    n = args.circuit_n
+    n = args.circuit_n or 262144
     _, det, lg = sample_dem(dem, n, rng)
     packed = pkg.pack_syndromes(det)
     d_syn = torch.from_numpy(packed).cuda()
@@ -1054,6 +1070,39 @@ def run_circuit(args):
             "decision_mismatch_vs_f64_on_sample": mism, "f64_sample": m,
             "compile_and_tune_seconds": compile_s,
             "tensor_steps": info["tensor_steps"], "shape_f32": {k: v for k, v in info.items() if k.endswith("_f32")},
+            "data": "synthetic: mechanisms sampled independently from the generated DEM (numpy PCG64)"}
+    print(json.dumps(line), flush=True)
+    ct.close()
+
+
+def run_circuit_wide(args, pkg, dem, ct, t0):
+    """The 7-round circuit (width-25 tree), whole or sliced: detector samples
+    decoded through the host-array API (float32 + recheck), timed on the
+    host; each sample is milliseconds of contraction, so the copies are a
+    rounding error.  With slices the 2^k slice programs run one after
+    another and their marginals are summed."""
+    from tensorqec_gb300.dem import sample_dem
+
+    info = ct.program.info
+    compile_s = time.time() - t0
+    n = args.circuit_n or 512
+    _, det, lg = sample_dem(dem, n, np.random.default_rng(SEED + 3))
+    ct.decode_batch(det[:min(n, 32)])  # warm-up (first-call allocations)
+    t1 = time.perf_counter()
+    cls = ct.decode_batch(det)
+    secs = time.perf_counter() - t1
+    k = len(dem.logical_list)
+    truth = (lg.astype(np.int64) * (1 << np.arange(k))).sum(1)
+    ler = float(np.mean(cls != truth))
+    line = {"config": "circuit", "metric": f"detector samples/s, circuit-level rotated Z-memory d=5, {args.rounds} "
+                                           "rounds, p=0.001, float32 + double-float recheck",
+            "samples": n, "seconds": secs, "samples_per_s": n / secs, "slices": info.get("slices", 1),
+            "mechanisms": len(dem.error_rates), "detectors": len(dem.detector_list), "observables": k,
+            "width": info["width"], "flops_per_sample": info["flops_per_syndrome"],
+            "achieved_tflops": info["flops_per_syndrome"] * n / secs / 1e12,
+            "arena_mb_per_sample": info["arena_elems"] * 4 / 2 ** 20, "logical_error_rate": ler,
+            "compile_seconds": compile_s,
+            "timing": "host wall clock around decode_batch (host arrays in and out)",
             "data": "synthetic: mechanisms sampled independently from the generated DEM (numpy PCG64)"}
     print(json.dumps(line), flush=True)
     ct.close()

@@ -219,6 +219,12 @@ int tqec_last_recheck_count(const tqec_program* prog, int64_t* count);
 int tqec_program_set_cluster(tqec_program* prog, int32_t precision, int32_t blocks, int32_t threads,
                              int32_t small_in_smem);
 
+/* Waits for the program's stream and frees its cached intermediate arenas
+ * (the next launch allocates them again).  A program of a wide network
+ * holds up to 16 GB of them; the 2^k programs of a sliced contraction run
+ * one after another and release theirs in turn.  No reference counterpart. */
+int tqec_program_trim(tqec_program* prog);
+
 /* Tries the launch shapes that fit and keeps the fastest for each
  * precision, timing n_probe synthetic syndromes. */
 int tqec_program_autotune(tqec_program* prog, int64_t n_probe);

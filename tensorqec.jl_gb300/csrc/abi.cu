@@ -333,10 +333,20 @@ tqec::KArgs base_args(tqec_program* p, int precision) {
 
 // Launches the batched kernel over up to n_rows_max rows with the shape
 // tuned for that many rows (`forced`: that shape instead).
+// Global-memory arenas of one launch stay within this many bytes: a wide
+// program (a circuit-level tree of width 25 holds 62 million elements per
+// syndrome) gets fewer blocks, which stride over the rows.
+constexpr size_t kArenaBudget = size_t(16) << 30;
+
 int launch_rows(tqec_program* p, int precision, tqec::KArgs a, int64_t n_rows_max, cudaStream_t st,
                 const Shape* forced = nullptr) {
   const Shape& s = forced ? *forced : pick_shape(p, precision, n_rows_max);
   int64_t want = (n_rows_max + s.G - 1) / s.G;
+  if (!s.smem_arena) {
+    const int64_t per = s.split ? p->plan.arena_elems - p->plan.arena_small : p->plan.arena_elems;
+    const size_t block_bytes = size_t(s.G) * size_t(std::max<int64_t>(per, 1)) * (precision == TQEC_F32 ? 4 : 8);
+    want = std::min<int64_t>(want, std::max<int64_t>(1, int64_t(kArenaBudget / block_bytes)));
+  }
   int grid = (int)std::max<int64_t>(1, std::min<int64_t>(want, s.grid_cap));
   int rc = ensure_arena(p, precision, s, grid);
   if (rc) return rc;
@@ -1140,6 +1150,18 @@ bool tune_cluster(tqec_program* p, int prec, bool plain, cudaEvent_t e0, cudaEve
 }
 
 }  // namespace
+
+int tqec_program_trim(tqec_program* p) {
+  if (!p) return fail(TQEC_ERR_INVALID, "NULL program");
+  std::lock_guard<std::mutex> lk(p->mu);
+  TQ_CUDA(cudaSetDevice(p->device));
+  TQ_CUDA(cudaStreamSynchronize(p->stream));
+  for (int i = 0; i < 3; ++i) {
+    p->arena[i].release();
+    p->carena[i].release();
+  }
+  return TQEC_OK;
+}
 
 int tqec_program_set_cluster(tqec_program* p, int32_t precision, int32_t blocks, int32_t threads,
                              int32_t small_in_smem) {

@@ -257,7 +257,14 @@ class SlicedProgram:
         return self.parts[0].syndrome_bytes
 
     def contract_packed(self, packed, precision, logp=None):
-        lps = np.stack([p.contract_packed(packed, precision) for p in self.parts])
+        lps = []
+        for p in self.parts:
+            lps.append(p.contract_packed(packed, precision))
+            # wide slices (more than 2^22 intermediate elements a syndrome)
+            # free their arenas before the next slice allocates its own
+            if p.info["arena_elems"] > (1 << 22):
+                p.trim()
+        lps = np.stack(lps)
         top = lps.max(axis=0)
         safe = np.where(np.isfinite(top), top, 0.0)
         with np.errstate(divide="ignore"):

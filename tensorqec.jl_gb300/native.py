@@ -108,6 +108,7 @@ def lib():
         "tqec_last_recheck_count": [vp, vp],
         "tqec_program_autotune": [vp, i64],
         "tqec_program_set_cluster": [vp, i32, i32, i32, i32],
+        "tqec_program_trim": [vp],
         "tqec_program_save": [vp, C.c_char_p],
         "tqec_program_load": [C.c_char_p, i32, vp],
         "tqec_plan_inspect": [vp, vp, vp, vp],
@@ -296,6 +297,10 @@ class Program:
         global memory / the first where it fits."""
         check(lib().tqec_program_set_cluster(self._h, precision, blocks, threads, small_in_smem))
         self._refresh_info()
+
+    def trim(self):
+        """Frees the cached intermediate arenas (allocated again on use)."""
+        check(lib().tqec_program_trim(self._h))
 
     def autotune(self, n_probe=4096):
         check(lib().tqec_program_autotune(self._h, n_probe))

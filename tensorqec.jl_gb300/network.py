@@ -239,22 +239,28 @@ def step_label_sets(graph: FactorGraph, steps):
 
 
 def choose_slice_labels(graph: FactorGraph, steps, k: int):
-    """k labels to fix, chosen greedily: each time the label that occurs in
-    the most of the widest step products (outputs and syndrome labels
-    excluded), which narrows the widest steps first."""
+    """k labels to fix, chosen greedily: each time the label carried by the
+    most of the widest intermediate results (the working set of a syndrome),
+    ties broken by the widest step products it occurs in (the multiply-adds);
+    output and syndrome labels are never fixed."""
     synd_labels = {v for p in graph.syndrome_positions for v in graph.ixs[p]}
     banned = set(graph.iy) | synd_labels
     chosen = []
     for _ in range(k):
         g = slice_graph(graph, chosen, 0) if chosen else graph
         sets = step_label_sets(g, steps)
-        widest = max(len(u) for u, _ in sets)
+        widest_res = max(len(r) for _, r in sets)
+        widest_u = max(len(u) for u, _ in sets)
         score = {}
-        for u, _ in sets:
-            if len(u) >= widest - 1:
-                for v in u:
-                    if v not in banned and v not in chosen:
-                        score[v] = score.get(v, 0) + (2 if len(u) == widest else 1)
+        for u, r in sets:
+            for v in (r if len(r) >= widest_res - 1 else ()):
+                if v not in banned and v not in chosen:
+                    s = score.get(v, (0, 0))
+                    score[v] = (s[0] + (2 if len(r) == widest_res else 1), s[1])
+            for v in (u if len(u) >= widest_u - 1 else ()):
+                if v not in banned and v not in chosen:
+                    s = score.get(v, (0, 0))
+                    score[v] = (s[0], s[1] + (2 if len(u) == widest_u else 1))
         if not score:
             break
         chosen.append(max(sorted(score), key=lambda v: score[v]))

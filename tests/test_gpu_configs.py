@@ -171,6 +171,39 @@ def test_sliced_program_on_gpu_vs_oracle(pkg, oracle, precision):
     ct.close()
 
 
+@pytest.mark.parametrize("slices", [0, 2])
+def test_circuit_d5_r7_width25_vs_oracle_fixture(pkg, slices):
+    """Rotated Z-memory d=5, 7 rounds, p=0.001: a width-25 contraction tree
+    (a 62-million-element arena per sample), whole and in 2^2 slices (each
+    slice a program of its own, marginals summed), on the seeded samples whose
+    oracle marginals tests/golden/circuit_d5_r7.json holds
+    (tests/golden/make_circuit_d5_r7.py)."""
+    import json
+
+    from tensorqec_gb300 import circuit as cz
+    from tensorqec_gb300.dem import sample_dem
+
+    fx = json.load(open(os.path.join(ROOT, "tests", "golden", "circuit_d5_r7.json")))
+    dm = cz.detector_error_model(cz.memory_z_circuit(5, 7, 0.001))
+    _, det, _ = sample_dem(dm, fx["samples"], np.random.default_rng(fx["seed"]))
+    assert np.array_equal(det.astype(int), np.array(fx["detectors"]))
+    want = np.array(fx["marginals"])
+    steps = pkg.load_order(os.path.join(ROOT, "tensorqec.jl_gb300", "orders", "circuit_d5_r7.tree"))
+    for precision in ("f32", "f64"):
+        ct = pkg.compile(pkg.TNMMAP(precision=precision, optimizer=pkg.FixedOrder(steps), slices=slices), dm)
+        assert ct.program.info["width"] >= 24
+        if slices:
+            assert ct.program.info["slices"] == 1 << slices
+        cls, logp = ct.decode_batch(det, return_logp=True)
+        assert_decisions(cls, want)
+        assert np.array_equal(cls, np.array(fx["classes"]))
+        if precision == "f64":
+            assert_class_logprobs(logp, want, 1e-10)
+        else:
+            assert_class_logprobs_within(logp, want, 2 * ct.program.info["err_bound_f32"])
+        ct.close()
+
+
 def test_config5_gated_d7_mismatch_and_ler(pkg):
     """Surrogate trained on 2^22 syndromes labelled by float64 contraction,
     calibrated at half the 1e-4 budget; on 2^18 fresh syndromes the gated
