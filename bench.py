@@ -634,6 +634,8 @@ def run_ours(args):
         line = {
             "metric": METRIC, "value": value, "unit": "syndromes/s", "n_gpus": world, "steps": K, "warmup": W,
             "ms_per_step": step_ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "batch_latency_ms": {"p50": float(np.percentile(ms, 50)), "p99": float(np.percentile(ms, 99)),
+                                 "max": float(max(ms)), "batches": K},
             "dtype": "f32", "data": "synthetic (seeded depolarizing errors, numpy PCG64)",
             "config": dict(config(B), decoder="gated surrogate (4x512 MLP, bf16/f32) + batched TN f32 with "
                                               "double-float recheck" if gd is not None

@@ -140,6 +140,9 @@ typedef struct {
   double err_bound_f32x2;    /* relative error bound of a TQEC_F32X2 marginal */
   int32_t shared_items_f32, shared_items_f64; /* 1: lanes share the work items of steps
                                                  that leave threads idle (TQEC_FLAG_SHARED_ITEMS) */
+  int32_t cluster_tuned_steps; /* steps whose cluster-form plan tqec_program_autotune changed
+                                  (barrier group on the first block or not, shared items) */
+  int32_t info_pad;
 } tqec_program_info_t;
 
 typedef struct tqec_program tqec_program;

@@ -131,6 +131,10 @@ struct tqec_program {
   // single-syndrome launches (the plain form, the recheck) as one syndrome
   // per thread-block cluster, per precision (size 0: one block per syndrome)
   ClusterShape cluster[3];
+  // per-step options of the cluster form found by tqec_program_autotune
+  // (kOpt*, per precision; empty: none) and their device copies
+  std::vector<int8_t> copts[3];
+  DevBuf d_copts[3];
   DevBuf arena[3], carena[3];
   DevBuf syn, cls, logp, err, list, count;
   int32_t* h_count = nullptr;  // pinned
@@ -417,6 +421,7 @@ int launch_cluster_rows(tqec_program* p, int precision, tqec::KArgs a, int64_t n
   a.arena_global = p->carena[precision].p;
   a.arena_small = c.split ? p->plan.arena_small : 0;
   a.tc = 0;
+  a.step_opts = p->copts[precision].empty() ? nullptr : static_cast<const int8_t*>(p->d_copts[precision].p);
   TQ_CUDA(tqec::contract_cluster_launch(precision, a, clusters, c.size, c.threads, c.smem, st));
   return TQEC_OK;
 }
@@ -656,6 +661,8 @@ int program_multi_view(tqec_program* p, ProgramMultiView* v) {
     a.arena_global = nullptr;
     a.arena_small = c.split ? p->plan.arena_small : 0;
     a.tc = 0;
+    const auto& o = p->copts[v->recheck_precision];
+    a.step_opts = o.empty() ? nullptr : static_cast<const int8_t*>(p->d_copts[v->recheck_precision].p);
     v->args_cluster = a;
   }
   return TQEC_OK;
@@ -890,6 +897,10 @@ int tqec_program_info(const tqec_program* p, tqec_program_info_t* info) {
   info->cluster_blocks = p->cluster[(p->flags & TQEC_FLAG_PLAIN) ? p->precision : info->recheck_precision].size;
   info->shared_items_f32 = p->shape[TQEC_F32].vsplit ? 1 : 0;
   info->shared_items_f64 = p->shape[TQEC_F64].vsplit ? 1 : 0;
+  {
+    const auto& o = p->copts[(p->flags & TQEC_FLAG_PLAIN) ? p->precision : info->recheck_precision];
+    info->cluster_tuned_steps = int32_t(std::count_if(o.begin(), o.end(), [](int8_t v) { return v != 0; }));
+  }
   info->err_bound_f32x2 = err_bound(p, TQEC_F32X2);
   return TQEC_OK;
 }
@@ -1096,6 +1107,59 @@ bool tune_shape(tqec_program* p, int prec, int64_t n, cudaEvent_t e0, cudaEvent_
 
 namespace {
 
+// The cluster form's plan, barrier group by barrier group: whether the group
+// runs on the first block alone (never; whenever its items fit) and whether
+// its steps share work items, each kept when it shortens the single-row
+// latency by more than 1 % (the fastest of five calls per setting).
+bool tune_cluster_steps(tqec_program* p, int prec, bool plain, cudaEvent_t e0, cudaEvent_t e1) {
+  const int n = (int)p->plan.steps.size();
+  std::vector<int8_t>& o = p->copts[prec];
+  o.assign(n, 0);
+  auto time_row = [&](float* ms_out) {
+    if (p->d_copts[prec].ensure(size_t(n)) != cudaSuccess) return false;
+    if (cudaMemcpy(p->d_copts[prec].p, o.data(), size_t(n), cudaMemcpyHostToDevice) != cudaSuccess) return false;
+    tqec::KArgs a = base_args(p, prec);
+    a.syn = (const uint8_t*)p->syn.p;
+    a.n = 1;
+    a.logp_out = (double*)p->logp.p;
+    auto run = [&]() { return plain ? launch_plain(p, prec, a, 1, p->stream) : launch_cluster_rows(p, prec, a, 1, p->stream); };
+    if (run() != TQEC_OK) return false;
+    float best = 1e30f;
+    for (int r = 0; r < 5; ++r) {
+      cudaEventRecord(e0, p->stream);
+      if (run() != TQEC_OK) return false;
+      cudaEventRecord(e1, p->stream);
+      if (cudaEventSynchronize(e1) != cudaSuccess) return false;
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, e0, e1);
+      best = std::min(best, ms);
+    }
+    *ms_out = best;
+    return true;
+  };
+  float cur = 0.f;
+  if (!time_row(&cur)) return false;
+  for (int s0 = 0; s0 < n;) {
+    int s1 = s0;
+    while (s1 + 1 < n && !(p->plan.steps[s1].flags & tqec::kStepSync)) ++s1;
+    for (int8_t bit : {tqec::kOptNoSolo, tqec::kOptSoloAlways, tqec::kOptNoShare}) {
+      for (int s = s0; s <= s1; ++s) o[s] ^= bit;
+      float t = 0.f;
+      if (!time_row(&t)) return false;
+      if (t < 0.99f * cur) {
+        cur = t;
+      } else {
+        for (int s = s0; s <= s1; ++s) o[s] ^= bit;
+      }
+    }
+    s0 = s1 + 1;
+  }
+  // keep the device copy in step with the options kept
+  if (cudaMemcpy(p->d_copts[prec].p, o.data(), size_t(n), cudaMemcpyHostToDevice) != cudaSuccess) return false;
+  if (std::all_of(o.begin(), o.end(), [](int8_t v) { return v == 0; })) o.clear();
+  return true;
+}
+
 // Single-syndrome launches of one precision: the block form (the recheck
 // shape, or one launch per row in the plain form) against clusters of 2-16
 // blocks of 128, 256 or 512 threads, timed on one row (the plain form: the
@@ -1146,6 +1210,8 @@ bool tune_cluster(tqec_program* p, int prec, bool plain, cudaEvent_t e0, cudaEve
     cudaGetLastError();
   }
   p->cluster[prec] = best;
+  p->copts[prec].clear();
+  if (best.size > 0) return tune_cluster_steps(p, prec, plain, e0, e1);
   return true;
 }
 
@@ -1170,6 +1236,7 @@ int tqec_program_set_cluster(tqec_program* p, int32_t precision, int32_t blocks,
     return fail(TQEC_ERR_INVALID, "clusters serve TQEC_F64 and TQEC_F32X2 launches");
   std::lock_guard<std::mutex> lk(p->mu);
   TQ_CUDA(cudaSetDevice(p->device));
+  p->copts[precision].clear();  // tuned for the previous form
   if (blocks == 0) {
     p->cluster[precision] = ClusterShape{};
     return TQEC_OK;

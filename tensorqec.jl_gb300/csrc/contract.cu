@@ -1077,16 +1077,18 @@ __device__ __forceinline__ void fill_step_plan(const KArgs& a, const StepDesc* s
     return make_int2(use.kind | (use.lt << 8) | (int(per_syndrome) << 16) | (contiguous << 17),
                      per_syndrome ? bd : sh.total_r);
   };
+  auto opt = [&](int st) { return a.step_opts ? int(a.step_opts[st]) : 0; };
   if (!CL) {
-    for (int st = threadIdx.x; st < a.n_steps; st += blockDim.x)
-      plan[st] = plan_of(steps[st], blockDim.x, VS && a.vsplit != 0);  // only kernels with the body
+    for (int st = threadIdx.x; st < a.n_steps; st += blockDim.x)  // only kernels with the body share items
+      plan[st] = plan_of(steps[st], blockDim.x, VS && a.vsplit != 0 && !(opt(st) & kOptNoShare));
     return;
   }
   int2* team_plan = scratch;
   int2* block_plan = scratch + a.n_steps;
   for (int st = threadIdx.x; st < a.n_steps; st += blockDim.x) {
-    team_plan[st] = plan_of(steps[st], team_size<CL>(), true);
-    block_plan[st] = plan_of(steps[st], blockDim.x, true);
+    const bool share = !(opt(st) & kOptNoShare);
+    team_plan[st] = plan_of(steps[st], team_size<CL>(), share);
+    block_plan[st] = plan_of(steps[st], blockDim.x, share);
   }
   __syncthreads();
   // k summed by one lane of a step planned as pl
@@ -1100,11 +1102,12 @@ __device__ __forceinline__ void fill_step_plan(const KArgs& a, const StepDesc* s
   auto solo_group = [&](int s0, int s1) {
     int items = 0;
     for (int s = s0; s <= s1; ++s) {
+      if (opt(s) & kOptNoSolo) return false;
       const int kb = k_per_lane(steps[s], block_plan[s]), kt = k_per_lane(steps[s], team_plan[s]);
-      if (kb > (kt > 8 ? kt : 8)) return false;
+      if (!(opt(s) & kOptSoloAlways) && kb > (kt > 8 ? kt : 8)) return false;
       items += block_plan[s].y;
     }
-    return items <= int(blockDim.x);
+    return items <= int(blockDim.x);  // always required: the items live on the first block
   };
   auto group_end = [&](int s) {
     while (s + 1 < a.n_steps && !(steps[s].flags & kStepSync)) ++s;

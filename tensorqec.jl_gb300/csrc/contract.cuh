@@ -60,7 +60,17 @@ struct KArgs {
   int32_t tc;
   int32_t vsplit;  // block launches: lanes may share four-output items (SK_VSPLIT)
   int32_t* tc_err;
+  // per step, options the autotuner chose (kOpt*; nullptr: all 0), read
+  // while the kernel plans its steps
+  const int8_t* step_opts;
+  int64_t opts_pad;
 };
+// step options: no shared work items; (cluster form) the step's barrier
+// group never runs on the first block alone; runs there whenever its items
+// fit, whatever the lanes' runs of k
+constexpr int8_t kOptNoShare = 1;
+constexpr int8_t kOptNoSolo = 2;
+constexpr int8_t kOptSoloAlways = 4;
 static_assert(sizeof(KArgs) % 16 == 0, "KArgs is copied in 16-byte units");
 
 // Threads per block of the multi-program kernel (128 registers each).

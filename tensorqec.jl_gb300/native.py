@@ -62,7 +62,8 @@ class ProgramInfo(C.Structure):
                 ("tables_smem_f64", C.c_int32), ("arena_small", C.c_int64), ("split_f32", C.c_int32),
                 ("split_f64", C.c_int32), ("tensor_steps", C.c_int32), ("tensor_f32", C.c_int32),
                 ("recheck_precision", C.c_int32), ("cluster_blocks", C.c_int32), ("err_bound_f32x2", C.c_double),
-                ("shared_items_f32", C.c_int32), ("shared_items_f64", C.c_int32)]
+                ("shared_items_f32", C.c_int32), ("shared_items_f64", C.c_int32),
+                ("cluster_tuned_steps", C.c_int32), ("info_pad", C.c_int32)]
 
 
 class PlanView(C.Structure):
