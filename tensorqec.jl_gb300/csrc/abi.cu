@@ -672,6 +672,22 @@ int program_multi_view(tqec_program* p, ProgramMultiView* v) {
 
 namespace {
 
+// The plan of a program.  A TQEC_FLAG_PLAIN program at least
+// kClusterMinWidth wide decodes each syndrome on a thread-block cluster,
+// whose time is one syndrome's latency: its steps run level by level
+// (PlanLimits::level_order), so independent chains of the tree share barrier
+// groups.
+std::string plan_program(const tqec::NetworkView& v, const tqec_tree& tree, uint32_t flags, tqec::PlanLimits lim,
+                         tqec::Plan* out, bool* unsupported) {
+  std::string err = tqec::build_plan(v, tree.n_steps, tree.steps, lim, out, unsupported);
+  if (!err.empty() || !(flags & TQEC_FLAG_PLAIN) || lim.map_mode || out->width < kClusterMinWidth) return err;
+  lim.level_order = true;
+  tqec::Plan lp;
+  bool u2 = false;
+  if (tqec::build_plan(v, tree.n_steps, tree.steps, lim, &lp, &u2).empty()) *out = std::move(lp);
+  return err;
+}
+
 // Copies a network and tree that build_plan accepted (so every offset, size
 // and position in them has been checked) into `in`.
 void keep_inputs(const tqec_network& net, const tqec_tree& tree, const tqec_options& o, ProgramInputs* in) {
@@ -735,7 +751,7 @@ int tqec_program_create(const tqec_network* net, const tqec_tree* tree, const tq
   if (o.big_elems > 0) lim.big_elems = o.big_elems;
   auto* p = new tqec_program();
   bool unsupported = false;
-  std::string err = tqec::build_plan(v, tree->n_steps, tree->steps, lim, &p->plan, &unsupported);
+  std::string err = plan_program(v, *tree, o.flags, lim, &p->plan, &unsupported);
   if (!err.empty()) {
     delete p;
     return fail(unsupported ? TQEC_ERR_UNSUPPORTED : TQEC_ERR_INVALID, err);
@@ -1317,7 +1333,7 @@ int tqec_plan_inspect_flags(const tqec_network* net, const tqec_tree* tree, uint
   tqec::PlanLimits lim;
   lim.map_mode = (flags & TQEC_FLAG_MAP) != 0;
   lim.tensor_steps = (flags & TQEC_FLAG_NO_TENSOR_CORES) == 0;
-  std::string err = tqec::build_plan(v, tree->n_steps, tree->steps, lim, P, &unsupported);
+  std::string err = plan_program(v, *tree, flags, lim, P, &unsupported);
   if (!err.empty()) {
     delete P;
     return fail(unsupported ? TQEC_ERR_UNSUPPORTED : TQEC_ERR_INVALID, err);

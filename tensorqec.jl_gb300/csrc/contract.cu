@@ -1323,9 +1323,22 @@ __device__ void contract_group(const KArgs& a, int64_t base, int64_t nrows, cons
 
 // Stages the program's tables (if requested) after the fixed layout; returns
 // the constants, the permutation tables and the shared arena pointer.
+// The mbarrier the table copies of stage_tables complete on (one per block).
+__shared__ uint64_t s_stage_bar;
+
+// Waits (bounded) for the bulk copies stage_tables issued with wait = false.
+__device__ __forceinline__ void stage_tables_wait(const KArgs& a) {
+  if (!a.tables_smem) return;
+  if (!tc::mbar_wait(&s_stage_bar, 0)) {
+    // the copies never completed (not expected): the results are flagged as
+    // invalid; the block still runs to its end, so no barrier waits for it
+    if (a.tc_err) *static_cast<volatile int32_t*>(a.tc_err) = 2;
+  }
+}
+
 template <typename T>
 __device__ __forceinline__ void stage_tables(const KArgs& a, unsigned char* smem, size_t* off, const T** consts,
-                                             PermTab* ptab) {
+                                             PermTab* ptab, bool wait = true) {
   *consts = reinterpret_cast<const T*>(a.consts);
   *ptab = PermTab{a.perm, false};
   if (!a.tables_smem) return;
@@ -1339,37 +1352,33 @@ __device__ __forceinline__ void stage_tables(const KArgs& a, unsigned char* smem
   // the 16-byte multiples by bulk asynchronous copies (one instruction each,
   // issued by thread 0, completing on one mbarrier) instead of a load and a
   // store per thread and 16 bytes; the few bytes past them by plain loads
-  __shared__ uint64_t s_bar;
+  uint64_t* const s_bar = &s_stage_bar;
   const uint32_t m0 = uint32_t(const_bytes & ~size_t(15)), m1 = uint32_t(perm_bytes & ~size_t(15));
   if (threadIdx.x == 0) {
-    tc::mbar_init(&s_bar, 1);
+    tc::mbar_init(s_bar, 1);
     asm volatile("fence.mbarrier_init.release.cluster;\n\tfence.proxy.async.shared::cta;" ::: "memory");
   }
   __syncthreads();
   if (threadIdx.x == 0) {
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(tc::smem_u32(&s_bar)),
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(tc::smem_u32(s_bar)),
                  "r"(m0 + m1)
                  : "memory");
     if (m0)
       asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
                        tc::smem_u32(s_consts)),
-                   "l"(a.consts), "r"(m0), "r"(tc::smem_u32(&s_bar))
+                   "l"(a.consts), "r"(m0), "r"(tc::smem_u32(s_bar))
                    : "memory");
     if (m1)
       asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
                        tc::smem_u32(s_perm)),
-                   "l"(perm_src), "r"(m1), "r"(tc::smem_u32(&s_bar))
+                   "l"(perm_src), "r"(m1), "r"(tc::smem_u32(s_bar))
                    : "memory");
   }
   for (int i = threadIdx.x; i < int(const_bytes - m0); i += blockDim.x)
     reinterpret_cast<unsigned char*>(s_consts)[m0 + i] = static_cast<const unsigned char*>(a.consts)[m0 + i];
   for (int i = threadIdx.x; i < int(perm_bytes - m1); i += blockDim.x)
     static_cast<unsigned char*>(s_perm)[m1 + i] = static_cast<const unsigned char*>(perm_src)[m1 + i];
-  if (!tc::mbar_wait(&s_bar, 0)) {
-    // the copies never completed (not expected): the results are flagged as
-    // invalid; the block still runs to its end, so no barrier waits for it
-    if (a.tc_err) *static_cast<volatile int32_t*>(a.tc_err) = 2;
-  }
+  if (wait) stage_tables_wait(a);
   *consts = s_consts;
   *ptab = PermTab{s_perm, a.perm16 != nullptr};
 }
@@ -1456,8 +1465,10 @@ __global__ void __launch_bounds__(512) tn_contract_cluster_kernel(KArgs a) {
   size_t off = sm.tail;
   const T* consts;
   PermTab ptab;
-  stage_tables<T>(a, smem, &off, &consts, &ptab);
+  // the table copies run while the step records are copied
+  stage_tables<T>(a, smem, &off, &consts, &ptab, false);
   copy16(sm.steps, a.steps, size_t(a.n_steps) * sizeof(StepDesc));
+  stage_tables_wait(a);
   __syncthreads();
   fill_step_plan<T, false, true>(a, sm.steps, sm.plan, ptab, static_cast<int2*>(sm.ptrs));
   if (NORM) sm.max = cluster_map(sm.max, 0);

@@ -464,6 +464,19 @@ static std::string build_plan_once(const NetworkView& net, int32_t n_steps, cons
     order.push_back(id);
   };
   post(root);
+  if (lim.level_order) {
+    // level of a runtime step: one more than the deepest runtime step it reads
+    std::vector<int> level(nodes.size(), 0);
+    for (int id : order) {  // children come first in the post-order
+      const PNode& n = nodes[id];
+      int l = 0;
+      for (int c : {n.left, n.right})
+        if (nodes[c].kind == NK_RUNTIME) l = std::max(l, level[c]);
+      level[id] = l + 1;
+    }
+    std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return level[x] < level[y]; });
+    for (int r = 0; r < (int)order.size(); ++r) nodes[order[r]].rstep = r;
+  }
   const int R = (int)order.size();
   // A parity operand of a runtime step becomes a two-variant table selected
   // by its syndrome bit: the kernel then reads only arena and constant
@@ -658,8 +671,8 @@ static std::string build_plan_once(const NetworkView& net, int32_t n_steps, cons
   // alone (they fill the block by themselves and dominate the arena).
   std::vector<char> group_end(R, 0);
   {
-    constexpr int kMaxGroup = 8;
-    constexpr int kMaxGroupedWidth = 12;
+    const int kMaxGroup = lim.level_order ? 16 : 8;
+    const int kMaxGroupedWidth = lim.level_order ? 64 : 12;
     std::vector<char> in_group(nodes.size(), 0);
     std::vector<int> members;
     for (int r = 0; r < R; ++r) {

@@ -99,6 +99,11 @@ struct PlanLimits {
   bool tensor_steps = true;   // mark GEMM-shaped steps (kStepTensor)
   // ... when they hold at least this share of the program's multiply-adds
   double tensor_min_share = 0.25;
+  // run the runtime steps level by level (each after everything it reads,
+  // the shallowest first), so independent chains of the tree share barrier
+  // groups, and group wide steps too: fewer barriers for the single-syndrome
+  // launches whose time is one syndrome's latency, more live intermediates
+  bool level_order = false;
 };
 
 // A step is GEMM-shaped when, per h, it multiplies a 2^lfa x 2^lk block by a

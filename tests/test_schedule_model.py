@@ -177,11 +177,39 @@ def test_cluster_plans_write_every_output_once(pkg, code):
     lx, lz = gf2.logical_operator(t)
     graph = network.tnmmap_css_graph(t, em, lx, lz)
     steps = decoder.optimize_code(graph, decoder.TreeSA(restarts=1))
-    plan = native.inspect_plan(graph, steps)
     kinds = set()
-    for blocks, threads in ((2, 128), (4, 256), (8, 256), (16, 128), (16, 256), (8, 512)):
-        assert check_cluster_program(plan, False, blocks, threads) == []
-        for d in plan["steps"]:
-            kinds.add(step_shape(int(d["lh"]), int(d["lfa"]), int(d["lfb"]), int(d["lk"]), 0, blocks * threads,
-                                 False, int(d["flags"]), vsplit=True)[0])
+    # the batch plan (the recheck's) and the plain form's level-by-level plan
+    for flags in (0, native.TQEC_FLAG_PLAIN):
+        plan = native.inspect_plan(graph, steps, flags)
+        for blocks, threads in ((2, 128), (4, 256), (8, 256), (16, 128), (16, 256), (8, 512)):
+            assert check_cluster_program(plan, False, blocks, threads) == []
+            for d in plan["steps"]:
+                kinds.add(step_shape(int(d["lh"]), int(d["lfa"]), int(d["lfb"]), int(d["lk"]), 0, blocks * threads,
+                                     False, int(d["flags"]), vsplit=True)[0])
     assert "vsplit" in kinds
+
+
+def test_plain_wide_plans_run_level_by_level(pkg):
+    """A wide TQEC_FLAG_PLAIN program orders its steps by level: no step
+    shares a barrier group with a step whose output it reads, and the
+    groups are fewer than the batch plan's."""
+    from tensorqec_gb300 import decoder, gf2, network, native
+    t = pkg.tanner_graph(pkg.SurfaceCode(7, 7))
+    em = pkg.depolarizing(0.05, t.nq)
+    lx, lz = gf2.logical_operator(t)
+    graph = network.tnmmap_css_graph(t, em, lx, lz)
+    steps = decoder.optimize_code(graph, decoder.TreeSA(restarts=1))
+    batch = native.inspect_plan(graph, steps)
+    plain = native.inspect_plan(graph, steps, native.TQEC_FLAG_PLAIN)
+    assert plain["width"] >= 12 and len(plain["steps"]) == len(batch["steps"])
+    groups = lambda pl: int(sum(int(d["flags"]) & 1 for d in pl["steps"]))
+    assert groups(plain) < groups(batch)
+    # every arena operand comes from an earlier barrier group
+    gid, g = [], 0
+    for d in plain["steps"]:
+        gid.append(g)
+        g += int(d["flags"]) & 1
+    for i, d in enumerate(plain["steps"]):
+        for kind, prod in ((int(d["a_kind"]), int(d["a_prod"])), (int(d["b_kind"]), int(d["b_prod"]))):
+            if kind == 0:
+                assert 0 <= prod < i and gid[prod] < gid[i]
