@@ -54,6 +54,11 @@ extern "C" {
  * at 1/64 of the float32 rate).  The default arithmetic of the recheck;
  * accepted by tqec_contract_batch. */
 #define TQEC_F32X2 2
+/* A numerical study of bfloat16 intermediates, for tqec_contract_batch only:
+ * the TQEC_F32 program with every stored intermediate rounded to bfloat16's
+ * 8 significant bits (kept in float32 words, so no speed is gained).  Its
+ * relative error bound is the float32 one plus 2^-9 per runtime step. */
+#define TQEC_F32_BF16 3
 
 /* Option flags. */
 #define TQEC_FLAG_PLAIN 1u   /* decode one syndrome per kernel launch (drop-in form) */

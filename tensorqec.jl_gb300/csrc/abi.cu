@@ -557,7 +557,7 @@ int unstage_outputs(tqec_program* p, int64_t n, int32_t* cls, double* logp, floa
 }
 
 int decode_locked(tqec_program* p, const uint8_t* syn, int64_t n, int32_t* cls, double* logp, float* err,
-                  int precision, bool recheck, bool plain, cudaStream_t st) {
+                  int precision, bool recheck, bool plain, cudaStream_t st, bool round_bf16 = false) {
   Staged s;
   int rc = stage_inputs(p, syn, n, cls, logp, err, st, &s);
   if (rc) return rc;
@@ -568,6 +568,7 @@ int decode_locked(tqec_program* p, const uint8_t* syn, int64_t n, int32_t* cls, 
     a.class_out = s.d_cls;
     a.logp_out = s.d_logp;
     a.err_out = s.d_err;
+    a.round_bf16 = round_bf16 ? 1 : 0;
     if (recheck && precision == TQEC_F32) {
       if (n > INT32_MAX) return fail(TQEC_ERR_INVALID, "batch above 2^31 rows");
       TQ_CUDA(p->list.ensure(sizeof(int32_t) * n));
@@ -995,15 +996,20 @@ int tqec_decode_rows(tqec_program* p, const uint8_t* syndromes, const int32_t* r
 int tqec_contract_batch(tqec_program* p, const uint8_t* syndromes, int64_t n, int32_t precision, double* logp_out,
                         void* stream) {
   if (!p || n < 0 || (n > 0 && (!syndromes || !logp_out))) return fail(TQEC_ERR_INVALID, "bad argument");
-  if (precision != TQEC_F32 && precision != TQEC_F64 && precision != TQEC_F32X2)
+  if (precision != TQEC_F32 && precision != TQEC_F64 && precision != TQEC_F32X2 && precision != TQEC_F32_BF16)
     return fail(TQEC_ERR_INVALID, "unknown precision");
+  if (precision == TQEC_F32_BF16 && p->plan.map_mode)
+    return fail(TQEC_ERR_INVALID, "a TQEC_FLAG_MAP program contracts in TQEC_F32 or TQEC_F64");
+  // the bf16 study runs the float32 program with its stored intermediates rounded
+  const bool bf16 = precision == TQEC_F32_BF16;
+  if (bf16) precision = TQEC_F32;
   if (precision == TQEC_F32X2 && p->plan.map_mode)
     return fail(TQEC_ERR_INVALID, "a TQEC_FLAG_MAP program contracts in TQEC_F32 or TQEC_F64");
   std::lock_guard<std::mutex> lk(p->mu);
   TQ_CUDA(cudaSetDevice(p->device));
   cudaStream_t st = stream ? (cudaStream_t)stream : p->stream;
   const bool plain = (p->flags & TQEC_FLAG_PLAIN) != 0;
-  int rc = decode_locked(p, syndromes, n, nullptr, logp_out, nullptr, precision, false, plain, st);
+  int rc = decode_locked(p, syndromes, n, nullptr, logp_out, nullptr, precision, false, plain, st, bf16);
   if (rc) return rc;
   if (!stream || !is_device_ptr(logp_out)) {
     TQ_CUDA(cudaStreamSynchronize(st));

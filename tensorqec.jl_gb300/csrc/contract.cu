@@ -15,6 +15,8 @@
 // the power of two that brings that maximum to [1, 2).  Scaling by powers of
 // two is exact, so the only rounding is that of the products and sums.  The
 // exponents are summed into the final log-probability.
+#include <cuda_bf16.h>
+
 #include <cstdio>
 #include <map>
 #include <mutex>
@@ -166,6 +168,14 @@ __device__ __forceinline__ void flush_max(bool had_items, uint32_t bits, uint32_
   if ((threadIdx.x & 31) == 0) atomicMax(slot, bits);
 }
 
+// RB (the bf16 study launches): a stored intermediate is rounded to
+// bfloat16's 8 significant bits (it stays in a float word); otherwise as is.
+template <bool RB, typename T>
+__device__ __forceinline__ T out_round(T v) {
+  if constexpr (RB && std::is_same<T, float>::value) return __bfloat162float(__float2bfloat16_rn(v));
+  return v;
+}
+
 // A team is the threads that contract one syndrome group together: the
 // block, or in the cluster kernel every block of a thread-block cluster
 // (threads numbered rank by rank).  Team sizes are powers of two.
@@ -247,7 +257,7 @@ __device__ __forceinline__ void segment_max(bool valid, uint32_t bits, int lw_it
 // One output per work item.  G1: the step runs for one syndrome (the
 // block's only one, or one of its G in turn), so its bases and normalisers
 // are step invariants.
-template <typename T, bool NORM, bool MAXP, bool G1, bool CL>
+template <typename T, bool NORM, bool MAXP, bool G1, bool CL, bool RB = false>
 __device__ void run_step(const KArgs& a, const StepDesc& dref, int st, int item_base, uint32_t* s_max,
                          const StepPtrs<T>* ptrs, const PermTab& ptab) {
   // a register copy: arena stores (same shared array) cannot alias it
@@ -301,6 +311,7 @@ __device__ void run_step(const KArgs& a, const StepDesc& dref, int st, int item_
         }
       }
       const int addr = d.perm_off < 0 ? e : perm_addr(ptab, d.perm_off, e, lw);
+      acc = out_round<RB>(acc);
       p.out[addr] = acc;
     }
     if (NORM && G1) {
@@ -359,7 +370,7 @@ __device__ __forceinline__ void store4<dfloat>(dfloat* p, const dfloat v[4]) {
 // so the vector accesses are aligned.  Permuted outputs are written in a
 // lane-rotated order where the planner found that it spreads the stores of
 // one warp instruction over more shared-memory banks.
-template <typename T, int VW, bool NORM, bool MAXP, bool G1, bool CL>
+template <typename T, int VW, bool NORM, bool MAXP, bool G1, bool CL, bool RB = false>
 __device__ void run_step_vec(const KArgs& a, const StepDesc& dref, int st, int item_base, uint32_t* s_max,
                              const StepPtrs<T>* ptrs, const PermTab& ptab, bool contiguous) {
   constexpr int LV = VW == 8 ? 3 : 2;
@@ -459,6 +470,10 @@ __device__ void run_step_vec(const KArgs& a, const StepDesc& dref, int st, int i
           body(k + 1);
         }
       }
+      if constexpr (RB) {
+#pragma unroll
+        for (int j = 0; j < VW; ++j) acc[j] = out_round<RB>(acc[j]);
+      }
       if (!permuted || contiguous) {
         // the permutation keeps the low log2(VW) index bits in place (or
         // there is none): the VW outputs are VW consecutive elements at the
@@ -517,7 +532,7 @@ __device__ void run_step_vec(const KArgs& a, const StepDesc& dref, int st, int i
 // A step with few outputs and a long k range: TPO (a power of two, at most
 // 32) consecutive lanes share one output, each summing every TPO-th k, and
 // combine their partial sums with shuffles (maxima in max-product mode).
-template <typename T, bool NORM, bool MAXP, bool G1, bool CL>
+template <typename T, bool NORM, bool MAXP, bool G1, bool CL, bool RB = false>
 __device__ void run_step_splitk(const KArgs& a, const StepDesc& dref, int st, int item_base, int lt,
                                 uint32_t* s_max, const StepPtrs<T>* ptrs, const PermTab& ptab) {
   const StepDesc d = dref;
@@ -571,6 +586,7 @@ __device__ void run_step_splitk(const KArgs& a, const StepDesc& dref, int st, in
     if (valid && sub == 0) {
       if (NORM) acc = scale(acc, fb_s);
       const int addr = d.perm_off < 0 ? e : perm_addr(ptab, d.perm_off, e, lw);
+      acc = out_round<RB>(acc);
       p.out[addr] = acc;
       if (NORM) {
         const uint32_t bits = __float_as_uint(float(acc));
@@ -588,7 +604,7 @@ __device__ void run_step_splitk(const KArgs& a, const StepDesc& dref, int st, in
 // multiply-adds), and the partial sums meet by shuffles.  Used where one
 // syndrome has a whole block or cluster to itself, so a step's chain of
 // dependent operand loads is shortened by the lanes that would otherwise idle.
-template <typename T, bool NORM, bool MAXP, bool G1, bool CL>
+template <typename T, bool NORM, bool MAXP, bool G1, bool CL, bool RB = false>
 __device__ void run_step_vsplit(const KArgs& a, const StepDesc& dref, int st, int item_base, int lt,
                                 uint32_t* s_max, const StepPtrs<T>* ptrs, const PermTab& ptab, bool contiguous) {
   const StepDesc d = dref;
@@ -658,6 +674,10 @@ __device__ void run_step_vsplit(const KArgs& a, const StepDesc& dref, int st, in
     }
     const bool writer = valid && sub == 0;
     if (writer) {
+      if constexpr (RB) {
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[j] = out_round<RB>(acc[j]);
+      }
       if (!permuted || contiguous) {
         store4<T>(p.out + (permuted ? perm_addr(ptab, d.perm_off, e0, lw) : e0), acc);
       } else {
@@ -962,11 +982,11 @@ __device__ void run_step_tc(const KArgs& a, const StepDesc& dref, int st, uint32
 // The planner hands the kernel arena and constant operands only (parity
 // operands become syndrome-selected tables), so each step shape has one code
 // path: the kernel stays small enough for the instruction caches.
-template <typename T, bool NORM, bool MAXP, bool G1, bool TENSOR, bool CL, bool VS = false>
+template <typename T, bool NORM, bool MAXP, bool G1, bool TENSOR, bool CL, bool VS = false, bool RB = false>
 __device__ __forceinline__ void dispatch_step(const KArgs& a, const StepDesc& d, const StepShape& sh, int st,
                                               int item_base, uint32_t* s_max, const StepPtrs<T>* ptrs,
                                               const PermTab& ptab, TcState* ts, unsigned char* tbuf) {
-  if constexpr (TENSOR && !CL && std::is_same<T, float>::value && NORM && !MAXP && G1) {
+  if constexpr (TENSOR && !CL && !RB && std::is_same<T, float>::value && NORM && !MAXP && G1) {
     if (sh.kind == SK_TENSOR) {
       run_step_tc<T, NORM>(a, d, st, s_max, ptrs, ptab, ts, tbuf);
       return;
@@ -974,21 +994,21 @@ __device__ __forceinline__ void dispatch_step(const KArgs& a, const StepDesc& d,
   }
   switch (sh.kind) {
     case SK_SPLITK:
-      run_step_splitk<T, NORM, MAXP, G1, CL>(a, d, st, item_base, sh.lt, s_max, ptrs, ptab);
+      run_step_splitk<T, NORM, MAXP, G1, CL, RB>(a, d, st, item_base, sh.lt, s_max, ptrs, ptab);
       break;
     case SK_VSPLIT:  // planned where the launch allows it (KArgs::vsplit, the cluster kernel)
-      if constexpr (VS) run_step_vsplit<T, NORM, MAXP, G1, CL>(a, d, st, item_base, sh.lt, s_max, ptrs, ptab,
-                                                               sh.contiguous);
+      if constexpr (VS) run_step_vsplit<T, NORM, MAXP, G1, CL, RB>(a, d, st, item_base, sh.lt, s_max, ptrs, ptab,
+                                                                   sh.contiguous);
       break;
     case SK_VEC8:  // float32 only (step_shape)
       if constexpr (sizeof(T) == 4)
-        run_step_vec<T, 8, NORM, MAXP, G1, CL>(a, d, st, item_base, s_max, ptrs, ptab, sh.contiguous);
+        run_step_vec<T, 8, NORM, MAXP, G1, CL, RB>(a, d, st, item_base, s_max, ptrs, ptab, sh.contiguous);
       break;
     case SK_VEC4:
-      run_step_vec<T, 4, NORM, MAXP, G1, CL>(a, d, st, item_base, s_max, ptrs, ptab, sh.contiguous);
+      run_step_vec<T, 4, NORM, MAXP, G1, CL, RB>(a, d, st, item_base, s_max, ptrs, ptab, sh.contiguous);
       break;
     default:
-      run_step<T, NORM, MAXP, G1, CL>(a, d, st, item_base, s_max, ptrs, ptab);
+      run_step<T, NORM, MAXP, G1, CL, RB>(a, d, st, item_base, s_max, ptrs, ptab);
   }
 }
 
@@ -1132,7 +1152,7 @@ __device__ __forceinline__ void fill_step_plan(const KArgs& a, const StepDesc* s
 // One group of up to G syndromes (rows base .. base+G-1 below nrows) through
 // the whole program: load the syndrome words, run every step, back-track
 // (MAP), then the epilogue.  Ends with a block barrier.
-template <typename T, bool NORM, bool MAXP, bool TENSOR, bool CL, bool VS>
+template <typename T, bool NORM, bool MAXP, bool TENSOR, bool CL, bool VS, bool RB = false>
 __device__ void contract_group(const KArgs& a, int64_t base, int64_t nrows, const BlockSmem& sm,
                                const Arena<T>& arena,
                                const T* consts, const PermTab& ptab) {
@@ -1195,15 +1215,15 @@ __device__ void contract_group(const KArgs& a, int64_t base, int64_t nrows, cons
     const int vt_warp = rotated(team_tid<CL>() & ~31, item_base, team_size<CL>());
     if (vt_warp < items) {
       if (a.G == 1) {
-        dispatch_step<T, NORM, MAXP, true, TENSOR, CL, VS>(a, d, sh, st, item_base, s_max, s_ptrs, ptab, sm.tc,
+        dispatch_step<T, NORM, MAXP, true, TENSOR, CL, VS, RB>(a, d, sh, st, item_base, s_max, s_ptrs, ptab, sm.tc,
                                                            sm.tbuf);
       } else if (per_syndrome) {
         // the block's syndromes one after another with hoisted invariants
         for (int g = 0; g < a.G; ++g)
-          dispatch_step<T, NORM, MAXP, true, TENSOR, CL, VS>(a, d, sh, st, item_base, s_max + g * a.n_steps,
+          dispatch_step<T, NORM, MAXP, true, TENSOR, CL, VS, RB>(a, d, sh, st, item_base, s_max + g * a.n_steps,
                                                              s_ptrs + g * a.n_steps, ptab, sm.tc, sm.tbuf);
       } else {
-        dispatch_step<T, NORM, MAXP, false, TENSOR, CL, VS>(a, d, sh, st, item_base, s_max, s_ptrs, ptab, sm.tc,
+        dispatch_step<T, NORM, MAXP, false, TENSOR, CL, VS, RB>(a, d, sh, st, item_base, s_max, s_ptrs, ptab, sm.tc,
                                                             sm.tbuf);
       }
     }
@@ -1403,7 +1423,7 @@ __device__ __forceinline__ Arena<T> block_arena(const KArgs& a, unsigned char* s
 // VS: the kernel has the SK_VSPLIT step body (launches with KArgs::vsplit
 // plan it); the float32 kernel without it is kept for launches that do not,
 // its 64 registers a thread being the tighter budget.
-template <typename T, bool NORM, bool MAXP, bool TENSOR, bool VS = (sizeof(T) == 8)>
+template <typename T, bool NORM, bool MAXP, bool TENSOR, bool VS = (sizeof(T) == 8), bool RB = false>
 __global__ void __launch_bounds__(sizeof(T) == 8 || TENSOR ? 512 : 1024) tn_contract_kernel(KArgs a) {
   extern __shared__ __align__(16) unsigned char smem[];
   const BlockSmem sm = carve_smem<NORM, MAXP>(a, smem);
@@ -1431,7 +1451,7 @@ __global__ void __launch_bounds__(sizeof(T) == 8 || TENSOR ? 512 : 1024) tn_cont
   }
   const int64_t nrows = a.list ? int64_t(*a.list_count) : a.n;
   for (int64_t base = int64_t(blockIdx.x) * a.G; base < nrows; base += int64_t(gridDim.x) * a.G)
-    contract_group<T, NORM, MAXP, TENSOR, false, VS>(a, base, nrows, sm, arena, consts, ptab);
+    contract_group<T, NORM, MAXP, TENSOR, false, VS, RB>(a, base, nrows, sm, arena, consts, ptab);
   if (tensor) {
     tc::fence_before();
     __syncthreads();
@@ -1651,6 +1671,8 @@ cudaError_t contract_launch(int precision, const KArgs& a, int grid, int threads
                             cudaStream_t stream) {
   if (precision == 1) {
     if (a.map_mode) return launch_with(tn_contract_kernel<float, true, true, false>, a, grid, threads, smem, stream);
+    if (a.round_bf16)  // the bf16 study: SIMT steps only, vsplit as planned
+      return launch_with(tn_contract_kernel<float, true, false, false, true, true>, a, grid, threads, smem, stream);
     if (a.tc) return launch_with(tn_contract_kernel<float, true, false, true>, a, grid, threads, smem, stream);
     return a.vsplit ? launch_with(tn_contract_kernel<float, true, false, false, true>, a, grid, threads, smem, stream)
                     : launch_with(tn_contract_kernel<float, true, false, false>, a, grid, threads, smem, stream);

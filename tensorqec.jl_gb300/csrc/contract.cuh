@@ -63,7 +63,10 @@ struct KArgs {
   // per step, options the autotuner chose (kOpt*; nullptr: all 0), read
   // while the kernel plans its steps
   const int8_t* step_opts;
-  int64_t opts_pad;
+  // float32 launches: round every stored intermediate to bfloat16 (a study
+  // of bf16 intermediates, TQEC_F32_BF16)
+  int32_t round_bf16;
+  int32_t opts_pad;
 };
 // step options: no shared work items; (cluster form) the step's barrier
 // group never runs on the first block alone; runs there whenever its items

@@ -370,7 +370,8 @@ class CompiledTNMMAP:
         (Julia linear order), contracted in the given precision."""
         packed = pack_syndromes(self._bits(syndromes))
         prec = self.decoder._native_precision() if precision is None else \
-            {"f64": native.TQEC_F64, "f32": native.TQEC_F32, "f32x2": native.TQEC_F32X2}[precision]
+            {"f64": native.TQEC_F64, "f32": native.TQEC_F32, "f32x2": native.TQEC_F32X2,
+             "bf16": native.TQEC_F32_BF16}[precision]
         return self.program.contract_packed(packed, prec)
 
     def error_pattern(self, cls: int, syndrome: CSSSyndrome):
@@ -469,7 +470,8 @@ class CompiledDEMTNMMAP:
     def class_logprobs(self, syndromes, precision=None):
         packed = pack_syndromes(simple_rows(syndromes))
         prec = self.decoder._native_precision() if precision is None else \
-            {"f64": native.TQEC_F64, "f32": native.TQEC_F32, "f32x2": native.TQEC_F32X2}[precision]
+            {"f64": native.TQEC_F64, "f32": native.TQEC_F32, "f32x2": native.TQEC_F32X2,
+             "bf16": native.TQEC_F32_BF16}[precision]
         return self.program.contract_packed(packed, prec)
 
     def error_pattern(self, cls: int, syndrome: SimpleSyndrome):

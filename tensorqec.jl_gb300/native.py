@@ -17,6 +17,7 @@ TQEC_OK = 0
 TQEC_F64 = 0
 TQEC_F32 = 1
 TQEC_F32X2 = 2
+TQEC_F32_BF16 = 3
 TQEC_FLAG_PLAIN = 1
 TQEC_FLAG_NORECHECK = 2
 TQEC_FLAG_MAP = 4

@@ -9,7 +9,8 @@ oracle at the tolerance the plain form promises.
 * d=5 and d=7 at p in {0.02, 0.05, 0.08, 0.11}, 8,192 seeded syndromes each:
   float32 + recheck decisions equal to the oracle's outside exact ties;
   float32 class log-probabilities within twice the program's rounding bound;
-  float64 within 1e-10 relative per class.
+  float64 within 1e-10 relative per class; bf16 intermediates within their
+  bound (the float32 one plus 2^-9 per runtime step).
 * circuit-level rotated Z-memory d=5, 5 rounds, p=0.001: 64 sampled detector
   patterns through the float32 decoder (with its recheck) and float64, against
   the oracle's float64 contraction of the same detector error model.
@@ -131,6 +132,10 @@ def test_config2_p_sweep_vs_oracle(pkg, oracle, d, p):
     assert_class_logprobs_within(ct.class_logprobs(bits, precision="f32"), want, 2 * info["err_bound_f32"])
     # float64 of the same program: 1e-10 relative per class
     assert_class_logprobs(ct.class_logprobs(bits, precision="f64"), want, 1e-10)
+    # bf16 intermediates (the float32 program, every stored intermediate rounded
+    # to 8 significant bits): within the float32 bound plus 2^-9 per step
+    bb = info["err_bound_f32"] + info["n_steps"] * 2.0 ** -9
+    assert_class_logprobs_within(ct.class_logprobs(bits, precision="bf16"), want, -np.log1p(-bb))
     ct.close()
 
 
