@@ -138,6 +138,10 @@ struct tqec_program {
   DevBuf arena[3], carena[3];
   DevBuf syn, cls, logp, err, list, count;
   int32_t* h_count = nullptr;  // pinned
+  // a wide float32 program's recheck twin: the same network compiled as a
+  // plain program, its steps level by level (fewer barrier groups for one
+  // syndrome's latency); the recheck runs on the twin's cluster form
+  tqec_program* twin = nullptr;
   int64_t last_recheck = 0;
   // the last call's count is still being copied to h_count on its stream
   // (a call on a caller's stream with device outputs returns before it ends)
@@ -499,8 +503,37 @@ void default_clusters(tqec_program* p) {
   cudaGetLastError();
 }
 
+// The program whose cluster form contracts single rows of `precision`: the
+// recheck twin for the recheck's arithmetic where the program has one.
+tqec_program* cluster_program(tqec_program* p, int precision) {
+  return p->twin && precision == recheck_precision(p) && p->twin->cluster[precision].size > 0 ? p->twin : p;
+}
+
+// Rows on clusters (cluster_program's form), `a` built for p.
+int launch_cluster_rows_of(tqec_program* p, int precision, const tqec::KArgs& a, int64_t n_max, cudaStream_t st) {
+  tqec_program* cp = cluster_program(p, precision);
+  if (cp == p) return launch_cluster_rows(p, precision, a, n_max, st);
+  // the twin's program (steps, tables, constants), these rows and outputs
+  tqec::KArgs t = base_args(cp, precision);
+  t.syn = a.syn;
+  t.n = a.n;
+  t.row_offset = a.row_offset;
+  t.list = a.list;
+  t.list_count = a.list_count;
+  t.class_out = a.class_out;
+  t.logp_out = a.logp_out;
+  t.err_out = a.err_out;
+  t.recheck_margin = a.recheck_margin;
+  t.recheck_list = a.recheck_list;
+  t.recheck_count = a.recheck_count;
+  t.round_bf16 = a.round_bf16;
+  t.tc_err = a.tc_err;  // a wait that gave up fails this program's call
+  return launch_cluster_rows(cp, precision, t, n_max, st);
+}
+
 int launch_recheck(tqec_program* p, const tqec::KArgs& b, int64_t n_max, cudaStream_t st) {
   const int rp = recheck_precision(p);
+  if (cluster_program(p, rp)->cluster[rp].size > 0) return launch_cluster_rows_of(p, rp, b, n_max, st);
   if (p->cluster[rp].size > 0) return launch_cluster_rows(p, rp, b, n_max, st);
   return launch_rows(p, rp, b, n_max, st, &p->recheck_shape);
 }
@@ -585,9 +618,10 @@ int decode_locked(tqec_program* p, const uint8_t* syn, int64_t n, int32_t* cls, 
     }
     // a batch no larger than one wave of clusters takes the cluster form
     // of its precision (float64, double-float) where the program has one
-    const bool few = precision != TQEC_F32 && p->cluster[precision].size > 0 && n <= p->cluster[precision].cap;
+    const ClusterShape& fc = cluster_program(p, precision)->cluster[precision];
+    const bool few = precision != TQEC_F32 && fc.size > 0 && n <= fc.cap;
     rc = plain ? launch_plain(p, precision, a, n, st)
-               : few ? launch_cluster_rows(p, precision, a, n, st) : launch_rows(p, precision, a, n, st);
+               : few ? launch_cluster_rows_of(p, precision, a, n, st) : launch_rows(p, precision, a, n, st);
     if (rc) return rc;
     if (recheck && precision == TQEC_F32) {
       tqec::KArgs b = base_args(p, recheck_precision(p));
@@ -647,23 +681,26 @@ int program_multi_view(tqec_program* p, ProgramMultiView* v) {
   v->map_mode = p->plan.map_mode;
   v->flops_per_syndrome = 2.0 * p->plan.macs_runtime;
   v->recheck_margin = p->margin >= 0.0 ? p->margin : 2.0 * err_bound(p, TQEC_F32);
-  const ClusterShape& c = p->cluster[v->recheck_precision];
+  // the recheck's cluster form: the twin's where the program has one
+  tqec_program* cp = p->twin ? p->twin : p;
+  const ClusterShape& c = cp->cluster[v->recheck_precision];
   v->cluster_blocks = c.size;
   if (c.size > 0) {
     v->cluster_threads = c.threads;
     v->cluster_cap = c.cap;
     v->cluster_smem = c.smem;
-    v->cluster_arena_elems = c.split ? p->plan.arena_elems - p->plan.arena_small : p->plan.arena_elems;
-    KArgs a = base_args(p, v->recheck_precision);
+    v->cluster_arena_elems = c.split ? cp->plan.arena_elems - cp->plan.arena_small : cp->plan.arena_elems;
+    KArgs a = base_args(cp, v->recheck_precision);
     a.G = 1;
     a.lg = 0;
     a.tables_smem = c.tables ? 1 : 0;
-    a.perm16 = c.tables ? p->d_perm16 : nullptr;
+    a.perm16 = c.tables ? cp->d_perm16 : nullptr;
     a.arena_global = nullptr;
-    a.arena_small = c.split ? p->plan.arena_small : 0;
+    a.arena_small = c.split ? cp->plan.arena_small : 0;
     a.tc = 0;
-    const auto& o = p->copts[v->recheck_precision];
-    a.step_opts = o.empty() ? nullptr : static_cast<const int8_t*>(p->d_copts[v->recheck_precision].p);
+    a.tc_err = p->d_tc_err;
+    const auto& o = cp->copts[v->recheck_precision];
+    a.step_opts = o.empty() ? nullptr : static_cast<const int8_t*>(cp->d_copts[v->recheck_precision].p);
     v->args_cluster = a;
   }
   return TQEC_OK;
@@ -854,6 +891,16 @@ int tqec_program_create(const tqec_network* net, const tqec_tree* tree, const tq
   // wide programs take their single-syndrome launches (the recheck; the
   // plain form) on 8-block clusters until tqec_program_autotune measures
   default_clusters(p);
+  if (!(o.flags & (TQEC_FLAG_PLAIN | TQEC_FLAG_NORECHECK | TQEC_FLAG_MAP)) && o.precision == TQEC_F32 &&
+      p->plan.width >= kClusterMinWidth) {
+    tqec_options o2 = o;
+    o2.flags |= TQEC_FLAG_PLAIN;
+    tqec_program* tw = nullptr;
+    if (tqec_program_create(net, tree, &o2, &tw) == TQEC_OK) {
+      if (tw->cluster[recheck_precision(p)].size > 0) p->twin = tw;
+      else tqec_program_destroy(tw);
+    }
+  }
   g_last_error.clear();
   *out = p;
   return TQEC_OK;
@@ -861,6 +908,7 @@ int tqec_program_create(const tqec_network* net, const tqec_tree* tree, const tq
 
 int tqec_program_destroy(tqec_program* p) {
   if (!p) return TQEC_OK;
+  if (p->twin) tqec_program_destroy(p->twin);
   cudaSetDevice(p->device);
   if (p->stream) cudaStreamSynchronize(p->stream);
   cudaFree(p->d_steps);
@@ -911,11 +959,14 @@ int tqec_program_info(const tqec_program* p, tqec_program_info_t* info) {
   info->split_f32 = p->shape[TQEC_F32].split ? 1 : 0;
   info->split_f64 = p->shape[TQEC_F64].split ? 1 : 0;
   info->recheck_precision = P.map_mode ? TQEC_F64 : recheck_precision(p);
-  info->cluster_blocks = p->cluster[(p->flags & TQEC_FLAG_PLAIN) ? p->precision : info->recheck_precision].size;
+  // the form of single-syndrome launches: the plain form's, else the
+  // recheck's (on the twin where the program has one)
+  const tqec_program* cp = (p->flags & TQEC_FLAG_PLAIN) || !p->twin ? p : p->twin;
+  info->cluster_blocks = cp->cluster[(p->flags & TQEC_FLAG_PLAIN) ? p->precision : info->recheck_precision].size;
   info->shared_items_f32 = p->shape[TQEC_F32].vsplit ? 1 : 0;
   info->shared_items_f64 = p->shape[TQEC_F64].vsplit ? 1 : 0;
   {
-    const auto& o = p->copts[(p->flags & TQEC_FLAG_PLAIN) ? p->precision : info->recheck_precision];
+    const auto& o = cp->copts[(p->flags & TQEC_FLAG_PLAIN) ? p->precision : info->recheck_precision];
     info->cluster_tuned_steps = int32_t(std::count_if(o.begin(), o.end(), [](int8_t v) { return v != 0; }));
   }
   info->err_bound_f32x2 = err_bound(p, TQEC_F32X2);
@@ -1256,6 +1307,11 @@ int tqec_program_set_cluster(tqec_program* p, int32_t precision, int32_t blocks,
   if (!p) return fail(TQEC_ERR_INVALID, "NULL program");
   if (precision != TQEC_F64 && precision != TQEC_F32X2)
     return fail(TQEC_ERR_INVALID, "clusters serve TQEC_F64 and TQEC_F32X2 launches");
+  if (p->twin && precision == recheck_precision(p)) {
+    // the recheck runs on the twin's cluster form
+    const int rc = tqec_program_set_cluster(p->twin, precision, blocks, threads, small_in_smem);
+    if (rc) return rc;
+  }
   std::lock_guard<std::mutex> lk(p->mu);
   TQ_CUDA(cudaSetDevice(p->device));
   p->copts[precision].clear();  // tuned for the previous form
@@ -1314,6 +1370,15 @@ int tqec_program_autotune(tqec_program* p, int64_t n_probe) {
     const bool plain = (p->flags & TQEC_FLAG_PLAIN) != 0;
     ok = tune_cluster(p, recheck_precision(p), false, e0, e1);
     if (ok && plain && p->precision != TQEC_F32) ok = tune_cluster(p, p->precision, true, e0, e1);
+    if (ok && p->twin) {
+      // the recheck runs on the twin's cluster form: tune that one on the same probes
+      tqec_program* tw = p->twin;
+      const size_t sb = size_t(n) * p->plan.syndrome_bytes;
+      ok = tw->syn.ensure(std::max<size_t>(sb, 16)) == cudaSuccess &&
+           cudaMemcpy(tw->syn.p, p->syn.p, sb, cudaMemcpyDeviceToDevice) == cudaSuccess &&
+           tw->logp.ensure(sizeof(double) * n * p->plan.n_classes) == cudaSuccess &&
+           tune_cluster(tw, recheck_precision(p), false, e0, e1);
+    }
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
