@@ -65,9 +65,18 @@ cudaError_t gather_rows(const uint8_t* src, int row_bytes, const int32_t* list, 
 // weight matrices [dout][din] and bias[l] the float32 biases.
 bool mlp_fused_supported(int n_in, int in_pad, int hidden, int n_layers, int n_out, const __nv_bfloat16* const W[4],
                          const float* const bias[4]);
+// The gate fused into the fused forward's last epilogue (see gate_rows):
+// classes, confidences (optional) and the rows below threshold (optional).
+struct FusedGate {
+  float threshold;
+  int32_t* cls;
+  float* conf;
+  int32_t* list;
+  int32_t* count;
+};
 cudaError_t mlp_fused_logits(const uint8_t* syn, int64_t n, int sb, int n_in, const __nv_bfloat16* const W[4],
                              const float* const bias[4], int n_out, float* logits, int ldl, int* err,
-                             cudaStream_t st);
+                             cudaStream_t st, const FusedGate* gate = nullptr);
 cudaError_t scatter_classes(const int32_t* src, const int32_t* list, int64_t n, int32_t* dst, cudaStream_t st);
 
 }  // namespace tqec

@@ -191,7 +191,11 @@ int forward(tqec_mlp* p, const uint8_t* dsyn, int64_t n, cudaStream_t st) {
 
 // Inference forward: the fused kernel (all layers in one persistent launch,
 // activations kept on chip) in mode 3 where the shape allows, else forward().
-int forward_infer(tqec_mlp* p, const uint8_t* dsyn, int64_t n, cudaStream_t st) {
+// The inference forward; with `gate` (and the fused kernel) the gate runs in
+// its last epilogue and *gated is set, else the caller runs gate_rows.
+int forward_infer(tqec_mlp* p, const uint8_t* dsyn, int64_t n, cudaStream_t st,
+                  const tqec::FusedGate* gate = nullptr, bool* gated = nullptr) {
+  if (gated) *gated = false;
   if (p->use_tensor_cores == 3) {
     const __nv_bfloat16* W[4];
     const float* B[4];
@@ -201,7 +205,8 @@ int forward_infer(tqec_mlp* p, const uint8_t* dsyn, int64_t n, cudaStream_t st) 
     }
     if (tqec::mlp_fused_supported(p->cfg.n_in, p->in_pad, p->cfg.hidden, p->L, p->cfg.n_out, W, B)) {
       SQ_CUDA(tqec::mlp_fused_logits(dsyn, n, (p->cfg.n_in + 7) / 8, p->cfg.n_in, W, B, p->cfg.n_out, p->logits,
-                                     p->out_pad, p->d_err, st));
+                                     p->out_pad, p->d_err, st, gate));
+      if (gated) *gated = gate != nullptr;
       return TQEC_OK;
     }
   }
@@ -521,10 +526,12 @@ int tqec_mlp_infer(tqec_mlp* p, const uint8_t* syn, int64_t n, int32_t* class_ou
     const int64_t m = std::min(chunk, n - r0);
     const uint8_t* ds;
     if ((rc = stage_syn(p, syn + r0 * sb, m, st, &ds))) return rc;
-    if ((rc = forward_infer(p, ds, m, st))) return rc;
     int32_t* c = host_cls ? p->cls : (class_out ? class_out + r0 : nullptr);
     float* f = host_conf ? p->conf : (conf_out ? conf_out + r0 : nullptr);
-    SQ_CUDA(tqec::gate_rows(p->logits, p->out_pad, m, p->cfg.n_out, 0.f, c, f, nullptr, nullptr, st));
+    const tqec::FusedGate g{0.f, c, f, nullptr, nullptr};
+    bool gated = false;
+    if ((rc = forward_infer(p, ds, m, st, c ? &g : nullptr, &gated))) return rc;
+    if (!gated) SQ_CUDA(tqec::gate_rows(p->logits, p->out_pad, m, p->cfg.n_out, 0.f, c, f, nullptr, nullptr, st));
     if (host_cls) SQ_CUDA(cudaMemcpyAsync(class_out + r0, p->cls, sizeof(int32_t) * m, cudaMemcpyDeviceToHost, st));
     if (host_conf) SQ_CUDA(cudaMemcpyAsync(conf_out + r0, p->conf, sizeof(float) * m, cudaMemcpyDeviceToHost, st));
     if (host_in || host_cls || host_conf) SQ_CUDA(cudaStreamSynchronize(st));
@@ -566,10 +573,13 @@ int tqec_gated_decode(tqec_mlp* p, tqec_program* prog, float threshold, const ui
     const int64_t m = std::min(chunk, n - r0);
     const uint8_t* ds;
     if ((rc = stage_syn(p, syn + r0 * sb, m, st, &ds))) return rc;
-    if ((rc = forward_infer(p, ds, m, st))) return rc;
     int32_t* cls = host_cls ? p->cls : class_out + r0;
     SQ_CUDA(cudaMemsetAsync(p->count, 0, sizeof(int32_t), st));
-    SQ_CUDA(tqec::gate_rows(p->logits, p->out_pad, m, p->cfg.n_out, threshold, cls, p->conf, p->list, p->count, st));
+    const tqec::FusedGate g{threshold, cls, p->conf, p->list, p->count};
+    bool gated = false;
+    if ((rc = forward_infer(p, ds, m, st, &g, &gated))) return rc;
+    if (!gated)
+      SQ_CUDA(tqec::gate_rows(p->logits, p->out_pad, m, p->cfg.n_out, threshold, cls, p->conf, p->list, p->count, st));
     rc = tqec_decode_rows(prog, ds, p->list, p->count, m, p->fallback_hint > 0 ? p->fallback_hint : m / 16, cls, st);
     if (rc) return rc;
     SQ_CUDA(cudaMemcpyAsync(p->h_counts + c, p->count, sizeof(int32_t), cudaMemcpyDeviceToHost, st));

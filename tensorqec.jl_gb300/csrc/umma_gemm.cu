@@ -293,6 +293,14 @@ struct FusedArgs {
   int n_out, ldl;
   float* logits;
   int* err;
+  // the gate, fused into the last epilogue when cls is set: the argmax class
+  // and the softmax confidence of every row, and the rows below threshold
+  // appended to list (count), exactly as gate_kernel computes them
+  float threshold;
+  int32_t* cls;
+  float* conf;
+  int32_t* list;
+  int32_t* count;
 };
 
 __device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
@@ -519,8 +527,28 @@ __global__ void __launch_bounds__(FTHREADS, 1)
           if (half == 1)
             for (int o = 0; o < a.n_out; ++o) partial[r * FMAX_OUT + o] = lg[o];
           asm volatile("bar.sync 1, %0;" ::"n"(FEPI) : "memory");
-          if (half == 0 && go && row < a.n)
-            for (int o = 0; o < a.n_out; ++o) a.logits[row * a.ldl + o] = lg[o] + partial[r * FMAX_OUT + o] + a.b4[o];
+          if (half == 0 && go && row < a.n) {
+            for (int o = 0; o < a.n_out; ++o) {
+              lg[o] = lg[o] + partial[r * FMAX_OUT + o] + a.b4[o];
+              a.logits[row * a.ldl + o] = lg[o];
+            }
+            if (a.cls) {
+              // the gate on this row's logits (the same arithmetic as gate_kernel)
+              float mx = lg[0];
+              int bc = 0;
+              for (int o = 1; o < a.n_out; ++o)
+                if (lg[o] > mx) {
+                  mx = lg[o];
+                  bc = o;
+                }
+              float sum = 0.f;
+              for (int o = 0; o < a.n_out; ++o) sum += __expf(lg[o] - mx);
+              const float pr = 1.0f / sum;
+              a.cls[row] = bc;
+              if (a.conf) a.conf[row] = pr;
+              if (a.list && !(pr >= a.threshold)) a.list[atomicAdd(a.count, 1)] = int32_t(row);
+            }
+          }
           // the next tile's layer-1 input overwrites that memory only after
           asm volatile("bar.sync 1, %0;" ::"n"(FEPI) : "memory");
         }
@@ -582,13 +610,43 @@ bool mlp_fused_supported(int n_in, int in_pad, int hidden, int n_layers, int n_o
 
 cudaError_t mlp_fused_logits(const uint8_t* syn, int64_t n, int sb, int n_in, const __nv_bfloat16* const W[4],
                              const float* const bias[4], int n_out, float* logits, int ldl, int* err,
-                             cudaStream_t st) {
+                             cudaStream_t st, const FusedGate* gate) {
   if (n <= 0) return cudaSuccess;
   if (sb > 8) return cudaErrorInvalidValue;
+  // the weights' tensor maps, the SM count and the kernel's shared-memory
+  // limit are set up once per weight buffers and device (the step's first
+  // kernel is then enqueued without host work in front of it)
+  struct Cached {
+    const void* w[3] = {nullptr, nullptr, nullptr};
+    int dev = -1, sms = 1;
+    CUtensorMap m[3];
+  };
+  static std::mutex mu;
+  static Cached cache[8];
+  int dev = 0;
+  cudaGetDevice(&dev);
   CUtensorMap m1, m2, m3;
-  if (!make_map(&m1, W[0], FH, UK, UK, FNH) || !make_map(&m2, W[1], FH, FH, FH, FNH) ||
-      !make_map(&m3, W[2], FH, FH, FH, FNH))
-    return cudaErrorInvalidValue;
+  int sms = 1;
+  {
+    std::lock_guard<std::mutex> lk(mu);
+    Cached& c = cache[dev & 7];
+    if (c.dev != dev || c.w[0] != W[0] || c.w[1] != W[1] || c.w[2] != W[2]) {
+      c.dev = -1;
+      if (!make_map(&c.m[0], W[0], FH, UK, UK, FNH) || !make_map(&c.m[1], W[1], FH, FH, FH, FNH) ||
+          !make_map(&c.m[2], W[2], FH, FH, FH, FNH))
+        return cudaErrorInvalidValue;
+      cudaDeviceGetAttribute(&c.sms, cudaDevAttrMultiProcessorCount, dev);
+      cudaError_t e = cudaFuncSetAttribute(mlp_fused_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           int(FUSED_SMEM));
+      if (e != cudaSuccess) return e;
+      for (int i = 0; i < 3; ++i) c.w[i] = W[i];
+      c.dev = dev;
+    }
+    m1 = c.m[0];
+    m2 = c.m[1];
+    m3 = c.m[2];
+    sms = c.sms;
+  }
   FusedArgs a;
   a.syn = syn;
   a.sb = sb;
@@ -601,11 +659,11 @@ cudaError_t mlp_fused_logits(const uint8_t* syn, int64_t n, int sb, int n_in, co
   a.ldl = ldl;
   a.logits = logits;
   a.err = err;
-  int dev = 0, sms = 1;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  cudaError_t e = cudaFuncSetAttribute(mlp_fused_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(FUSED_SMEM));
-  if (e != cudaSuccess) return e;
+  a.threshold = gate ? gate->threshold : 0.f;
+  a.cls = gate ? gate->cls : nullptr;
+  a.conf = gate ? gate->conf : nullptr;
+  a.list = gate ? gate->list : nullptr;
+  a.count = gate ? gate->count : nullptr;
   const int64_t ntiles = (n + FM - 1) / FM;
   const int grid = int(std::min<int64_t>(ntiles, sms));
   mlp_fused_kernel<<<grid, FTHREADS, FUSED_SMEM, st>>>(m1, m2, m3, a);

@@ -183,3 +183,23 @@ def test_fused_forward_matches_layer_by_layer(pkg, rows):
     assert not ((cf != cl) & ~close).any()
     assert np.max(np.abs(pf - pl)) <= 1e-4
     sur.close()
+
+
+def test_fused_gate_matches_gate_on_the_logits(pkg):
+    """The gate fused into the forward's last epilogue (the default
+    inference path, and the gated decoder's): the first maximum of each row's
+    logits and the softmax confidence 1 / sum(exp(l - max)), as the separate
+    gate kernel computes them from the same logits."""
+    from tensorqec_gb300.surrogate import Surrogate
+
+    rng = np.random.default_rng(31)
+    sur = Surrogate(48, 4, 512, 4, seed=11)
+    sur.set_params(sur.params() * 2.0)
+    packed = pkg.pack_syndromes((rng.random((70000, 48)) < 0.15).astype(np.uint8))
+    sur.use_tensor_cores(True)
+    lf = sur.logits(packed).astype(np.float64)
+    cf, pf = sur.infer(packed)
+    assert np.array_equal(cf, np.argmax(lf, axis=1))
+    want = 1.0 / np.exp(lf - lf.max(axis=1, keepdims=True)).sum(axis=1)
+    assert np.max(np.abs(pf - want)) <= 1e-5
+    sur.close()
