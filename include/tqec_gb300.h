@@ -304,6 +304,10 @@ typedef struct {
   int32_t target_width;  /* widths above this are penalised (0 = none) */
   double width_penalty;  /* energy per label above target_width (default 1) */
   uint64_t seed;         /* random seed (0 = 1) */
+  double tensor_discount; /* > 1: the multiply-adds of GEMM-shaped steps (>= 2^7 x 2^5
+                             outputs per batch index, >= 2^5 contracted, the planner's
+                             tensor-core criterion) count this many times less, steering
+                             the search toward tensor-core steps (0 or 1: off) */
 } tqec_order_options;
 
 int tqec_optimize_order(const tqec_network* net, const tqec_order_options* opts,

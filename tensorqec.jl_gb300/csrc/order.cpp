@@ -37,6 +37,7 @@ struct Problem {
   std::vector<std::vector<int>> leaf; // labels per leaf
   std::vector<int> total;             // leaves carrying each label
   std::vector<char> is_out;
+  double tdisc = 1.0;                 // cost divisor of GEMM-shaped steps
 };
 
 // kept labels of merging x and y (each sorted by label)
@@ -64,9 +65,36 @@ struct Tree {
   int root = -1;
 };
 
-double tree_macs(const Tree& t, int T) {
+// The cost of internal node n: its multiply-adds, divided by P.tdisc when
+// the step is GEMM-shaped -- labels kept from one child only (fa, fb), labels
+// summed (k): |k| >= 5 and one of fa, fb >= 7 with the other >= 5.
+double node_cost(const Problem& P, const Tree& t, int n) {
+  const double m = std::ldexp(1.0, t.uni[n]);
+  if (P.tdisc <= 1.0) return m;
+  const std::vector<VC>& X = t.sets[t.l[n]];
+  const std::vector<VC>& Y = t.sets[t.r[n]];
+  const std::vector<VC>& O = t.sets[n];
+  size_t i = 0, j = 0, o = 0;
+  int fx = 0, fy = 0, kk = 0;
+  while (i < X.size() || j < Y.size()) {
+    int v;
+    bool inx = false, iny = false;
+    if (j >= Y.size() || (i < X.size() && X[i].v < Y[j].v)) { v = X[i++].v; inx = true; }
+    else if (i >= X.size() || Y[j].v < X[i].v) { v = Y[j++].v; iny = true; }
+    else { v = X[i].v; ++i; ++j; inx = iny = true; }
+    while (o < O.size() && O[o].v < v) ++o;
+    const bool kept = o < O.size() && O[o].v == v;
+    if (!kept) ++kk;
+    else if (inx && !iny) ++fx;
+    else if (iny && !inx) ++fy;
+  }
+  const bool gemm = kk >= 5 && ((fx >= 7 && fy >= 5) || (fy >= 7 && fx >= 5));
+  return gemm ? m / P.tdisc : m;
+}
+
+double tree_macs(const Problem& P, const Tree& t) {
   double s = 0;
-  for (int i = T; i < (int)t.l.size(); ++i) s += std::ldexp(1.0, t.uni[i]);
+  for (int i = P.T; i < (int)t.l.size(); ++i) s += node_cost(P, t, i);
   return s;
 }
 
@@ -184,7 +212,7 @@ void anneal(const Problem& P, Tree* t, std::mt19937_64& rng, int sweeps, int tar
   std::vector<int> wcount(64, 0);
   double macs = 0;
   for (int i = T; i < N; ++i) {
-    macs += std::ldexp(1.0, t->uni[i]);
+    macs += node_cost(P, *t, i);
     wcount[std::min<int>(63, (int)t->sets[i].size())]++;
   }
   auto width_of = [&]() {
@@ -214,7 +242,7 @@ void anneal(const Problem& P, Tree* t, std::mt19937_64& rng, int sweeps, int tar
       const int join = keep_c ? c : d;
       const int other = keep_c ? d : c;
       // old local cost
-      const double old_local = std::ldexp(1.0, t->uni[inner]) + std::ldexp(1.0, t->uni[x]);
+      const double old_local = node_cost(P, *t, inner) + node_cost(P, *t, x);
       const int old_w_inner = (int)t->sets[inner].size();
       save_set = t->sets[inner];
       const int save_uni = t->uni[inner];
@@ -226,7 +254,7 @@ void anneal(const Problem& P, Tree* t, std::mt19937_64& rng, int sweeps, int tar
       recompute(P, t, inner);
       const int old_ux = t->uni[x];
       recompute(P, t, x);  // x's set is unchanged (same leaves), union may differ
-      const double new_local = std::ldexp(1.0, t->uni[inner]) + std::ldexp(1.0, t->uni[x]);
+      const double new_local = node_cost(P, *t, inner) + node_cost(P, *t, x);
       const double nmacs = macs - old_local + new_local;
       wcount[std::min(63, old_w_inner)]--;
       wcount[std::min<int>(63, (int)t->sets[inner].size())]++;
@@ -360,6 +388,7 @@ extern "C" int tqec_optimize_order(const tqec_network* net, const tqec_order_opt
   }
   P.T = (int)members.size();
   P.V = V;
+  P.tdisc = o.tensor_discount > 1.0 ? o.tensor_discount : 1.0;
   P.total = total;
   P.is_out = is_out;
   P.leaf.resize(P.T);
@@ -399,17 +428,21 @@ extern "C" int tqec_optimize_order(const tqec_network* net, const tqec_order_opt
     Tree t;
     const double temp = tr == 0 ? 0.0 : std::ldexp(1.0, tr % 8);
     greedy(P, rng, temp, &t);
-    double E = energy(tree_macs(t, P.T), tree_width(t, P.T), target, o.width_penalty);
+    double E = energy(tree_macs(P, t), tree_width(t, P.T), target, o.width_penalty);
     if (E < bestE) { bestE = E; best = t; }
   }
   if (o.sweeps > 0) {
     Tree t = best;
     anneal(P, &t, rng, o.sweeps, target, o.width_penalty);
-    double E = energy(tree_macs(t, P.T), tree_width(t, P.T), target, o.width_penalty);
+    double E = energy(tree_macs(P, t), tree_width(t, P.T), target, o.width_penalty);
     if (E < bestE) { bestE = E; best = t; }
   }
   emit(best, P.T, leaf_id, next_step, NT, steps_out);
-  if (log2_macs_out) *log2_macs_out = std::log2(tree_macs(best, P.T));
+  if (log2_macs_out) {  // the multiply-adds themselves, whatever the discount
+    double m = 0;
+    for (int i = P.T; i < (int)best.l.size(); ++i) m += std::ldexp(1.0, best.uni[i]);
+    *log2_macs_out = std::log2(m);
+  }
   if (width_out) *width_out = tree_width(best, P.T);
   return TQEC_OK;
 }

@@ -49,6 +49,9 @@ class TreeSA:
     width_penalty: float = 1.0
     seed: int = 1
     restarts: int = 4
+    # > 1: GEMM-shaped steps (the planner's tensor-core criterion) cost this
+    # many times fewer multiply-adds in the search
+    tensor_discount: float = 0.0
 
 
 @dataclass
@@ -112,7 +115,8 @@ def optimize_code(graph: FactorGraph, optimizer) -> np.ndarray:
         if optimizer.restarts <= 1:
             steps, _, _ = native.optimize_order(graph, trials=optimizer.trials, sweeps=optimizer.sweeps,
                                                 target_width=optimizer.target_width,
-                                                width_penalty=optimizer.width_penalty, seed=optimizer.seed)
+                                                width_penalty=optimizer.width_penalty, seed=optimizer.seed,
+                                                tensor_discount=optimizer.tensor_discount)
             return steps
         return _search_fitting(graph, optimizer)
     raise TypeError(f"unknown optimizer {optimizer!r}")
@@ -140,7 +144,7 @@ def _search_fitting(graph, opt):
         for tw in widths:
             steps, _, w = native.optimize_order(graph, trials=opt.trials, sweeps=opt.sweeps, target_width=tw,
                                                 width_penalty=max(2.0, opt.width_penalty) if tw else opt.width_penalty,
-                                                seed=opt.seed + r)
+                                                seed=opt.seed + r, tensor_discount=opt.tensor_discount)
             plan = native.inspect_plan(graph, steps)
             cost = _estimated_cost(plan)
             if best is None or cost < best[0]:

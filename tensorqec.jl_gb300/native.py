@@ -79,7 +79,7 @@ class PlanView(C.Structure):
 
 class OrderOptions(C.Structure):
     _fields_ = [("trials", C.c_int32), ("sweeps", C.c_int32), ("target_width", C.c_int32),
-                ("width_penalty", C.c_double), ("seed", C.c_uint64)]
+                ("width_penalty", C.c_double), ("seed", C.c_uint64), ("tensor_discount", C.c_double)]
 
 
 STEP_DTYPE = np.dtype([("a_kind", "<i4"), ("b_kind", "<i4"), ("a_ref", "<i4"), ("b_ref", "<i4"),
@@ -169,15 +169,16 @@ class NetworkArrays:
                               _ptr(self.data), len(self.iy), _ptr(self.iy), len(self.synd), _ptr(self.synd))
 
 
-def optimize_order(graph, trials=32, sweeps=60, target_width=0, width_penalty=1.0, seed=1):
+def optimize_order(graph, trials=32, sweeps=60, target_width=0, width_penalty=1.0, seed=1, tensor_discount=0.0):
     """Contraction order for a FactorGraph: an (n_tensors - 1, 2) int32 array
     of node ids (tqec_tree convention), log2 of its multiply-adds and its
-    width."""
+    width.  tensor_discount > 1 counts the multiply-adds of GEMM-shaped steps
+    that many times less."""
     na = NetworkArrays(graph)
     steps = np.zeros((max(graph.n_tensors - 1, 0), 2), dtype=np.int32)
     lm = C.c_double(0)
     w = C.c_int32(0)
-    o = OrderOptions(trials, sweeps, target_width, width_penalty, seed)
+    o = OrderOptions(trials, sweeps, target_width, width_penalty, seed, tensor_discount)
     check(lib().tqec_optimize_order(C.byref(na.struct), C.byref(o), _ptr(steps), C.byref(lm), C.byref(w)))
     return steps, lm.value, w.value
 

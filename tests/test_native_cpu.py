@@ -189,3 +189,31 @@ def test_tensor_steps_need_a_share_of_the_work(pkg):
     steps = pkg.optimize_code(g, pkg.TreeSA(trials=16, sweeps=1000, seed=1, restarts=2))
     assert share(pkg.native.inspect_plan(g, steps)) >= 0.25
     assert share(pkg.native.inspect_plan(g, steps, pkg.native.TQEC_FLAG_NO_TENSOR_CORES)) == 0.0
+
+
+def test_tensor_aware_order_search(pkg):
+    """TreeSA(tensor_discount=D): GEMM-shaped steps cost D times fewer
+    multiply-adds in the search, which trades flops for tensor-core work: at
+    surface d=7 the default search plans no tensor-core step, a discount of 4
+    puts most of the multiply-adds on them (at more flops), and the tree stays
+    a valid contraction of the network."""
+    from tensorqec_gb300 import gf2
+    from tensorqec_gb300.network import tnmmap_css_graph
+
+    def share(plan):
+        m = np.array([1 << int(d["lh"] + d["lfa"] + d["lfb"] + d["lk"]) for d in plan["steps"]], dtype=np.float64)
+        tc = np.array([int(d["flags"]) & 8 != 0 for d in plan["steps"]])
+        return m[tc].sum() / m.sum()
+
+    t = pkg.tanner_graph(pkg.SurfaceCode(7, 7))
+    lx, lz = gf2.logical_operator(t)
+    g = tnmmap_css_graph(t, pkg.depolarizing(0.05, t.nq), lx, lz)
+    plain = pkg.native.inspect_plan(g, pkg.optimize_code(g, pkg.TreeSA(trials=16, sweeps=1000, restarts=2)))
+    steps = pkg.optimize_code(g, pkg.TreeSA(trials=16, sweeps=1000, restarts=2, tensor_discount=4.0))
+    tensor = pkg.native.inspect_plan(g, steps)
+    assert share(plain) == 0.0
+    assert share(tensor) >= 0.5
+    assert tensor["flops_per_syndrome"] > plain["flops_per_syndrome"]
+    # a valid tree: every node id used once, n - 1 steps
+    ids = np.asarray(steps).ravel()
+    assert len(steps) == g.n_tensors - 1 and len(np.unique(ids)) == len(ids)
