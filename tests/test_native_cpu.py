@@ -77,6 +77,25 @@ def test_plan_emulation_matches_oracle(pkg, oracle, code, nsyn):
     np.testing.assert_allclose(got, want, rtol=1e-10, atol=1e-12 * want.max())
 
 
+def test_level_ordered_plan_emulation_matches_oracle(pkg, oracle):
+    """The plain form's level-by-level plan (TQEC_FLAG_PLAIN, width >= 12:
+    steps reordered, more steps per barrier group, a different arena) computes
+    the same marginals as the oracle."""
+    t, em, g = _graph(pkg, pkg.SurfaceCode(7, 7), 0.08)
+    steps = pkg.optimize_code(g, pkg.TreeSA(trials=4, sweeps=200))
+    batch = pkg.native.inspect_plan(g, steps)
+    plan = pkg.native.inspect_plan(g, steps, pkg.native.TQEC_FLAG_PLAIN)
+    assert plan["width"] >= 12 and plan["arena_elems"] != batch["arena_elems"]
+    rng = np.random.default_rng(13)
+    ep = pkg.random_error_pattern(em, rng, nsamples=3)
+    syn = pkg.syndrome_extraction(ep, t)
+    bits = np.concatenate([syn.sx, syn.sz], axis=1)
+    got = run_plan(plan, bits)
+    st, nq = oracle.surface_code_stabilizers(7, 7)
+    want = oracle.OracleDecoder(oracle.css_tanner(st, nq), em.px, em.py, em.pz).marginals(bits)
+    np.testing.assert_allclose(got, want, rtol=1e-10, atol=1e-12 * want.max())
+
+
 def test_plan_emulation_dem(pkg, oracle):
     import json
 

@@ -108,18 +108,23 @@ def check_program(plan, is_float, vsplit=False):
     return bad
 
 
-def check_cluster_program(plan, is_float, blocks, threads):
+def check_cluster_program(plan, is_float, blocks, threads, opts=None):
     """The cluster form (one syndrome per cluster of `blocks` blocks): every
     output written once, and a group planned for the first block alone keeps
-    all its items on that block's threads."""
+    all its items on that block's threads.  `opts`: per-step options the
+    autotuner may set (1 no shared items, 2 never on the first block alone,
+    4 on the first block whenever the items fit)."""
     steps = plan["steps"]
     n = len(steps)
     sync = [bool(int(d["flags"]) & 1) for d in steps]
     team = blocks * threads
 
-    def shape(d, bd):
+    opts = np.zeros(n, dtype=np.int64) if opts is None else np.asarray(opts)
+
+    def shape(d, bd, st=None):
+        share = st is None or not (opts[st] & 1)
         return step_shape(int(d["lh"]), int(d["lfa"]), int(d["lfb"]), int(d["lk"]), 0, bd, is_float,
-                          int(d["flags"]), vsplit=True)
+                          int(d["flags"]), vsplit=share)
 
     groups, s0 = [], 0
     for st in range(n):
@@ -132,15 +137,17 @@ def check_cluster_program(plan, is_float, blocks, threads):
 
     bad = []
     for s0, s1 in groups:
-        solo = (sum(shape(steps[s], threads)[2] for s in range(s0, s1 + 1)) <= threads and
-                all(k_per_lane(steps[s], shape(steps[s], threads)) <=
-                    max(8, k_per_lane(steps[s], shape(steps[s], team))) for s in range(s0, s1 + 1)))
+        rng = range(s0, s1 + 1)
+        solo = (sum(shape(steps[s], threads, s)[2] for s in rng) <= threads and
+                not any(opts[s] & 2 for s in rng) and
+                all((opts[s] & 4) or k_per_lane(steps[s], shape(steps[s], threads, s)) <=
+                    max(8, k_per_lane(steps[s], shape(steps[s], team, s))) for s in rng))
         bd = threads if solo else team
         item_base = 0
         for st in range(s0, s1 + 1):
             d = steps[st]
             lw = int(d["lh"]) + int(d["lfa"]) + int(d["lfb"])
-            kind, lt, tr = shape(d, bd)
+            kind, lt, tr = shape(d, bd, st)
             cover = np.zeros((1, 1 << lw), dtype=np.int64)
             _run(kind, lt, lw, 0, True, bd, item_base, tr, cover, 0)
             if not (cover == 1).all():
@@ -179,10 +186,15 @@ def test_cluster_plans_write_every_output_once(pkg, code):
     steps = decoder.optimize_code(graph, decoder.TreeSA(restarts=1))
     kinds = set()
     # the batch plan (the recheck's) and the plain form's level-by-level plan
+    rng = np.random.default_rng(3)
     for flags in (0, native.TQEC_FLAG_PLAIN):
         plan = native.inspect_plan(graph, steps, flags)
         for blocks, threads in ((2, 128), (4, 256), (8, 256), (16, 128), (16, 256), (8, 512)):
             assert check_cluster_program(plan, False, blocks, threads) == []
+            # options the per-group tuning may set
+            for _ in range(3):
+                opts = rng.integers(0, 8, size=len(plan["steps"]))
+                assert check_cluster_program(plan, False, blocks, threads, opts) == []
             for d in plan["steps"]:
                 kinds.add(step_shape(int(d["lh"]), int(d["lfa"]), int(d["lfb"]), int(d["lk"]), 0, blocks * threads,
                                      False, int(d["flags"]), vsplit=True)[0])
