@@ -285,15 +285,17 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(sm), "source": self.source}
 
 
-def read_traffic():
-    """Per-launch DRAM bytes of the dominant kernel from the committed ncu
-    summary (profiles/roofline_traffic.txt: 'key value' lines)."""
+def read_traffic(key=None):
+    """DRAM bytes from the committed ncu summary (profiles/roofline_traffic.txt:
+    'key value' lines): by default per full-batch launch of the float32
+    contraction."""
+    key = key or f"tn_contract_f32_d{D}_bytes_per_launch_{BATCH}"
     path = os.path.join(ROOT, "profiles", "roofline_traffic.txt")
     if not os.path.exists(path):
         return None
     for line in open(path):
         parts = line.split()
-        if len(parts) >= 2 and parts[0] == f"tn_contract_f32_d{D}_bytes_per_launch_{BATCH}":
+        if len(parts) >= 2 and parts[0] == key:
             return float(parts[1])
     return None
 
@@ -622,9 +624,14 @@ def run_ours(args):
                             "unit": "TFLOP/s", "peak": bf16_peak, "frac": mlp_part["frac"]})
         if kernels:
             top = max(kernels, key=lambda k: k["ms"])
-            dominant = dict(top, traffic=None,
+            # the fallback contraction's DRAM bytes per row from the committed capture of the
+            # gated step's launches (~880 rows each), times this step's rows
+            per_row = read_traffic(f"tn_contract_f32_d{D}_fallback_bytes_per_row") \
+                if top["kernel"].startswith("tn_contract_kernel<float>") else None
+            dominant = dict(top, traffic=per_row * top["rows"] if per_row else None,
                             note=f"the longest kernel of the timed step ({top['ms']:.3f} of {step_ms:.3f} ms), timed "
-                                 f"alone on the same rows; peak = measured bf16 tensor rate ({peak_kind})")
+                                 f"alone on the same rows; peak = measured bf16 tensor rate ({peak_kind}); traffic = "
+                                 "DRAM bytes per row of the gated step's fallback launches (ncu) x rows")
         else:
             dominant = {"kernel": "tn_contract_kernel<float>", "bound": "fp32_simt", "achieved": achieved_tflops,
                         "peak": bf16_peak, "unit": "TFLOP/s", "frac": achieved_tflops / bf16_peak, "traffic": traffic}
