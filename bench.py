@@ -70,6 +70,11 @@ def parse():
                     help="single-syndrome latency of the d=7 plain float64 decode and of the float32 decode whose "
                          "row is always rechecked, for each single-syndrome launch form (one block, clusters of "
                          "2-16 blocks), then the autotuned form; one JSON line per form")
+    ap.add_argument("--tensor-orders", action="store_true",
+                    help="the tensor-aware order search: trees found with TreeSA(tensor_discount=D) at d=7 "
+                         "(65,536 rows; D = 0, 4, 16) and d=9 (8,192 rows; D = 0, 4), each contracted in float32 "
+                         "with its GEMM-shaped steps on tcgen05 and on the SIMT path (autotuned shapes; about "
+                         "20 minutes); one JSON line per tree and path")
     ap.add_argument("--circuit", action="store_true",
                     help="circuit-level rotated Z-memory d=5, 5 rounds, p=0.001: DEM from the generator, "
                          "--circuit-n seeded detector samples, float32 + recheck")
@@ -994,6 +999,72 @@ def run_latency(args):
     rech.close()
 
 
+def run_tensor_orders(args):
+    """Trees that trade flops for tensor-core-shaped steps (TreeSA's
+    tensor_discount) against the best SIMT tree: float32 contraction of the
+    whole batch, autotuned shape, tcgen05 and SIMT paths."""
+    import statistics
+
+    import torch
+
+    import __graft_entry__ as G
+
+    pkg = G.load_package()
+    N = pkg.native
+    st = torch.cuda.current_stream()
+    flush = torch.empty(64 << 20, dtype=torch.float32, device="cuda")
+
+    def timed(fn, reps=3):
+        out = []
+        for _ in range(reps):
+            flush.fill_(1.0)
+            torch.cuda.synchronize()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(st)
+            fn()
+            b.record(st)
+            torch.cuda.synchronize()
+            out.append(a.elapsed_time(b))
+        return statistics.median(out)
+
+    for d, n, discounts in ((7, 65536, (0.0, 4.0, 16.0)), (9, 8192, (0.0, 4.0))):
+        t = pkg.tanner_graph(pkg.SurfaceCode(d, d))
+        em = pkg.depolarizing(0.05, t.nq)
+        lx, lz = pkg.logical_operator(t)
+        g = pkg.tnmmap_css_graph(t, em, lx, lz)
+        ep = pkg.random_error_pattern(em, np.random.default_rng(77 + d), nsamples=n)
+        s = pkg.syndrome_extraction(ep, t)
+        packed = pkg.pack_syndromes(np.concatenate([s.sx, s.sz], axis=1))
+        d_syn = torch.from_numpy(packed).cuda()
+        d_lp = torch.empty((n, 4), dtype=torch.float64, device="cuda")
+        trees = [("committed", read_order())] if d == 7 else []
+        for D in discounts:
+            steps = pkg.optimize_code(g, pkg.TreeSA(trials=16, sweeps=1000, restarts=2, tensor_discount=D))
+            trees.append((f"tensor_discount={D:g}", steps))
+        for name, steps in trees:
+            for tc in (True, False):
+                ct = pkg.compile(pkg.TNMMAP(precision="f32", optimizer=pkg.FixedOrder(steps), tensor_cores=tc), t, em)
+                plan = N.inspect_plan(ct.graph, ct.steps)
+                macs = np.array([2.0 ** (int(x["lh"]) + int(x["lfa"]) + int(x["lfb"]) + int(x["lk"]))
+                                 for x in plan["steps"]])
+                on_tc = np.array([(int(x["flags"]) & 8) != 0 for x in plan["steps"]])
+                ct.program.autotune(min(n, 16384))
+                info = ct.program.info
+
+                def fn():
+                    ct.program.contract_ptrs(d_syn.data_ptr(), n, N.TQEC_F32, d_lp.data_ptr(), st.cuda_stream)
+
+                fn()
+                torch.cuda.synchronize()
+                ms = timed(fn)
+                print(json.dumps({"tensor_orders": True, "d": d, "rows": n, "tree": name, "tensor_cores": tc,
+                                  "flops_per_syndrome": info["flops_per_syndrome"],
+                                  "tensor_share_of_macs": float(macs[on_tc].sum() / macs.sum()),
+                                  "tensor_f32": info["tensor_f32"], "f32_ms": ms,
+                                  "syn_per_s": n / (ms / 1e3)}), flush=True)
+                ct.close()
+
+
 def circuit_program(args):
     """The Z-memory circuit (d=5, 5 rounds, p=0.001), its detector error
     model and the compiled float32 program of its factor graph."""
@@ -1141,6 +1212,8 @@ def main():
         run_mixed(args)
     elif args.latency:
         run_latency(args)
+    elif args.tensor_orders:
+        run_tensor_orders(args)
     elif args.precision_sweep:
         run_precision_sweep(args)
     elif args.profile_recheck:
