@@ -1426,6 +1426,9 @@ __device__ __forceinline__ Arena<T> block_arena(const KArgs& a, unsigned char* s
 template <typename T, bool NORM, bool MAXP, bool TENSOR, bool VS = (sizeof(T) == 8), bool RB = false>
 __global__ void __launch_bounds__(sizeof(T) == 8 || TENSOR ? 512 : 1024) tn_contract_kernel(KArgs a) {
   extern __shared__ __align__(16) unsigned char smem[];
+  // a dependent launch (the recheck's clusters) may be scheduled once every
+  // block has started; it waits for this grid before reading what it writes
+  asm volatile("griddepcontrol.launch_dependents;");
   const BlockSmem sm = carve_smem<NORM, MAXP>(a, smem);
   size_t off = sm.tail;
   const T* consts;
@@ -1478,9 +1481,6 @@ __global__ void __launch_bounds__(sizeof(T) == 8 || TENSOR ? 512 : 1024) tn_cont
 template <typename T, bool NORM>
 __global__ void __launch_bounds__(512) tn_contract_cluster_kernel(KArgs a) {
   extern __shared__ __align__(16) unsigned char smem[];
-  // a cluster without rows (the same answer for all its blocks) leaves at
-  // once: it reaches no cluster barrier and no other block's memory
-  if (int64_t(cluster_id()) * a.G >= (a.list ? int64_t(*a.list_count) : a.n)) return;
   BlockSmem sm = carve_smem<NORM, false>(a, smem);
   size_t off = sm.tail;
   const T* consts;
@@ -1491,6 +1491,14 @@ __global__ void __launch_bounds__(512) tn_contract_cluster_kernel(KArgs a) {
   stage_tables_wait(a);
   __syncthreads();
   fill_step_plan<T, false, true>(a, sm.steps, sm.plan, ptab, static_cast<int2*>(sm.ptrs));
+  // everything above reads only the program (steps, tables); a launch that
+  // may start while the preceding kernel of its stream finishes (programmatic
+  // dependent launch) waits for that kernel here, before the rows, their
+  // count and the outputs it may have written
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+  // a cluster without rows (the same answer for all its blocks) leaves now:
+  // it has reached no cluster barrier and no other block's memory
+  if (int64_t(cluster_id()) * a.G >= (a.list ? int64_t(*a.list_count) : a.n)) return;
   if (NORM) sm.max = cluster_map(sm.max, 0);
   const int64_t nrows = a.list ? int64_t(*a.list_count) : a.n;
   const int64_t cid = cluster_id(), ncl = cluster_count();
@@ -1738,13 +1746,21 @@ cudaError_t cluster_launch_with(K kernel, const KArgs& a, int clusters, int csiz
   cfg.blockDim = dim3(threads);
   cfg.dynamicSmemBytes = smem;
   cfg.stream = stream;
-  cudaLaunchAttribute at[1];
+  cudaLaunchAttribute at[2];
   at[0].id = cudaLaunchAttributeClusterDimension;
   at[0].val.clusterDim.x = csize;
   at[0].val.clusterDim.y = 1;
   at[0].val.clusterDim.z = 1;
   cfg.attrs = at;
   cfg.numAttrs = 1;
+  if (configure) {
+    // a standalone launch (not one captured into a graph) may begin its
+    // prologue while the stream's preceding kernel finishes; the kernel
+    // waits for that kernel (griddepcontrol.wait) before touching its data
+    at[1].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[1].val.programmaticStreamSerializationAllowed = 1;
+    cfg.numAttrs = 2;
+  }
   return cudaLaunchKernelEx(&cfg, kernel, a);
 }
 
