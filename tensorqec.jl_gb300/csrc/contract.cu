@@ -21,6 +21,7 @@
 #include <map>
 #include <mutex>
 #include <type_traits>
+#include <utility>
 
 #include "contract.cuh"
 #include "dfloat.cuh"
@@ -1629,13 +1630,15 @@ size_t contract_smem_limit(int device) {
 // only ever grows (to the largest any program or program set asked for), so a
 // launch prepared earlier -- one captured in a CUDA graph among them -- stays
 // valid after another program's set-up. The kernels of one family share a
-// function type, so the limit is kept per kernel address.
+// function type, so the limit is kept per kernel address (and device).
 template <typename K>
 cudaError_t grow_smem_limit(K kernel, size_t smem) {
   static std::mutex mu;
-  static std::map<const void*, size_t> granted;
+  static std::map<std::pair<const void*, int>, size_t> granted;  // per kernel and device
+  int dev = 0;
+  cudaGetDevice(&dev);
   std::lock_guard<std::mutex> lk(mu);
-  size_t& g = granted[reinterpret_cast<const void*>(kernel)];
+  size_t& g = granted[{reinterpret_cast<const void*>(kernel), dev}];
   if (smem <= g) return cudaSuccess;
   cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
   if (e == cudaSuccess) g = smem;
@@ -1699,9 +1702,11 @@ cudaError_t cluster_config(K kernel, int csize, int threads, size_t smem) {
   if (e != cudaSuccess || csize <= 8) return e;
   // clusters above the portable 8 blocks: allowed once per kernel
   static std::mutex mu;
-  static std::map<const void*, bool> allowed;
+  static std::map<std::pair<const void*, int>, bool> allowed;  // per kernel and device
+  int dev = 0;
+  cudaGetDevice(&dev);
   std::lock_guard<std::mutex> lk(mu);
-  bool& ok = allowed[reinterpret_cast<const void*>(kernel)];
+  bool& ok = allowed[{reinterpret_cast<const void*>(kernel), dev}];
   if (!ok) {
     e = cudaFuncSetAttribute(kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
     ok = e == cudaSuccess;
