@@ -378,11 +378,39 @@ def test_recheck_every_row(pkg, recheck_f64):
     bound = info["err_bound_f64"] if recheck_f64 else info["err_bound_f32x2"]
     np.testing.assert_allclose(err, np.float32(bound), rtol=1e-6)
     lp64 = ct.class_logprobs(bits, precision="f64")
-    top = lp64.max(axis=1, keepdims=True)
-    assert np.max(np.abs(np.exp(logp - top) - np.exp(lp64 - top))) <= 2 * bound + 1e-15
+    # class by class within the recheck arithmetic's bound of float64
+    assert_class_logprobs_within(logp, np.exp(lp64), 2 * bound + 1e-15)
     srt = np.sort(lp64, axis=1)
     tie = (srt[:, -1] - srt[:, -2]) <= 1e-9
     assert not ((cls != np.argmax(lp64, axis=1)) & ~tie).any()
+    ct.close()
+
+
+@pytest.mark.parametrize("small_in_smem", [1, 0])
+def test_cluster_placements_vs_plain_block_form(pkg, small_in_smem):
+    """The plain float64 form at d=7 on 16-block clusters with the small
+    intermediates in the first block's shared memory (1) or with every
+    intermediate in global memory (0), one row per call and a batch: per
+    class within 1e-10 of the one-block form, the same decisions."""
+    t = pkg.tanner_graph(pkg.SurfaceCode(7, 7))
+    em = pkg.depolarizing(0.07, t.nq)
+    ep = pkg.random_error_pattern(em, np.random.default_rng(41), nsamples=64)
+    syn = pkg.syndrome_extraction(ep, t)
+    bits = np.concatenate([syn.sx, syn.sz], axis=1)
+    ct = pkg.compile(pkg.TNMMAP(precision="f64", plain=True), t, em)
+    ct.program.set_cluster(pkg.native.TQEC_F64, 0)
+    want = np.exp(ct.class_logprobs(bits))
+    ct.program.set_cluster(pkg.native.TQEC_F64, 16, 128, small_in_smem)
+    assert ct.program.info["cluster_blocks"] == 16
+    cls, logp = ct.decode_batch(bits, return_logp=True)
+    assert_class_logprobs(logp, want)
+    for r in range(0, 64, 13):
+        c1, l1 = ct.decode_batch(bits[r:r + 1], return_logp=True)
+        assert c1[0] == cls[r]
+        assert_class_logprobs(l1, want[r:r + 1])
+    srt = np.sort(want, axis=1)
+    tie = (srt[:, -1] - srt[:, -2]) <= 1e-9 * srt[:, -1]
+    assert not ((cls != np.argmax(want, axis=1)) & ~tie).any()
     ct.close()
 
 
