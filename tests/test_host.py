@@ -341,3 +341,19 @@ def test_reference_error_model_known_answers(pkg):
     assert not pkg.check_logical_error(zero, np.array([1, 1, 0, 1, 1, 0, 0, 0, 0], np.uint8), lz)
     css = pkg.CSSErrorPattern(zero, zero)
     assert not pkg.check_logical_error(css, pkg.CSSErrorPattern(zero.copy(), zero.copy()), lx, lz)
+
+
+def test_bench_reads_the_committed_traffic_figures():
+    """bench.py's roofline traffic comes from profiles/roofline_traffic.txt:
+    the full-batch launch's bytes and the gated step's fallback bytes per row."""
+    import importlib.util
+    import os
+
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    spec = importlib.util.spec_from_file_location("bench_for_test", os.path.join(root, "bench.py"))
+    bench = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(bench)
+    full = bench.read_traffic()
+    per_row = bench.read_traffic(f"tn_contract_f32_d{bench.D}_fallback_bytes_per_row")
+    assert full is not None and full > 1e9
+    assert per_row is not None and 1e4 < per_row < 1e7

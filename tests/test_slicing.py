@@ -32,13 +32,17 @@ def test_slices_sum_to_the_whole_and_narrow_the_tree(pkg, oracle):
     lx, lz = pkg.logical_operator(t)
     g = pkg.tnmmap_css_graph(t, em, lx, lz)
     steps = pkg.optimize_code(g, pkg.TreeSA(trials=4, sweeps=200, restarts=1))
-    width = max(len(u) for u, _ in network.step_label_sets(g, steps))
+    sets = network.step_label_sets(g, steps)
+    width = max(len(u) for u, _ in sets)
+    res_width = max(len(r) for _, r in sets)  # the widest intermediate: a syndrome's working set
     labels = network.choose_slice_labels(g, steps, 3)
     assert len(labels) == 3 and not set(labels) & set(g.iy)
     total = 0
     for v in range(8):
         gs = network.slice_graph(g, labels, v)
-        assert max(len(u) for u, _ in network.step_label_sets(gs, steps)) < width
+        sliced = network.step_label_sets(gs, steps)
+        assert max(len(u) for u, _ in sliced) < width
+        assert max(len(r) for _, r in sliced) < res_width
         total = total + run_plan(pkg.native.inspect_plan(gs, steps), bits)
     want = oracle.OracleDecoder(oracle.css_tanner(*oracle.surface_code_stabilizers(7, 7)), em.px, em.py,
                                 em.pz).marginals(bits)
