@@ -1212,6 +1212,10 @@ bool tune_cluster_steps(tqec_program* p, int prec, bool plain, cudaEvent_t e0, c
   };
   float cur = 0.f;
   if (!time_row(&cur)) return false;
+  if (cur > 2.f) {  // a row of milliseconds: per-group tuning would take minutes; keep the plan as is
+    o.clear();
+    return true;
+  }
   for (int s0 = 0; s0 < n;) {
     int s1 = s0;
     while (s1 + 1 < n && !(p->plan.steps[s1].flags & tqec::kStepSync)) ++s1;
@@ -1239,17 +1243,22 @@ bool tune_cluster_steps(tqec_program* p, int prec, bool plain, cudaEvent_t e0, c
 // drop-in decodes one syndrome a call) or on one and on four rows (the
 // recheck: a few rows a batch; the sum decides).
 bool tune_cluster(tqec_program* p, int prec, bool plain, cudaEvent_t e0, cudaEvent_t e1) {
-  std::vector<ClusterShape> cands(1);  // the block form
-  for (int cs : {2, 4, 8, 16})
+  // the largest clusters first and the block form last: a program so wide
+  // that one row takes milliseconds stops trying shapes once the tuning has
+  // spent about two seconds of GPU time, keeping the best so far
+  std::vector<ClusterShape> cands;
+  for (int cs : {16, 8, 4, 2})
     for (int th : {128, 256, 512})
       for (int split : {1, 0}) {
         ClusterShape c;
         if (choose_cluster(p, prec, cs, th, &c, split)) cands.push_back(c);
       }
+  cands.push_back(ClusterShape{});  // the block form
   cudaGetLastError();
   ClusterShape best;
-  float best_ms = 1e30f;
+  float best_ms = 1e30f, spent_ms = 0.f;
   for (const ClusterShape& c : cands) {
+    if (spent_ms > 2000.f && best_ms < 1e30f) break;
     p->cluster[prec] = c;
     float total = 0.f;
     bool ok = true;
@@ -1275,6 +1284,7 @@ bool tune_cluster(tqec_program* p, int prec, bool plain, cudaEvent_t e0, cudaEve
       float ms = 0.f;
       cudaEventElapsedTime(&ms, e0, e1);
       total += ms;
+      spent_ms += ms * 4.f / 3.f;  // the warm-up call and the three timed ones
     }
     if (ok && total < best_ms) {
       best_ms = total;
